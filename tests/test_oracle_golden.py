@@ -1,0 +1,41 @@
+"""Pin the CPU oracles to the reference's own known-answer tests.
+
+The 18 cases (14 test functions, the two 1-4 scaling tests holding three systems each)
+come from platforms/reference/tests/TestReferenceMPIDForce.cpp, extracted as text by
+tests/golden/extract_reference_tests.py.  Tolerances are the ones those tests assert:
+energy 1e-4 relative (1e-5 / 1e-3 absolute-or-relative for the 1-4 scaling cases) and
+per-atom forces 1e-4 relative to max(|F_ref|, 1), as OpenMM's ASSERT_EQUAL_TOL/VEC do.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_tests.json")))
+CASES = GOLDEN["tests"]
+
+
+def assert_equal_tol(expected, found, tol):
+    scale = max(abs(expected), 1.0)
+    assert abs(expected - found) / scale <= tol, (expected, found)
+
+
+def assert_equal_vec(expected, found, tol):
+    scale = max(float(np.linalg.norm(expected)), 1.0)
+    assert np.all(np.abs(np.asarray(expected) - np.asarray(found)) / scale <= tol), (expected, found)
+
+
+def check_case(result, case):
+    assert_equal_tol(case["ref_energy"], result.energy, case["energy_tol"])
+    if case["ref_forces"] is not None:
+        for exp, got in zip(case["ref_forces"], result.forces):
+            assert_equal_vec(exp, got, case["force_tol"])
+
+
+@pytest.mark.skipif(not O.available("ref"), reason="reference oracle not built (needs the reference tree)")
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_reference_build_matches_golden(case):
+    check_case(O.evaluate(O.system_from_golden(GOLDEN, case), "ref"), case)
