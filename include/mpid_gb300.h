@@ -1,0 +1,121 @@
+/* C ABI of the GB300 MPIDForce evaluation (libmpid_gb300.so).
+ *
+ * This is the drop-in boundary for the reference's platform kernel
+ * CalcMPIDForceKernel (openmmapi/include/openmm/mpidKernels.h:50-104): a context holds
+ * one MPIDForce's parameters on one GPU and evaluates energy, forces and induced
+ * dipoles under PME (or no cutoff) with Direct, Mutual or Extrapolated polarisation.
+ * Plain pointers and sizes only; no exceptions cross the boundary.  Every function
+ * returns MPID_OK (0) or a negative status; mpid_last_error() gives the message of the
+ * last failure on the calling thread.
+ *
+ * Units: nm, e, kJ/mol.  Atom order is the caller's; the library sorts internally.
+ * Parameter orders follow MPIDForce::addMultipole (openmmapi/include/openmm/MPIDForce.h:245):
+ *   dipole X Y Z; quadrupole XX XY YY XZ YZ ZZ;
+ *   octopole XXX XXY XYY YYY XXZ XYZ YYZ XZZ YZZ ZZZ.
+ */
+#ifndef MPID_GB300_H
+#define MPID_GB300_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPID_OK 0
+#define MPID_ERR_INVALID -1        /* invalid argument or parameter (MPIDForceImpl.cpp:56-150) */
+#define MPID_ERR_CUDA -2           /* CUDA / cuFFT failure */
+#define MPID_ERR_NOT_CONVERGED -3  /* mutual induced dipoles did not converge (MPIDReferenceForce.cpp:2229-2235) */
+#define MPID_ERR_STATE -4          /* call made before the required set-up */
+
+/* Nonbonded methods and polarisation types: values of MPIDForce::NonbondedMethod and
+ * MPIDForce::PolarizationType (MPIDForce.h:58-94). */
+#define MPID_NO_CUTOFF 0
+#define MPID_PME 1
+#define MPID_MUTUAL 0
+#define MPID_DIRECT 1
+#define MPID_EXTRAPOLATED 2
+
+/* Arithmetic of the evaluation. */
+#define MPID_PRECISION_MIXED 0   /* FP32 pair/PME/solver, 64-bit fixed-point forces, FP64 energy and refinement */
+#define MPID_PRECISION_DOUBLE 1  /* FP64 throughout */
+
+/* mpid_settings.flags */
+#define MPID_FLAG_EXACT_ANISO_TORQUE 1u  /* use the energy-consistent induced-induced torque on
+                                            anisotropic atoms instead of the reference's */
+
+typedef struct mpid_context mpid_context;
+
+/* Force-wide settings; the fields mirror MPIDForce's getters/setters
+ * (MPIDForce.h:106-232, defaults MPIDForce.cpp:43-50). */
+typedef struct {
+    int num_atoms;
+    int nonbonded_method;      /* MPID_PME or MPID_NO_CUTOFF */
+    int polarization_type;     /* MPID_MUTUAL, MPID_DIRECT, MPID_EXTRAPOLATED */
+    double cutoff;             /* nm (PME) */
+    double ewald_alpha;        /* nm^-1, must be > 0 for PME */
+    int grid[3];               /* PME grid, each > 0 for PME */
+    int pme_order;             /* 5 or 6 (the reference fixes 6) */
+    double mutual_eps;         /* Debye RMS target of the mutual solver */
+    int max_iter;              /* mutual solver iteration limit */
+    int n_extrap;              /* number of extrapolation coefficients (<= 8) */
+    double extrap_coeffs[8];
+    double default_thole;      /* MPIDForce::setDefaultTholeWidth */
+    double scale14;            /* MPIDForce::set14ScaleFactor */
+    int precision;             /* MPID_PRECISION_MIXED or MPID_PRECISION_DOUBLE */
+    unsigned flags;
+} mpid_settings;
+
+/* Per-evaluation statistics. */
+typedef struct {
+    int solver_iterations;     /* FP32/FP64 CG iterations (mutual), PT orders (extrapolated) */
+    int refinement_steps;      /* FP64 residual evaluations (mixed mutual) */
+    double solver_residual;    /* final Debye RMS residual */
+    int num_tile_pairs;
+    double ms_total;           /* device time of the last evaluation */
+} mpid_stats;
+
+/* Fill `s` with the MPIDForce defaults for n atoms (PME not configured). */
+void mpid_default_settings(mpid_settings* s, int num_atoms);
+
+/* Create a context on CUDA device `device`.  Replaces
+ * CudaCalcMPIDForceKernel::initialize (platforms/cuda/src/MPIDCudaKernels.cpp:210-662)
+ * and the validation of MPIDForceImpl::initialize (openmmapi/src/MPIDForceImpl.cpp:51-150). */
+int mpid_create(const mpid_settings* settings, int device, mpid_context** out);
+void mpid_destroy(mpid_context* ctx);
+
+/* Multipole parameters of every atom (MPIDForce::addMultipole / setMultipoleParameters,
+ * MPIDForce.h:245-282); validated as MPIDForceImpl.cpp:84-150 does.  Host arrays. */
+int mpid_set_multipoles(mpid_context* ctx, const double* charge, const double* dipole, const double* quadrupole,
+                        const double* octopole, const int* axis_type, const int* atom_z, const int* atom_x,
+                        const int* atom_y, const double* thole, const double* polarity);
+
+/* Covalent maps (MPIDForce::setCovalentMap, MPIDForce.h:291-308) as CSR over (atom, type):
+ * offsets has 8*num_atoms+1 entries, type order Covalent12..15, PolarizationCovalent11..14. */
+int mpid_set_covalent(mpid_context* ctx, const int* offsets, const int* index);
+
+/* Evaluate with host buffers (CalcMPIDForceKernel::execute, mpidKernels.h:77).
+ * positions: 3n; box: 9 (row vectors, rectangular); forces: 3n, ADDED to;
+ * energy: returns the energy (may be NULL). */
+int mpid_evaluate(mpid_context* ctx, const double* positions, const double* box, double* forces, double* energy);
+
+/* Same with device pointers on `stream` (cudaStream_t, may be NULL for the legacy stream).
+ * d_forces is added to; d_energy (1 double) is overwritten.  Returns after enqueueing only
+ * when the mutual solver's convergence allows; results are ready when the stream is. */
+int mpid_evaluate_device(mpid_context* ctx, const double* d_positions, const double* box, double* d_forces,
+                         double* d_energy, void* stream);
+
+/* Dipoles of the last evaluation in caller order, 3n host doubles (e nm):
+ * which 0 induced (getInducedDipoles), 1 lab-frame permanent (getLabFramePermanentDipoles),
+ * 2 total (getTotalDipoles); mpidKernels.h:79-81. */
+int mpid_get_dipoles(mpid_context* ctx, int which, double* out);
+
+/* PME parameters in use (CalcMPIDForceKernel::getPMEParameters, mpidKernels.h:103). */
+int mpid_get_pme_parameters(mpid_context* ctx, double* alpha, int* nx, int* ny, int* nz);
+
+int mpid_get_stats(mpid_context* ctx, mpid_stats* out);
+
+/* Message of the last failure on this thread ("" if none). */
+const char* mpid_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

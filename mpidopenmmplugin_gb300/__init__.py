@@ -1,0 +1,10 @@
+"""GB300-native MPIDForce energy/force evaluation.
+
+`MPIDForce` mirrors the reference's force class (parameters, covalent maps, PME and
+solver settings); `MPIDContext` evaluates it on one GPU through the C ABI of
+libmpid_gb300.so (include/mpid_gb300.h).
+"""
+from .force import MPIDError, MPIDForce
+from .context import MPIDContext, load_library, library_path
+
+__all__ = ["MPIDForce", "MPIDContext", "MPIDError", "load_library", "library_path"]

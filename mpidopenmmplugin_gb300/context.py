@@ -1,0 +1,212 @@
+"""GPU evaluation of an MPIDForce through the C ABI of libmpid_gb300.so.
+
+`MPIDContext(force, num_particles)` creates the device context (the part of an OpenMM
+Context that owns the CalcMPIDForce kernel, MPIDCudaKernels.cpp:210-662) and
+`evaluate(positions, box)` runs CalcMPIDForceKernel::execute (mpidKernels.h:77).
+There is no CPU fallback: without the library or a CUDA device the calls raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+from .force import MPIDError, MPIDForce
+
+MPID_PRECISION_MIXED = 0
+MPID_PRECISION_DOUBLE = 1
+MPID_FLAG_EXACT_ANISO_TORQUE = 1
+
+# Entry points declared in include/mpid_gb300.h
+C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multipoles", "mpid_set_covalent",
+         "mpid_evaluate", "mpid_evaluate_device", "mpid_get_dipoles", "mpid_get_pme_parameters", "mpid_get_stats",
+         "mpid_last_error"]
+
+
+class Settings(ctypes.Structure):
+    _fields_ = [
+        ("num_atoms", ctypes.c_int),
+        ("nonbonded_method", ctypes.c_int),
+        ("polarization_type", ctypes.c_int),
+        ("cutoff", ctypes.c_double),
+        ("ewald_alpha", ctypes.c_double),
+        ("grid", ctypes.c_int * 3),
+        ("pme_order", ctypes.c_int),
+        ("mutual_eps", ctypes.c_double),
+        ("max_iter", ctypes.c_int),
+        ("n_extrap", ctypes.c_int),
+        ("extrap_coeffs", ctypes.c_double * 8),
+        ("default_thole", ctypes.c_double),
+        ("scale14", ctypes.c_double),
+        ("precision", ctypes.c_int),
+        ("flags", ctypes.c_uint),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("solver_iterations", ctypes.c_int),
+        ("refinement_steps", ctypes.c_int),
+        ("solver_residual", ctypes.c_double),
+        ("num_tile_pairs", ctypes.c_int),
+        ("ms_total", ctypes.c_double),
+    ]
+
+
+_LIB = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load_library(build=True):
+    """Load libmpid_gb300.so (building it in place when missing or stale)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if build:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise MPIDError("libmpid_gb300.so is not built; run mpidopenmmplugin_gb300._build.build()")
+    lib = ctypes.CDLL(_build.LIB)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    vp = ctypes.c_void_p
+    lib.mpid_default_settings.argtypes = [ctypes.POINTER(Settings), ctypes.c_int]
+    lib.mpid_default_settings.restype = None
+    lib.mpid_create.argtypes = [ctypes.POINTER(Settings), ctypes.c_int, ctypes.POINTER(vp)]
+    lib.mpid_destroy.argtypes = [vp]
+    lib.mpid_destroy.restype = None
+    lib.mpid_set_multipoles.argtypes = [vp, dp, dp, dp, dp, ip, ip, ip, ip, dp, dp]
+    lib.mpid_set_covalent.argtypes = [vp, ip, ip]
+    lib.mpid_evaluate.argtypes = [vp, dp, dp, dp, dp]
+    lib.mpid_evaluate_device.argtypes = [vp, vp, dp, vp, vp, vp]
+    lib.mpid_get_dipoles.argtypes = [vp, ctypes.c_int, dp]
+    lib.mpid_get_pme_parameters.argtypes = [vp, dp, ip, ip, ip]
+    lib.mpid_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    lib.mpid_last_error.argtypes = []
+    lib.mpid_last_error.restype = ctypes.c_char_p
+    for name in C_API:
+        if name not in ("mpid_default_settings", "mpid_destroy", "mpid_last_error"):
+            getattr(lib, name).restype = ctypes.c_int
+    _LIB = lib
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+class MPIDContext:
+    """One MPIDForce on one GPU.
+
+    precision: "mixed" (FP32 pair/PME/solver, 64-bit fixed-point forces, FP64 energy and
+    FP64 residual refinement) or "double" (FP64 throughout).
+    """
+
+    def __init__(self, force: MPIDForce, num_particles=None, device=0, precision="mixed",
+                 exact_aniso_torque=False, box=None):
+        self.lib = load_library()
+        n = force.getNumMultipoles() if num_particles is None else int(num_particles)
+        force.validate(n, box)
+        s = Settings()
+        self.lib.mpid_default_settings(ctypes.byref(s), n)
+        s.nonbonded_method = force.getNonbondedMethod()
+        s.polarization_type = force.getPolarizationType()
+        s.cutoff = force.getCutoffDistance()
+        alpha, nx, ny, nz = force.getPMEParameters()
+        s.ewald_alpha = alpha
+        s.grid[0], s.grid[1], s.grid[2] = nx, ny, nz
+        s.pme_order = force.getPmeBSplineOrder()
+        s.mutual_eps = force.getMutualInducedTargetEpsilon()
+        s.max_iter = force.getMutualInducedMaxIterations()
+        c = force.getExtrapolationCoefficients()
+        if len(c) > 8:
+            raise MPIDError("at most 8 extrapolation coefficients are supported")
+        s.n_extrap = len(c)
+        for i, v in enumerate(c):
+            s.extrap_coeffs[i] = v
+        s.default_thole = force.getDefaultTholeWidth()
+        s.scale14 = force.get14ScaleFactor()
+        s.precision = {"mixed": MPID_PRECISION_MIXED, "double": MPID_PRECISION_DOUBLE}[precision]
+        s.flags = MPID_FLAG_EXACT_ANISO_TORQUE if exact_aniso_torque else 0
+        self.n = n
+        self.precision = precision
+        self._h = ctypes.c_void_p()
+        self._check(self.lib.mpid_create(ctypes.byref(s), int(device), ctypes.byref(self._h)))
+        self.update_parameters(force)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise MPIDError(self.lib.mpid_last_error().decode(errors="replace"))
+
+    def update_parameters(self, force: MPIDForce):
+        """updateParametersInContext (MPIDForce.h:435): copy multipoles and covalent maps."""
+        if force.getNumMultipoles() != self.n:
+            raise MPIDError("updateParametersInContext: The number of multipoles has changed")
+        a = force.arrays()
+        self._arrays = a  # keep alive
+        self._check(self.lib.mpid_set_multipoles(self._h, _dp(a["charge"]), _dp(a["dipole"]), _dp(a["quadrupole"]),
+                                                 _dp(a["octopole"]), _ip(a["axis_type"]), _ip(a["atom_z"]),
+                                                 _ip(a["atom_x"]), _ip(a["atom_y"]), _dp(a["thole"]),
+                                                 _dp(a["polarity"])))
+        self._check(self.lib.mpid_set_covalent(self._h, _ip(a["cov_offsets"]), _ip(a["cov_index"])))
+
+    def evaluate(self, positions, box, forces=None):
+        """Energy (kJ/mol) and forces (n, 3) (kJ/mol/nm); forces are ADDED to `forces` if given."""
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(self.n, 3)
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        f = np.zeros((self.n, 3)) if forces is None else np.ascontiguousarray(forces, dtype=np.float64)
+        e = ctypes.c_double(0.0)
+        self._check(self.lib.mpid_evaluate(self._h, _dp(pos), _dp(b), _dp(f), ctypes.byref(e)))
+        return e.value, f
+
+    def evaluate_device(self, d_positions, box, d_forces, d_energy=0, stream=0):
+        """Device-pointer evaluation (integers are raw CUDA addresses)."""
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        self._check(self.lib.mpid_evaluate_device(self._h, ctypes.c_void_p(d_positions), _dp(b),
+                                                  ctypes.c_void_p(d_forces), ctypes.c_void_p(d_energy),
+                                                  ctypes.c_void_p(stream)))
+
+    def _dipoles(self, which):
+        out = np.zeros((self.n, 3))
+        self._check(self.lib.mpid_get_dipoles(self._h, int(which), _dp(out)))
+        return out
+
+    def getInducedDipoles(self):
+        return self._dipoles(0)
+
+    def getLabFramePermanentDipoles(self):
+        return self._dipoles(1)
+
+    def getTotalDipoles(self):
+        return self._dipoles(2)
+
+    def getPMEParametersInContext(self):
+        a = ctypes.c_double()
+        nx, ny, nz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.mpid_get_pme_parameters(self._h, ctypes.byref(a), ctypes.byref(nx), ctypes.byref(ny),
+                                                     ctypes.byref(nz)))
+        return a.value, nx.value, ny.value, nz.value
+
+    def stats(self):
+        s = Stats()
+        self._check(self.lib.mpid_get_stats(self._h, ctypes.byref(s)))
+        return dict(solver_iterations=s.solver_iterations, refinement_steps=s.refinement_steps,
+                    solver_residual=s.solver_residual, num_tile_pairs=s.num_tile_pairs, ms_total=s.ms_total)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.mpid_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,965 @@
+// Host side of the GB300 MPIDForce evaluation: device buffers, cuFFT plans, the
+// evaluation sequence and the induced-dipole solvers, behind the C ABI declared in
+// include/mpid_gb300.h.  Replaces the reference's CUDA platform kernel
+// (platforms/cuda/src/MPIDCudaKernels.cpp:711-1054).
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <cub/device/device_radix_sort.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mpid_gb300.h"
+#include "mpid_kernels.cuh"
+#include "pme_host.h"
+
+namespace mpid {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CUDA_CHECK(x)                                                                              \
+    do {                                                                                           \
+        cudaError_t e_ = (x);                                                                      \
+        if (e_ != cudaSuccess)                                                                     \
+            throw Error(MPID_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));           \
+    } while (0)
+#define CUFFT_CHECK(x)                                                                             \
+    do {                                                                                           \
+        cufftResult r_ = (x);                                                                      \
+        if (r_ != CUFFT_SUCCESS) throw Error(MPID_ERR_CUDA, std::string(#x) + " failed, code " + std::to_string((int) r_)); \
+    } while (0)
+
+static inline int nblk(long long n, int b) { return (int) ((n + b - 1) / b); }
+
+// Simple owning device buffer.
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    void alloc(size_t count) {
+        if (count <= n && p) return;
+        free();
+        CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
+        n = count;
+    }
+    void free() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DBuf() { free(); }
+};
+
+// ---------------------------------------------------------------------------
+template <typename real> struct FftTypes;
+template <> struct FftTypes<float> {
+    static constexpr cufftType fwd = CUFFT_R2C, inv = CUFFT_C2R;
+    static void exec_fwd(cufftHandle h, float* in, float2* out) { CUFFT_CHECK(cufftExecR2C(h, in, (cufftComplex*) out)); }
+    static void exec_inv(cufftHandle h, float2* in, float* out) { CUFFT_CHECK(cufftExecC2R(h, (cufftComplex*) in, out)); }
+};
+template <> struct FftTypes<double> {
+    static constexpr cufftType fwd = CUFFT_D2Z, inv = CUFFT_Z2D;
+    static void exec_fwd(cufftHandle h, double* in, double2* out) { CUFFT_CHECK(cufftExecD2Z(h, in, (cufftDoubleComplex*) out)); }
+    static void exec_inv(cufftHandle h, double2* in, double* out) { CUFFT_CHECK(cufftExecZ2D(h, (cufftDoubleComplex*) in, out)); }
+};
+
+// One precision's PME machinery: B-spline tables of the sorted atoms, accumulation
+// grid, real / half-complex FFT grids and plans.
+template <typename real>
+struct PmeStage {
+    int order = 6, nx = 0, ny = 0, nz = 0;
+    size_t G = 0, Gh = 0;
+    DBuf<typename GridAcc<real>::type> acc;
+    DBuf<real> rgrid;
+    DBuf<typename Cplx<real>::type> cgrid;
+    DBuf<real> theta;
+    DBuf<int> igrid;
+    cufftHandle fwd = 0, inv = 0;
+    bool planned = false;
+
+    void init(int ord, int gx, int gy, int gz, int npad) {
+        order = ord;
+        nx = gx; ny = gy; nz = gz;
+        G = (size_t) nx * ny * nz;
+        Gh = (size_t) nx * ny * (nz / 2 + 1);
+        acc.alloc(G);
+        rgrid.alloc(G);
+        cgrid.alloc(Gh);
+        theta.alloc((size_t) 3 * 5 * order * npad);
+        igrid.alloc((size_t) 3 * npad);
+        CUDA_CHECK(cudaMemset(acc.p, 0, G * sizeof(typename GridAcc<real>::type)));
+        CUFFT_CHECK(cufftPlan3d(&fwd, nx, ny, nz, FftTypes<real>::fwd));
+        CUFFT_CHECK(cufftPlan3d(&inv, nx, ny, nz, FftTypes<real>::inv));
+        planned = true;
+    }
+    ~PmeStage() {
+        if (planned) {
+            cufftDestroy(fwd);
+            cufftDestroy(inv);
+        }
+    }
+    void set_stream(cudaStream_t s) {
+        CUFFT_CHECK(cufftSetStream(fwd, s));
+        CUFFT_CHECK(cufftSetStream(inv, s));
+    }
+    void bsplines(int n, int npad, const unsigned long long* keys, const double* wpos, const BoxDev& box, cudaStream_t st) {
+        if (order == 5)
+            k_bsplines<real, 5><<<nblk(npad, 128), 128, 0, st>>>(npad, n, keys, wpos, box, theta.p, igrid.p);
+        else
+            k_bsplines<real, 6><<<nblk(npad, 128), 128, 0, st>>>(npad, n, keys, wpos, box, theta.p, igrid.p);
+    }
+    template <int NCOMP>
+    void spread(int n, int npad, const BoxDev& box, const real* mf, const int* skip, cudaStream_t st) {
+        const long long threads = (long long) n * order * order;
+        if (order == 5)
+            k_spread<real, 5, NCOMP><<<nblk(threads, 256), 256, 0, st>>>(n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
+        else
+            k_spread<real, 6, NCOMP><<<nblk(threads, 256), 256, 0, st>>>(n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
+        k_grid_finish<real><<<std::min<long long>(nblk(G, 256), 152 * 16), 256, 0, st>>>(G, acc.p, rgrid.p, skip);
+    }
+    void convolve(const double* influence, const int* skip, cudaStream_t st) {
+        FftTypes<real>::exec_fwd(fwd, rgrid.p, cgrid.p);
+        k_convolve<real><<<std::min<long long>(nblk(Gh, 256), 152 * 16), 256, 0, st>>>(Gh, influence, cgrid.p, skip);
+        FftTypes<real>::exec_inv(inv, cgrid.p, rgrid.p);
+    }
+    template <int NTERM>
+    void gather(int n, int npad, const BoxDev& box, real* phi, const int* skip, cudaStream_t st) {
+        if (order == 5)
+            k_gather<real, 5, NTERM><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, theta.p, igrid.p, rgrid.p, phi, skip);
+        else
+            k_gather<real, 6, NTERM><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, theta.p, igrid.p, rgrid.p, phi, skip);
+    }
+};
+
+// Per-precision engine: sorted atom arrays, PME stage, field / force accumulators.
+template <typename real>
+struct Engine {
+    int n = 0, npad = 0;
+    DBuf<real> off, mom, alab, sroot;
+    DBuf<float4> prm;
+    DBuf<int> orig, rank;
+    DBuf<real> mf, mfd;                       // [20][npad], [4][npad]
+    DBuf<real> phiP, phiD, phiT;              // [35][npad] each; phiT scratch
+    DBuf<unsigned long long> fieldFx, gradFx;  // [3][npad], [6][npad]
+    DBuf<real> Efix, muD, SE, mu, Etmp, Gtmp, sp;
+    PmeStage<real> pme;
+    bool usePme = false;
+
+    AtomArrays<real> arrays() {
+        AtomArrays<real> a;
+        a.n = n; a.npad = npad;
+        a.off = off.p; a.mom = mom.p; a.alab = alab.p; a.sroot = sroot.p;
+        a.prm = prm.p; a.orig = orig.p; a.rank = rank.p;
+        return a;
+    }
+    void init(int natoms, int pad, bool pme_, int order, const int* grid) {
+        n = natoms;
+        npad = pad;
+        usePme = pme_;
+        off.alloc(3 * (size_t) npad);
+        mom.alloc(20 * (size_t) npad);
+        alab.alloc(6 * (size_t) npad);
+        sroot.alloc(6 * (size_t) npad);
+        prm.alloc(npad);
+        orig.alloc(npad);
+        rank.alloc(std::max(n, 1));
+        mf.alloc(20 * (size_t) npad);
+        mfd.alloc(4 * (size_t) npad);
+        phiP.alloc(35 * (size_t) npad);
+        phiD.alloc(35 * (size_t) npad);
+        phiT.alloc(35 * (size_t) npad);
+        fieldFx.alloc(3 * (size_t) npad);
+        gradFx.alloc(6 * (size_t) npad);
+        Efix.alloc(3 * (size_t) npad);
+        muD.alloc(3 * (size_t) npad);
+        SE.alloc(3 * (size_t) npad);
+        mu.alloc(3 * (size_t) npad);
+        Etmp.alloc(3 * (size_t) npad);
+        Gtmp.alloc(6 * (size_t) npad);
+        sp.alloc(3 * (size_t) npad);
+        if (usePme) pme.init(order, grid[0], grid[1], grid[2], npad);
+    }
+};
+
+// ---------------------------------------------------------------------------
+struct Context {
+    mpid_settings set;
+    int device = 0;
+    int n = 0, npad = 0, ntiles = 0;
+    bool usePme = false, mixed = true;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+
+    // parameters (device, original order)
+    DBuf<double> charge, dipole, quad, oct, thole, pol;
+    DBuf<int> axis, az, ax, ay;
+    std::vector<int> h_axis, h_az, h_ax, h_ay;
+    bool haveParams = false;
+    // covalent partners: symmetric CSR over original indices
+    DBuf<int> covOff, covJ;
+    DBuf<float> covS;
+    // sort / tiles
+    DBuf<unsigned long long> keys, keysAlt;
+    DBuf<char> cubTemp;
+    size_t cubBytes = 0;
+    DBuf<double> pos, wpos, center, half;
+    DBuf<int2> pairs;
+    DBuf<int> npairs;
+    int pairCapacity = 0;
+    int lastPairs = 0;
+    // PME tables
+    DBuf<double> modx, mody, modz, influence;
+    double lastBox[9] = {0};
+    // engines
+    std::unique_ptr<Engine<float>> ef;
+    std::unique_ptr<Engine<double>> ed;
+    // accumulators (sorted order)
+    DBuf<unsigned long long> forceFx, torqueFx, energyFx;
+    DBuf<double> energyPartial, energyOut;
+    DBuf<double> forcesOut;
+    // solver scratch
+    DBuf<double> partial, red, sc;
+    DBuf<int> iter, done;
+    DBuf<float> r32, p32, q32, x32, b32;
+    DBuf<double> r64, p64, q64, y64, b64, res64, Efix64;
+    DBuf<float> res32;
+    // extrapolated
+    DBuf<float> ptMuF, ptEF, ptGF;
+    DBuf<double> ptMuD, ptED, ptGD;
+    int* hostDone = nullptr;
+    std::vector<cudaEvent_t> iterEvents;
+    cudaEvent_t evStart = nullptr, evStop = nullptr;
+    mpid_stats stats{};
+    bool evaluated = false;
+    BoxDev box{};
+
+    ~Context() {
+        if (hostDone) cudaFreeHost(hostDone);
+        for (auto e : iterEvents) cudaEventDestroy(e);
+        if (evStart) cudaEventDestroy(evStart);
+        if (evStop) cudaEventDestroy(evStop);
+        if (ownStream && stream) cudaStreamDestroy(stream);
+    }
+
+    // ----- set-up -----
+    void create(const mpid_settings& s, int dev) {
+        set = s;
+        device = dev;
+        n = s.num_atoms;
+        if (n <= 0) throw Error(MPID_ERR_INVALID, "MPIDForce must have at least one particle");
+        if (s.nonbonded_method != MPID_PME && s.nonbonded_method != MPID_NO_CUTOFF)
+            throw Error(MPID_ERR_INVALID, "MPIDForce: Illegal value for nonbonded method");
+        if (s.polarization_type < 0 || s.polarization_type > 2)
+            throw Error(MPID_ERR_INVALID, "Polarization type not recognzied.");
+        if (s.precision != MPID_PRECISION_MIXED && s.precision != MPID_PRECISION_DOUBLE)
+            throw Error(MPID_ERR_INVALID, "unknown precision");
+        usePme = s.nonbonded_method == MPID_PME;
+        if (usePme) {
+            if (!(s.ewald_alpha > 0) || s.grid[0] <= 0 || s.grid[1] <= 0 || s.grid[2] <= 0)
+                throw Error(MPID_ERR_INVALID, "PME needs explicit ewald_alpha > 0 and grid dimensions > 0");
+            if (s.pme_order != 5 && s.pme_order != 6)
+                throw Error(MPID_ERR_INVALID, "pme_order must be 5 or 6");
+            if (!(s.cutoff > 0)) throw Error(MPID_ERR_INVALID, "cutoff must be positive");
+        }
+        if (s.polarization_type == MPID_EXTRAPOLATED && (s.n_extrap < 1 || s.n_extrap > 8))
+            throw Error(MPID_ERR_INVALID, "extrapolation needs 1..8 coefficients");
+        mixed = s.precision == MPID_PRECISION_MIXED;
+        CUDA_CHECK(cudaSetDevice(device));
+        npad = ((n + 31) / 32) * 32;
+        ntiles = npad / 32;
+        charge.alloc(n); dipole.alloc(3 * n); quad.alloc(6 * n); oct.alloc(10 * n); thole.alloc(n); pol.alloc(3 * n);
+        axis.alloc(n); az.alloc(n); ax.alloc(n); ay.alloc(n);
+        keys.alloc(n); keysAlt.alloc(n);
+        cub::DeviceRadixSort::SortKeys(nullptr, cubBytes, keys.p, keysAlt.p, n);
+        cubTemp.alloc(cubBytes);
+        pos.alloc(3 * n); wpos.alloc(3 * n); center.alloc(3 * ntiles); half.alloc(3 * ntiles);
+        npairs.alloc(1);
+        pairCapacity = std::max(1024, std::min(ntiles * (ntiles + 1) / 2, ntiles * 160));
+        pairs.alloc(pairCapacity);
+        forceFx.alloc(3 * (size_t) npad); torqueFx.alloc(3 * (size_t) npad); energyFx.alloc(1);
+        energyPartial.alloc(nblk(npad, 256)); energyOut.alloc(1);
+        forcesOut.alloc(3 * (size_t) n);
+        partial.alloc(2 * (size_t) nblk(npad, 256)); red.alloc(4); sc.alloc(8);
+        iter.alloc(1); done.alloc(1);
+        CUDA_CHECK(cudaMallocHost(&hostDone, 256 * sizeof(int)));
+        CUDA_CHECK(cudaEventCreate(&evStart));
+        CUDA_CHECK(cudaEventCreate(&evStop));
+        iterEvents.resize(256);
+        for (auto& e : iterEvents) CUDA_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        const int nPT = s.polarization_type == MPID_EXTRAPOLATED ? s.n_extrap : 0;
+        if (mixed) {
+            ef.reset(new Engine<float>());
+            ef->init(n, npad, usePme, s.pme_order, s.grid);
+            r32.alloc(3 * (size_t) npad); p32.alloc(3 * (size_t) npad); q32.alloc(3 * (size_t) npad);
+            x32.alloc(3 * (size_t) npad); b32.alloc(3 * (size_t) npad); res32.alloc(3 * (size_t) npad);
+            if (nPT) { ptMuF.alloc((size_t) nPT * 3 * npad); ptEF.alloc((size_t) nPT * 3 * npad); ptGF.alloc((size_t) nPT * 6 * npad); }
+            if (s.polarization_type == MPID_MUTUAL) {
+                ed.reset(new Engine<double>());  // FP64 residual of the refinement loop
+                ed->init(n, npad, usePme, s.pme_order, s.grid);
+            }
+        } else {
+            ed.reset(new Engine<double>());
+            ed->init(n, npad, usePme, s.pme_order, s.grid);
+            if (nPT) { ptMuD.alloc((size_t) nPT * 3 * npad); ptED.alloc((size_t) nPT * 3 * npad); ptGD.alloc((size_t) nPT * 6 * npad); }
+        }
+        if (s.polarization_type == MPID_MUTUAL) {
+            r64.alloc(3 * (size_t) npad); p64.alloc(3 * (size_t) npad); q64.alloc(3 * (size_t) npad);
+            y64.alloc(3 * (size_t) npad); b64.alloc(3 * (size_t) npad); res64.alloc(3 * (size_t) npad);
+            Efix64.alloc(3 * (size_t) npad);
+        }
+        if (usePme) {
+            std::vector<double> mx = bspline_moduli(s.pme_order, s.grid[0]);
+            std::vector<double> my = bspline_moduli(s.pme_order, s.grid[1]);
+            std::vector<double> mz = bspline_moduli(s.pme_order, s.grid[2]);
+            modx.alloc(mx.size()); mody.alloc(my.size()); modz.alloc(mz.size());
+            CUDA_CHECK(cudaMemcpy(modx.p, mx.data(), mx.size() * 8, cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(mody.p, my.data(), my.size() * 8, cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(modz.p, mz.data(), mz.size() * 8, cudaMemcpyHostToDevice));
+            influence.alloc((size_t) s.grid[0] * s.grid[1] * (s.grid[2] / 2 + 1));
+        }
+        // empty covalent lists until set
+        std::vector<int> off0(n + 1, 0);
+        covOff.alloc(n + 1);
+        CUDA_CHECK(cudaMemcpy(covOff.p, off0.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        covJ.alloc(1);
+        covS.alloc(1);
+    }
+
+    void set_multipoles(const double* q, const double* d, const double* Q, const double* O, const int* at, const int* z,
+                        const int* x, const int* y, const double* th, const double* p) {
+        // MPIDForceImpl::initialize validation (openmmapi/src/MPIDForceImpl.cpp:72-150)
+        const double tol = 1.0e-5;
+        for (int i = 0; i < n; ++i) {
+            double tr = std::fabs(Q[6 * i] + Q[6 * i + 2] + Q[6 * i + 5]);
+            if (tr > tol) {
+                std::ostringstream m;
+                m << "MPIDForce: quadrupole for particle=" << i << " has nonzero trace: " << tr
+                  << "; MPID plugin assumes traceless quadrupole.";
+                throw Error(MPID_ERR_INVALID, m.str());
+            }
+            const int tr3[3][3] = {{0, 2, 7}, {1, 3, 8}, {4, 6, 9}};
+            const char* names[3] = {"(XXX,XYY,XZZ)", "(YXX,YYY,YZZ)", "(ZXX,ZYY,ZZZ)"};
+            for (int k = 0; k < 3; ++k) {
+                double t = std::fabs(O[10 * i + tr3[k][0]] + O[10 * i + tr3[k][1]] + O[10 * i + tr3[k][2]]);
+                if (t > tol) {
+                    std::ostringstream m;
+                    m << "MPIDForce: " << names[k] << " octopole for particle=" << i << " has nonzero trace: " << t
+                      << "; MPID plugin assumes traceless octopoles.";
+                    throw Error(MPID_ERR_INVALID, m.str());
+                }
+            }
+            if (at[i] < 0 || at[i] > NoAxisType) {
+                std::ostringstream m;
+                m << "MPIDForce: axis type=" << at[i] << " not currently handled";
+                throw Error(MPID_ERR_INVALID, m.str());
+            }
+            if (at[i] != NoAxisType && (z[i] < 0 || z[i] >= n)) {
+                std::ostringstream m;
+                m << "MPIDForce: invalid z axis particle: " << z[i];
+                throw Error(MPID_ERR_INVALID, m.str());
+            }
+            if (at[i] != NoAxisType && at[i] != ZOnly && (x[i] < 0 || x[i] >= n)) {
+                std::ostringstream m;
+                m << "MPIDForce: invalid x axis particle: " << x[i];
+                throw Error(MPID_ERR_INVALID, m.str());
+            }
+            if ((at[i] == ZBisect || at[i] == ThreeFold) && (y[i] < 0 || y[i] >= n)) {
+                std::ostringstream m;
+                m << "MPIDForce: invalid y axis particle: " << y[i];
+                throw Error(MPID_ERR_INVALID, m.str());
+            }
+            if (y[i] >= n) throw Error(MPID_ERR_INVALID, "MPIDForce: invalid y axis particle");
+            for (int k = 0; k < 3; ++k)
+                if (p[3 * i + k] < 0) throw Error(MPID_ERR_INVALID, "MPIDForce: negative polarizability");
+        }
+        h_axis.assign(at, at + n); h_az.assign(z, z + n); h_ax.assign(x, x + n); h_ay.assign(y, y + n);
+        CUDA_CHECK(cudaMemcpy(charge.p, q, n * 8, cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(dipole.p, d, 3 * n * 8, cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(quad.p, Q, 6 * n * 8, cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(oct.p, O, 10 * n * 8, cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(thole.p, th, n * 8, cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(pol.p, p, 3 * n * 8, cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(axis.p, at, n * 4, cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(az.p, z, n * 4, cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(ax.p, x, n * 4, cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(ay.p, y, n * 4, cudaMemcpyHostToDevice));
+        haveParams = true;
+    }
+
+    // Pair scale from covalent maps as MPIDReferenceForce::setupScaleMaps
+    // (MPIDReferenceForce.cpp:190-225): the lower-index atom's lists decide, types
+    // 1-2, 1-3 -> 0, 1-4 -> scale14, 1-5 -> 1, later types overwrite earlier ones.
+    void set_covalent(const int* offsets, const int* index) {
+        const double sval[4] = {0.0, 0.0, set.scale14, 1.0};
+        std::map<std::pair<int, int>, double> sc;
+        for (int i = 0; i < n; ++i)
+            for (int t = 0; t < 4; ++t)
+                for (int k = offsets[8 * i + t]; k < offsets[8 * i + t + 1]; ++k) {
+                    const int j = index[k];
+                    if (j < 0 || j >= n) throw Error(MPID_ERR_INVALID, "MPIDForce: covalent index out of range");
+                    if (j < i) continue;
+                    sc[{i, j}] = sval[t];
+                }
+        std::vector<std::vector<std::pair<int, float>>> lists(n);
+        for (auto& kv : sc) {
+            if (kv.second == 1.0 || kv.first.first == kv.first.second) continue;
+            lists[kv.first.first].push_back({kv.first.second, (float) kv.second});
+            lists[kv.first.second].push_back({kv.first.first, (float) kv.second});
+        }
+        std::vector<int> off(n + 1, 0), js;
+        std::vector<float> ss;
+        for (int i = 0; i < n; ++i) {
+            for (auto& e : lists[i]) { js.push_back(e.first); ss.push_back(e.second); }
+            off[i + 1] = (int) js.size();
+        }
+        covJ.alloc(std::max<size_t>(js.size(), 1));
+        covS.alloc(std::max<size_t>(ss.size(), 1));
+        CUDA_CHECK(cudaMemcpy(covOff.p, off.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        if (!js.empty()) {
+            CUDA_CHECK(cudaMemcpy(covJ.p, js.data(), js.size() * sizeof(int), cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(covS.p, ss.data(), ss.size() * sizeof(float), cudaMemcpyHostToDevice));
+        }
+    }
+
+    MolArrays mol() const {
+        MolArrays m;
+        m.charge = charge.p; m.dipole = dipole.p; m.quad = quad.p; m.oct = oct.p; m.thole = thole.p; m.pol = pol.p;
+        m.axis = axis.p; m.az = az.p; m.ax = ax.p; m.ay = ay.p;
+        return m;
+    }
+
+    void set_box(const double* b) {
+        for (int k = 0; k < 9; ++k)
+            if ((k % 4) != 0 && b[k] != 0.0)
+                throw Error(MPID_ERR_INVALID, "only rectangular periodic boxes are supported");
+        const double L[3] = {b[0], b[4], b[8]};
+        if (usePme) {
+            for (int k = 0; k < 3; ++k)
+                if (!(L[k] > 0)) throw Error(MPID_ERR_INVALID, "Box size of zero is invalid.");
+            const double minAllowed = 1.999999 * set.cutoff;  // MPIDReferenceKernels.cpp:193-197
+            if (L[0] < minAllowed || L[1] < minAllowed || L[2] < minAllowed)
+                throw Error(MPID_ERR_INVALID, "The periodic box size has decreased to less than twice the nonbonded cutoff.");
+        }
+        for (int k = 0; k < 3; ++k) {
+            box.L[k] = usePme ? L[k] : 1.0;
+            box.invL[k] = usePme ? 1.0 / L[k] : 1.0;
+            box.grid[k] = usePme ? set.grid[k] : 1;
+        }
+        for (int j = 0; j < 3; ++j)
+            for (int i = 0; i < 3; ++i) box.A[j][i] = (usePme && i == j) ? set.grid[j] / L[j] : 0.0;
+        if (usePme && std::memcmp(lastBox, b, sizeof(lastBox)) != 0) {
+            const size_t Gh = (size_t) set.grid[0] * set.grid[1] * (set.grid[2] / 2 + 1);
+            k_influence<<<std::min<long long>(nblk(Gh, 256), 152 * 8), 256, 0, stream>>>(
+                box, set.ewald_alpha, modx.p, mody.p, modz.p, 1.0 / L[0], 1.0 / L[1], 1.0 / L[2], L[0] * L[1] * L[2],
+                influence.p);
+            CUDA_CHECK(cudaGetLastError());
+            std::memcpy(lastBox, b, sizeof(lastBox));
+        }
+    }
+
+    TileCtx tile_ctx() const {
+        TileCtx c;
+        c.pairs = pairs.p;
+        c.npairs = npairs.p;
+        c.center = center.p;
+        c.box = box;
+        c.usePbc = usePme ? 1 : 0;
+        c.cutoff = usePme ? set.cutoff : 1e30;
+        c.ewald = usePme ? set.ewald_alpha : 0.0;
+        c.defaultThole = set.default_thole;
+        c.covOff = covOff.p;
+        c.covJ = covJ.p;
+        c.covS = covS.p;
+        return c;
+    }
+
+    int pair_blocks() const { return std::max(1, std::min(nblk(std::max(lastPairs, 1), kWarpsPerBlock), 152 * 64)); }
+
+    // Sort, tiles, tile pairs.
+    void neighbour_setup() {
+        cudaStream_t st = stream;
+        if (usePme) {
+            k_sort_keys<<<nblk(n, 256), 256, 0, st>>>(n, pos.p, box, 0.25, keys.p, wpos.p);
+            CUDA_CHECK(cub::DeviceRadixSort::SortKeys(cubTemp.p, cubBytes, keys.p, keysAlt.p, n, 0, 64, st));
+            std::swap(keys.p, keysAlt.p);
+        } else {
+            // No periodic box: keep the caller's order (all pairs interact).
+            std::vector<unsigned long long> k(n);
+            for (int i = 0; i < n; ++i) k[i] = (unsigned long long) i;
+            CUDA_CHECK(cudaMemcpyAsync(keys.p, k.data(), n * 8, cudaMemcpyHostToDevice, st));
+            CUDA_CHECK(cudaMemcpyAsync(wpos.p, pos.p, 3 * n * 8, cudaMemcpyDeviceToDevice, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+        }
+        k_tile_bounds<<<nblk(ntiles, 128), 128, 0, st>>>(n, ntiles, keys.p, wpos.p, center.p, half.p);
+        for (int attempt = 0; attempt < 3; ++attempt) {
+            CUDA_CHECK(cudaMemsetAsync(npairs.p, 0, sizeof(int), st));
+            const long long total = (long long) ntiles * (ntiles + 1) / 2;
+            k_tile_pairs<<<nblk(total, 256), 256, 0, st>>>(ntiles, center.p, half.p, box, usePme ? set.cutoff : 1e30,
+                                                           usePme ? 1 : 0, pairs.p, npairs.p, pairCapacity);
+            CUDA_CHECK(cudaGetLastError());
+            int cnt = 0;
+            CUDA_CHECK(cudaMemcpyAsync(&cnt, npairs.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            lastPairs = cnt;
+            if (cnt <= pairCapacity) return;
+            pairCapacity = (int) (cnt * 1.25) + 1024;  // regrow and rebuild
+            pairs.alloc(pairCapacity);
+        }
+        throw Error(MPID_ERR_CUDA, "tile pair list overflow");
+    }
+
+    template <typename real>
+    void prepare_engine(Engine<real>& e) {
+        cudaStream_t st = stream;
+        k_gather_atoms<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, keys.p, mol(), pos.p, wpos.p, center.p, e.arrays());
+        if (usePme) {
+            e.pme.set_stream(st);
+            e.pme.bsplines(n, npad, keys.p, wpos.p, box, st);
+            k_frac_multipoles<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, e.mom.p, e.mf.p);
+        }
+        CUDA_CHECK(cudaGetLastError());
+    }
+
+    double self_coef() const {
+        return usePme ? 4.0 / 3.0 * set.ewald_alpha * set.ewald_alpha * set.ewald_alpha / kSqrtPiRef : 0.0;
+    }
+
+    // Permanent field -> Efix, muD, SE (and phiP for the reciprocal forces).
+    template <typename real>
+    void fixed_field(Engine<real>& e) {
+        cudaStream_t st = stream;
+        CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
+        k_fixed_field<real><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tile_ctx(), e.arrays(), e.fieldFx.p);
+        if (usePme) {
+            e.pme.template spread<20>(n, npad, box, e.mf.p, nullptr, st);
+            e.pme.convolve(influence.p, nullptr, st);
+            e.pme.template gather<35>(n, npad, box, e.phiP.p, nullptr, st);
+        }
+        k_record_fixed<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, self_coef(), e.fieldFx.p,
+                                                               usePme ? e.phiP.p : nullptr, e.arrays(), e.Efix.p, e.muD.p,
+                                                               e.SE.p);
+        CUDA_CHECK(cudaGetLastError());
+    }
+
+    // Field (and optionally gradient) of dipoles mu: real + reciprocal + self -> E, G.
+    template <typename real>
+    void dipole_field(Engine<real>& e, const real* mu, real* E, real* G, const int* skip, int nterm = 4) {
+        cudaStream_t st = stream;
+        CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
+        if (G) {
+            CUDA_CHECK(cudaMemsetAsync(e.gradFx.p, 0, 6 * (size_t) npad * 8, st));
+            k_dipole_field<real, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tile_ctx(), e.arrays(), mu, e.fieldFx.p,
+                                                                                     e.gradFx.p, skip);
+        } else {
+            k_dipole_field<real, false><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tile_ctx(), e.arrays(), mu,
+                                                                                      e.fieldFx.p, nullptr, skip);
+        }
+        if (usePme) {
+            k_frac_dipoles<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, mu, e.mfd.p, skip);
+            e.pme.template spread<4>(n, npad, box, e.mfd.p, skip, st);
+            e.pme.convolve(influence.p, skip, st);
+            if (nterm == 4)
+                e.pme.template gather<4>(n, npad, box, e.phiT.p, skip, st);
+            else if (nterm == 10)
+                e.pme.template gather<10>(n, npad, box, e.phiT.p, skip, st);
+            else
+                e.pme.template gather<35>(n, npad, box, e.phiT.p, skip, st);
+        }
+        k_dipole_field_total<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, self_coef(), e.fieldFx.p, e.gradFx.p,
+                                                                     usePme ? e.phiT.p : nullptr, nterm, mu, E, G, skip);
+        CUDA_CHECK(cudaGetLastError());
+    }
+
+    // Preconditioned CG on B y = b, B = I - S T S, in precision `real`; x accumulates in xreal.
+    // Convergence: 48.033324 sqrt(|S r|^2/n) < target.  Returns iterations used.
+    template <typename real, typename xreal>
+    int cg_solve(Engine<real>& e, const real* b, xreal* x, real* r, real* p, real* q, double target, int maxIter,
+                 double* finalMetric) {
+        cudaStream_t st = stream;
+        const int nb = nblk(npad, 256);
+        k_cg_start<real, xreal><<<nb, 256, 0, st>>>(npad, e.sroot.p, b, x, r, p, partial.p, nb);
+        k_reduce_partials<<<1, 1024, 0, st>>>(nb, 2, partial.p, red.p, nullptr);
+        k_cg_init_scalars<<<1, 1, 0, st>>>(sc.p, red.p, n, target, iter.p, done.p);
+        CUDA_CHECK(cudaGetLastError());
+        int it = 0;
+        for (it = 0; it < maxIter; ++it) {
+            // q = B p
+            k_apply_sroot<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, e.sroot.p, p, e.sp.p, nullptr, done.p);
+            dipole_field(e, e.sp.p, e.Etmp.p, (real*) nullptr, done.p, 4);
+            k_cg_finish_matvec<real><<<nb, 256, 0, st>>>(npad, e.sroot.p, p, e.Etmp.p, q, partial.p, done.p);
+            k_reduce_partials<<<1, 1024, 0, st>>>(nb, 1, partial.p, sc.p + 1, done.p);
+            k_cg_update<real, xreal><<<nb, 256, 0, st>>>(npad, e.sroot.p, sc.p, p, q, x, r, partial.p, nb, done.p);
+            k_reduce_partials<<<1, 1024, 0, st>>>(nb, 2, partial.p, red.p, done.p);
+            k_cg_scalars<<<1, 1, 0, st>>>(sc.p, red.p, n, target, iter.p, maxIter, done.p);
+            k_cg_direction<real><<<nblk(npad, 128), 128, 0, st>>>(npad, sc.p, r, p, done.p);
+            CUDA_CHECK(cudaGetLastError());
+            const int slot = it % (int) iterEvents.size();
+            CUDA_CHECK(cudaMemcpyAsync(hostDone + (slot % 256), done.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaEventRecord(iterEvents[slot], st));
+            // Check the previous iteration's flag while this one runs (one-iteration lag).
+            if (it >= 1) {
+                const int prev = (it - 1) % (int) iterEvents.size();
+                CUDA_CHECK(cudaEventSynchronize(iterEvents[prev]));
+                if (hostDone[prev % 256]) break;
+            }
+        }
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        int used = 0;
+        double h_sc[8];
+        CUDA_CHECK(cudaMemcpy(&used, iter.p, sizeof(int), cudaMemcpyDeviceToHost));
+        CUDA_CHECK(cudaMemcpy(h_sc, sc.p, 8 * sizeof(double), cudaMemcpyDeviceToHost));
+        if (finalMetric) *finalMetric = h_sc[6];
+        return used;
+    }
+
+    template <typename real>
+    void alpha_times(Engine<real>& e, const real* E, real* out) {
+        k_alpha_times<real><<<nblk(npad, 128), 128, 0, stream>>>(npad, e.alab.p, E, out);
+    }
+
+    // Induced dipoles into e.mu (sorted) for the configured polarisation type.
+    template <typename real>
+    void solve_dipoles(Engine<real>& e, real* ptMu, real* ptE, real* ptG) {
+        cudaStream_t st = stream;
+        const size_t n3 = 3 * (size_t) npad;
+        stats.solver_iterations = 0;
+        stats.refinement_steps = 0;
+        stats.solver_residual = 0.0;
+        if (set.polarization_type == MPID_DIRECT) {
+            CUDA_CHECK(cudaMemcpyAsync(e.mu.p, e.muD.p, n3 * sizeof(real), cudaMemcpyDeviceToDevice, st));
+            return;
+        }
+        if (set.polarization_type == MPID_EXTRAPOLATED) {
+            // mu_0 = alpha E_fixed; mu_(m+1) = alpha E[mu_m]; mu = sum_m cbar_m mu_m
+            // (MPIDReferenceForce.cpp:1125-1180).
+            const int nPT = set.n_extrap;
+            double cbar[8];
+            for (int i = 0; i < nPT; ++i) {
+                cbar[i] = 0.0;
+                for (int j = i; j < nPT; ++j) cbar[i] += set.extrap_coeffs[j];
+            }
+            CUDA_CHECK(cudaMemcpyAsync(ptMu, e.muD.p, n3 * sizeof(real), cudaMemcpyDeviceToDevice, st));
+            for (int m = 0; m + 1 < nPT; ++m) {
+                dipole_field(e, ptMu + m * n3, ptE + m * n3, ptG + m * 2 * n3, nullptr, 10);
+                alpha_times(e, ptE + m * n3, ptMu + (m + 1) * n3);
+            }
+            CUDA_CHECK(cudaMemsetAsync(e.mu.p, 0, n3 * sizeof(real), st));
+            for (int m = 0; m < nPT; ++m)
+                k_axpy<real><<<nblk((long long) n3, 256), 256, 0, st>>>((int) n3, real(cbar[m]), ptMu + m * n3, e.mu.p);
+            stats.solver_iterations = nPT - 1;
+            CUDA_CHECK(cudaGetLastError());
+            return;
+        }
+        throw Error(MPID_ERR_STATE, "mutual solve dispatched to the generic path");
+    }
+
+    void solve_mutual_double(Engine<double>& e) {
+        double metric = 0.0;
+        int it = cg_solve<double, double>(e, e.SE.p, y64.p, r64.p, p64.p, q64.p, set.mutual_eps, set.max_iter, &metric);
+        stats.solver_iterations = it;
+        stats.solver_residual = metric;
+        k_mu_from_y<double, double><<<nblk(npad, 128), 128, 0, stream>>>(npad, e.sroot.p, y64.p, e.mu.p);
+        if (!(metric < set.mutual_eps)) not_converged(it, metric);
+    }
+
+    // Mixed precision: FP32 CG inner solves, FP64 residual and accumulation of y.
+    void solve_mutual_mixed(Engine<float>& e, Engine<double>& d) {
+        cudaStream_t st = stream;
+        const int nb = nblk(npad, 256);
+        const size_t n3 = 3 * (size_t) npad;
+        // Efix in FP64 for the residual
+        CUDA_CHECK(cudaMemsetAsync(Efix64.p, 0, n3 * 8, st));
+        k_axpy_to_double<float><<<nblk((long long) n3, 256), 256, 0, st>>>((int) n3, e.Efix.p, Efix64.p);
+        CUDA_CHECK(cudaMemsetAsync(y64.p, 0, n3 * 8, st));
+        CUDA_CHECK(cudaMemcpyAsync(b32.p, e.SE.p, n3 * 4, cudaMemcpyDeviceToDevice, st));
+        int total = 0;
+        double metric = 1e300;
+        const double innerTarget = 0.25 * set.mutual_eps;
+        for (int outer = 0; outer < 6; ++outer) {
+            double innerMetric = 0.0;
+            const int it = cg_solve<float, float>(e, b32.p, x32.p, r32.p, p32.p, q32.p, innerTarget,
+                                                  std::max(1, set.max_iter - total), &innerMetric);
+            total += it;
+            k_axpy_to_double<float><<<nblk((long long) n3, 256), 256, 0, st>>>((int) n3, x32.p, y64.p);
+            // FP64 residual res = S (E + T S y) - y
+            k_mu_from_y<double, double><<<nblk(npad, 128), 128, 0, st>>>(npad, d.sroot.p, y64.p, d.mu.p);
+            dipole_field(d, d.mu.p, d.Etmp.p, (double*) nullptr, nullptr, 4);
+            k_refine_residual<<<nb, 256, 0, st>>>(npad, d.sroot.p, Efix64.p, d.Etmp.p, y64.p, res64.p, res32.p, partial.p);
+            k_reduce_partials<<<1, 1024, 0, st>>>(nb, 1, partial.p, red.p, nullptr);
+            double s2 = 0.0;
+            CUDA_CHECK(cudaMemcpyAsync(&s2, red.p, 8, cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            metric = 48.033324 * std::sqrt(s2 / n);
+            stats.refinement_steps = outer + 1;
+            if (metric < set.mutual_eps || total >= set.max_iter || !(metric == metric)) break;
+            CUDA_CHECK(cudaMemcpyAsync(b32.p, res32.p, n3 * 4, cudaMemcpyDeviceToDevice, st));
+        }
+        stats.solver_iterations = total;
+        stats.solver_residual = metric;
+        k_mu_from_y<double, float><<<nblk(npad, 128), 128, 0, st>>>(npad, d.sroot.p, y64.p, e.mu.p);
+        if (!(metric < set.mutual_eps)) not_converged(total, metric);
+    }
+
+    [[noreturn]] void not_converged(int it, double eps) {
+        std::ostringstream m;
+        m << "Induced dipoles did not converge:  iterations=" << it << " eps=" << eps;
+        throw Error(MPID_ERR_NOT_CONVERGED, m.str());
+    }
+
+    template <typename real>
+    void finish(Engine<real>& e, real* ptMu, real* ptE, real* ptG) {
+        cudaStream_t st = stream;
+        if (usePme) {
+            // reciprocal potential of the final induced dipoles (35 terms)
+            k_frac_dipoles<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, e.mu.p, e.mfd.p, nullptr);
+            e.pme.template spread<4>(n, npad, box, e.mfd.p, nullptr, st);
+            e.pme.convolve(influence.p, nullptr, st);
+            e.pme.template gather<35>(n, npad, box, e.phiD.p, nullptr, st);
+        }
+        CUDA_CHECK(cudaMemsetAsync(forceFx.p, 0, 3 * (size_t) npad * 8, st));
+        CUDA_CHECK(cudaMemsetAsync(torqueFx.p, 0, 3 * (size_t) npad * 8, st));
+        CUDA_CHECK(cudaMemsetAsync(energyFx.p, 0, 8, st));
+        const bool exact = (set.flags & MPID_FLAG_EXACT_ANISO_TORQUE) != 0;
+        const TileCtx tc = tile_ctx();
+        const AtomArrays<real> aa = e.arrays();
+        if (set.polarization_type == MPID_MUTUAL && !exact)
+            k_electrostatics<real, true, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
+                                                                                             torqueFx.p, energyFx.p);
+        else if (set.polarization_type == MPID_MUTUAL)
+            k_electrostatics<real, true, false><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
+                                                                                              torqueFx.p, energyFx.p);
+        else
+            k_electrostatics<real, false, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
+                                                                                              torqueFx.p, energyFx.p);
+        OptArgs opt{};
+        if (set.polarization_type == MPID_EXTRAPOLATED) {
+            opt.nPT = set.n_extrap;
+            for (int i = 0; i < opt.nPT; ++i) {
+                opt.cbar[i] = 0.0;
+                for (int j = i; j < opt.nPT; ++j) opt.cbar[i] += set.extrap_coeffs[j];
+            }
+            opt.mu = ptMu;
+            opt.E = ptE;
+            opt.G = ptG;
+        }
+        const int nb = nblk(npad, 256);
+        k_recip_self<real><<<nb, 256, 0, st>>>(n, npad, box, set.ewald_alpha, set.polarization_type,
+                                                usePme ? e.phiP.p : nullptr, e.phiD.p, e.mu.p, e.arrays(), opt, forceFx.p,
+                                                torqueFx.p, energyPartial.p);
+        k_reduce_partials<<<1, 1024, 0, st>>>(nb, 1, energyPartial.p, energyOut.p, nullptr);
+        k_torque_map<<<nblk(n, 128), 128, 0, st>>>(n, npad, pos.p, mol(), e.rank.p, torqueFx.p, forceFx.p);
+        CUDA_CHECK(cudaGetLastError());
+    }
+
+    template <typename real>
+    int* rank_of(Engine<real>& e) { return e.rank.p; }
+
+    // Full evaluation; d_pos / d_forces are device pointers.  Returns energy.
+    double evaluate_device(const double* d_pos, const double* hbox, double* d_forces, double* d_energy) {
+        if (!haveParams) throw Error(MPID_ERR_STATE, "mpid_set_multipoles must be called before evaluating");
+        CUDA_CHECK(cudaSetDevice(device));
+        cudaStream_t st = stream;
+        CUDA_CHECK(cudaEventRecord(evStart, st));
+        if (d_pos != pos.p) CUDA_CHECK(cudaMemcpyAsync(pos.p, d_pos, 3 * (size_t) n * 8, cudaMemcpyDeviceToDevice, st));
+        set_box(hbox);
+        neighbour_setup();
+        stats.num_tile_pairs = lastPairs;
+        if (mixed) {
+            Engine<float>& e = *ef;
+            prepare_engine(e);
+            if (ed) prepare_engine(*ed);
+            fixed_field(e);
+            if (set.polarization_type == MPID_MUTUAL)
+                solve_mutual_mixed(e, *ed);
+            else
+                solve_dipoles(e, ptMuF.p, ptEF.p, ptGF.p);
+            finish(e, ptMuF.p, ptEF.p, ptGF.p);
+            k_forces_out<<<nblk(n, 128), 128, 0, st>>>(n, npad, e.rank.p, forceFx.p, d_forces);
+        } else {
+            Engine<double>& e = *ed;
+            prepare_engine(e);
+            fixed_field(e);
+            if (set.polarization_type == MPID_MUTUAL)
+                solve_mutual_double(e);
+            else
+                solve_dipoles(e, ptMuD.p, ptED.p, ptGD.p);
+            finish(e, ptMuD.p, ptED.p, ptGD.p);
+            k_forces_out<<<nblk(n, 128), 128, 0, st>>>(n, npad, e.rank.p, forceFx.p, d_forces);
+        }
+        CUDA_CHECK(cudaGetLastError());
+        unsigned long long efx = 0;
+        double erecip = 0.0;
+        CUDA_CHECK(cudaMemcpyAsync(&efx, energyFx.p, 8, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaMemcpyAsync(&erecip, energyOut.p, 8, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaEventRecord(evStop, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        const double energy = (double) (long long) efx * kFixedInv + erecip;
+        if (d_energy) CUDA_CHECK(cudaMemcpyAsync(d_energy, &energy, 8, cudaMemcpyHostToDevice, st));
+        float ms = 0.f;
+        CUDA_CHECK(cudaEventElapsedTime(&ms, evStart, evStop));
+        stats.ms_total = ms;
+        evaluated = true;
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        return energy;
+    }
+
+    void get_dipoles(int which, double* host) {
+        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+        if (which < 0 || which > 2) throw Error(MPID_ERR_INVALID, "which must be 0, 1 or 2");
+        if (mixed)
+            k_dipoles_out<float><<<nblk(n, 128), 128, 0, stream>>>(n, npad, which, ef->rank.p, ef->mom.p, ef->mu.p, forcesOut.p);
+        else
+            k_dipoles_out<double><<<nblk(n, 128), 128, 0, stream>>>(n, npad, which, ed->rank.p, ed->mom.p, ed->mu.p, forcesOut.p);
+        CUDA_CHECK(cudaGetLastError());
+        CUDA_CHECK(cudaMemcpyAsync(host, forcesOut.p, 3 * (size_t) n * 8, cudaMemcpyDeviceToHost, stream));
+        CUDA_CHECK(cudaStreamSynchronize(stream));
+    }
+};
+
+}  // namespace mpid
+
+// ---------------------------------------------------------------------------
+// C ABI
+using mpid::Context;
+using mpid::Error;
+
+static thread_local std::string g_lastError;
+
+#define MPID_API_BEGIN try {
+#define MPID_API_END                                   \
+    }                                                  \
+    catch (const Error& e) {                           \
+        g_lastError = e.what();                        \
+        return e.code;                                 \
+    }                                                  \
+    catch (const std::exception& e) {                  \
+        g_lastError = e.what();                        \
+        return MPID_ERR_CUDA;                          \
+    }
+
+struct mpid_context {
+    Context ctx;
+};
+
+extern "C" {
+
+void mpid_default_settings(mpid_settings* s, int num_atoms) {
+    std::memset(s, 0, sizeof(*s));
+    s->num_atoms = num_atoms;
+    s->nonbonded_method = MPID_NO_CUTOFF;
+    s->polarization_type = MPID_EXTRAPOLATED;
+    s->cutoff = 1.0;
+    s->pme_order = 6;
+    s->mutual_eps = 1.0e-5;
+    s->max_iter = 60;
+    s->n_extrap = 4;
+    s->extrap_coeffs[0] = -0.154;
+    s->extrap_coeffs[1] = 0.017;
+    s->extrap_coeffs[2] = 0.658;
+    s->extrap_coeffs[3] = 0.474;
+    s->default_thole = 5.0;
+    s->scale14 = 1.0;
+    s->precision = MPID_PRECISION_MIXED;
+}
+
+int mpid_create(const mpid_settings* settings, int device, mpid_context** out) {
+    MPID_API_BEGIN
+    if (!settings || !out) throw Error(MPID_ERR_INVALID, "null argument");
+    std::unique_ptr<mpid_context> c(new mpid_context());
+    c->ctx.create(*settings, device);
+    *out = c.release();
+    return MPID_OK;
+    MPID_API_END
+}
+
+void mpid_destroy(mpid_context* ctx) { delete ctx; }
+
+int mpid_set_multipoles(mpid_context* ctx, const double* charge, const double* dipole, const double* quadrupole,
+                        const double* octopole, const int* axis_type, const int* atom_z, const int* atom_x,
+                        const int* atom_y, const double* thole, const double* polarity) {
+    MPID_API_BEGIN
+    if (!ctx || !charge || !dipole || !quadrupole || !octopole || !axis_type || !atom_z || !atom_x || !atom_y || !thole ||
+        !polarity)
+        throw Error(MPID_ERR_INVALID, "null argument");
+    ctx->ctx.set_multipoles(charge, dipole, quadrupole, octopole, axis_type, atom_z, atom_x, atom_y, thole, polarity);
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_set_covalent(mpid_context* ctx, const int* offsets, const int* index) {
+    MPID_API_BEGIN
+    if (!ctx || !offsets) throw Error(MPID_ERR_INVALID, "null argument");
+    ctx->ctx.set_covalent(offsets, index);
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_evaluate(mpid_context* ctx, const double* positions, const double* box, double* forces, double* energy) {
+    MPID_API_BEGIN
+    if (!ctx || !positions || !box || !forces) throw Error(MPID_ERR_INVALID, "null argument");
+    Context& c = ctx->ctx;
+    CUDA_CHECK(cudaSetDevice(c.device));
+    const size_t n3 = 3 * (size_t) c.n;
+    CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions, n3 * 8, cudaMemcpyHostToDevice, c.stream));
+    CUDA_CHECK(cudaMemcpyAsync(c.forcesOut.p, forces, n3 * 8, cudaMemcpyHostToDevice, c.stream));
+    double e = c.evaluate_device(c.pos.p, box, c.forcesOut.p, nullptr);
+    CUDA_CHECK(cudaMemcpyAsync(forces, c.forcesOut.p, n3 * 8, cudaMemcpyDeviceToHost, c.stream));
+    CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    if (energy) *energy = e;
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_evaluate_device(mpid_context* ctx, const double* d_positions, const double* box, double* d_forces,
+                         double* d_energy, void* stream) {
+    MPID_API_BEGIN
+    if (!ctx || !d_positions || !box || !d_forces) throw Error(MPID_ERR_INVALID, "null argument");
+    ctx->ctx.stream = (cudaStream_t) stream;
+    ctx->ctx.evaluate_device(d_positions, box, d_forces, d_energy);
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_get_dipoles(mpid_context* ctx, int which, double* out) {
+    MPID_API_BEGIN
+    if (!ctx || !out) throw Error(MPID_ERR_INVALID, "null argument");
+    ctx->ctx.get_dipoles(which, out);
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_get_pme_parameters(mpid_context* ctx, double* alpha, int* nx, int* ny, int* nz) {
+    MPID_API_BEGIN
+    if (!ctx) throw Error(MPID_ERR_INVALID, "null argument");
+    if (ctx->ctx.set.nonbonded_method != MPID_PME)
+        throw Error(MPID_ERR_INVALID, "getPMEParametersInContext: MPIDForce is not using PME");
+    if (alpha) *alpha = ctx->ctx.set.ewald_alpha;
+    if (nx) *nx = ctx->ctx.set.grid[0];
+    if (ny) *ny = ctx->ctx.set.grid[1];
+    if (nz) *nz = ctx->ctx.set.grid[2];
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_get_stats(mpid_context* ctx, mpid_stats* out) {
+    MPID_API_BEGIN
+    if (!ctx || !out) throw Error(MPID_ERR_INVALID, "null argument");
+    *out = ctx->ctx.stats;
+    return MPID_OK;
+    MPID_API_END
+}
+
+const char* mpid_last_error(void) { return g_lastError.c_str(); }
+
+}  // extern "C"

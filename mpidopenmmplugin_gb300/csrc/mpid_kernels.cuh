@@ -1,0 +1,1224 @@
+// CUDA kernels of the MPIDForce evaluation (sm_103a).  Templated on the arithmetic
+// type: float for the mixed-precision path, double for the FP64 path.
+//
+// Layout in HBM (all per-atom arrays in spatially sorted order, SoA, padded to a
+// multiple of 32 so that each 32-atom tile is one warp):
+//   off[3][npad]       position minus its tile centre (real)
+//   mom[20][npad]      lab-frame q, dipole[3], Q6[6], O10[10] (real)
+//   alab[6][npad]      lab-frame polarisability, sroot[6][npad] its square root
+//   prm[npad]          float4 (thole, damp, aniso flag, unused); orig[npad] original index
+// Forces, torques and fields accumulate as 64-bit fixed point with 2^32 units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "mpid_math.cuh"
+
+namespace mpid {
+
+constexpr double kFixedScale = 4294967296.0;       // 2^32
+constexpr double kFixedInv = 1.0 / 4294967296.0;
+constexpr double kElectric = 138.935455846;        // MPIDReferenceForce.cpp:38
+
+__device__ __forceinline__ void fx_add(unsigned long long* p, float v) {
+    atomicAdd(p, (unsigned long long) __float2ll_rn(v * 4294967296.0f));
+}
+__device__ __forceinline__ void fx_add(unsigned long long* p, double v) {
+    atomicAdd(p, (unsigned long long) __double2ll_rn(v * kFixedScale));
+}
+__device__ __forceinline__ double fx_get(const unsigned long long* p, int i) {
+    return (double) (long long) p[i] * kFixedInv;
+}
+
+struct BoxDev {
+    double L[3], invL[3];    // rectangular box edge lengths
+    double A[3][3];          // Cartesian -> fractional grid, frac_j = sum_i A[j][i] x_i
+    int grid[3];
+};
+
+// ---------------------------------------------------------------------------
+// Spatial sort: wrap into the box and key by the Morton code of a 0.25 nm voxel.
+__device__ __forceinline__ unsigned int spread_bits10(unsigned int v) {
+    v &= 0x3ff;
+    v = (v | (v << 16)) & 0x030000FF;
+    v = (v | (v << 8)) & 0x0300F00F;
+    v = (v | (v << 4)) & 0x030C30C3;
+    v = (v | (v << 2)) & 0x09249249;
+    return v;
+}
+
+__global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, double voxel,
+                            unsigned long long* __restrict__ keys, double* __restrict__ wpos) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned int c[3];
+    for (int k = 0; k < 3; ++k) {
+        double x = pos[3 * i + k];
+        x -= box.L[k] * floor(x * box.invL[k]);
+        if (x >= box.L[k]) x -= box.L[k];
+        wpos[3 * i + k] = x;
+        int nv = (int) (box.L[k] / voxel) + 1;
+        int v = (int) (x / voxel);
+        if (v >= nv) v = nv - 1;
+        c[k] = (unsigned int) v;
+    }
+    unsigned int m = spread_bits10(c[0]) | (spread_bits10(c[1]) << 1) | (spread_bits10(c[2]) << 2);
+    keys[i] = ((unsigned long long) m << 32) | (unsigned int) i;
+}
+
+// Tile centres and half extents from the wrapped positions of the sorted atoms.
+__global__ void k_tile_bounds(int n, int ntiles, const unsigned long long* __restrict__ keys,
+                              const double* __restrict__ wpos, double* __restrict__ center,
+                              double* __restrict__ half) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int s = t * 32; s < min(n, t * 32 + 32); ++s) {
+        int i = (int) (keys[s] & 0xffffffffu);
+        for (int k = 0; k < 3; ++k) {
+            double x = wpos[3 * i + k];
+            lo[k] = fmin(lo[k], x);
+            hi[k] = fmax(hi[k], x);
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        center[3 * t + k] = 0.5 * (lo[k] + hi[k]);
+        half[3 * t + k] = 0.5 * (hi[k] - lo[k]);
+    }
+}
+
+// Candidate tile pairs (I <= J) whose bounding boxes come within the cutoff.  A
+// dimension whose extents plus the cutoff reach half the box is treated as always
+// overlapping, so minimum imaging of the centres can never drop a pair.
+__global__ void k_tile_pairs(int ntiles, const double* __restrict__ center, const double* __restrict__ half,
+                             BoxDev box, double cutoff, int usePbc, int2* __restrict__ pairs, int* __restrict__ count,
+                             int capacity) {
+    long long idx = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    long long total = (long long) ntiles * (ntiles + 1) / 2;
+    if (idx >= total) return;
+    // invert idx -> (I, J) with I <= J over rows of decreasing length
+    long long I = (long long) ((2.0 * ntiles + 1.0 - sqrt((2.0 * ntiles + 1.0) * (2.0 * ntiles + 1.0) - 8.0 * idx)) / 2.0);
+    while (I > 0 && I * (2LL * ntiles - I + 1) / 2 > idx) --I;
+    while ((I + 1) * (2LL * ntiles - I) / 2 <= idx) ++I;
+    long long J = idx - I * (2LL * ntiles - I + 1) / 2 + I;
+    double d2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        double dc = center[3 * J + k] - center[3 * I + k];
+        double ext = half[3 * I + k] + half[3 * J + k];
+        if (usePbc) {
+            if (ext + cutoff >= 0.5 * box.L[k]) continue;
+            dc -= box.L[k] * rint(dc * box.invL[k]);
+        }
+        double g = fabs(dc) - ext;
+        if (g > 0) d2 += g * g;
+    }
+    if (d2 < cutoff * cutoff) {
+        int slot = atomicAdd(count, 1);
+        if (slot < capacity) pairs[slot] = make_int2((int) I, (int) J);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-atom parameters in sorted order: lab frame, polarisability and its square root.
+template <typename real>
+struct AtomArrays {
+    int n, npad;
+    real* off;       // [3][npad]
+    real* mom;       // [20][npad]
+    real* alab;      // [6][npad]
+    real* sroot;     // [6][npad]
+    float4* prm;     // thole, damp, aniso, 0
+    int* orig;       // [npad], -1 for padding
+    int* rank;       // [n]  sorted slot of each original atom
+};
+
+struct MolArrays {  // original order, FP64, as given through the API
+    const double* charge;
+    const double* dipole;
+    const double* quad;
+    const double* oct;
+    const double* thole;
+    const double* pol;
+    const int* axis;
+    const int* az;
+    const int* ax;
+    const int* ay;
+};
+
+template <typename real>
+__global__ void k_gather_atoms(int n, int npad, const unsigned long long* __restrict__ keys, MolArrays mol,
+                               const double* __restrict__ pos, const double* __restrict__ wpos,
+                               const double* __restrict__ center, AtomArrays<real> at) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    if (s >= n) {
+        for (int k = 0; k < 3; ++k) at.off[k * npad + s] = real(0);
+        for (int k = 0; k < 20; ++k) at.mom[k * npad + s] = real(0);
+        for (int k = 0; k < 6; ++k) { at.alab[k * npad + s] = real(0); at.sroot[k * npad + s] = real(0); }
+        at.prm[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        at.orig[s] = -1;
+        return;
+    }
+    const int i = (int) (keys[s] & 0xffffffffu);
+    at.orig[s] = i;
+    at.rank[i] = s;
+    const int t = s >> 5;
+    for (int k = 0; k < 3; ++k) at.off[k * npad + s] = real(wpos[3 * i + k] - center[3 * t + k]);
+    MolParams<double> p;
+    p.q = mol.charge[i];
+    for (int k = 0; k < 3; ++k) p.d[k] = mol.dipole[3 * i + k];
+    for (int k = 0; k < 6; ++k) p.Q[k] = mol.quad[6 * i + k];
+    for (int k = 0; k < 10; ++k) p.O[k] = mol.oct[10 * i + k];
+    for (int k = 0; k < 3; ++k) p.pol[k] = mol.pol[3 * i + k];
+    const int ax = mol.axis[i], iz = mol.az[i], ix = mol.ax[i], iy = mol.ay[i];
+    const double* pI = pos + 3 * i;
+    const double* pZ = (iz >= 0 && iz < n) ? pos + 3 * iz : pI;
+    const double* pX = (ix >= 0 && ix < n) ? pos + 3 * ix : pI;
+    const double* pY = (iy >= 0 && iy < n) ? pos + 3 * iy : pI;
+    double R[3][3];
+    local_frame<double>(ax, pI, pZ, pX, pY, R);
+    const bool flip = chiral_flip<double>(ax, iy >= 0, pI, pZ, pX, pY);
+    LabMoments<double> L;
+    double al[6];
+    rotate_to_lab(p, R, flip, L, al);
+    at.mom[s] = real(L.q);
+    for (int k = 0; k < 3; ++k) at.mom[(1 + k) * npad + s] = real(L.d[k]);
+    for (int k = 0; k < 6; ++k) at.mom[(4 + k) * npad + s] = real(L.Q[k]);
+    for (int k = 0; k < 10; ++k) at.mom[(10 + k) * npad + s] = real(L.O[k]);
+    for (int k = 0; k < 6; ++k) at.alab[k * npad + s] = real(al[k]);
+    for (int a = 0; a < 3; ++a)
+        for (int b = a; b < 3; ++b) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k) acc += R[k][a] * R[k][b] * sqrt(fmax(p.pol[k], 0.0));
+            at.sroot[q6(a, b) * npad + s] = real(acc);
+        }
+    const bool aniso = p.pol[0] != p.pol[1] || p.pol[0] != p.pol[2];
+    const double damp = pow((p.pol[0] + p.pol[1] + p.pol[2]) / 3.0, 1.0 / 6.0);
+    at.prm[s] = make_float4((float) mol.thole[i], (float) damp, aniso ? 1.f : 0.f, 0.f);
+}
+
+template <typename real>
+__device__ __forceinline__ void load_moments(const real* mom, int npad, int s, LabMoments<real>& m) {
+    m.q = mom[s];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) m.d[k] = mom[(1 + k) * npad + s];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) m.Q[k] = mom[(4 + k) * npad + s];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) m.O[k] = mom[(10 + k) * npad + s];
+}
+
+// Covalent scale of an (original-index) pair from the symmetric partner list.
+__device__ __forceinline__ float pair_scale(int oi, int oj, const int* __restrict__ covOff,
+                                            const int* __restrict__ covJ, const float* __restrict__ covS) {
+    const int b = covOff[oi], e = covOff[oi + 1];
+    for (int k = b; k < e; ++k)
+        if (covJ[k] == oj) return covS[k];
+    return 1.0f;
+}
+
+struct TileCtx {
+    const int2* pairs;
+    const int* npairs;
+    const double* center;
+    BoxDev box;
+    int usePbc;
+    double cutoff;
+    double ewald;
+    double defaultThole;
+    const int* covOff;
+    const int* covJ;
+    const float* covS;
+};
+
+// Displacement R_j - R_i of two sorted atoms from the tile-centre shift and offsets.
+template <typename real>
+__device__ __forceinline__ void tile_shift(const TileCtx& c, int I, int J, real* sh) {
+    for (int k = 0; k < 3; ++k) {
+        double d = c.center[3 * J + k] - c.center[3 * I + k];
+        if (c.usePbc) d -= c.box.L[k] * rint(d * c.box.invL[k]);
+        sh[k] = real(d);
+    }
+}
+
+template <typename real>
+__device__ __forceinline__ void pair_delta(const TileCtx& c, const real* sh, const real* oi, const real* oj, real* d) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        real x = sh[k] + (oj[k] - oi[k]);
+        if (c.usePbc) x -= real(c.box.L[k]) * rint(x * real(c.box.invL[k]));
+        d[k] = x;
+    }
+}
+
+constexpr int kWarpsPerBlock = 4;
+
+// ---------------------------------------------------------------------------
+// Real-space permanent field at every atom (kernel K_i with the pair's covalent scale):
+// the PME real-space part of MPIDReferenceForce.cpp:2812-2920 / :911-934.
+template <typename real>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_fixed_field(TileCtx c, AtomArrays<real> at, unsigned long long* __restrict__ field) {
+    __shared__ real shOff[kWarpsPerBlock][3][32];
+    __shared__ real shMom[kWarpsPerBlock][20][32];
+    __shared__ float4 shPrm[kWarpsPerBlock][32];
+    __shared__ int shOrig[kWarpsPerBlock][32];
+    __shared__ real shAcc[kWarpsPerBlock][3][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int np = *c.npairs;
+    const int npad = at.npad;
+    for (int p = blockIdx.x * kWarpsPerBlock + w; p < np; p += gridDim.x * kWarpsPerBlock) {
+        const int2 IJ = c.pairs[p];
+        const int si = IJ.x * 32 + lane, sj = IJ.y * 32 + lane;
+        // i in registers
+        real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+        LabMoments<real> mi;
+        load_moments(at.mom, npad, si, mi);
+        const float4 pi = at.prm[si];
+        const int origI = at.orig[si];
+        // j in shared memory
+        for (int k = 0; k < 3; ++k) shOff[w][k][lane] = at.off[k * npad + sj];
+        for (int k = 0; k < 20; ++k) shMom[w][k][lane] = at.mom[k * npad + sj];
+        shPrm[w][lane] = at.prm[sj];
+        shOrig[w][lane] = at.orig[sj];
+        for (int k = 0; k < 3; ++k) shAcc[w][k][lane] = real(0);
+        __syncwarp();
+        real sh[3];
+        tile_shift(c, IJ.x, IJ.y, sh);
+        real Ei[3] = {real(0), real(0), real(0)};
+        const bool diag = IJ.x == IJ.y;
+        const real rc2 = real(c.cutoff * c.cutoff);
+        for (int k = 0; k < 32; ++k) {
+            const int jl = (lane + k) & 31;
+            const int origJ = shOrig[w][jl];
+            if (origI < 0 || origJ < 0 || (diag && jl <= lane)) continue;
+            real oj[3] = {shOff[w][0][jl], shOff[w][1][jl], shOff[w][2][jl]};
+            real d[3];
+            pair_delta(c, sh, oi, oj, d);
+            const real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (c.usePbc && r2 > rc2) continue;
+            const real r = sqrt(r2);
+            const float scale = pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
+            const float4 pj = shPrm[w][jl];
+            const real a = scale == 0.0f ? real(pi.x + pj.x) : real(c.defaultThole);
+            PairRadial<real, 0, 4, 0> pr;
+            pair_radial<real, -1, 4, -1>(r, real(c.ewald), real(scale), a, real(pi.y) * real(pj.y), pr);
+            LabMoments<real> mj;
+            mj.q = shMom[w][0][jl];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) mj.d[q] = shMom[w][1 + q][jl];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) mj.Q[q] = shMom[w][4 + q][jl];
+#pragma unroll
+            for (int q = 0; q < 10; ++q) mj.O[q] = shMom[w][10 + q][jl];
+            real sI[3] = {-d[0], -d[1], -d[2]};
+            real e[3];
+            multipole_field(mj, sI, pr.bI, e);
+            Ei[0] += e[0]; Ei[1] += e[1]; Ei[2] += e[2];
+            multipole_field(mi, d, pr.bI, e);
+            shAcc[w][0][jl] += e[0];
+            shAcc[w][1][jl] += e[1];
+            shAcc[w][2][jl] += e[2];
+        }
+        __syncwarp();
+        if (origI >= 0)
+            for (int k = 0; k < 3; ++k) fx_add(field + k * npad + si, Ei[k]);
+        if (shOrig[w][lane] >= 0)
+            for (int k = 0; k < 3; ++k) fx_add(field + k * npad + sj, shAcc[w][k][lane]);
+        __syncwarp();
+    }
+}
+
+// Real-space field of point dipoles (kernel K_u), optionally with its gradient:
+// MPIDReferenceForce.cpp:4161-4281.  mu is [3][npad] in sorted order.
+template <typename real, bool GRAD>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_dipole_field(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ field,
+               unsigned long long* __restrict__ grad, const int* __restrict__ skip) {
+    constexpr int NACC = GRAD ? 9 : 3;
+    __shared__ real shOff[kWarpsPerBlock][3][32];
+    __shared__ real shMu[kWarpsPerBlock][3][32];
+    __shared__ float4 shPrm[kWarpsPerBlock][32];
+    __shared__ int shOrig[kWarpsPerBlock][32];
+    __shared__ real shAcc[kWarpsPerBlock][NACC][32];
+    if (skip && *skip) return;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int np = *c.npairs;
+    const int npad = at.npad;
+    for (int p = blockIdx.x * kWarpsPerBlock + w; p < np; p += gridDim.x * kWarpsPerBlock) {
+        const int2 IJ = c.pairs[p];
+        const int si = IJ.x * 32 + lane, sj = IJ.y * 32 + lane;
+        real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+        real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
+        const float4 pi = at.prm[si];
+        const int origI = at.orig[si];
+        for (int k = 0; k < 3; ++k) {
+            shOff[w][k][lane] = at.off[k * npad + sj];
+            shMu[w][k][lane] = mu[k * npad + sj];
+        }
+        shPrm[w][lane] = at.prm[sj];
+        shOrig[w][lane] = at.orig[sj];
+        for (int k = 0; k < NACC; ++k) shAcc[w][k][lane] = real(0);
+        __syncwarp();
+        real sh[3];
+        tile_shift(c, IJ.x, IJ.y, sh);
+        real acc[NACC];
+#pragma unroll
+        for (int k = 0; k < NACC; ++k) acc[k] = real(0);
+        const bool diag = IJ.x == IJ.y;
+        const real rc2 = real(c.cutoff * c.cutoff);
+        for (int k = 0; k < 32; ++k) {
+            const int jl = (lane + k) & 31;
+            const int origJ = shOrig[w][jl];
+            if (origI < 0 || origJ < 0 || (diag && jl <= lane)) continue;
+            real oj[3] = {shOff[w][0][jl], shOff[w][1][jl], shOff[w][2][jl]};
+            real d[3];
+            pair_delta(c, sh, oi, oj, d);
+            const real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (c.usePbc && r2 > rc2) continue;
+            const real r = sqrt(r2);
+            const float scale = pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
+            const float4 pj = shPrm[w][jl];
+            const real a = scale == 0.0f ? real(pi.x + pj.x) : real(c.defaultThole);
+            PairRadial<real, 0, 0, GRAD ? 3 : 2> pr;
+            pair_radial<real, -1, -1, GRAD ? 3 : 2>(r, real(c.ewald), real(1), a, real(pi.y) * real(pj.y), pr);
+            real b[4] = {real(0), pr.bU[1], pr.bU[2], GRAD ? pr.bU[GRAD ? 3 : 2] : real(0)};
+            real uj[3] = {shMu[w][0][jl], shMu[w][1][jl], shMu[w][2][jl]};
+            real sI[3] = {-d[0], -d[1], -d[2]};
+            real e[3], g[6];
+            dipole_field<real, GRAD>(uj, sI, b, e, g);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) acc[q] += e[q];
+            if (GRAD)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) acc[3 + q] += g[q];
+            dipole_field<real, GRAD>(ui, d, b, e, g);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) shAcc[w][q][jl] += e[q];
+            if (GRAD)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) shAcc[w][3 + q][jl] += g[q];
+        }
+        __syncwarp();
+        if (origI >= 0) {
+            for (int k = 0; k < 3; ++k) fx_add(field + k * npad + si, acc[k]);
+            if (GRAD)
+                for (int k = 0; k < 6; ++k) fx_add(grad + k * npad + si, acc[3 + k]);
+        }
+        if (shOrig[w][lane] >= 0) {
+            for (int k = 0; k < 3; ++k) fx_add(field + k * npad + sj, shAcc[w][k][lane]);
+            if (GRAD)
+                for (int k = 0; k < 6; ++k) fx_add(grad + k * npad + sj, shAcc[w][3 + k][lane]);
+        }
+        __syncwarp();
+    }
+}
+
+// Real-space energy, forces and torques (MPIDReferenceForce.cpp:4335-4920).
+// out: force[3][npad], torque[3][npad] fixed point; energy: fixed point scalar.
+template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_electrostatics(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ force,
+                 unsigned long long* __restrict__ torque, unsigned long long* __restrict__ energy) {
+    __shared__ real shOff[kWarpsPerBlock][3][32];
+    __shared__ real shMom[kWarpsPerBlock][20][32];
+    __shared__ real shMu[kWarpsPerBlock][3][32];
+    __shared__ float4 shPrm[kWarpsPerBlock][32];
+    __shared__ int shOrig[kWarpsPerBlock][32];
+    __shared__ real shAcc[kWarpsPerBlock][6][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int np = *c.npairs;
+    const int npad = at.npad;
+    double eLane = 0.0;
+    for (int p = blockIdx.x * kWarpsPerBlock + w; p < np; p += gridDim.x * kWarpsPerBlock) {
+        const int2 IJ = c.pairs[p];
+        const int si = IJ.x * 32 + lane, sj = IJ.y * 32 + lane;
+        real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+        real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
+        LabMoments<real> mi;
+        load_moments(at.mom, npad, si, mi);
+        const float4 pi = at.prm[si];
+        const int origI = at.orig[si];
+        for (int k = 0; k < 3; ++k) {
+            shOff[w][k][lane] = at.off[k * npad + sj];
+            shMu[w][k][lane] = mu[k * npad + sj];
+        }
+        for (int k = 0; k < 20; ++k) shMom[w][k][lane] = at.mom[k * npad + sj];
+        shPrm[w][lane] = at.prm[sj];
+        shOrig[w][lane] = at.orig[sj];
+        for (int k = 0; k < 6; ++k) shAcc[w][k][lane] = real(0);
+        __syncwarp();
+        real sh[3];
+        tile_shift(c, IJ.x, IJ.y, sh);
+        real accF[3] = {real(0), real(0), real(0)}, accT[3] = {real(0), real(0), real(0)};
+        const bool diag = IJ.x == IJ.y;
+        const real rc2 = real(c.cutoff * c.cutoff);
+        for (int k = 0; k < 32; ++k) {
+            const int jl = (lane + k) & 31;
+            const int origJ = shOrig[w][jl];
+            if (origI < 0 || origJ < 0 || (diag && jl <= lane)) continue;
+            real oj[3] = {shOff[w][0][jl], shOff[w][1][jl], shOff[w][2][jl]};
+            real d[3];
+            pair_delta(c, sh, oi, oj, d);
+            const real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (c.usePbc && r2 > rc2) continue;
+            const real r = sqrt(r2);
+            const float scale = pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
+            const float4 pj = shPrm[w][jl];
+            const real a = scale == 0.0f ? real(pi.x + pj.x) : real(c.defaultThole);
+            PairRadial<real, 7, 5, MUTUAL ? 3 : 0> pr;
+            pair_radial<real, 7, 5, MUTUAL ? 3 : -1>(r, real(c.ewald), real(scale), a, real(pi.y) * real(pj.y), pr);
+            LabMoments<real> mj;
+            mj.q = shMom[w][0][jl];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) mj.d[q] = shMom[w][1 + q][jl];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) mj.Q[q] = shMom[w][4 + q][jl];
+#pragma unroll
+            for (int q = 0; q < 10; ++q) mj.O[q] = shMom[w][10 + q][jl];
+            real uj[3] = {shMu[w][0][jl], shMu[w][1][jl], shMu[w][2][jl]};
+            PairOut<real> po;
+            qi_pair<real, MUTUAL, REF_ANISO_TORQUE>(d, r, mi, mj, ui, uj, pi.z != 0.f, pj.z != 0.f, pr.bP, pr.bI, pr.bU, po);
+            eLane += (double) po.energy;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                accF[q] -= po.fJ[q];
+                accT[q] += po.tI[q];
+                shAcc[w][q][jl] += po.fJ[q];
+                shAcc[w][3 + q][jl] += po.tJ[q];
+            }
+        }
+        __syncwarp();
+        const real E = real(kElectric);
+        if (origI >= 0)
+            for (int k = 0; k < 3; ++k) {
+                fx_add(force + k * npad + si, E * accF[k]);
+                fx_add(torque + k * npad + si, E * accT[k]);
+            }
+        if (shOrig[w][lane] >= 0)
+            for (int k = 0; k < 3; ++k) {
+                fx_add(force + k * npad + sj, E * shAcc[w][k][lane]);
+                fx_add(torque + k * npad + sj, E * shAcc[w][3 + k][lane]);
+            }
+        __syncwarp();
+    }
+    // warp-reduce the energy in FP64 and add once per warp in fixed point
+    for (int o = 16; o > 0; o >>= 1) eLane += __shfl_down_sync(0xffffffffu, eLane, o);
+    if (lane == 0 && eLane != 0.0) atomicAdd(energy, (unsigned long long) __double2ll_rn(eLane * kElectric * kFixedScale));
+}
+
+// ---------------------------------------------------------------------------
+// PME.  B-spline coefficients and weighted fractional multipoles per sorted atom.
+// theta layout: [3 dims][5 derivs][ORDER][npad]; igrid [3][npad].
+template <typename real, int ORDER>
+__global__ void k_bsplines(int npad, int n, const unsigned long long* __restrict__ keys, const double* __restrict__ wpos,
+                           BoxDev box, real* __restrict__ theta, int* __restrict__ igrid) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    if (s >= n) {
+        for (int d = 0; d < 3; ++d) {
+            igrid[d * npad + s] = 0;
+            for (int k = 0; k < 5 * ORDER; ++k) theta[(d * 5 * ORDER + k) * npad + s] = real(0);
+        }
+        return;
+    }
+    const int i = (int) (keys[s] & 0xffffffffu);
+    for (int d = 0; d < 3; ++d) {
+        // Fractional coordinate with the grid origin of MPIDReferenceForce.cpp:3058-3060:
+        // the minimum-image coordinate w in [-1/2, 1/2) maps to n (w + 1/2).
+        double w = wpos[3 * i + d] * box.invL[d] + 0.5;
+        w -= floor(w);
+        double fr = box.grid[d] * w;
+        int ifr = (int) floor(fr);
+        if (ifr >= box.grid[d]) ifr -= box.grid[d];
+        const real ww = real(fr - floor(fr));
+        int ig = ifr - ORDER + 1;
+        if (ig < 0) ig += box.grid[d];
+        igrid[d * npad + s] = ig;
+        real th[5][ORDER];
+        bspline_derivs<real, ORDER>(ww, th);
+        for (int k = 0; k < 5; ++k)
+            for (int m = 0; m < ORDER; ++m) theta[((d * 5 + k) * ORDER + m) * npad + s] = th[k][m];
+    }
+}
+
+template <typename real>
+__global__ void k_frac_multipoles(int npad, BoxDev box, const real* __restrict__ mom, real* __restrict__ mf) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    LabMoments<real> m;
+    load_moments(mom, npad, s, m);
+    real A[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) A[a][b] = real(box.A[a][b]);
+    real f[20];
+    frac_multipole(m, A, f);
+    for (int k = 0; k < 20; ++k) mf[k * npad + s] = f[k];
+}
+
+template <typename real> struct GridAcc;
+template <> struct GridAcc<float> {
+    typedef unsigned long long type;
+    static __device__ __forceinline__ void add(type* g, size_t idx, float v) { fx_add(g + idx, v); }
+};
+template <> struct GridAcc<double> {
+    typedef double type;
+    static __device__ __forceinline__ void add(type* g, size_t idx, double v) { atomicAdd(g + idx, v); }
+};
+
+// Spread NCOMP weighted fractional components (20 = full multipole, 4 = charge +
+// dipole) on the grid: one thread per (atom, x, y) stencil column.
+template <typename real, int ORDER, int NCOMP>
+__global__ void k_spread(int n, int npad, BoxDev box, const real* __restrict__ mf, const real* __restrict__ theta,
+                         const int* __restrict__ igrid, typename GridAcc<real>::type* __restrict__ grid,
+                         const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    const long long tid = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (long long) n * ORDER * ORDER) return;
+    const int s = (int) (tid / (ORDER * ORDER));
+    const int ix = (int) (tid % (ORDER * ORDER)) / ORDER, iy = (int) (tid % ORDER);
+    const int nx = box.grid[0], ny = box.grid[1], nz = box.grid[2];
+    auto TH = [&](int d, int k, int m) { return theta[((d * 5 + k) * ORDER + m) * npad + s]; };
+    // z polynomial coefficients c_v = sum over components with z-order v
+    real cv[4] = {real(0), real(0), real(0), real(0)};
+#pragma unroll
+    for (int c = 0; c < NCOMP; ++c) {
+        int t, u, v;
+        hermite_tuv(c, t, u, v);
+        cv[v] += mf[c * npad + s] * TH(0, t, ix) * TH(1, u, iy);
+    }
+    int gx = igrid[s] + ix;
+    if (gx >= nx) gx -= nx;
+    int gy = igrid[npad + s] + iy;
+    if (gy >= ny) gy -= ny;
+    const int gz0 = igrid[2 * npad + s];
+    const size_t base = ((size_t) gx * ny + gy) * nz;
+#pragma unroll
+    for (int iz = 0; iz < ORDER; ++iz) {
+        int gz = gz0 + iz;
+        if (gz >= nz) gz -= nz;
+        real v = cv[0] * TH(2, 0, iz);
+        if (NCOMP > 1) v += cv[1] * TH(2, 1, iz);
+        if (NCOMP > 4) v += cv[2] * TH(2, 2, iz) + cv[3] * TH(2, 3, iz);
+        GridAcc<real>::add(grid, base + gz, v);
+    }
+}
+
+// Fixed-point (or FP64) accumulation grid -> FFT input, clearing the accumulator.
+template <typename real>
+__global__ void k_grid_finish(size_t total, typename GridAcc<real>::type* __restrict__ acc, real* __restrict__ out,
+                              const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    for (size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t) gridDim.x * blockDim.x) {
+        if constexpr (sizeof(real) == 4) {
+            out[i] = (real) ((double) (long long) acc[i] * kFixedInv);
+        } else {
+            out[i] = (real) acc[i];
+        }
+        acc[i] = 0;
+    }
+}
+
+// Reciprocal influence function on the half-complex grid (kx, ky, kz <= nz/2),
+// MPIDReferenceForce.cpp:3329-3366: exp(-pi^2 m^2/alpha^2)/(pi V m^2 B(m)), 0 at m = 0.
+__global__ void k_influence(BoxDev box, double alpha, const double* __restrict__ modx, const double* __restrict__ mody,
+                            const double* __restrict__ modz, double recip00, double recip11, double recip22,
+                            double volume, double* __restrict__ out) {
+    const int nx = box.grid[0], ny = box.grid[1], nz = box.grid[2], nzh = nz / 2 + 1;
+    const size_t total = (size_t) nx * ny * nzh;
+    for (size_t idx = (size_t) blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t) gridDim.x * blockDim.x) {
+        const int kz = (int) (idx % nzh);
+        const int ky = (int) ((idx / nzh) % ny);
+        const int kx = (int) (idx / ((size_t) nzh * ny));
+        if (kx == 0 && ky == 0 && kz == 0) { out[idx] = 0.0; continue; }
+        const int mx = kx < (nx + 1) / 2 ? kx : kx - nx;
+        const int my = ky < (ny + 1) / 2 ? ky : ky - ny;
+        const int mz = kz < (nz + 1) / 2 ? kz : kz - nz;
+        const double hx = mx * recip00, hy = my * recip11, hz = mz * recip22;
+        const double m2 = hx * hx + hy * hy + hz * hz;
+        const double expF = M_PI * M_PI / (alpha * alpha);
+        out[idx] = exp(-expF * m2) / (M_PI * volume * m2 * modx[kx] * mody[ky] * modz[kz]);
+    }
+}
+
+template <typename real> struct Cplx;
+template <> struct Cplx<float> { typedef float2 type; };
+template <> struct Cplx<double> { typedef double2 type; };
+
+template <typename real>
+__global__ void k_convolve(size_t total, const double* __restrict__ influence, typename Cplx<real>::type* __restrict__ g,
+                           const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    for (size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t) gridDim.x * blockDim.x) {
+        const real f = (real) influence[i];
+        typename Cplx<real>::type v = g[i];
+        v.x *= f;
+        v.y *= f;
+        g[i] = v;
+    }
+}
+
+// Gather NTERM fractional potential derivatives (4, 10 or 35) at each atom;
+// MPIDReferenceForce.cpp:3368-3530.  phi layout [NTERM][npad].
+template <typename real, int ORDER, int NTERM>
+__global__ void k_gather(int n, int npad, BoxDev box, const real* __restrict__ theta, const int* __restrict__ igrid,
+                         const real* __restrict__ grid, real* __restrict__ phi, const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    if (s >= n) {
+        for (int k = 0; k < NTERM; ++k) phi[k * npad + s] = real(0);
+        return;
+    }
+    constexpr int MAXD = NTERM == 4 ? 1 : (NTERM == 10 ? 2 : 4);
+    const int nx = box.grid[0], ny = box.grid[1], nz = box.grid[2];
+    auto TH = [&](int d, int k, int m) { return theta[((d * 5 + k) * ORDER + m) * npad + s]; };
+    real acc[NTERM];
+#pragma unroll
+    for (int k = 0; k < NTERM; ++k) acc[k] = real(0);
+    const int gx0 = igrid[s], gy0 = igrid[npad + s], gz0 = igrid[2 * npad + s];
+    for (int iz = 0; iz < ORDER; ++iz) {
+        int gz = gz0 + iz;
+        if (gz >= nz) gz -= nz;
+        real v[MAXD + 1];
+#pragma unroll
+        for (int k = 0; k <= MAXD; ++k) v[k] = TH(2, k, iz);
+        real tu[MAXD + 1][MAXD + 1];
+#pragma unroll
+        for (int a = 0; a <= MAXD; ++a)
+#pragma unroll
+            for (int b = 0; b <= MAXD; ++b) tu[a][b] = real(0);
+        for (int iy = 0; iy < ORDER; ++iy) {
+            int gy = gy0 + iy;
+            if (gy >= ny) gy -= ny;
+            real u[MAXD + 1];
+#pragma unroll
+            for (int k = 0; k <= MAXD; ++k) u[k] = TH(1, k, iy);
+            real t[MAXD + 1];
+#pragma unroll
+            for (int k = 0; k <= MAXD; ++k) t[k] = real(0);
+#pragma unroll
+            for (int ix = 0; ix < ORDER; ++ix) {
+                int gx = gx0 + ix;
+                if (gx >= nx) gx -= nx;
+                const real q = grid[((size_t) gx * ny + gy) * nz + gz];
+#pragma unroll
+                for (int k = 0; k <= MAXD; ++k) t[k] += q * TH(0, k, ix);
+            }
+#pragma unroll
+            for (int a = 0; a <= MAXD; ++a)
+#pragma unroll
+                for (int b = 0; a + b <= MAXD; ++b) tu[a][b] += t[a] * u[b];
+        }
+#pragma unroll
+        for (int a = 0; a <= MAXD; ++a)
+#pragma unroll
+            for (int b = 0; a + b <= MAXD; ++b)
+#pragma unroll
+                for (int c = 0; a + b + c <= MAXD; ++c) acc[hermite_index(a, b, c)] += tu[a][b] * v[c];
+    }
+#pragma unroll
+    for (int k = 0; k < NTERM; ++k) phi[k * npad + s] = acc[k];
+}
+
+}  // namespace mpid
+
+namespace mpid {
+
+// ---------------------------------------------------------------------------
+// Per-atom kernels.
+
+template <typename real>
+__device__ __forceinline__ void sym_mul(const real* S, int npad, int s, const real* v, real* o) {
+    const real a0 = S[s], a1 = S[npad + s], a2 = S[2 * npad + s], a3 = S[3 * npad + s], a4 = S[4 * npad + s],
+               a5 = S[5 * npad + s];
+    o[0] = a0 * v[0] + a1 * v[1] + a2 * v[2];
+    o[1] = a1 * v[0] + a3 * v[1] + a4 * v[2];
+    o[2] = a2 * v[0] + a4 * v[1] + a5 * v[2];
+}
+
+// Total permanent field E = real space (fixed point) - A^T grad phi_recip + self term
+// (MPIDReferenceForce.cpp:2922-2949), then mu_direct = alpha E and S E.
+template <typename real>
+__global__ void k_record_fixed(int n, int npad, BoxDev box, double selfCoef, const unsigned long long* __restrict__ fx,
+                               const real* __restrict__ phi, AtomArrays<real> at, real* __restrict__ Efix,
+                               real* __restrict__ muD, real* __restrict__ SE) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    real E[3] = {real(0), real(0), real(0)};
+    if (s < n) {
+        for (int c = 0; c < 3; ++c) {
+            double e = fx_get(fx, c * npad + s);
+            if (phi) e -= box.A[0][c] * (double) phi[npad + s] + box.A[1][c] * (double) phi[2 * npad + s] +
+                          box.A[2][c] * (double) phi[3 * npad + s];
+            e += selfCoef * (double) at.mom[(1 + c) * npad + s];
+            E[c] = real(e);
+        }
+    }
+    real m[3], se[3];
+    sym_mul(at.alab, npad, s, E, m);
+    sym_mul(at.sroot, npad, s, E, se);
+    for (int c = 0; c < 3; ++c) {
+        Efix[c * npad + s] = E[c];
+        muD[c * npad + s] = m[c];
+        SE[c * npad + s] = se[c];
+    }
+}
+
+// sp = S p, and its fractional dipole for the spread (charge slot zero).
+template <typename real>
+__global__ void k_apply_sroot(int npad, BoxDev box, const real* __restrict__ S, const real* __restrict__ p,
+                              real* __restrict__ sp, real* __restrict__ mfd, const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    real v[3] = {p[s], p[npad + s], p[2 * npad + s]}, o[3];
+    sym_mul(S, npad, s, v, o);
+    for (int c = 0; c < 3; ++c) sp[c * npad + s] = o[c];
+    if (mfd) {
+        mfd[s] = real(0);
+        for (int j = 0; j < 3; ++j)
+            mfd[(1 + j) * npad + s] = real(box.A[j][0]) * o[0] + real(box.A[j][1]) * o[1] + real(box.A[j][2]) * o[2];
+    }
+}
+
+// Fractional dipoles of a dipole field (for spreading mu directly).
+template <typename real>
+__global__ void k_frac_dipoles(int npad, BoxDev box, const real* __restrict__ mu, real* __restrict__ mfd,
+                               const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    const real o[3] = {mu[s], mu[npad + s], mu[2 * npad + s]};
+    mfd[s] = real(0);
+    for (int j = 0; j < 3; ++j)
+        mfd[(1 + j) * npad + s] = real(box.A[j][0]) * o[0] + real(box.A[j][1]) * o[1] + real(box.A[j][2]) * o[2];
+}
+
+// Induced-dipole field at every atom: real space (fixed point) + reciprocal + self
+// (MPIDReferenceForce.cpp:4073-4141).  Writes E (and optionally the gradient with the
+// reciprocal part added, MPIDReferenceForce.cpp:4094-4130).
+template <typename real>
+__global__ void k_dipole_field_total(int n, int npad, BoxDev box, double selfCoef, const unsigned long long* __restrict__ fx,
+                                     const unsigned long long* __restrict__ gfx, const real* __restrict__ phi, int nterm,
+                                     const real* __restrict__ mu, real* __restrict__ E, real* __restrict__ G,
+                                     const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    for (int c = 0; c < 3; ++c) {
+        double e = 0.0;
+        if (s < n) {
+            e = fx_get(fx, c * npad + s) + selfCoef * (double) mu[c * npad + s];
+            if (phi) e -= box.A[0][c] * (double) phi[npad + s] + box.A[1][c] * (double) phi[2 * npad + s] +
+                          box.A[2][c] * (double) phi[3 * npad + s];
+        }
+        E[c * npad + s] = real(e);
+    }
+    if (G) {
+        const int ia[6] = {0, 1, 2, 0, 0, 1}, ib[6] = {0, 1, 2, 1, 2, 2};
+        double H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        if (phi && nterm >= 10) {
+            H[0][0] = phi[4 * npad + s]; H[1][1] = phi[5 * npad + s]; H[2][2] = phi[6 * npad + s];
+            H[0][1] = H[1][0] = phi[7 * npad + s];
+            H[0][2] = H[2][0] = phi[8 * npad + s];
+            H[1][2] = H[2][1] = phi[9 * npad + s];
+        }
+        for (int g = 0; g < 6; ++g) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) acc += box.A[k][ia[g]] * H[k][l] * box.A[l][ib[g]];
+            G[g * npad + s] = s < n ? real(fx_get(gfx, g * npad + s) - acc) : real(0);
+        }
+    }
+}
+
+// q = p - S E (the CG operator B = I - S T S applied to p) and per-block partial p.q.
+template <typename real>
+__global__ void k_cg_finish_matvec(int npad, const real* __restrict__ S, const real* __restrict__ p,
+                                   const real* __restrict__ E, real* __restrict__ q, double* __restrict__ partial,
+                                   const int* __restrict__ skip) {
+    __shared__ double red[256];
+    if (skip && *skip) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (s < npad) {
+        real e[3] = {E[s], E[npad + s], E[2 * npad + s]}, se[3];
+        sym_mul(S, npad, s, e, se);
+        for (int c = 0; c < 3; ++c) {
+            const real pv = p[c * npad + s];
+            const real qv = pv - se[c];
+            q[c * npad + s] = qv;
+            acc += (double) pv * (double) qv;
+        }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// Deterministic final reduction of per-block partials (one block).
+__global__ void k_reduce_partials(int nblocks, int nvals, const double* __restrict__ partial, double* __restrict__ out,
+                                  const int* __restrict__ skip) {
+    __shared__ double red[1024];
+    if (skip && *skip) return;
+    for (int v = 0; v < nvals; ++v) {
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partial[v * nblocks + b];
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[v] = red[0];
+        __syncthreads();
+    }
+}
+
+// CG scalars: slot 0 rr, 1 pq, 2 rr_new, 3 |S r|^2, 4 alpha, 5 beta, 6 metric.
+// x += a p, r -= a q; partials of r.r and |S r|^2.
+template <typename real, typename xreal>
+__global__ void k_cg_update(int npad, const real* __restrict__ S, double* __restrict__ sc, const real* __restrict__ p,
+                            const real* __restrict__ q, xreal* __restrict__ x, real* __restrict__ r,
+                            double* __restrict__ partial, int nblocks, const int* __restrict__ skip) {
+    __shared__ double red[2][256];
+    if (skip && *skip) return;
+    const double a = sc[0] / sc[1];
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, sr = 0.0;
+    if (s < npad) {
+        real rv[3];
+        for (int c = 0; c < 3; ++c) {
+            x[c * npad + s] += xreal(a * (double) p[c * npad + s]);
+            rv[c] = real((double) r[c * npad + s] - a * (double) q[c * npad + s]);
+            r[c * npad + s] = rv[c];
+            rr += (double) rv[c] * (double) rv[c];
+        }
+        real z[3];
+        sym_mul(S, npad, s, rv, z);
+        sr = (double) z[0] * z[0] + (double) z[1] * z[1] + (double) z[2] * z[2];
+    }
+    red[0][threadIdx.x] = rr;
+    red[1][threadIdx.x] = sr;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + o];
+            red[1][threadIdx.x] += red[1][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = red[0][0];
+        partial[nblocks + blockIdx.x] = red[1][0];
+    }
+}
+
+// After the reductions: beta, convergence test 48.033324 sqrt(|S r|^2 / n) < target
+// (MPIDReferenceForce.cpp:1219), iteration limit.  done[0] = 1 stops the loop.
+__global__ void k_cg_scalars(double* __restrict__ sc, const double* __restrict__ red, int n, double target,
+                             int* __restrict__ iter, int maxIter, int* __restrict__ done) {
+    if (*done) return;
+    sc[2] = red[0];
+    sc[3] = red[1];
+    sc[5] = sc[2] / sc[0];
+    sc[0] = sc[2];
+    sc[6] = 48.033324 * sqrt(sc[3] / n);
+    *iter += 1;
+    if (sc[6] < target || *iter >= maxIter || !(sc[6] == sc[6])) *done = 1;
+}
+
+template <typename real>
+__global__ void k_cg_direction(int npad, const double* __restrict__ sc, const real* __restrict__ r, real* __restrict__ p,
+                               const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    const double b = sc[5];
+    for (int c = 0; c < 3; ++c) p[c * npad + s] = real((double) r[c * npad + s] + b * (double) p[c * npad + s]);
+}
+
+// Initial CG state from the right-hand side: r = p = b, x = 0, partials of r.r and |S r|^2.
+template <typename real, typename xreal>
+__global__ void k_cg_start(int npad, const real* __restrict__ S, const real* __restrict__ b, xreal* __restrict__ x,
+                           real* __restrict__ r, real* __restrict__ p, double* __restrict__ partial, int nblocks) {
+    __shared__ double red[2][256];
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, sr = 0.0;
+    if (s < npad) {
+        real v[3];
+        for (int c = 0; c < 3; ++c) {
+            v[c] = b[c * npad + s];
+            x[c * npad + s] = xreal(0);
+            r[c * npad + s] = v[c];
+            p[c * npad + s] = v[c];
+            rr += (double) v[c] * v[c];
+        }
+        real z[3];
+        sym_mul(S, npad, s, v, z);
+        sr = (double) z[0] * z[0] + (double) z[1] * z[1] + (double) z[2] * z[2];
+    }
+    red[0][threadIdx.x] = rr;
+    red[1][threadIdx.x] = sr;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + o];
+            red[1][threadIdx.x] += red[1][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = red[0][0];
+        partial[nblocks + blockIdx.x] = red[1][0];
+    }
+}
+
+__global__ void k_cg_init_scalars(double* __restrict__ sc, const double* __restrict__ red, int n, double target,
+                                  int* __restrict__ iter, int* __restrict__ done) {
+    sc[0] = red[0];
+    sc[3] = red[1];
+    sc[6] = 48.033324 * sqrt(red[1] / n);
+    *iter = 0;
+    *done = (sc[6] < target) ? 1 : 0;
+}
+
+// mu = S y (sorted), in the precision of the pair kernels.
+template <typename xreal, typename real>
+__global__ void k_mu_from_y(int npad, const xreal* __restrict__ S, const xreal* __restrict__ y, real* __restrict__ mu) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    xreal v[3] = {y[s], y[npad + s], y[2 * npad + s]}, o[3];
+    sym_mul(S, npad, s, v, o);
+    for (int c = 0; c < 3; ++c) mu[c * npad + s] = real(o[c]);
+}
+
+// FP64 residual of the refinement loop: res = S (E + T S y) - y with T S y already in E2
+// (E2 = field of mu = S y, including reciprocal and self terms).  Partial |S res|^2.
+__global__ void k_refine_residual(int npad, const double* __restrict__ S, const double* __restrict__ Efix,
+                                  const double* __restrict__ E2, const double* __restrict__ y, double* __restrict__ res,
+                                  float* __restrict__ res32, double* __restrict__ partial) {
+    __shared__ double red[256];
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (s < npad) {
+        double e[3] = {Efix[s] + E2[s], Efix[npad + s] + E2[npad + s], Efix[2 * npad + s] + E2[2 * npad + s]}, se[3];
+        sym_mul(S, npad, s, e, se);
+        double rv[3];
+        for (int c = 0; c < 3; ++c) {
+            rv[c] = se[c] - y[c * npad + s];
+            res[c * npad + s] = rv[c];
+            res32[c * npad + s] = (float) rv[c];
+        }
+        double z[3];
+        sym_mul(S, npad, s, rv, z);
+        acc = z[0] * z[0] + z[1] * z[1] + z[2] * z[2];
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+template <typename real>
+__global__ void k_axpy_to_double(int npad3, const real* __restrict__ d, double* __restrict__ y) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < npad3) y[i] += (double) d[i];
+}
+
+// mu_(m+1) = alpha E_m for the extrapolated solver; mu_out accumulates cbar-weighted sum.
+template <typename real>
+__global__ void k_alpha_times(int npad, const real* __restrict__ alab, const real* __restrict__ E, real* __restrict__ out) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    real v[3] = {E[s], E[npad + s], E[2 * npad + s]}, o[3];
+    sym_mul(alab, npad, s, v, o);
+    for (int c = 0; c < 3; ++c) out[c * npad + s] = o[c];
+}
+
+template <typename real>
+__global__ void k_axpy(int n3, real a, const real* __restrict__ x, real* __restrict__ y) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n3) y[i] += a * x[i];
+}
+
+// Reciprocal-space and self terms per atom (MPIDReferenceForce.cpp:3739-4024,
+// 4283-4333) and the extrapolated-solver response (MPIDReferenceForce.cpp:4956-4984).
+struct OptArgs {
+    int nPT;                 // number of perturbation orders (0 when not extrapolated)
+    double cbar[8];
+    const void* mu;          // nPT x [3][npad]
+    const void* E;           // (nPT-1) x [3][npad]
+    const void* G;           // (nPT-1) x [6][npad]
+};
+
+template <typename real>
+__global__ void k_recip_self(int n, int npad, BoxDev box, double alpha, int polType, const real* __restrict__ phiP,
+                             const real* __restrict__ phiD, const real* __restrict__ mu, AtomArrays<real> at,
+                             OptArgs opt, unsigned long long* __restrict__ force, unsigned long long* __restrict__ torque,
+                             double* __restrict__ energyPartial) {
+    __shared__ double red[256];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double eAcc = 0.0;
+    if (s < n) {
+        const bool aniso = at.prm[s].z != 0.f;
+        LabMoments<real> m;
+        load_moments(at.mom, npad, s, m);
+        const real ui[3] = {mu[s], mu[npad + s], mu[2 * npad + s]};
+        real A[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) A[a][b] = real(box.A[a][b]);
+        double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
+        if (phiP) {
+            real Mf[20];
+            frac_multipole(m, A, Mf);
+            real muf[3];
+            for (int j = 0; j < 3; ++j) muf[j] = A[j][0] * ui[0] + A[j][1] * ui[1] + A[j][2] * ui[2];
+            auto PP = [&](int t, int u, int v) { return (double) phiP[hermite_index(t, u, v) * npad + s]; };
+            auto PD = [&](int t, int u, int v) { return (double) phiD[hermite_index(t, u, v) * npad + s]; };
+            double ef = 0.0, ei = 0.0, f[3] = {0, 0, 0};
+            for (int k = 0; k < 20; ++k) {
+                int t, u, v;
+                hermite_tuv(k, t, u, v);
+                ef += (double) Mf[k] * PP(t, u, v);
+                f[0] += (double) Mf[k] * (PP(t + 1, u, v) + PD(t + 1, u, v));
+                f[1] += (double) Mf[k] * (PP(t, u + 1, v) + PD(t, u + 1, v));
+                f[2] += (double) Mf[k] * (PP(t, u, v + 1) + PD(t, u, v + 1));
+            }
+            for (int k = 0; k < 3; ++k) {
+                const int t = k == 0, u = k == 1, v = k == 2;
+                ei += (double) muf[k] * PP(t, u, v);
+                double g0 = PP(t + 1, u, v), g1 = PP(t, u + 1, v), g2 = PP(t, u, v + 1);
+                if (polType == 0) { g0 += PD(t + 1, u, v); g1 += PD(t, u + 1, v); g2 += PD(t, u, v + 1); }
+                f[0] += (double) muf[k] * g0;
+                f[1] += (double) muf[k] * g1;
+                f[2] += (double) muf[k] * g2;
+            }
+            eAcc += 0.5 * kElectric * (ef + ei);
+            for (int c = 0; c < 3; ++c) F[c] -= kElectric * (box.A[0][c] * f[0] + box.A[1][c] * f[1] + box.A[2][c] * f[2]);
+            // torques from the permanent and induced reciprocal potentials
+            real P0, P1[3], P2[3][3], P3[3][3][3], tau[3], dtot[3];
+            for (int c = 0; c < 3; ++c) dtot[c] = m.d[c] + (aniso ? ui[c] : real(0));
+            real ph[35];
+            for (int k = 0; k < 35; ++k) ph[k] = phiP[k * npad + s];
+            cartesian_potential(ph, A, P0, P1, P2, P3);
+            multipole_torque(dtot, m.Q, m.O, P1, P2, P3, tau);
+            for (int c = 0; c < 3; ++c) T[c] += kElectric * (double) tau[c];
+            for (int c = 0; c < 3; ++c) dtot[c] = m.d[c] + ((aniso && polType == 0) ? ui[c] : real(0));
+            for (int k = 0; k < 35; ++k) ph[k] = phiD[k * npad + s];
+            cartesian_potential(ph, A, P0, P1, P2, P3);
+            multipole_torque(dtot, m.Q, m.O, P1, P2, P3, tau);
+            for (int c = 0; c < 3; ++c) T[c] += kElectric * (double) tau[c];
+            // self torque (isotropic atoms) and self energy
+            const double a3 = alpha * alpha * alpha;
+            if (!aniso) {
+                const double term = 2.0 / 3.0 * kElectric * a3 / kSqrtPiRef;
+                const double u2[3] = {2.0 * ui[0], 2.0 * ui[1], 2.0 * ui[2]};
+                T[0] += term * ((double) m.d[1] * u2[2] - (double) m.d[2] * u2[1]);
+                T[1] += term * ((double) m.d[2] * u2[0] - (double) m.d[0] * u2[2]);
+                T[2] += term * ((double) m.d[0] * u2[1] - (double) m.d[1] * u2[0]);
+            }
+            real ex[3] = {real(1), real(0), real(0)}, ey[3] = {real(0), real(1), real(0)}, ez[3] = {real(0), real(0), real(1)};
+            real S[16];
+            frame_spherical(m, ex, ey, ez, S);
+            double qii = 0, oii = 0, dii = 0;
+            for (int k = 4; k < 9; ++k) qii += (double) S[k] * S[k];
+            for (int k = 9; k < 16; ++k) oii += (double) S[k] * S[k];
+            for (int c = 0; c < 3; ++c) dii += (double) m.d[c] * ((double) m.d[c] + (double) ui[c]);
+            const double a2 = alpha * alpha;
+            eAcc += -alpha * kElectric / kSqrtPiRef *
+                    ((double) m.q * m.q + 2.0 / 3.0 * a2 * dii + 4.0 / 15.0 * a2 * a2 * qii + 8.0 / 105.0 * a2 * a2 * a2 * oii);
+        }
+        if (opt.nPT > 0) {
+            const real* MU = (const real*) opt.mu;
+            const real* EE = (const real*) opt.E;
+            const real* GG = (const real*) opt.G;
+            const size_t st3 = (size_t) 3 * npad, st6 = (size_t) 6 * npad;
+            for (int l = 0; l < opt.nPT - 1; ++l)
+                for (int mm = 0; mm < opt.nPT - 1 - l; ++mm) {
+                    const double pw = opt.cbar[l + mm + 1];
+                    if (fabs(pw) < 1e-6) continue;
+                    const double u[3] = {MU[l * st3 + s], MU[l * st3 + npad + s], MU[l * st3 + 2 * npad + s]};
+                    double g[6];
+                    for (int q = 0; q < 6; ++q) g[q] = GG[mm * st6 + q * npad + s];
+                    F[0] += pw * kElectric * (u[0] * g[0] + u[1] * g[3] + u[2] * g[4]);
+                    F[1] += pw * kElectric * (u[0] * g[3] + u[1] * g[1] + u[2] * g[5]);
+                    F[2] += pw * kElectric * (u[0] * g[4] + u[1] * g[5] + u[2] * g[2]);
+                    if (aniso) {
+                        const double e[3] = {EE[mm * st3 + s], EE[mm * st3 + npad + s], EE[mm * st3 + 2 * npad + s]};
+                        T[0] += pw * kElectric * (u[1] * e[2] - u[2] * e[1]);
+                        T[1] += pw * kElectric * (u[2] * e[0] - u[0] * e[2]);
+                        T[2] += pw * kElectric * (u[0] * e[1] - u[1] * e[0]);
+                    }
+                }
+        }
+        for (int c = 0; c < 3; ++c) {
+            fx_add(force + c * npad + s, F[c]);
+            fx_add(torque + c * npad + s, T[c]);
+        }
+    }
+    red[threadIdx.x] = eAcc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) energyPartial[blockIdx.x] = red[0];
+}
+
+// Torque on each atom -> forces on it and its frame atoms (original order loop).
+__global__ void k_torque_map(int n, int npad, const double* __restrict__ pos, MolArrays mol, const int* __restrict__ rank,
+                             const unsigned long long* __restrict__ torque, unsigned long long* __restrict__ force) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int ax = mol.axis[i];
+    if (ax == NoAxisType) return;
+    const int s = rank[i];
+    const double T[3] = {fx_get(torque, s), fx_get(torque, npad + s), fx_get(torque, 2 * npad + s)};
+    const int iz = mol.az[i], ix = mol.ax[i], iy = mol.ay[i];
+    const double* pI = pos + 3 * i;
+    const double* pZ = pos + 3 * iz;
+    const double* pX = ix >= 0 ? pos + 3 * ix : pI;
+    const double* pY = iy >= 0 ? pos + 3 * iy : pI;
+    double fI[3], fZ[3], fX[3], fY[3];
+    torque_to_force<double>(ax, pI, pZ, pX, pY, iy >= 0, T, fI, fZ, fX, fY);
+    for (int c = 0; c < 3; ++c) {
+        fx_add(force + c * npad + s, fI[c]);
+        fx_add(force + c * npad + rank[iz], fZ[c]);
+        if (ix >= 0) fx_add(force + c * npad + rank[ix], fX[c]);
+        if (iy >= 0) fx_add(force + c * npad + rank[iy], fY[c]);
+    }
+}
+
+// out[i] += F (accumulate, as OpenMM kernels add into the context force buffer).
+__global__ void k_forces_out(int n, int npad, const int* __restrict__ rank, const unsigned long long* __restrict__ force,
+                             double* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = rank[i];
+    for (int c = 0; c < 3; ++c) out[3 * i + c] += fx_get(force, c * npad + s);
+}
+
+// Dipoles in original order: which 0 induced, 1 lab permanent, 2 total.
+template <typename real>
+__global__ void k_dipoles_out(int n, int npad, int which, const int* __restrict__ rank, const real* __restrict__ mom,
+                              const real* __restrict__ mu, double* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = rank[i];
+    for (int c = 0; c < 3; ++c) {
+        double v = 0.0;
+        if (which != 1) v += (double) mu[c * npad + s];
+        if (which != 0) v += (double) mom[(1 + c) * npad + s];
+        out[3 * i + c] = v;
+    }
+}
+
+}  // namespace mpid

@@ -975,6 +975,15 @@ MPID_HD void torque_to_force(int axis, const real* pI, const real* pZ, const rea
     real u[3], v[3], w[3];
     for (int k = 0; k < 3; ++k) { u[k] = pZ[k] - pI[k]; v[k] = pX[k] - pI[k]; }
     const real nu = normalize3(u);
+    if (axis == ZOnly) {
+        // The second frame vector of a Z-only frame is the fixed lab axis chosen in
+        // local_frame (as the reference CUDA platform does, multipoles.cu:527-533); the
+        // reference CPU code reads an x atom that Z-only frames do not have.
+        const bool useX = m_fabs(u[0]) < real(0.866);
+        v[0] = useX ? real(1) : real(0);
+        v[1] = useX ? real(0) : real(1);
+        v[2] = real(0);
+    }
     const real nv = normalize3(v);
     if (hasY && (axis == ZBisect || axis == ThreeFold)) {
         for (int k = 0; k < 3; ++k) w[k] = pY[k] - pI[k];

@@ -1,0 +1,142 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's FP64 CPU force.
+
+Oracle outputs are committed fixtures (tests/golden/): the reference's 18 known-answer
+cases (reference_tests.json) and reference runs on seeded systems (make_fixtures.py).
+
+Tolerances
+* FP64 path: relative RMS force error <= 1e-7, relative energy error <= 1e-8,
+  induced dipoles <= 1e-6 relative RMS (the mutual fixtures converge to 1e-9 D).
+* mixed path: relative RMS force error <= 5e-6 and relative energy error <= 1e-6 on the
+  water box (the accuracy gates of the mixed-precision evaluation); the 4-12 atom
+  known-answer cases use the reference tests' own tolerance, 1e-4 relative to
+  max(|x|, 1), because their energies are small differences of large terms.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from mpidopenmmplugin_gb300 import MPIDContext, MPIDForce, synthetic
+
+import helpers
+from test_oracle_golden import assert_equal_tol, assert_equal_vec
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = helpers.load_reference_tests()
+CASES = GOLDEN["tests"]
+
+
+def run(force, pos, box, precision, **kw):
+    ctx = MPIDContext(force, precision=precision, **kw)
+    e, f = ctx.evaluate(pos, box)
+    return ctx, e, f
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_reference_known_answers(case, precision):
+    from oracle import oracle as O
+    s = O.system_from_golden(GOLDEN, case)
+    f = helpers.force_from_oracle_system(s)
+    box = s.box if s.nonbonded_method == 1 else np.eye(3) * 10.0
+    ctx, e, forces = run(f, s.pos, box, precision)
+    assert_equal_tol(case["ref_energy"], e, case["energy_tol"])
+    if case["ref_forces"] is not None:
+        for exp, got in zip(case["ref_forces"], forces):
+            assert_equal_vec(exp, got, case["force_tol"])
+
+
+def _fixture_case(name):
+    fx = helpers.load_npz_fixture(name)
+    s = helpers.system_from_fixture(fx)
+    return fx, s, helpers.force_from_oracle_system(s)
+
+
+def _torque_mapped_zonly(s):
+    """Atoms whose forces include a Z-only torque mapping.  The reference CPU code maps
+    those through an x atom that Z-only frames do not have (undefined there), so they are
+    checked against finite differences of its energy in test_zonly_matches_energy_gradient."""
+    z = [i for i in range(s.n) if int(s.axis_type[i]) == MPIDForce.ZOnly]
+    return set(z) | set(int(s.atom_z[i]) for i in z)
+
+
+@pytest.mark.parametrize("pol", ["direct", "mutual", "extrapolated"])
+@pytest.mark.parametrize("system", ["water648", "frames"])
+def test_fixture_double(system, pol):
+    fx, s, f = _fixture_case("%s_%s.npz" % (system, pol))
+    ctx, e, forces = run(f, s.pos, s.box, "double")
+    skip = _torque_mapped_zonly(s)
+    mask = np.array([i not in skip for i in range(s.n)])
+    assert abs(e - fx["ref_energy"]) / abs(fx["ref_energy"]) < 1e-8
+    assert helpers.rel_rms(forces[mask], fx["ref_forces"][mask]) < 1e-7
+    assert helpers.rel_rms(ctx.getInducedDipoles(), fx["ref_induced"]) < 1e-6
+    assert helpers.rel_rms(ctx.getLabFramePermanentDipoles(), fx["ref_labdipoles"]) < 1e-12
+    tot = ctx.getTotalDipoles()
+    assert np.allclose(tot, ctx.getInducedDipoles() + ctx.getLabFramePermanentDipoles(), rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("pol", ["direct", "mutual", "extrapolated"])
+@pytest.mark.parametrize("system", ["water648", "frames"])
+def test_fixture_mixed(system, pol):
+    fx, s, f = _fixture_case("%s_%s.npz" % (system, pol))
+    ctx, e, forces = run(f, s.pos, s.box, "mixed")
+    skip = _torque_mapped_zonly(s)
+    mask = np.array([i not in skip for i in range(s.n)])
+    ferr = helpers.rel_rms(forces[mask], fx["ref_forces"][mask])
+    eerr = abs(e - fx["ref_energy"]) / abs(fx["ref_energy"])
+    print("%s %s mixed: energy rel err %.3e force rel RMS %.3e stats %s" % (system, pol, eerr, ferr, ctx.stats()))
+    assert ferr < 5e-6
+    assert eerr < 1e-6
+    assert helpers.rel_rms(ctx.getInducedDipoles(), fx["ref_induced"]) < 5e-6
+
+
+def test_zonly_matches_energy_gradient():
+    """Z-only torque mapping of the GPU path against central differences of the energy."""
+    fx, s, f = _fixture_case("frames_direct.npz")
+    ctx = MPIDContext(f, precision="double")
+    e0, forces = ctx.evaluate(s.pos, s.box)
+    h = 1e-5
+    for atom in sorted(_torque_mapped_zonly(s))[:6]:
+        for c in range(3):
+            p = s.pos.copy()
+            p[atom, c] += h
+            ep, _ = ctx.evaluate(p, s.box)
+            p[atom, c] -= 2 * h
+            em, _ = ctx.evaluate(p, s.box)
+            fd = -(ep - em) / (2 * h)
+            assert abs(fd - forces[atom, c]) < 1e-5 * max(1.0, abs(fd)), (atom, c, fd, forces[atom, c])
+
+
+def test_forces_are_accumulated_and_deterministic():
+    f, pos, box = synthetic.workload("water648", polarization=MPIDForce.Mutual, order=5)
+    ctx = MPIDContext(f, precision="mixed")
+    e1, f1 = ctx.evaluate(pos, box)
+    e2, f2 = ctx.evaluate(pos, box)
+    assert e1 == e2
+    assert np.array_equal(f1, f2)
+    base = np.full_like(f1, 3.0)
+    _, f3 = ctx.evaluate(pos, box, forces=base.copy())
+    assert np.array_equal(f3, f1 + 3.0)
+
+
+def test_mixed_against_double_order5():
+    """Order-5 PME (which the reference cannot run) : mixed path against the FP64 path."""
+    for pol in (MPIDForce.Direct, MPIDForce.Mutual, MPIDForce.Extrapolated):
+        f, pos, box = synthetic.workload("water648", polarization=pol, order=5)
+        _, ed, fd = run(f, pos, box, "double")
+        ctx, em, fm = run(f, pos, box, "mixed")
+        assert helpers.rel_rms(fm, fd) < 5e-6, pol
+        assert abs(em - ed) / abs(ed) < 1e-6, pol
+
+
+def test_validation_errors_on_device():
+    f, pos, box = synthetic.workload("water648", polarization=MPIDForce.Direct, order=5)
+    ctx = MPIDContext(f, precision="mixed")
+    with pytest.raises(Exception, match="twice the nonbonded cutoff"):
+        ctx.evaluate(pos, np.eye(3) * 1.0)
+    f.setMutualInducedMaxIterations(1)
+    f.setPolarizationType(MPIDForce.Mutual)
+    ctx = MPIDContext(f, precision="double")
+    with pytest.raises(Exception, match="did not converge"):
+        ctx.evaluate(pos, box)
