@@ -147,7 +147,7 @@ template <typename real>
 struct Engine {
     int n = 0, npad = 0;
     DBuf<real> off, mom, alab, sroot;
-    DBuf<float4> prm;
+    DBuf<typename Vec4<real>::type> prm;
     DBuf<int> orig, rank;
     DBuf<real> mf, mfd;                       // [20][npad], [4][npad]
     DBuf<real> phiP, phiD, phiT;              // [35][npad] each; phiT scratch
@@ -208,7 +208,7 @@ struct Context {
     bool haveParams = false;
     // covalent partners: symmetric CSR over original indices
     DBuf<int> covOff, covJ;
-    DBuf<float> covS;
+    DBuf<double> covS;
     // sort / tiles
     DBuf<unsigned long long> keys, keysAlt;
     DBuf<char> cubTemp;
@@ -225,7 +225,15 @@ struct Context {
     std::unique_ptr<Engine<float>> ef;
     std::unique_ptr<Engine<double>> ed;
     // accumulators (sorted order)
-    DBuf<unsigned long long> forceFx, torqueFx, energyFx;
+    DBuf<unsigned long long> forceFx, torqueFx;
+    DBuf<double> energyBlocks;          // per-block real-space energy
+    DBuf<double> mom64, prm64;          // FP64 lab moments (sorted) and (thole, damp) by atom
+    DBuf<int2> scaledPairs;             // covalently scaled pairs (i < j), original indices
+    DBuf<double> scaledScale, scaledPartial;
+    int nScaled = 0;
+    DBuf<unsigned long long> pairKeys, pairKeysAlt;
+    DBuf<char> cubTemp2;
+    size_t cubBytes2 = 0;
     DBuf<double> energyPartial, energyOut;
     DBuf<double> forcesOut;
     // solver scratch
@@ -287,8 +295,14 @@ struct Context {
         npairs.alloc(1);
         pairCapacity = std::max(1024, std::min(ntiles * (ntiles + 1) / 2, ntiles * 160));
         pairs.alloc(pairCapacity);
-        forceFx.alloc(3 * (size_t) npad); torqueFx.alloc(3 * (size_t) npad); energyFx.alloc(1);
-        energyPartial.alloc(nblk(npad, 256)); energyOut.alloc(1);
+        pairKeys.alloc(pairCapacity); pairKeysAlt.alloc(pairCapacity);
+        cub::DeviceRadixSort::SortKeys(nullptr, cubBytes2, pairKeys.p, pairKeysAlt.p, pairCapacity);
+        cubTemp2.alloc(cubBytes2);
+        forceFx.alloc(3 * (size_t) npad); torqueFx.alloc(3 * (size_t) npad);
+        energyBlocks.alloc(152 * 64);
+        mom64.alloc(20 * (size_t) npad); prm64.alloc(2 * (size_t) n);
+        scaledPairs.alloc(1); scaledScale.alloc(1); scaledPartial.alloc(1);
+        energyPartial.alloc(nblk(npad, 256)); energyOut.alloc(4);
         forcesOut.alloc(3 * (size_t) n);
         partial.alloc(2 * (size_t) nblk(npad, 256)); red.alloc(4); sc.alloc(8);
         iter.alloc(1); done.alloc(1);
@@ -411,14 +425,29 @@ struct Context {
                     if (j < i) continue;
                     sc[{i, j}] = sval[t];
                 }
-        std::vector<std::vector<std::pair<int, float>>> lists(n);
+        std::vector<int2> sp;
+        std::vector<double> ssc;
+        for (auto& kv : sc)
+            if (kv.second != 1.0 && kv.first.first != kv.first.second) {
+                sp.push_back(make_int2(kv.first.first, kv.first.second));
+                ssc.push_back(kv.second);
+            }
+        nScaled = (int) sp.size();
+        scaledPairs.alloc(std::max(nScaled, 1));
+        scaledScale.alloc(std::max(nScaled, 1));
+        scaledPartial.alloc(std::max(nblk(nScaled, 128), 1));
+        if (nScaled) {
+            CUDA_CHECK(cudaMemcpy(scaledPairs.p, sp.data(), nScaled * sizeof(int2), cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(scaledScale.p, ssc.data(), nScaled * sizeof(double), cudaMemcpyHostToDevice));
+        }
+        std::vector<std::vector<std::pair<int, double>>> lists(n);
         for (auto& kv : sc) {
             if (kv.second == 1.0 || kv.first.first == kv.first.second) continue;
-            lists[kv.first.first].push_back({kv.first.second, (float) kv.second});
-            lists[kv.first.second].push_back({kv.first.first, (float) kv.second});
+            lists[kv.first.first].push_back({kv.first.second, kv.second});
+            lists[kv.first.second].push_back({kv.first.first, kv.second});
         }
         std::vector<int> off(n + 1, 0), js;
-        std::vector<float> ss;
+        std::vector<double> ss;
         for (int i = 0; i < n; ++i) {
             for (auto& e : lists[i]) { js.push_back(e.first); ss.push_back(e.second); }
             off[i + 1] = (int) js.size();
@@ -428,7 +457,7 @@ struct Context {
         CUDA_CHECK(cudaMemcpy(covOff.p, off.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
         if (!js.empty()) {
             CUDA_CHECK(cudaMemcpy(covJ.p, js.data(), js.size() * sizeof(int), cudaMemcpyHostToDevice));
-            CUDA_CHECK(cudaMemcpy(covS.p, ss.data(), ss.size() * sizeof(float), cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(covS.p, ss.data(), ss.size() * sizeof(double), cudaMemcpyHostToDevice));
         }
     }
 
@@ -512,17 +541,36 @@ struct Context {
             CUDA_CHECK(cudaMemcpyAsync(&cnt, npairs.p, sizeof(int), cudaMemcpyDeviceToHost, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
             lastPairs = cnt;
-            if (cnt <= pairCapacity) return;
+            if (cnt <= pairCapacity) {
+                sort_pairs(cnt);
+                return;
+            }
             pairCapacity = (int) (cnt * 1.25) + 1024;  // regrow and rebuild
             pairs.alloc(pairCapacity);
+            pairKeys.alloc(pairCapacity);
+            pairKeysAlt.alloc(pairCapacity);
+            cub::DeviceRadixSort::SortKeys(nullptr, cubBytes2, pairKeys.p, pairKeysAlt.p, pairCapacity);
+            cubTemp2.alloc(cubBytes2);
         }
         throw Error(MPID_ERR_CUDA, "tile pair list overflow");
     }
 
-    template <typename real>
-    void prepare_engine(Engine<real>& e) {
+    // Sort the tile-pair list (I, J) so kernels see a reproducible order with each I's
+    // pairs adjacent.
+    void sort_pairs(int cnt) {
+        if (cnt <= 1) return;
         cudaStream_t st = stream;
-        k_gather_atoms<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, keys.p, mol(), pos.p, wpos.p, center.p, e.arrays());
+        CUDA_CHECK(cudaMemcpyAsync(pairKeys.p, pairs.p, cnt * sizeof(int2), cudaMemcpyDeviceToDevice, st));
+        // int2 (x = I, y = J) read as a 64-bit key: J in the high word, so sort by (J, I)
+        CUDA_CHECK(cub::DeviceRadixSort::SortKeys(cubTemp2.p, cubBytes2, pairKeys.p, pairKeysAlt.p, cnt, 0, 64, st));
+        CUDA_CHECK(cudaMemcpyAsync(pairs.p, pairKeysAlt.p, cnt * sizeof(int2), cudaMemcpyDeviceToDevice, st));
+    }
+
+    template <typename real>
+    void prepare_engine(Engine<real>& e, bool main) {
+        cudaStream_t st = stream;
+        k_gather_atoms<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, keys.p, mol(), pos.p, wpos.p, center.p, e.arrays(),
+                                                               main ? mom64.p : nullptr, main ? prm64.p : nullptr);
         if (usePme) {
             e.pme.set_stream(st);
             e.pme.bsplines(n, npad, keys.p, wpos.p, box, st);
@@ -729,19 +777,20 @@ struct Context {
         }
         CUDA_CHECK(cudaMemsetAsync(forceFx.p, 0, 3 * (size_t) npad * 8, st));
         CUDA_CHECK(cudaMemsetAsync(torqueFx.p, 0, 3 * (size_t) npad * 8, st));
-        CUDA_CHECK(cudaMemsetAsync(energyFx.p, 0, 8, st));
+        const int eb = pair_blocks();
+        CUDA_CHECK(cudaMemsetAsync(energyBlocks.p, 0, eb * sizeof(double), st));
         const bool exact = (set.flags & MPID_FLAG_EXACT_ANISO_TORQUE) != 0;
         const TileCtx tc = tile_ctx();
         const AtomArrays<real> aa = e.arrays();
         if (set.polarization_type == MPID_MUTUAL && !exact)
             k_electrostatics<real, true, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
-                                                                                             torqueFx.p, energyFx.p);
+                                                                                             torqueFx.p, energyBlocks.p);
         else if (set.polarization_type == MPID_MUTUAL)
             k_electrostatics<real, true, false><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
-                                                                                              torqueFx.p, energyFx.p);
+                                                                                              torqueFx.p, energyBlocks.p);
         else
             k_electrostatics<real, false, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
-                                                                                              torqueFx.p, energyFx.p);
+                                                                                              torqueFx.p, energyBlocks.p);
         OptArgs opt{};
         if (set.polarization_type == MPID_EXTRAPOLATED) {
             opt.nPT = set.n_extrap;
@@ -755,9 +804,27 @@ struct Context {
         }
         const int nb = nblk(npad, 256);
         k_recip_self<real><<<nb, 256, 0, st>>>(n, npad, box, set.ewald_alpha, set.polarization_type,
-                                                usePme ? e.phiP.p : nullptr, e.phiD.p, e.mu.p, e.arrays(), opt, forceFx.p,
-                                                torqueFx.p, energyPartial.p);
+                                                usePme ? e.phiP.p : nullptr, e.phiD.p, e.mu.p, e.arrays(), mom64.p, opt,
+                                                forceFx.p, torqueFx.p, energyPartial.p);
         k_reduce_partials<<<1, 1024, 0, st>>>(nb, 1, energyPartial.p, energyOut.p, nullptr);
+        k_reduce_partials<<<1, 1024, 0, st>>>(eb, 1, energyBlocks.p, energyOut.p + 1, nullptr);
+        if (nScaled) {
+            const int sb = nblk(nScaled, 128);
+            const int muIsFloat = sizeof(real) == 4 ? 1 : 0;
+            if (set.polarization_type == MPID_MUTUAL)
+                k_scaled_pair_energy<true><<<sb, 128, 0, st>>>(nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad, mom64.p,
+                                                               prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0,
+                                                               set.cutoff, usePme ? set.ewald_alpha : 0.0,
+                                                               set.default_thole, scaledPartial.p);
+            else
+                k_scaled_pair_energy<false><<<sb, 128, 0, st>>>(nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad, mom64.p,
+                                                                prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0,
+                                                                set.cutoff, usePme ? set.ewald_alpha : 0.0,
+                                                                set.default_thole, scaledPartial.p);
+            k_reduce_partials<<<1, 1024, 0, st>>>(sb, 1, scaledPartial.p, energyOut.p + 2, nullptr);
+        } else {
+            CUDA_CHECK(cudaMemsetAsync(energyOut.p + 2, 0, sizeof(double), st));
+        }
         k_torque_map<<<nblk(n, 128), 128, 0, st>>>(n, npad, pos.p, mol(), e.rank.p, torqueFx.p, forceFx.p);
         CUDA_CHECK(cudaGetLastError());
     }
@@ -777,8 +844,8 @@ struct Context {
         stats.num_tile_pairs = lastPairs;
         if (mixed) {
             Engine<float>& e = *ef;
-            prepare_engine(e);
-            if (ed) prepare_engine(*ed);
+            prepare_engine(e, true);
+            if (ed) prepare_engine(*ed, false);
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL)
                 solve_mutual_mixed(e, *ed);
@@ -788,7 +855,7 @@ struct Context {
             k_forces_out<<<nblk(n, 128), 128, 0, st>>>(n, npad, e.rank.p, forceFx.p, d_forces);
         } else {
             Engine<double>& e = *ed;
-            prepare_engine(e);
+            prepare_engine(e, true);
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL)
                 solve_mutual_double(e);
@@ -798,13 +865,11 @@ struct Context {
             k_forces_out<<<nblk(n, 128), 128, 0, st>>>(n, npad, e.rank.p, forceFx.p, d_forces);
         }
         CUDA_CHECK(cudaGetLastError());
-        unsigned long long efx = 0;
-        double erecip = 0.0;
-        CUDA_CHECK(cudaMemcpyAsync(&efx, energyFx.p, 8, cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaMemcpyAsync(&erecip, energyOut.p, 8, cudaMemcpyDeviceToHost, st));
+        double eparts[3] = {0, 0, 0};  // reciprocal + self, real space, scaled pairs
+        CUDA_CHECK(cudaMemcpyAsync(eparts, energyOut.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaEventRecord(evStop, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
-        const double energy = (double) (long long) efx * kFixedInv + erecip;
+        const double energy = eparts[0] + eparts[1] + eparts[2];
         if (d_energy) CUDA_CHECK(cudaMemcpyAsync(d_energy, &energy, 8, cudaMemcpyHostToDevice, st));
         float ms = 0.f;
         CUDA_CHECK(cudaEventElapsedTime(&ms, evStart, evStop));

@@ -6,7 +6,7 @@
 //   off[3][npad]       position minus its tile centre (real)
 //   mom[20][npad]      lab-frame q, dipole[3], Q6[6], O10[10] (real)
 //   alab[6][npad]      lab-frame polarisability, sroot[6][npad] its square root
-//   prm[npad]          float4 (thole, damp, aniso flag, unused); orig[npad] original index
+//   prm[npad]          (thole, damp, aniso flag, unused) in the arithmetic type; orig[npad]
 // Forces, torques and fields accumulate as 64-bit fixed point with 2^32 units.
 #pragma once
 #include <cuda_runtime.h>
@@ -28,6 +28,16 @@ __device__ __forceinline__ void fx_add(unsigned long long* p, double v) {
 __device__ __forceinline__ double fx_get(const unsigned long long* p, int i) {
     return (double) (long long) p[i] * kFixedInv;
 }
+
+template <typename real> struct Vec4;
+template <> struct Vec4<float> {
+    typedef float4 type;
+    static __host__ __device__ __forceinline__ float4 make(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+};
+template <> struct Vec4<double> {
+    typedef double4 type;
+    static __host__ __device__ __forceinline__ double4 make(double a, double b, double c, double d) { return make_double4(a, b, c, d); }
+};
 
 struct BoxDev {
     double L[3], invL[3];    // rectangular box edge lengths
@@ -126,7 +136,7 @@ struct AtomArrays {
     real* mom;       // [20][npad]
     real* alab;      // [6][npad]
     real* sroot;     // [6][npad]
-    float4* prm;     // thole, damp, aniso, 0
+    typename Vec4<real>::type* prm;  // thole, damp, aniso, 0
     int* orig;       // [npad], -1 for padding
     int* rank;       // [n]  sorted slot of each original atom
 };
@@ -147,15 +157,18 @@ struct MolArrays {  // original order, FP64, as given through the API
 template <typename real>
 __global__ void k_gather_atoms(int n, int npad, const unsigned long long* __restrict__ keys, MolArrays mol,
                                const double* __restrict__ pos, const double* __restrict__ wpos,
-                               const double* __restrict__ center, AtomArrays<real> at) {
+                               const double* __restrict__ center, AtomArrays<real> at, double* __restrict__ mom64,
+                               double* __restrict__ prm64) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     if (s >= n) {
         for (int k = 0; k < 3; ++k) at.off[k * npad + s] = real(0);
         for (int k = 0; k < 20; ++k) at.mom[k * npad + s] = real(0);
         for (int k = 0; k < 6; ++k) { at.alab[k * npad + s] = real(0); at.sroot[k * npad + s] = real(0); }
-        at.prm[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        at.prm[s] = Vec4<real>::make(real(0), real(0), real(0), real(0));
         at.orig[s] = -1;
+        if (mom64)
+            for (int k = 0; k < 20; ++k) mom64[k * npad + s] = 0.0;
         return;
     }
     const int i = (int) (keys[s] & 0xffffffffu);
@@ -180,6 +193,12 @@ __global__ void k_gather_atoms(int n, int npad, const unsigned long long* __rest
     LabMoments<double> L;
     double al[6];
     rotate_to_lab(p, R, flip, L, al);
+    if (mom64) {
+        mom64[s] = L.q;
+        for (int k = 0; k < 3; ++k) mom64[(1 + k) * npad + s] = L.d[k];
+        for (int k = 0; k < 6; ++k) mom64[(4 + k) * npad + s] = L.Q[k];
+        for (int k = 0; k < 10; ++k) mom64[(10 + k) * npad + s] = L.O[k];
+    }
     at.mom[s] = real(L.q);
     for (int k = 0; k < 3; ++k) at.mom[(1 + k) * npad + s] = real(L.d[k]);
     for (int k = 0; k < 6; ++k) at.mom[(4 + k) * npad + s] = real(L.Q[k]);
@@ -193,7 +212,11 @@ __global__ void k_gather_atoms(int n, int npad, const unsigned long long* __rest
         }
     const bool aniso = p.pol[0] != p.pol[1] || p.pol[0] != p.pol[2];
     const double damp = pow((p.pol[0] + p.pol[1] + p.pol[2]) / 3.0, 1.0 / 6.0);
-    at.prm[s] = make_float4((float) mol.thole[i], (float) damp, aniso ? 1.f : 0.f, 0.f);
+    at.prm[s] = Vec4<real>::make(real(mol.thole[i]), real(damp), aniso ? real(1) : real(0), real(0));
+    if (prm64) {
+        prm64[2 * i] = mol.thole[i];
+        prm64[2 * i + 1] = damp;
+    }
 }
 
 template <typename real>
@@ -208,12 +231,12 @@ __device__ __forceinline__ void load_moments(const real* mom, int npad, int s, L
 }
 
 // Covalent scale of an (original-index) pair from the symmetric partner list.
-__device__ __forceinline__ float pair_scale(int oi, int oj, const int* __restrict__ covOff,
-                                            const int* __restrict__ covJ, const float* __restrict__ covS) {
+__device__ __forceinline__ double pair_scale(int oi, int oj, const int* __restrict__ covOff,
+                                             const int* __restrict__ covJ, const double* __restrict__ covS) {
     const int b = covOff[oi], e = covOff[oi + 1];
     for (int k = b; k < e; ++k)
         if (covJ[k] == oj) return covS[k];
-    return 1.0f;
+    return 1.0;
 }
 
 struct TileCtx {
@@ -227,7 +250,7 @@ struct TileCtx {
     double defaultThole;
     const int* covOff;
     const int* covJ;
-    const float* covS;
+    const double* covS;
 };
 
 // Displacement R_j - R_i of two sorted atoms from the tile-centre shift and offsets.
@@ -260,7 +283,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 k_fixed_field(TileCtx c, AtomArrays<real> at, unsigned long long* __restrict__ field) {
     __shared__ real shOff[kWarpsPerBlock][3][32];
     __shared__ real shMom[kWarpsPerBlock][20][32];
-    __shared__ float4 shPrm[kWarpsPerBlock][32];
+    __shared__ typename Vec4<real>::type shPrm[kWarpsPerBlock][32];
     __shared__ int shOrig[kWarpsPerBlock][32];
     __shared__ real shAcc[kWarpsPerBlock][3][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -273,7 +296,7 @@ k_fixed_field(TileCtx c, AtomArrays<real> at, unsigned long long* __restrict__ f
         real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
         LabMoments<real> mi;
         load_moments(at.mom, npad, si, mi);
-        const float4 pi = at.prm[si];
+        const typename Vec4<real>::type pi = at.prm[si];
         const int origI = at.orig[si];
         // j in shared memory
         for (int k = 0; k < 3; ++k) shOff[w][k][lane] = at.off[k * npad + sj];
@@ -297,11 +320,11 @@ k_fixed_field(TileCtx c, AtomArrays<real> at, unsigned long long* __restrict__ f
             const real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
             if (c.usePbc && r2 > rc2) continue;
             const real r = sqrt(r2);
-            const float scale = pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
-            const float4 pj = shPrm[w][jl];
-            const real a = scale == 0.0f ? real(pi.x + pj.x) : real(c.defaultThole);
+            const real scale = (real) pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
+            const typename Vec4<real>::type pj = shPrm[w][jl];
+            const real a = scale == real(0) ? pi.x + pj.x : real(c.defaultThole);
             PairRadial<real, 0, 4, 0> pr;
-            pair_radial<real, -1, 4, -1>(r, real(c.ewald), real(scale), a, real(pi.y) * real(pj.y), pr);
+            pair_radial<real, -1, 4, -1>(r, real(c.ewald), scale, a, pi.y * pj.y, pr);
             LabMoments<real> mj;
             mj.q = shMom[w][0][jl];
 #pragma unroll
@@ -337,7 +360,7 @@ k_dipole_field(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsi
     constexpr int NACC = GRAD ? 9 : 3;
     __shared__ real shOff[kWarpsPerBlock][3][32];
     __shared__ real shMu[kWarpsPerBlock][3][32];
-    __shared__ float4 shPrm[kWarpsPerBlock][32];
+    __shared__ typename Vec4<real>::type shPrm[kWarpsPerBlock][32];
     __shared__ int shOrig[kWarpsPerBlock][32];
     __shared__ real shAcc[kWarpsPerBlock][NACC][32];
     if (skip && *skip) return;
@@ -349,7 +372,7 @@ k_dipole_field(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsi
         const int si = IJ.x * 32 + lane, sj = IJ.y * 32 + lane;
         real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
         real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
-        const float4 pi = at.prm[si];
+        const typename Vec4<real>::type pi = at.prm[si];
         const int origI = at.orig[si];
         for (int k = 0; k < 3; ++k) {
             shOff[w][k][lane] = at.off[k * npad + sj];
@@ -376,11 +399,11 @@ k_dipole_field(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsi
             const real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
             if (c.usePbc && r2 > rc2) continue;
             const real r = sqrt(r2);
-            const float scale = pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
-            const float4 pj = shPrm[w][jl];
-            const real a = scale == 0.0f ? real(pi.x + pj.x) : real(c.defaultThole);
+            const real scale = (real) pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
+            const typename Vec4<real>::type pj = shPrm[w][jl];
+            const real a = scale == real(0) ? pi.x + pj.x : real(c.defaultThole);
             PairRadial<real, 0, 0, GRAD ? 3 : 2> pr;
-            pair_radial<real, -1, -1, GRAD ? 3 : 2>(r, real(c.ewald), real(1), a, real(pi.y) * real(pj.y), pr);
+            pair_radial<real, -1, -1, GRAD ? 3 : 2>(r, real(c.ewald), real(1), a, pi.y * pj.y, pr);
             real b[4] = {real(0), pr.bU[1], pr.bU[2], GRAD ? pr.bU[GRAD ? 3 : 2] : real(0)};
             real uj[3] = {shMu[w][0][jl], shMu[w][1][jl], shMu[w][2][jl]};
             real sI[3] = {-d[0], -d[1], -d[2]};
@@ -418,11 +441,11 @@ k_dipole_field(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsi
 template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 k_electrostatics(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ force,
-                 unsigned long long* __restrict__ torque, unsigned long long* __restrict__ energy) {
+                 unsigned long long* __restrict__ torque, double* __restrict__ energy) {
     __shared__ real shOff[kWarpsPerBlock][3][32];
     __shared__ real shMom[kWarpsPerBlock][20][32];
     __shared__ real shMu[kWarpsPerBlock][3][32];
-    __shared__ float4 shPrm[kWarpsPerBlock][32];
+    __shared__ typename Vec4<real>::type shPrm[kWarpsPerBlock][32];
     __shared__ int shOrig[kWarpsPerBlock][32];
     __shared__ real shAcc[kWarpsPerBlock][6][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -436,7 +459,7 @@ k_electrostatics(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, un
         real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
         LabMoments<real> mi;
         load_moments(at.mom, npad, si, mi);
-        const float4 pi = at.prm[si];
+        const typename Vec4<real>::type pi = at.prm[si];
         const int origI = at.orig[si];
         for (int k = 0; k < 3; ++k) {
             shOff[w][k][lane] = at.off[k * npad + sj];
@@ -462,11 +485,11 @@ k_electrostatics(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, un
             const real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
             if (c.usePbc && r2 > rc2) continue;
             const real r = sqrt(r2);
-            const float scale = pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
-            const float4 pj = shPrm[w][jl];
-            const real a = scale == 0.0f ? real(pi.x + pj.x) : real(c.defaultThole);
+            const real scale = (real) pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
+            const typename Vec4<real>::type pj = shPrm[w][jl];
+            const real a = scale == real(0) ? pi.x + pj.x : real(c.defaultThole);
             PairRadial<real, 7, 5, MUTUAL ? 3 : 0> pr;
-            pair_radial<real, 7, 5, MUTUAL ? 3 : -1>(r, real(c.ewald), real(scale), a, real(pi.y) * real(pj.y), pr);
+            pair_radial<real, 7, 5, MUTUAL ? 3 : -1>(r, real(c.ewald), scale, a, pi.y * pj.y, pr);
             LabMoments<real> mj;
             mj.q = shMom[w][0][jl];
 #pragma unroll
@@ -477,8 +500,8 @@ k_electrostatics(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, un
             for (int q = 0; q < 10; ++q) mj.O[q] = shMom[w][10 + q][jl];
             real uj[3] = {shMu[w][0][jl], shMu[w][1][jl], shMu[w][2][jl]};
             PairOut<real> po;
-            qi_pair<real, MUTUAL, REF_ANISO_TORQUE>(d, r, mi, mj, ui, uj, pi.z != 0.f, pj.z != 0.f, pr.bP, pr.bI, pr.bU, po);
-            eLane += (double) po.energy;
+            qi_pair<real, MUTUAL, REF_ANISO_TORQUE>(d, r, mi, mj, ui, uj, pi.z != real(0), pj.z != real(0), pr.bP, pr.bI, pr.bU, po);
+            if (scale == real(1)) eLane += (double) po.energy;  // scaled pairs: k_scaled_pair_energy
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 accF[q] -= po.fJ[q];
@@ -501,9 +524,66 @@ k_electrostatics(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, un
             }
         __syncwarp();
     }
-    // warp-reduce the energy in FP64 and add once per warp in fixed point
+    // FP64 energy: warp reduction, then a fixed-order sum of the warps of this block
+    // into energy[blockIdx.x] (the tile-pair list is sorted, so the result is reproducible).
+    __shared__ double shE[kWarpsPerBlock];
     for (int o = 16; o > 0; o >>= 1) eLane += __shfl_down_sync(0xffffffffu, eLane, o);
-    if (lane == 0 && eLane != 0.0) atomicAdd(energy, (unsigned long long) __double2ll_rn(eLane * kElectric * kFixedScale));
+    if (lane == 0) shE[w] = eLane;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double e = 0.0;
+        for (int k = 0; k < kWarpsPerBlock; ++k) e += shE[k];
+        energy[blockIdx.x] = e * kElectric;
+    }
+}
+
+// Energy of covalently scaled pairs (scale != 1) in FP64.  Their real-space terms remove
+// most of the reciprocal interaction of bonded atoms and are far larger than the total,
+// so they are summed at full precision; forces and torques stay in the tile kernel.
+template <bool MUTUAL>
+__global__ void k_scaled_pair_energy(int npairs, const int2* __restrict__ pr, const double* __restrict__ prs,
+                                     const int* __restrict__ rank, int npad, const double* __restrict__ mom64,
+                                     const double* __restrict__ prm64, const void* __restrict__ muv, int muIsFloat,
+                                     const double* __restrict__ pos, BoxDev box, int usePbc, double cutoff,
+                                     double ewald, double defaultThole, double* __restrict__ partial) {
+    __shared__ double red[128];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    if (p < npairs) {
+        const int i = pr[p].x, j = pr[p].y;
+        const int si = rank[i], sj = rank[j];
+        double d[3];
+        for (int k = 0; k < 3; ++k) {
+            double x = pos[3 * j + k] - pos[3 * i + k];
+            if (usePbc) x -= box.L[k] * rint(x * box.invL[k]);
+            d[k] = x;
+        }
+        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (!usePbc || r2 <= cutoff * cutoff) {
+            const double r = sqrt(r2), s = prs[p];
+            const double a = s == 0.0 ? prm64[2 * i] + prm64[2 * j] : defaultThole;
+            PairRadial<double, 7, 5, MUTUAL ? 3 : 0> rad;
+            pair_radial<double, 7, 5, MUTUAL ? 3 : -1>(r, ewald, s, a, prm64[2 * i + 1] * prm64[2 * j + 1], rad);
+            LabMoments<double> mi, mj;
+            load_moments(mom64, npad, si, mi);
+            load_moments(mom64, npad, sj, mj);
+            double ui[3], uj[3];
+            for (int c = 0; c < 3; ++c) {
+                ui[c] = muIsFloat ? (double) ((const float*) muv)[c * npad + si] : ((const double*) muv)[c * npad + si];
+                uj[c] = muIsFloat ? (double) ((const float*) muv)[c * npad + sj] : ((const double*) muv)[c * npad + sj];
+            }
+            PairOut<double> po;
+            qi_pair<double, MUTUAL>(d, r, mi, mj, ui, uj, false, false, rad.bP, rad.bI, rad.bU, po);
+            e = po.energy * kElectric;
+        }
+    }
+    red[threadIdx.x] = e;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -1062,13 +1142,13 @@ struct OptArgs {
 template <typename real>
 __global__ void k_recip_self(int n, int npad, BoxDev box, double alpha, int polType, const real* __restrict__ phiP,
                              const real* __restrict__ phiD, const real* __restrict__ mu, AtomArrays<real> at,
-                             OptArgs opt, unsigned long long* __restrict__ force, unsigned long long* __restrict__ torque,
-                             double* __restrict__ energyPartial) {
+                             const double* __restrict__ mom64, OptArgs opt, unsigned long long* __restrict__ force,
+                             unsigned long long* __restrict__ torque, double* __restrict__ energyPartial) {
     __shared__ double red[256];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     double eAcc = 0.0;
     if (s < n) {
-        const bool aniso = at.prm[s].z != 0.f;
+        const bool aniso = at.prm[s].z != real(0);
         LabMoments<real> m;
         load_moments(at.mom, npad, s, m);
         const real ui[3] = {mu[s], mu[npad + s], mu[2 * npad + s]};
@@ -1125,16 +1205,26 @@ __global__ void k_recip_self(int n, int npad, BoxDev box, double alpha, int polT
                 T[1] += term * ((double) m.d[2] * u2[0] - (double) m.d[0] * u2[2]);
                 T[2] += term * ((double) m.d[0] * u2[1] - (double) m.d[1] * u2[0]);
             }
-            real ex[3] = {real(1), real(0), real(0)}, ey[3] = {real(0), real(1), real(0)}, ez[3] = {real(0), real(0), real(1)};
-            real S[16];
-            frame_spherical(m, ex, ey, ez, S);
+            // Ewald self energy in FP64 from the FP64 lab moments
+            LabMoments<double> m64;
+            if (mom64) {
+                load_moments(mom64, npad, s, m64);
+            } else {
+                m64.q = m.q;
+                for (int k = 0; k < 3; ++k) m64.d[k] = m.d[k];
+                for (int k = 0; k < 6; ++k) m64.Q[k] = m.Q[k];
+                for (int k = 0; k < 10; ++k) m64.O[k] = m.O[k];
+            }
+            double ex[3] = {1, 0, 0}, ey[3] = {0, 1, 0}, ez[3] = {0, 0, 1};
+            double S[16];
+            frame_spherical(m64, ex, ey, ez, S);
             double qii = 0, oii = 0, dii = 0;
-            for (int k = 4; k < 9; ++k) qii += (double) S[k] * S[k];
-            for (int k = 9; k < 16; ++k) oii += (double) S[k] * S[k];
-            for (int c = 0; c < 3; ++c) dii += (double) m.d[c] * ((double) m.d[c] + (double) ui[c]);
+            for (int k = 4; k < 9; ++k) qii += S[k] * S[k];
+            for (int k = 9; k < 16; ++k) oii += S[k] * S[k];
+            for (int c = 0; c < 3; ++c) dii += m64.d[c] * (m64.d[c] + (double) ui[c]);
             const double a2 = alpha * alpha;
             eAcc += -alpha * kElectric / kSqrtPiRef *
-                    ((double) m.q * m.q + 2.0 / 3.0 * a2 * dii + 4.0 / 15.0 * a2 * a2 * qii + 8.0 / 105.0 * a2 * a2 * a2 * oii);
+                    (m64.q * m64.q + 2.0 / 3.0 * a2 * dii + 4.0 / 15.0 * a2 * a2 * qii + 8.0 / 105.0 * a2 * a2 * a2 * oii);
         }
         if (opt.nPT > 0) {
             const real* MU = (const real*) opt.mu;

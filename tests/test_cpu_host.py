@@ -1,0 +1,114 @@
+"""CPU tests: host-side API, C ABI exports, synthetic inputs, and the oracle port pinned
+to the reference's known answers and to reference runs (no GPU needed)."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from mpidopenmmplugin_gb300 import MPIDError, MPIDForce, synthetic
+from mpidopenmmplugin_gb300 import _build, context
+from oracle import oracle as O
+
+import helpers
+from test_oracle_golden import CASES, GOLDEN, check_case
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def port():
+    O.build("port")
+    return True
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_port_matches_golden(port, case):
+    check_case(O.evaluate(O.system_from_golden(GOLDEN, case), "port"), case)
+
+
+@pytest.mark.parametrize("name", ["water648_direct", "water648_mutual", "water648_extrapolated", "frames_direct",
+                                  "frames_mutual", "frames_extrapolated"])
+def test_port_matches_reference_fixtures(port, name):
+    fx = helpers.load_npz_fixture(name + ".npz")
+    s = helpers.system_from_fixture(fx)
+    p = O.evaluate(s, "port")
+    z = [i for i in range(s.n) if int(s.axis_type[i]) == MPIDForce.ZOnly]
+    skip = set(z) | set(int(s.atom_z[i]) for i in z)
+    mask = np.array([i not in skip for i in range(s.n)])
+    assert abs(p.energy - fx["ref_energy"]) / abs(fx["ref_energy"]) < 1e-10
+    assert helpers.rel_rms(p.forces[mask], fx["ref_forces"][mask]) < 1e-9
+    assert helpers.rel_rms(p.induced, fx["ref_induced"]) < 1e-8
+
+
+def test_library_exports_every_declared_symbol():
+    """libmpid_gb300.so loads without a GPU and exports each function in include/*.h."""
+    lib = _build.build()
+    decl = open(os.path.join(ROOT, "include", "mpid_gb300.h")).read()
+    names = set(re.findall(r"\b(mpid_[a-z_]+)\s*\(", decl))
+    assert names == set(context.C_API)
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True, check=True).stdout
+    exported = set(l.split()[-1] for l in out.splitlines() if l.strip())
+    assert names <= exported, names - exported
+    import ctypes
+    ctypes.CDLL(lib)
+
+
+def test_force_api_mirrors_reference_defaults():
+    f = MPIDForce()
+    assert f.getNonbondedMethod() == MPIDForce.NoCutoff
+    assert f.getPolarizationType() == MPIDForce.Extrapolated
+    assert f.getPmeBSplineOrder() == 6
+    assert f.getMutualInducedMaxIterations() == 60
+    assert f.getMutualInducedTargetEpsilon() == 1e-5
+    assert f.getDefaultTholeWidth() == 5.0
+    assert f.getExtrapolationCoefficients() == [-0.154, 0.017, 0.658, 0.474]
+    i = f.addMultipole(1.0, [0, 0, 0.1], [0] * 6, [0] * 10, MPIDForce.NoAxisType, -1, -1, -1, 0.3, [1e-3] * 3)
+    assert i == 0 and f.getNumMultipoles() == 1
+    f.setCovalentMap(0, MPIDForce.Covalent13, [4, 5])
+    assert f.getCovalentMap(0, MPIDForce.Covalent13) == [4, 5]
+    assert f.getCovalentMaps(0)[MPIDForce.Covalent13] == [4, 5]
+    with pytest.raises(MPIDError):
+        f.setNonbondedMethod(7)
+
+
+@pytest.mark.parametrize("bad,match", [
+    (dict(quadrupole=[1e-3, 0, 0, 0, 0, 0]), "nonzero trace"),
+    (dict(octopole=[1e-3] + [0] * 9), "octopole for particle"),
+    (dict(axis=9), "axis type"),
+    (dict(z=5), "invalid z axis"),
+    (dict(x=-1), "invalid x axis"),
+])
+def test_validation_rules(bad, match):
+    f = MPIDForce()
+    q = bad.get("quadrupole", [0] * 6)
+    o = bad.get("octopole", [0] * 10)
+    f.addMultipole(0.5, [0, 0, 0], q, o, bad.get("axis", MPIDForce.ZThenX), bad.get("z", 1), bad.get("x", 1), -1,
+                   0.3, [1e-3] * 3)
+    f.addMultipole(-0.5, [0, 0, 0], [0] * 6, [0] * 10, MPIDForce.NoAxisType, -1, -1, -1, 0.3, [1e-3] * 3)
+    with pytest.raises(MPIDError, match=match):
+        f.validate(2)
+
+
+def test_cutoff_against_box():
+    f, pos, box = synthetic.workload("water648", order=5)
+    f.validate(f.getNumMultipoles(), box)
+    with pytest.raises(MPIDError, match="half the periodic box"):
+        f.validate(f.getNumMultipoles(), np.eye(3) * 1.0)
+
+
+def test_synthetic_multipoles_are_traceless():
+    rng = np.random.default_rng(0)
+    q = synthetic.traceless_quadrupole(rng, 1.0, 50)
+    assert np.abs(q[:, 0] + q[:, 2] + q[:, 5]).max() < 1e-12
+    o = synthetic.traceless_octopole(rng, 1.0, 50)
+    for a, b, c in ((0, 2, 7), (1, 3, 8), (4, 6, 9)):
+        assert np.abs(o[:, a] + o[:, b] + o[:, c]).max() < 1e-12
+    f, pos, box = synthetic.workload("water648")
+    assert f.getNumMultipoles() == 648
+    d = pos[0::3, None, :] - pos[None, 0::3, :]
+    d -= box[0, 0] * np.round(d / box[0, 0])
+    r = np.sqrt((d ** 2).sum(-1))
+    np.fill_diagonal(r, 10)
+    assert r.min() >= 0.26 - 1e-9
