@@ -1,0 +1,334 @@
+"""Benchmark: MPIDForce energy+force evaluations per second on one GB300.
+
+Workload (one step = one full evaluation: sort/tiles, permanent field, mutual induced
+dipoles to 1e-7 D, energy/forces/torques, torque mapping): 8,000 rigid waters
+(24,000 atoms) in a 62.14 A cubic box, PME cutoff 0.9 nm, alpha 3.4 /nm, 72^3 grid,
+B-spline order 5, mutual polarisation, seeded synthetic multipoles.
+
+Arms
+* default: the mixed-precision path (FP32 pair/PME/solver kernels, 64-bit fixed-point
+  forces, FP64 energies and residual refinement).  `value` is evaluations/s with inputs
+  resident in HBM (device-pointer API); `e2e` runs the host-buffer C-ABI call
+  (positions and forces copied in, forces and energy copied out each step).  The FP64
+  path is timed on the same box for the mixed-vs-FP64 speed-up and accuracy.
+* --impl reference: the reference's CPU algorithm on the host cores.  The reference's
+  own build needs its source tree, absent on the GPU machine, so the oracle port
+  (oracle/mpid_port.cpp, pinned to the reference in tests) is timed with all host
+  threads, one full evaluation per step.
+
+With torchrun (N > 1) every rank evaluates its own replica (replicas only; no data is
+exchanged) and `value` is the sum over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "force+energy evals/s, 24k-atom water PME mutual pol: mixed vs FP64 at 5e-6"
+WORKLOAD = ("water24k: 8000 waters (24,000 atoms), 62.14 A box, cutoff 0.9 nm, alpha 3.4/nm, 72^3 grid, "
+            "B-spline order 5, mutual polarisation to 1e-7 D, seeded synthetic multipoles")
+L2_FLUSH_BYTES = 512 << 20
+
+
+def dist_setup(ngpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else "/tmp/mpid_bench_clocks.csv"
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def count_pairs_within(pos, box, cutoff):
+    from scipy.spatial import cKDTree
+    L = np.diag(box)
+    wrapped = pos - L * np.floor(pos / L)
+    tree = cKDTree(wrapped, boxsize=L)
+    return int(len(tree.query_pairs(cutoff, output_type="ndarray")))
+
+
+# Source-counted FP32 operations (FMA = 2) per interacting pair of the energy/force/torque
+# pair kernel (pair_radial<7,5,3> + qi_pair<MUTUAL>, mpid_math.cuh), used for the
+# algorithmic throughput of that kernel.
+PAIR_KERNEL_FLOP_PER_PAIR = 1900
+
+
+def run_reference(args, world, rank):
+    """CPU arm: the oracle port, all host threads, one full evaluation per step."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from mpidopenmmplugin_gb300 import MPIDForce, synthetic
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import helpers
+    O.build("port")
+    f, pos, box = synthetic.workload("water24k", polarization=MPIDForce.Mutual)
+    s = helpers.oracle_system(f, pos, box)
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    for _ in range(args.warmup):
+        O.evaluate(s, "port")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.evaluate(s, "port")
+    dt = time.perf_counter() - t0
+    val = args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "evals/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "precision": "fp64 CPU"},
+            "cpu_baseline": {"value": val, "unit": "evals/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+                             "kind": "port",
+                             "sample": "one full evaluation of the 24,000-atom box per step (oracle/mpid_port.cpp, "
+                                       "OpenMP; the reference's own build needs its source tree, absent here)"},
+            "e2e": {"value": val, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def cpu_baseline_sample():
+    """The oracle port on the host cores, one 24k-atom evaluation (about 5-15 s)."""
+    from oracle import oracle as O
+    from mpidopenmmplugin_gb300 import MPIDForce, synthetic
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import helpers
+    O.build("port")
+    f, pos, box = synthetic.workload("water24k", polarization=MPIDForce.Mutual)
+    s = helpers.oracle_system(f, pos, box)
+    t0 = time.perf_counter()
+    O.evaluate(s, "port")
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "evals/s", "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+            "kind": "port",
+            "sample": "one full evaluation of the 24,000-atom box (oracle/mpid_port.cpp, FP64, OpenMP)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    from mpidopenmmplugin_gb300 import MPIDContext, MPIDForce, synthetic
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import helpers
+
+    torch.cuda.set_device(local)
+    f, pos, box = synthetic.workload("water24k", polarization=MPIDForce.Mutual)
+    n = f.getNumMultipoles()
+    ctx = MPIDContext(f, precision="mixed", device=local)
+    stream = torch.cuda.current_stream()
+    d_pos = torch.tensor(pos, dtype=torch.float64, device="cuda").contiguous()
+    d_force = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
+    d_energy = torch.zeros(1, dtype=torch.float64, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        ctx.evaluate_device(d_pos.data_ptr(), box, d_force.data_ptr(), d_energy.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        d_force.zero_()
+        step()
+    torch.cuda.synchronize()
+    # timed region: events around each step on the launching stream, L2 flushed between steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stage_ms = {}
+    with ClockSampler(local) as clocks:
+        barrier(world)
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            step()
+            ends[k].record(stream)
+            st = ctx.stats()
+            for name, v in st["ms_stage"].items():
+                stage_ms[name] = stage_ms.get(name, 0.0) + v
+        torch.cuda.synchronize()
+        barrier(world)
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+    ms = max_over_ranks(ms, world)
+    value = world * 1000.0 / ms
+    stats = ctx.stats()
+
+    # end to end through the host-buffer API: positions + forces in, forces + energy out
+    hpos = np.ascontiguousarray(pos)
+    hforce = np.zeros((n, 3))
+    for _ in range(2):
+        ctx.evaluate(hpos, box, forces=hforce)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        hforce[:] = 0.0
+        e_mixed, fm = ctx.evaluate(hpos, box, forces=hforce)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    e2e_ms = max_over_ranks(e2e_ms, world)
+
+    # kernel launches per step (CUDA activity of one untimed step)
+    launches = None
+    try:
+        from torch.profiler import ProfilerActivity, profile
+        with profile(activities=[ProfilerActivity.CUDA]) as prof:
+            step()
+            torch.cuda.synchronize()
+        names = [e.name for e in prof.events() if e.device_type is not None and str(e.device_type).endswith("CUDA")]
+        ours = [nm for nm in names if "mpid" in nm or nm.startswith("_ZN4mpid") or nm.startswith("void mpid::")]
+        launches = len(ours) * args.steps
+    except Exception:
+        launches = None
+
+    line = None
+    if rank == 0:
+        # FP64 path on the same box: throughput and accuracy of the mixed path against it
+        fp64 = {}
+        if not args.no_fp64:
+            cd = MPIDContext(f, precision="double", device=local)
+            ed, fd = cd.evaluate(pos, box)
+            t0 = time.perf_counter()
+            reps = 3
+            for _ in range(reps):
+                ed, fd = cd.evaluate(pos, box)
+            fp64_ms = (time.perf_counter() - t0) * 1000.0 / reps
+            em, fmix = ctx.evaluate(pos, box)
+            fp64 = {"fp64_evals_per_s": 1000.0 / fp64_ms, "speedup_vs_fp64": fp64_ms / ms,
+                    "energy_rel_err": abs(em - ed) / abs(ed), "force_rel_rms_err": helpers.rel_rms(fmix, fd),
+                    "dipole_rel_rms_err": helpers.rel_rms(ctx.getInducedDipoles(), cd.getInducedDipoles())}
+        # roofline of the dominant kernel (the energy/force/torque pair kernel)
+        npairs = count_pairs_within(pos, box, 0.9)
+        pair_ms = stage_ms.get("pair_kernel", 0.0) / args.steps
+        achieved = PAIR_KERNEL_FLOP_PER_PAIR * npairs / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else None
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        clk = clocks.summary()
+        # FP32 CUDA-core peak: 152 SMs x 128 FP32 lanes x 2 FLOP/FMA x SM clock
+        sm_mhz = clk.get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roofline = {"bound": "fp32", "kernel": "k_electrostatics (energy/force/torque pair kernel)",
+                    "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                    "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
+                    "peak_source": "152 SMs x 128 FP32 lanes x 2 x max SM clock (no measured FP32 peak in "
+                                   "MEASURED_PEAKS.json)",
+                    "pairs_within_cutoff": npairs, "flop_per_pair": PAIR_KERNEL_FLOP_PER_PAIR,
+                    "ms_per_launch": pair_ms}
+        cpu = None
+        if not args.no_cpu_baseline:
+            try:
+                cpu = cpu_baseline_sample()
+            except Exception as exc:
+                cpu = {"value": None, "unit": "evals/s", "cores": 0, "kind": "port", "sample": "failed: %s" % exc}
+        nbytes = 3 * n * 8
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "precision": "mixed (FP32 kernels, FP64 energies and refinement)",
+                       "l2": "flushed between timed steps (512 MB write)", "replicas": world,
+                       "parallelism": "replicas only"},
+            "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "evals/s", "h2d_bytes_per_step": 2 * nbytes,
+                    "d2h_bytes_per_step": nbytes + 8},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
+            "solver": {"iterations": stats["solver_iterations"], "refinement_steps": stats["refinement_steps"],
+                       "residual_debye": stats["solver_residual"], "tile_pairs": stats["num_tile_pairs"]},
+        }
+        line.update(fp64)
+        print(json.dumps(line))
+    barrier(world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

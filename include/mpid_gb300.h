@@ -70,6 +70,13 @@ typedef struct {
     double solver_residual;    /* final Debye RMS residual */
     int num_tile_pairs;
     double ms_total;           /* device time of the last evaluation */
+    /* device time (ms) and timed launch groups per stage: 0 sort/tiles/atom set-up,
+     * 1 permanent-field pair kernel, 2 PME spread/FFT/convolution/gather, 3 dipole-field
+     * pair kernels, 4 solver vector work, 5 energy/force/torque pair kernel,
+     * 6 reciprocal/self terms and torque mapping */
+    double ms_stage[8];
+    int stage_launches[8];
+    double energy_parts[3];    /* reciprocal + self, real-space pairs, covalently scaled pairs */
 } mpid_stats;
 
 /* Fill `s` with the MPIDForce defaults for n atoms (PME not configured). */
@@ -104,7 +111,8 @@ int mpid_evaluate_device(mpid_context* ctx, const double* d_positions, const dou
 
 /* Dipoles of the last evaluation in caller order, 3n host doubles (e nm):
  * which 0 induced (getInducedDipoles), 1 lab-frame permanent (getLabFramePermanentDipoles),
- * 2 total (getTotalDipoles); mpidKernels.h:79-81. */
+ * 2 total (getTotalDipoles); mpidKernels.h:79-81.  which 3 returns the permanent
+ * electric field at each atom (e/nm^2, before multiplication by the polarisability). */
 int mpid_get_dipoles(mpid_context* ctx, int which, double* out);
 
 /* PME parameters in use (CalcMPIDForceKernel::getPMEParameters, mpidKernels.h:103). */

@@ -50,7 +50,13 @@ class Stats(ctypes.Structure):
         ("solver_residual", ctypes.c_double),
         ("num_tile_pairs", ctypes.c_int),
         ("ms_total", ctypes.c_double),
+        ("ms_stage", ctypes.c_double * 8),
+        ("stage_launches", ctypes.c_int * 8),
+        ("energy_parts", ctypes.c_double * 3),
     ]
+
+
+STAGES = ["setup", "fixed_field_pairs", "pme", "dipole_field_pairs", "solver_vectors", "pair_kernel", "recip_self_torque"]
 
 
 _LIB = None
@@ -187,6 +193,10 @@ class MPIDContext:
     def getTotalDipoles(self):
         return self._dipoles(2)
 
+    def getPermanentField(self):
+        """Permanent electric field at each atom (e/nm^2) of the last evaluation."""
+        return self._dipoles(3)
+
     def getPMEParametersInContext(self):
         a = ctypes.c_double()
         nx, ny, nz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
@@ -198,7 +208,11 @@ class MPIDContext:
         s = Stats()
         self._check(self.lib.mpid_get_stats(self._h, ctypes.byref(s)))
         return dict(solver_iterations=s.solver_iterations, refinement_steps=s.refinement_steps,
-                    solver_residual=s.solver_residual, num_tile_pairs=s.num_tile_pairs, ms_total=s.ms_total)
+                    solver_residual=s.solver_residual, num_tile_pairs=s.num_tile_pairs, ms_total=s.ms_total,
+                    ms_stage={STAGES[k]: s.ms_stage[k] for k in range(len(STAGES))},
+                    stage_launches={STAGES[k]: s.stage_launches[k] for k in range(len(STAGES))},
+                    energy_parts=dict(recip_self=s.energy_parts[0], real_space=s.energy_parts[1],
+                                      scaled_pairs=s.energy_parts[2]))
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -113,11 +113,11 @@ struct PmeStage {
         CUFFT_CHECK(cufftSetStream(fwd, s));
         CUFFT_CHECK(cufftSetStream(inv, s));
     }
-    void bsplines(int n, int npad, const unsigned long long* keys, const double* wpos, const BoxDev& box, cudaStream_t st) {
+    void bsplines(int n, int npad, const int* sorted, const double* wpos, const BoxDev& box, cudaStream_t st) {
         if (order == 5)
-            k_bsplines<real, 5><<<nblk(npad, 128), 128, 0, st>>>(npad, n, keys, wpos, box, theta.p, igrid.p);
+            k_bsplines<real, 5><<<nblk(npad, 128), 128, 0, st>>>(npad, n, sorted, wpos, box, theta.p, igrid.p);
         else
-            k_bsplines<real, 6><<<nblk(npad, 128), 128, 0, st>>>(npad, n, keys, wpos, box, theta.p, igrid.p);
+            k_bsplines<real, 6><<<nblk(npad, 128), 128, 0, st>>>(npad, n, sorted, wpos, box, theta.p, igrid.p);
     }
     template <int NCOMP>
     void spread(int n, int npad, const BoxDev& box, const real* mf, const int* skip, cudaStream_t st) {
@@ -192,6 +192,54 @@ struct Engine {
     }
 };
 
+// Device time of the evaluation stages, from CUDA events on the launching stream.
+enum Stage { ST_SETUP = 0, ST_FIXED_REAL, ST_PME, ST_DIPOLE_REAL, ST_SOLVER, ST_PAIR, ST_FINISH, ST_COUNT };
+
+struct StageTimer {
+    static constexpr int kMax = 4096;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> stage;
+    int count = 0, open = -1;
+    double ms[ST_COUNT] = {0};
+    int launches[ST_COUNT] = {0};
+    void init() {
+        ev.resize(2 * kMax);
+        stage.resize(kMax);
+        for (auto& e : ev) CUDA_CHECK(cudaEventCreate(&e));
+    }
+    void destroy() {
+        for (auto e : ev) cudaEventDestroy(e);
+        ev.clear();
+    }
+    void reset() {
+        count = 0;
+        open = -1;
+        for (int s = 0; s < ST_COUNT; ++s) { ms[s] = 0; launches[s] = 0; }
+    }
+    void begin(int s, cudaStream_t st) {
+        if (count >= kMax || ev.empty()) return;
+        stage[count] = s;
+        CUDA_CHECK(cudaEventRecord(ev[2 * count], st));
+        open = count;
+    }
+    void end(cudaStream_t st) {
+        if (open < 0) return;
+        CUDA_CHECK(cudaEventRecord(ev[2 * open + 1], st));
+        ++count;
+        open = -1;
+    }
+    // after the stream has been synchronised
+    void collect() {
+        for (int i = 0; i < count; ++i) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]) == cudaSuccess) {
+                ms[stage[i]] += t;
+                launches[stage[i]] += 1;
+            }
+        }
+    }
+};
+
 // ---------------------------------------------------------------------------
 struct Context {
     mpid_settings set;
@@ -211,6 +259,7 @@ struct Context {
     DBuf<double> covS;
     // sort / tiles
     DBuf<unsigned long long> keys, keysAlt;
+    DBuf<int> order, orderAlt;          // atom index of each sorted slot
     DBuf<char> cubTemp;
     size_t cubBytes = 0;
     DBuf<double> pos, wpos, center, half;
@@ -249,10 +298,12 @@ struct Context {
     std::vector<cudaEvent_t> iterEvents;
     cudaEvent_t evStart = nullptr, evStop = nullptr;
     mpid_stats stats{};
+    StageTimer timer;
     bool evaluated = false;
     BoxDev box{};
 
     ~Context() {
+        timer.destroy();
         if (hostDone) cudaFreeHost(hostDone);
         for (auto e : iterEvents) cudaEventDestroy(e);
         if (evStart) cudaEventDestroy(evStart);
@@ -288,8 +339,8 @@ struct Context {
         ntiles = npad / 32;
         charge.alloc(n); dipole.alloc(3 * n); quad.alloc(6 * n); oct.alloc(10 * n); thole.alloc(n); pol.alloc(3 * n);
         axis.alloc(n); az.alloc(n); ax.alloc(n); ay.alloc(n);
-        keys.alloc(n); keysAlt.alloc(n);
-        cub::DeviceRadixSort::SortKeys(nullptr, cubBytes, keys.p, keysAlt.p, n);
+        keys.alloc(n); keysAlt.alloc(n); order.alloc(n); orderAlt.alloc(n);
+        cub::DeviceRadixSort::SortPairs(nullptr, cubBytes, keys.p, keysAlt.p, order.p, orderAlt.p, n);
         cubTemp.alloc(cubBytes);
         pos.alloc(3 * n); wpos.alloc(3 * n); center.alloc(3 * ntiles); half.alloc(3 * ntiles);
         npairs.alloc(1);
@@ -309,6 +360,7 @@ struct Context {
         CUDA_CHECK(cudaMallocHost(&hostDone, 256 * sizeof(int)));
         CUDA_CHECK(cudaEventCreate(&evStart));
         CUDA_CHECK(cudaEventCreate(&evStop));
+        timer.init();
         iterEvents.resize(256);
         for (auto& e : iterEvents) CUDA_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         const int nPT = s.polarization_type == MPID_EXTRAPOLATED ? s.n_extrap : 0;
@@ -519,18 +571,23 @@ struct Context {
     void neighbour_setup() {
         cudaStream_t st = stream;
         if (usePme) {
-            k_sort_keys<<<nblk(n, 256), 256, 0, st>>>(n, pos.p, box, 0.25, keys.p, wpos.p);
-            CUDA_CHECK(cub::DeviceRadixSort::SortKeys(cubTemp.p, cubBytes, keys.p, keysAlt.p, n, 0, 64, st));
-            std::swap(keys.p, keysAlt.p);
+            // columns about (32 / density)^(1/3) wide
+            const double vol = box.L[0] * box.L[1] * box.L[2];
+            const double edge = std::cbrt(32.0 * vol / n);
+            const int ncx = std::max(1, (int) std::lround(box.L[0] / edge));
+            const int ncy = std::max(1, (int) std::lround(box.L[1] / edge));
+            k_sort_keys<<<nblk(n, 256), 256, 0, st>>>(n, pos.p, box, ncx, ncy, keys.p, orderAlt.p, wpos.p);
+            CUDA_CHECK(cub::DeviceRadixSort::SortPairs(cubTemp.p, cubBytes, keys.p, keysAlt.p, orderAlt.p, order.p, n, 0,
+                                                        64, st));
         } else {
             // No periodic box: keep the caller's order (all pairs interact).
-            std::vector<unsigned long long> k(n);
-            for (int i = 0; i < n; ++i) k[i] = (unsigned long long) i;
-            CUDA_CHECK(cudaMemcpyAsync(keys.p, k.data(), n * 8, cudaMemcpyHostToDevice, st));
+            std::vector<int> k(n);
+            for (int i = 0; i < n; ++i) k[i] = i;
+            CUDA_CHECK(cudaMemcpyAsync(order.p, k.data(), n * 4, cudaMemcpyHostToDevice, st));
             CUDA_CHECK(cudaMemcpyAsync(wpos.p, pos.p, 3 * n * 8, cudaMemcpyDeviceToDevice, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
         }
-        k_tile_bounds<<<nblk(ntiles, 128), 128, 0, st>>>(n, ntiles, keys.p, wpos.p, center.p, half.p);
+        k_tile_bounds<<<nblk(ntiles, 128), 128, 0, st>>>(n, ntiles, order.p, wpos.p, center.p, half.p);
         for (int attempt = 0; attempt < 3; ++attempt) {
             CUDA_CHECK(cudaMemsetAsync(npairs.p, 0, sizeof(int), st));
             const long long total = (long long) ntiles * (ntiles + 1) / 2;
@@ -569,11 +626,11 @@ struct Context {
     template <typename real>
     void prepare_engine(Engine<real>& e, bool main) {
         cudaStream_t st = stream;
-        k_gather_atoms<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, keys.p, mol(), pos.p, wpos.p, center.p, e.arrays(),
+        k_gather_atoms<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, order.p, mol(), pos.p, wpos.p, center.p, e.arrays(),
                                                                main ? mom64.p : nullptr, main ? prm64.p : nullptr);
         if (usePme) {
             e.pme.set_stream(st);
-            e.pme.bsplines(n, npad, keys.p, wpos.p, box, st);
+            e.pme.bsplines(n, npad, order.p, wpos.p, box, st);
             k_frac_multipoles<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, e.mom.p, e.mf.p);
         }
         CUDA_CHECK(cudaGetLastError());
@@ -588,11 +645,15 @@ struct Context {
     void fixed_field(Engine<real>& e) {
         cudaStream_t st = stream;
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
+        timer.begin(ST_FIXED_REAL, st);
         k_fixed_field<real><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tile_ctx(), e.arrays(), e.fieldFx.p);
+        timer.end(st);
         if (usePme) {
+            timer.begin(ST_PME, st);
             e.pme.template spread<20>(n, npad, box, e.mf.p, nullptr, st);
             e.pme.convolve(influence.p, nullptr, st);
             e.pme.template gather<35>(n, npad, box, e.phiP.p, nullptr, st);
+            timer.end(st);
         }
         k_record_fixed<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, self_coef(), e.fieldFx.p,
                                                                usePme ? e.phiP.p : nullptr, e.arrays(), e.Efix.p, e.muD.p,
@@ -605,6 +666,7 @@ struct Context {
     void dipole_field(Engine<real>& e, const real* mu, real* E, real* G, const int* skip, int nterm = 4) {
         cudaStream_t st = stream;
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
+        timer.begin(ST_DIPOLE_REAL, st);
         if (G) {
             CUDA_CHECK(cudaMemsetAsync(e.gradFx.p, 0, 6 * (size_t) npad * 8, st));
             k_dipole_field<real, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tile_ctx(), e.arrays(), mu, e.fieldFx.p,
@@ -613,7 +675,9 @@ struct Context {
             k_dipole_field<real, false><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tile_ctx(), e.arrays(), mu,
                                                                                       e.fieldFx.p, nullptr, skip);
         }
+        timer.end(st);
         if (usePme) {
+            timer.begin(ST_PME, st);
             k_frac_dipoles<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, mu, e.mfd.p, skip);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, skip, st);
             e.pme.convolve(influence.p, skip, st);
@@ -623,6 +687,7 @@ struct Context {
                 e.pme.template gather<10>(n, npad, box, e.phiT.p, skip, st);
             else
                 e.pme.template gather<35>(n, npad, box, e.phiT.p, skip, st);
+            timer.end(st);
         }
         k_dipole_field_total<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, self_coef(), e.fieldFx.p, e.gradFx.p,
                                                                      usePme ? e.phiT.p : nullptr, nterm, mu, E, G, skip);
@@ -770,15 +835,18 @@ struct Context {
         cudaStream_t st = stream;
         if (usePme) {
             // reciprocal potential of the final induced dipoles (35 terms)
+            timer.begin(ST_PME, st);
             k_frac_dipoles<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, e.mu.p, e.mfd.p, nullptr);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, nullptr, st);
             e.pme.convolve(influence.p, nullptr, st);
             e.pme.template gather<35>(n, npad, box, e.phiD.p, nullptr, st);
+            timer.end(st);
         }
         CUDA_CHECK(cudaMemsetAsync(forceFx.p, 0, 3 * (size_t) npad * 8, st));
         CUDA_CHECK(cudaMemsetAsync(torqueFx.p, 0, 3 * (size_t) npad * 8, st));
         const int eb = pair_blocks();
         CUDA_CHECK(cudaMemsetAsync(energyBlocks.p, 0, eb * sizeof(double), st));
+        timer.begin(ST_PAIR, st);
         const bool exact = (set.flags & MPID_FLAG_EXACT_ANISO_TORQUE) != 0;
         const TileCtx tc = tile_ctx();
         const AtomArrays<real> aa = e.arrays();
@@ -791,6 +859,8 @@ struct Context {
         else
             k_electrostatics<real, false, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
+        timer.end(st);
+        timer.begin(ST_FINISH, st);
         OptArgs opt{};
         if (set.polarization_type == MPID_EXTRAPOLATED) {
             opt.nPT = set.n_extrap;
@@ -826,6 +896,7 @@ struct Context {
             CUDA_CHECK(cudaMemsetAsync(energyOut.p + 2, 0, sizeof(double), st));
         }
         k_torque_map<<<nblk(n, 128), 128, 0, st>>>(n, npad, pos.p, mol(), e.rank.p, torqueFx.p, forceFx.p);
+        timer.end(st);
         CUDA_CHECK(cudaGetLastError());
     }
 
@@ -839,6 +910,8 @@ struct Context {
         cudaStream_t st = stream;
         CUDA_CHECK(cudaEventRecord(evStart, st));
         if (d_pos != pos.p) CUDA_CHECK(cudaMemcpyAsync(pos.p, d_pos, 3 * (size_t) n * 8, cudaMemcpyDeviceToDevice, st));
+        timer.reset();
+        timer.begin(ST_SETUP, st);
         set_box(hbox);
         neighbour_setup();
         stats.num_tile_pairs = lastPairs;
@@ -846,6 +919,7 @@ struct Context {
             Engine<float>& e = *ef;
             prepare_engine(e, true);
             if (ed) prepare_engine(*ed, false);
+            timer.end(st);
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL)
                 solve_mutual_mixed(e, *ed);
@@ -856,6 +930,7 @@ struct Context {
         } else {
             Engine<double>& e = *ed;
             prepare_engine(e, true);
+            timer.end(st);
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL)
                 solve_mutual_double(e);
@@ -870,10 +945,18 @@ struct Context {
         CUDA_CHECK(cudaEventRecord(evStop, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
         const double energy = eparts[0] + eparts[1] + eparts[2];
+        stats.energy_parts[0] = eparts[0];
+        stats.energy_parts[1] = eparts[1];
+        stats.energy_parts[2] = eparts[2];
         if (d_energy) CUDA_CHECK(cudaMemcpyAsync(d_energy, &energy, 8, cudaMemcpyHostToDevice, st));
         float ms = 0.f;
         CUDA_CHECK(cudaEventElapsedTime(&ms, evStart, evStop));
         stats.ms_total = ms;
+        timer.collect();
+        for (int s = 0; s < ST_COUNT; ++s) {
+            stats.ms_stage[s] = timer.ms[s];
+            stats.stage_launches[s] = timer.launches[s];
+        }
         evaluated = true;
         CUDA_CHECK(cudaStreamSynchronize(st));
         return energy;
@@ -881,8 +964,13 @@ struct Context {
 
     void get_dipoles(int which, double* host) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
-        if (which < 0 || which > 2) throw Error(MPID_ERR_INVALID, "which must be 0, 1 or 2");
-        if (mixed)
+        if (which < 0 || which > 3) throw Error(MPID_ERR_INVALID, "which must be 0, 1, 2 or 3");
+        if (which == 3) {  // permanent field: reuse the induced-dipole output path with mom = 0
+            if (mixed)
+                k_dipoles_out<float><<<nblk(n, 128), 128, 0, stream>>>(n, npad, 0, ef->rank.p, ef->mom.p, ef->Efix.p, forcesOut.p);
+            else
+                k_dipoles_out<double><<<nblk(n, 128), 128, 0, stream>>>(n, npad, 0, ed->rank.p, ed->mom.p, ed->Efix.p, forcesOut.p);
+        } else if (mixed)
             k_dipoles_out<float><<<nblk(n, 128), 128, 0, stream>>>(n, npad, which, ef->rank.p, ef->mom.p, ef->mu.p, forcesOut.p);
         else
             k_dipoles_out<double><<<nblk(n, 128), 128, 0, stream>>>(n, npad, which, ed->rank.p, ed->mom.p, ed->mu.p, forcesOut.p);

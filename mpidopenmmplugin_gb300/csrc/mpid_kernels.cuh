@@ -46,44 +46,42 @@ struct BoxDev {
 };
 
 // ---------------------------------------------------------------------------
-// Spatial sort: wrap into the box and key by the Morton code of a 0.25 nm voxel.
-__device__ __forceinline__ unsigned int spread_bits10(unsigned int v) {
-    v &= 0x3ff;
-    v = (v | (v << 16)) & 0x030000FF;
-    v = (v | (v << 8)) & 0x0300F00F;
-    v = (v | (v << 4)) & 0x030C30C3;
-    v = (v | (v << 2)) & 0x09249249;
-    return v;
-}
-
-__global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, double voxel,
-                            unsigned long long* __restrict__ keys, double* __restrict__ wpos) {
+// Spatial sort into near-cubic 32-atom tiles: the box is cut into x-y columns about
+// (32 / density)^(1/3) wide, columns are visited in a snake order, and atoms are sorted
+// along z inside each column (ascending in even, descending in odd columns so that a
+// tile running past the end of a column continues next to it).  Key: column index in
+// the high word, quantised z in the low word; the value is the atom index.
+__global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, int ncx, int ncy,
+                            unsigned long long* __restrict__ keys, int* __restrict__ vals, double* __restrict__ wpos) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    unsigned int c[3];
+    double w[3];
     for (int k = 0; k < 3; ++k) {
         double x = pos[3 * i + k];
         x -= box.L[k] * floor(x * box.invL[k]);
         if (x >= box.L[k]) x -= box.L[k];
         wpos[3 * i + k] = x;
-        int nv = (int) (box.L[k] / voxel) + 1;
-        int v = (int) (x / voxel);
-        if (v >= nv) v = nv - 1;
-        c[k] = (unsigned int) v;
+        w[k] = x * box.invL[k];
     }
-    unsigned int m = spread_bits10(c[0]) | (spread_bits10(c[1]) << 1) | (spread_bits10(c[2]) << 2);
-    keys[i] = ((unsigned long long) m << 32) | (unsigned int) i;
+    int cx = min(ncx - 1, (int) (w[0] * ncx));
+    int cy = min(ncy - 1, (int) (w[1] * ncy));
+    if (cx & 1) cy = ncy - 1 - cy;  // snake through the columns
+    const unsigned int col = (unsigned int) (cx * ncy + cy);
+    double zf = (col & 1) ? 1.0 - w[2] : w[2];
+    unsigned int zq = (unsigned int) fmin(4294967295.0, zf * 4294967296.0);
+    keys[i] = ((unsigned long long) col << 32) | zq;
+    vals[i] = i;
 }
 
 // Tile centres and half extents from the wrapped positions of the sorted atoms.
-__global__ void k_tile_bounds(int n, int ntiles, const unsigned long long* __restrict__ keys,
+__global__ void k_tile_bounds(int n, int ntiles, const int* __restrict__ order,
                               const double* __restrict__ wpos, double* __restrict__ center,
                               double* __restrict__ half) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntiles) return;
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int s = t * 32; s < min(n, t * 32 + 32); ++s) {
-        int i = (int) (keys[s] & 0xffffffffu);
+        int i = order[s];
         for (int k = 0; k < 3; ++k) {
             double x = wpos[3 * i + k];
             lo[k] = fmin(lo[k], x);
@@ -155,7 +153,7 @@ struct MolArrays {  // original order, FP64, as given through the API
 };
 
 template <typename real>
-__global__ void k_gather_atoms(int n, int npad, const unsigned long long* __restrict__ keys, MolArrays mol,
+__global__ void k_gather_atoms(int n, int npad, const int* __restrict__ order, MolArrays mol,
                                const double* __restrict__ pos, const double* __restrict__ wpos,
                                const double* __restrict__ center, AtomArrays<real> at, double* __restrict__ mom64,
                                double* __restrict__ prm64) {
@@ -171,7 +169,7 @@ __global__ void k_gather_atoms(int n, int npad, const unsigned long long* __rest
             for (int k = 0; k < 20; ++k) mom64[k * npad + s] = 0.0;
         return;
     }
-    const int i = (int) (keys[s] & 0xffffffffu);
+    const int i = order[s];
     at.orig[s] = i;
     at.rank[i] = s;
     const int t = s >> 5;
@@ -288,6 +286,7 @@ k_fixed_field(TileCtx c, AtomArrays<real> at, unsigned long long* __restrict__ f
     __shared__ real shAcc[kWarpsPerBlock][3][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int np = *c.npairs;
+    const EwaldAlpha<real> ew(c.ewald);
     const int npad = at.npad;
     for (int p = blockIdx.x * kWarpsPerBlock + w; p < np; p += gridDim.x * kWarpsPerBlock) {
         const int2 IJ = c.pairs[p];
@@ -324,7 +323,7 @@ k_fixed_field(TileCtx c, AtomArrays<real> at, unsigned long long* __restrict__ f
             const typename Vec4<real>::type pj = shPrm[w][jl];
             const real a = scale == real(0) ? pi.x + pj.x : real(c.defaultThole);
             PairRadial<real, 0, 4, 0> pr;
-            pair_radial<real, -1, 4, -1>(r, real(c.ewald), scale, a, pi.y * pj.y, pr);
+            pair_radial<real, -1, 4, -1>(r, ew, scale, a, pi.y * pj.y, pr);
             LabMoments<real> mj;
             mj.q = shMom[w][0][jl];
 #pragma unroll
@@ -366,6 +365,7 @@ k_dipole_field(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsi
     if (skip && *skip) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int np = *c.npairs;
+    const EwaldAlpha<real> ew(c.ewald);
     const int npad = at.npad;
     for (int p = blockIdx.x * kWarpsPerBlock + w; p < np; p += gridDim.x * kWarpsPerBlock) {
         const int2 IJ = c.pairs[p];
@@ -403,7 +403,7 @@ k_dipole_field(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsi
             const typename Vec4<real>::type pj = shPrm[w][jl];
             const real a = scale == real(0) ? pi.x + pj.x : real(c.defaultThole);
             PairRadial<real, 0, 0, GRAD ? 3 : 2> pr;
-            pair_radial<real, -1, -1, GRAD ? 3 : 2>(r, real(c.ewald), real(1), a, pi.y * pj.y, pr);
+            pair_radial<real, -1, -1, GRAD ? 3 : 2>(r, ew, real(1), a, pi.y * pj.y, pr);
             real b[4] = {real(0), pr.bU[1], pr.bU[2], GRAD ? pr.bU[GRAD ? 3 : 2] : real(0)};
             real uj[3] = {shMu[w][0][jl], shMu[w][1][jl], shMu[w][2][jl]};
             real sI[3] = {-d[0], -d[1], -d[2]};
@@ -450,6 +450,7 @@ k_electrostatics(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, un
     __shared__ real shAcc[kWarpsPerBlock][6][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int np = *c.npairs;
+    const EwaldAlpha<real> ew(c.ewald);
     const int npad = at.npad;
     double eLane = 0.0;
     for (int p = blockIdx.x * kWarpsPerBlock + w; p < np; p += gridDim.x * kWarpsPerBlock) {
@@ -489,7 +490,7 @@ k_electrostatics(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, un
             const typename Vec4<real>::type pj = shPrm[w][jl];
             const real a = scale == real(0) ? pi.x + pj.x : real(c.defaultThole);
             PairRadial<real, 7, 5, MUTUAL ? 3 : 0> pr;
-            pair_radial<real, 7, 5, MUTUAL ? 3 : -1>(r, real(c.ewald), scale, a, pi.y * pj.y, pr);
+            pair_radial<real, 7, 5, MUTUAL ? 3 : -1>(r, ew, scale, a, pi.y * pj.y, pr);
             LabMoments<real> mj;
             mj.q = shMom[w][0][jl];
 #pragma unroll
@@ -548,6 +549,7 @@ __global__ void k_scaled_pair_energy(int npairs, const int2* __restrict__ pr, co
                                      double ewald, double defaultThole, double* __restrict__ partial) {
     __shared__ double red[128];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const EwaldAlpha<double> ew(ewald);
     double e = 0.0;
     if (p < npairs) {
         const int i = pr[p].x, j = pr[p].y;
@@ -563,7 +565,7 @@ __global__ void k_scaled_pair_energy(int npairs, const int2* __restrict__ pr, co
             const double r = sqrt(r2), s = prs[p];
             const double a = s == 0.0 ? prm64[2 * i] + prm64[2 * j] : defaultThole;
             PairRadial<double, 7, 5, MUTUAL ? 3 : 0> rad;
-            pair_radial<double, 7, 5, MUTUAL ? 3 : -1>(r, ewald, s, a, prm64[2 * i + 1] * prm64[2 * j + 1], rad);
+            pair_radial<double, 7, 5, MUTUAL ? 3 : -1>(r, ew, s, a, prm64[2 * i + 1] * prm64[2 * j + 1], rad);
             LabMoments<double> mi, mj;
             load_moments(mom64, npad, si, mi);
             load_moments(mom64, npad, sj, mj);
@@ -590,7 +592,7 @@ __global__ void k_scaled_pair_energy(int npairs, const int2* __restrict__ pr, co
 // PME.  B-spline coefficients and weighted fractional multipoles per sorted atom.
 // theta layout: [3 dims][5 derivs][ORDER][npad]; igrid [3][npad].
 template <typename real, int ORDER>
-__global__ void k_bsplines(int npad, int n, const unsigned long long* __restrict__ keys, const double* __restrict__ wpos,
+__global__ void k_bsplines(int npad, int n, const int* __restrict__ order, const double* __restrict__ wpos,
                            BoxDev box, real* __restrict__ theta, int* __restrict__ igrid) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= npad) return;
@@ -601,7 +603,7 @@ __global__ void k_bsplines(int npad, int n, const unsigned long long* __restrict
         }
         return;
     }
-    const int i = (int) (keys[s] & 0xffffffffu);
+    const int i = order[s];
     for (int d = 0; d < 3; ++d) {
         // Fractional coordinate with the grid origin of MPIDReferenceForce.cpp:3058-3060:
         // the minimum-image coordinate w in [-1/2, 1/2) maps to n (w + 1/2).

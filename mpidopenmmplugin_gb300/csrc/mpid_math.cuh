@@ -81,14 +81,34 @@ struct GaussLegendre01<real, 14> {
     }
 };
 
+// Ewald parameter split so that products with alpha are formed without rounding alpha
+// itself: alpha = hi + lo with hi = real(alpha).  Rounding alpha once would bias every
+// erfc(alpha r) the same way (by up to ~13x its relative error near alpha r = 2.5).
+template <typename real>
+struct EwaldAlpha {
+    real hi, lo;        // alpha
+    real pre_hi, pre_lo;  // 2 alpha / sqrt(pi)
+    real a2x2;          // 2 alpha^2
+    MPID_HD explicit EwaldAlpha(double a) {
+        hi = real(a);
+        lo = real(a - double(hi));
+        const double p = 2.0 / kSqrtPi * a;
+        pre_hi = real(p);
+        pre_lo = real(p - double(pre_hi));
+        a2x2 = real(2.0 * a * a);
+    }
+    MPID_HD real times(real r) const { return hi * r + lo * r; }
+};
+
 // b_n (n = 0..NMAX) of erf(alpha r)/r for alpha r below the quadrature threshold.
 template <typename real, int NMAX>
-MPID_HD void erf_part_quadrature(real r, real alpha, real* bF) {
+MPID_HD void erf_part_quadrature(real r, const EwaldAlpha<real>& al, real* bF) {
     constexpr int K = Prec<real>::kQuadNodes;
     real acc[NMAX + 1];
 #pragma unroll
     for (int n = 0; n <= NMAX; ++n) acc[n] = real(0);
-    const real x2 = alpha * alpha * r * r;
+    const real x = al.times(r);
+    const real x2 = x * x;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const real v = GaussLegendre01<real, K>::node(k);
@@ -100,29 +120,27 @@ MPID_HD void erf_part_quadrature(real r, real alpha, real* bF) {
             term *= v2;
         }
     }
-    // prefactor 2^(n+1) alpha^(2n+1) / sqrt(pi)
-    real pre = real(2.0 / kSqrtPi) * alpha;
-    const real twoA2 = real(2) * alpha * alpha;
+    // prefactor 2^(n+1) alpha^(2n+1) / sqrt(pi), the leading factor kept as hi + lo
+    real scale = real(1);
 #pragma unroll
     for (int n = 0; n <= NMAX; ++n) {
-        bF[n] = pre * acc[n];
-        pre *= twoA2;
+        bF[n] = (al.pre_hi * acc[n] + al.pre_lo * acc[n]) * scale;
+        scale *= al.a2x2;
     }
 }
 
 // b_n of erfc(alpha r)/r by upward recursion (all terms positive).
 template <typename real, int NMAX>
-MPID_HD void erfc_part(real r, real rinv2, real alpha, real* bE) {
-    const real ar = alpha * r;
+MPID_HD void erfc_part(real r, real rinv2, const EwaldAlpha<real>& al, real* bE) {
+    const real ar = al.times(r);
     const real ex = m_exp(-ar * ar);
     bE[0] = m_erfc(ar) / r;
     // c_n = (2 alpha^2)^n / (alpha sqrt(pi)) * exp(-alpha^2 r^2), starting at n = 1
-    real c = real(2.0 / kSqrtPi) * alpha * ex;
-    const real twoA2 = real(2) * alpha * alpha;
+    real c = (al.pre_hi + al.pre_lo) * ex;
 #pragma unroll
     for (int n = 1; n <= NMAX; ++n) {
         bE[n] = (real(2 * n - 1) * bE[n - 1] + c) * rinv2;
-        c *= twoA2;
+        c *= al.a2x2;
     }
 }
 
@@ -202,7 +220,7 @@ struct PairRadial {
 
 // Compute the requested radial arrays.  NP/NI/NU < 0 disables a kernel.
 template <typename real, int NP, int NI, int NU>
-MPID_HD void pair_radial(real r, real alpha, real scale, real tholeA, real dampProd, PairRadial<real, (NP > 0 ? NP : 0), (NI > 0 ? NI : 0), (NU > 0 ? NU : 0)>& out) {
+MPID_HD void pair_radial(real r, const EwaldAlpha<real>& alpha, real scale, real tholeA, real dampProd, PairRadial<real, (NP > 0 ? NP : 0), (NI > 0 ? NI : 0), (NU > 0 ? NU : 0)>& out) {
     constexpr int NMAX = (NP > NI ? (NP > NU ? NP : NU) : (NI > NU ? NI : NU));
     const real rinv = real(1) / r;
     const real rinv2 = rinv * rinv;
@@ -221,7 +239,7 @@ MPID_HD void pair_radial(real r, real alpha, real scale, real tholeA, real dampP
             thole_lambdas<real, NT>(sT, lam, oneMinus);
         }
     }
-    const real x = alpha * r;
+    const real x = alpha.times(r);
     if (x < real(Prec<real>::kQuadX)) {
         real bF[NMAX + 1];
         erf_part_quadrature<real, NMAX>(r, alpha, bF);

@@ -99,7 +99,9 @@ def test_zonly_matches_energy_gradient():
     fx, s, f = _fixture_case("frames_direct.npz")
     ctx = MPIDContext(f, precision="double")
     e0, forces = ctx.evaluate(s.pos, s.box)
-    h = 2e-4
+    # a small step keeps every pair on its side of the cutoff, where the real-space
+    # energy is discontinuous; FP64 energies make the difference quotient precise
+    h = 1e-5
 
     def energy_at(atom, c, delta):
         p = s.pos.copy()
@@ -108,10 +110,8 @@ def test_zonly_matches_energy_gradient():
 
     for atom in sorted(_torque_mapped_zonly(s))[:6]:
         for c in range(3):
-            # fourth-order central difference
-            fd = -(8 * (energy_at(atom, c, h) - energy_at(atom, c, -h)) -
-                   (energy_at(atom, c, 2 * h) - energy_at(atom, c, -2 * h))) / (12 * h)
-            assert abs(fd - forces[atom, c]) < 2e-5 * max(1.0, abs(fd)), (atom, c, fd, forces[atom, c])
+            fd = -(energy_at(atom, c, h) - energy_at(atom, c, -h)) / (2 * h)
+            assert abs(fd - forces[atom, c]) < 1e-5 * max(1.0, abs(fd)), (atom, c, fd, forces[atom, c])
 
 
 def test_forces_are_accumulated_and_deterministic():
