@@ -20,6 +20,7 @@ With torchrun (N > 1) every rank evaluates its own replica (replicas only; no da
 exchanged) and `value` is the sum over ranks.
 """
 import argparse
+import datetime
 import json
 import os
 import subprocess
@@ -75,7 +76,7 @@ class ClockSampler:
             os.path.join(ROOT, "gpurun_out")) else "/tmp/mpid_bench_clocks.csv"
 
     def __enter__(self):
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
@@ -93,21 +94,28 @@ class ClockSampler:
             self.proc.wait()
             self.f.close()
 
+    def mark(self, which):
+        setattr(self, which, datetime.datetime.now())
+
     def summary(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        t0, t1 = getattr(self, "start", None), getattr(self, "stop", None)
         for line in open(self.path):
             p = [x.strip() for x in line.split(",")]
-            if len(p) < 9:
+            if len(p) < 10:
                 continue
             try:
-                sm.append(float(p[1]))
-                smax = float(p[2])
+                ts = datetime.datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f")
+                if t0 and t1 and not (t0 <= ts <= t1):
+                    continue
+                sm.append(float(p[2]))
+                smax = float(p[3])
             except ValueError:
                 continue
-            for nm, v in zip(names, p[5:9]):
+            for nm, v in zip(names, p[6:10]):
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
@@ -122,10 +130,15 @@ def count_pairs_within(pos, box, cutoff):
     return int(len(tree.query_pairs(cutoff, output_type="ndarray")))
 
 
-# Source-counted FP32 operations (FMA = 2) per interacting pair of the energy/force/torque
-# pair kernel (pair_radial<7,5,3> + qi_pair<MUTUAL>, mpid_math.cuh), used for the
-# algorithmic throughput of that kernel.
-PAIR_KERNEL_FLOP_PER_PAIR = 1900
+# FP32 operations per interacting pair (add/mul = 1, FMA = 2, div/sqrt/exp/erfc = 1),
+# counted from the kernels' own source by mpidopenmmplugin_gb300/csrc/flop_count.cpp and
+# averaged over the pair-distance distribution of a 0.9 nm cutoff with alpha = 3.4/nm.
+FLOP_PER_PAIR = {"pair_kernel": 2714,          # k_electrostatics<float, MUTUAL>
+                 "dipole_field_pairs": 148,    # k_dipole_field<float>
+                 "fixed_field_pairs": 464}     # k_fixed_field<float>
+KERNEL_NAMES = {"pair_kernel": "k_electrostatics<float, mutual> (energy/force/torque pair kernel)",
+                "dipole_field_pairs": "k_dipole_field<float> (T.mu pair kernel of the CG solver)",
+                "fixed_field_pairs": "k_fixed_field<float> (permanent-field pair kernel)"}
 
 
 def run_reference(args, world, rank):
@@ -180,7 +193,7 @@ def cpu_baseline_sample():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -217,19 +230,25 @@ def main():
     # timed region: events around each step on the launching stream, L2 flushed between steps
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    stage_ms = {}
+    stage_ms, stage_n = {}, {}
+    launches = 0
     with ClockSampler(local) as clocks:
+        time.sleep(0.5)  # let the sampler start
         barrier(world)
         torch.cuda.synchronize()
+        clocks.mark("start")
         for k in range(args.steps):
             flush.zero_()
             starts[k].record(stream)
             step()
             ends[k].record(stream)
             st = ctx.stats()
+            launches += st["kernel_launches"]
             for name, v in st["ms_stage"].items():
                 stage_ms[name] = stage_ms.get(name, 0.0) + v
+                stage_n[name] = stage_n.get(name, 0) + st["stage_launches"][name]
         torch.cuda.synchronize()
+        clocks.mark("stop")
         barrier(world)
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
     ms = max_over_ranks(ms, world)
@@ -237,8 +256,10 @@ def main():
     stats = ctx.stats()
 
     # end to end through the host-buffer API: positions + forces in, forces + energy out
-    hpos = np.ascontiguousarray(pos)
-    hforce = np.zeros((n, 3))
+    # pinned host buffers (the caller's positions and force array)
+    hpos = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hpos[:] = pos
+    hforce = torch.zeros((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     for _ in range(2):
         ctx.evaluate(hpos, box, forces=hforce)
     torch.cuda.synchronize()
@@ -248,19 +269,6 @@ def main():
         e_mixed, fm = ctx.evaluate(hpos, box, forces=hforce)
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
     e2e_ms = max_over_ranks(e2e_ms, world)
-
-    # kernel launches per step (CUDA activity of one untimed step)
-    launches = None
-    try:
-        from torch.profiler import ProfilerActivity, profile
-        with profile(activities=[ProfilerActivity.CUDA]) as prof:
-            step()
-            torch.cuda.synchronize()
-        names = [e.name for e in prof.events() if e.device_type is not None and str(e.device_type).endswith("CUDA")]
-        ours = [nm for nm in names if "mpid" in nm or nm.startswith("_ZN4mpid") or nm.startswith("void mpid::")]
-        launches = len(ours) * args.steps
-    except Exception:
-        launches = None
 
     line = None
     if rank == 0:
@@ -278,10 +286,13 @@ def main():
             fp64 = {"fp64_evals_per_s": 1000.0 / fp64_ms, "speedup_vs_fp64": fp64_ms / ms,
                     "energy_rel_err": abs(em - ed) / abs(ed), "force_rel_rms_err": helpers.rel_rms(fmix, fd),
                     "dipole_rel_rms_err": helpers.rel_rms(ctx.getInducedDipoles(), cd.getInducedDipoles())}
-        # roofline of the dominant kernel (the energy/force/torque pair kernel)
+        # roofline of the dominant kernel: the pair kernel with the largest device time in
+        # the timed region; per launch = FLOP/pair x pairs within the cutoff
         npairs = count_pairs_within(pos, box, 0.9)
-        pair_ms = stage_ms.get("pair_kernel", 0.0) / args.steps
-        achieved = PAIR_KERNEL_FLOP_PER_PAIR * npairs / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else None
+        dom = max(FLOP_PER_PAIR, key=lambda k: stage_ms.get(k, 0.0))
+        nl = max(1, stage_n.get(dom, 0))
+        pair_ms = stage_ms.get(dom, 0.0) / nl
+        achieved = FLOP_PER_PAIR[dom] * npairs / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else None
         peaks = {}
         try:
             peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -291,13 +302,14 @@ def main():
         # FP32 CUDA-core peak: 152 SMs x 128 FP32 lanes x 2 FLOP/FMA x SM clock
         sm_mhz = clk.get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-        roofline = {"bound": "fp32", "kernel": "k_electrostatics (energy/force/torque pair kernel)",
+        roofline = {"bound": "fp32", "kernel": KERNEL_NAMES[dom],
                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                     "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
                     "peak_source": "152 SMs x 128 FP32 lanes x 2 x max SM clock (no measured FP32 peak in "
                                    "MEASURED_PEAKS.json)",
-                    "pairs_within_cutoff": npairs, "flop_per_pair": PAIR_KERNEL_FLOP_PER_PAIR,
-                    "ms_per_launch": pair_ms}
+                    "pairs_within_cutoff": npairs, "flop_per_pair": FLOP_PER_PAIR[dom],
+                    "ms_per_launch": pair_ms, "launches_per_step": nl / args.steps,
+                    "share_of_step": stage_ms.get(dom, 0.0) / args.steps / ms}
         cpu = None
         if not args.no_cpu_baseline:
             try:

@@ -73,10 +73,13 @@ typedef struct {
     /* device time (ms) and timed launch groups per stage: 0 sort/tiles/atom set-up,
      * 1 permanent-field pair kernel, 2 PME spread/FFT/convolution/gather, 3 dipole-field
      * pair kernels, 4 solver vector work, 5 energy/force/torque pair kernel,
-     * 6 reciprocal/self terms and torque mapping */
+     * 6 reciprocal/self terms and torque mapping, 7 FP64 dipole-field pair kernel of the
+     * mixed path's residual refinement */
     double ms_stage[8];
     int stage_launches[8];
     double energy_parts[3];    /* reciprocal + self, real-space pairs, covalently scaled pairs */
+    int kernel_launches;       /* launches of this library's kernels in the last evaluation */
+    int library_calls;         /* cuFFT executions and cub sorts in the last evaluation */
 } mpid_stats;
 
 /* Fill `s` with the MPIDForce defaults for n atoms (PME not configured). */

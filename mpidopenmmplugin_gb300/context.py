@@ -53,10 +53,13 @@ class Stats(ctypes.Structure):
         ("ms_stage", ctypes.c_double * 8),
         ("stage_launches", ctypes.c_int * 8),
         ("energy_parts", ctypes.c_double * 3),
+        ("kernel_launches", ctypes.c_int),
+        ("library_calls", ctypes.c_int),
     ]
 
 
-STAGES = ["setup", "fixed_field_pairs", "pme", "dipole_field_pairs", "solver_vectors", "pair_kernel", "recip_self_torque"]
+STAGES = ["setup", "fixed_field_pairs", "pme", "dipole_field_pairs", "solver_vectors", "pair_kernel", "recip_self_torque",
+          "refinement_field_pairs"]
 
 
 _LIB = None
@@ -212,7 +215,8 @@ class MPIDContext:
                     ms_stage={STAGES[k]: s.ms_stage[k] for k in range(len(STAGES))},
                     stage_launches={STAGES[k]: s.stage_launches[k] for k in range(len(STAGES))},
                     energy_parts=dict(recip_self=s.energy_parts[0], real_space=s.energy_parts[1],
-                                      scaled_pairs=s.energy_parts[2]))
+                                      scaled_pairs=s.energy_parts[2]),
+                    kernel_launches=s.kernel_launches, library_calls=s.library_calls)
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

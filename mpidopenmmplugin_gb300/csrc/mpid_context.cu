@@ -15,6 +15,7 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "mpid_gb300.h"
@@ -42,6 +43,18 @@ struct Error : std::runtime_error {
 
 static inline int nblk(long long n, int b) { return (int) ((n + b - 1) / b); }
 
+// Kernel launches made by this thread (every launch of the library goes through
+// launch(); evaluations report their own count).
+static thread_local long long t_launches = 0;
+
+template <typename... KArgs, typename... Args>
+static inline void launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args&&... args) {
+    kernel<<<grid, block, smem, st>>>(std::forward<Args>(args)...);
+    ++t_launches;
+}
+// cuFFT executions and cub sorts (library code launching its own kernels).
+static thread_local long long t_library_calls = 0;
+
 // Simple owning device buffer.
 template <typename T>
 struct DBuf {
@@ -65,13 +78,13 @@ struct DBuf {
 template <typename real> struct FftTypes;
 template <> struct FftTypes<float> {
     static constexpr cufftType fwd = CUFFT_R2C, inv = CUFFT_C2R;
-    static void exec_fwd(cufftHandle h, float* in, float2* out) { CUFFT_CHECK(cufftExecR2C(h, in, (cufftComplex*) out)); }
-    static void exec_inv(cufftHandle h, float2* in, float* out) { CUFFT_CHECK(cufftExecC2R(h, (cufftComplex*) in, out)); }
+    static void exec_fwd(cufftHandle h, float* in, float2* out) { ++t_library_calls; CUFFT_CHECK(cufftExecR2C(h, in, (cufftComplex*) out)); }
+    static void exec_inv(cufftHandle h, float2* in, float* out) { ++t_library_calls; CUFFT_CHECK(cufftExecC2R(h, (cufftComplex*) in, out)); }
 };
 template <> struct FftTypes<double> {
     static constexpr cufftType fwd = CUFFT_D2Z, inv = CUFFT_Z2D;
-    static void exec_fwd(cufftHandle h, double* in, double2* out) { CUFFT_CHECK(cufftExecD2Z(h, in, (cufftDoubleComplex*) out)); }
-    static void exec_inv(cufftHandle h, double2* in, double* out) { CUFFT_CHECK(cufftExecZ2D(h, (cufftDoubleComplex*) in, out)); }
+    static void exec_fwd(cufftHandle h, double* in, double2* out) { ++t_library_calls; CUFFT_CHECK(cufftExecD2Z(h, in, (cufftDoubleComplex*) out)); }
+    static void exec_inv(cufftHandle h, double2* in, double* out) { ++t_library_calls; CUFFT_CHECK(cufftExecZ2D(h, (cufftDoubleComplex*) in, out)); }
 };
 
 // One precision's PME machinery: B-spline tables of the sorted atoms, accumulation
@@ -115,30 +128,30 @@ struct PmeStage {
     }
     void bsplines(int n, int npad, const int* sorted, const double* wpos, const BoxDev& box, cudaStream_t st) {
         if (order == 5)
-            k_bsplines<real, 5><<<nblk(npad, 128), 128, 0, st>>>(npad, n, sorted, wpos, box, theta.p, igrid.p);
+            launch(k_bsplines<real, 5>, nblk(npad, 128), 128, 0, st, npad, n, sorted, wpos, box, theta.p, igrid.p);
         else
-            k_bsplines<real, 6><<<nblk(npad, 128), 128, 0, st>>>(npad, n, sorted, wpos, box, theta.p, igrid.p);
+            launch(k_bsplines<real, 6>, nblk(npad, 128), 128, 0, st, npad, n, sorted, wpos, box, theta.p, igrid.p);
     }
     template <int NCOMP>
     void spread(int n, int npad, const BoxDev& box, const real* mf, const int* skip, cudaStream_t st) {
         const long long threads = (long long) n * order * order;
         if (order == 5)
-            k_spread<real, 5, NCOMP><<<nblk(threads, 256), 256, 0, st>>>(n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
+            launch(k_spread<real, 5, NCOMP>, nblk(threads, 256), 256, 0, st, n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
         else
-            k_spread<real, 6, NCOMP><<<nblk(threads, 256), 256, 0, st>>>(n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
-        k_grid_finish<real><<<std::min<long long>(nblk(G, 256), 152 * 16), 256, 0, st>>>(G, acc.p, rgrid.p, skip);
+            launch(k_spread<real, 6, NCOMP>, nblk(threads, 256), 256, 0, st, n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
+        launch(k_grid_finish<real>, std::min<long long>(nblk(G, 256), 152 * 16), 256, 0, st, G, acc.p, rgrid.p, skip);
     }
     void convolve(const double* influence, const int* skip, cudaStream_t st) {
         FftTypes<real>::exec_fwd(fwd, rgrid.p, cgrid.p);
-        k_convolve<real><<<std::min<long long>(nblk(Gh, 256), 152 * 16), 256, 0, st>>>(Gh, influence, cgrid.p, skip);
+        launch(k_convolve<real>, std::min<long long>(nblk(Gh, 256), 152 * 16), 256, 0, st, Gh, influence, cgrid.p, skip);
         FftTypes<real>::exec_inv(inv, cgrid.p, rgrid.p);
     }
     template <int NTERM>
     void gather(int n, int npad, const BoxDev& box, real* phi, const int* skip, cudaStream_t st) {
         if (order == 5)
-            k_gather<real, 5, NTERM><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, theta.p, igrid.p, rgrid.p, phi, skip);
+            launch(k_gather<real, 5, NTERM>, nblk(npad, 128), 128, 0, st, n, npad, box, theta.p, igrid.p, rgrid.p, phi, skip);
         else
-            k_gather<real, 6, NTERM><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, theta.p, igrid.p, rgrid.p, phi, skip);
+            launch(k_gather<real, 6, NTERM>, nblk(npad, 128), 128, 0, st, n, npad, box, theta.p, igrid.p, rgrid.p, phi, skip);
     }
 };
 
@@ -193,7 +206,7 @@ struct Engine {
 };
 
 // Device time of the evaluation stages, from CUDA events on the launching stream.
-enum Stage { ST_SETUP = 0, ST_FIXED_REAL, ST_PME, ST_DIPOLE_REAL, ST_SOLVER, ST_PAIR, ST_FINISH, ST_COUNT };
+enum Stage { ST_SETUP = 0, ST_FIXED_REAL, ST_PME, ST_DIPOLE_REAL, ST_SOLVER, ST_PAIR, ST_FINISH, ST_REFINE_REAL, ST_COUNT };
 
 struct StageTimer {
     static constexpr int kMax = 4096;
@@ -541,7 +554,7 @@ struct Context {
             for (int i = 0; i < 3; ++i) box.A[j][i] = (usePme && i == j) ? set.grid[j] / L[j] : 0.0;
         if (usePme && std::memcmp(lastBox, b, sizeof(lastBox)) != 0) {
             const size_t Gh = (size_t) set.grid[0] * set.grid[1] * (set.grid[2] / 2 + 1);
-            k_influence<<<std::min<long long>(nblk(Gh, 256), 152 * 8), 256, 0, stream>>>(
+            launch(k_influence, std::min<long long>(nblk(Gh, 256), 152 * 8), 256, 0, stream, 
                 box, set.ewald_alpha, modx.p, mody.p, modz.p, 1.0 / L[0], 1.0 / L[1], 1.0 / L[2], L[0] * L[1] * L[2],
                 influence.p);
             CUDA_CHECK(cudaGetLastError());
@@ -576,7 +589,8 @@ struct Context {
             const double edge = std::cbrt(32.0 * vol / n);
             const int ncx = std::max(1, (int) std::lround(box.L[0] / edge));
             const int ncy = std::max(1, (int) std::lround(box.L[1] / edge));
-            k_sort_keys<<<nblk(n, 256), 256, 0, st>>>(n, pos.p, box, ncx, ncy, keys.p, orderAlt.p, wpos.p);
+            launch(k_sort_keys, nblk(n, 256), 256, 0, st, n, pos.p, box, ncx, ncy, keys.p, orderAlt.p, wpos.p);
+            ++t_library_calls;
             CUDA_CHECK(cub::DeviceRadixSort::SortPairs(cubTemp.p, cubBytes, keys.p, keysAlt.p, orderAlt.p, order.p, n, 0,
                                                         64, st));
         } else {
@@ -587,11 +601,11 @@ struct Context {
             CUDA_CHECK(cudaMemcpyAsync(wpos.p, pos.p, 3 * n * 8, cudaMemcpyDeviceToDevice, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
         }
-        k_tile_bounds<<<nblk(ntiles, 128), 128, 0, st>>>(n, ntiles, order.p, wpos.p, center.p, half.p);
+        launch(k_tile_bounds, nblk(ntiles, 128), 128, 0, st, n, ntiles, order.p, wpos.p, center.p, half.p);
         for (int attempt = 0; attempt < 3; ++attempt) {
             CUDA_CHECK(cudaMemsetAsync(npairs.p, 0, sizeof(int), st));
             const long long total = (long long) ntiles * (ntiles + 1) / 2;
-            k_tile_pairs<<<nblk(total, 256), 256, 0, st>>>(ntiles, center.p, half.p, box, usePme ? set.cutoff : 1e30,
+            launch(k_tile_pairs, nblk(total, 256), 256, 0, st, ntiles, center.p, half.p, box, usePme ? set.cutoff : 1e30,
                                                            usePme ? 1 : 0, pairs.p, npairs.p, pairCapacity);
             CUDA_CHECK(cudaGetLastError());
             int cnt = 0;
@@ -619,6 +633,7 @@ struct Context {
         cudaStream_t st = stream;
         CUDA_CHECK(cudaMemcpyAsync(pairKeys.p, pairs.p, cnt * sizeof(int2), cudaMemcpyDeviceToDevice, st));
         // int2 (x = I, y = J) read as a 64-bit key: J in the high word, so sort by (J, I)
+        ++t_library_calls;
         CUDA_CHECK(cub::DeviceRadixSort::SortKeys(cubTemp2.p, cubBytes2, pairKeys.p, pairKeysAlt.p, cnt, 0, 64, st));
         CUDA_CHECK(cudaMemcpyAsync(pairs.p, pairKeysAlt.p, cnt * sizeof(int2), cudaMemcpyDeviceToDevice, st));
     }
@@ -626,12 +641,12 @@ struct Context {
     template <typename real>
     void prepare_engine(Engine<real>& e, bool main) {
         cudaStream_t st = stream;
-        k_gather_atoms<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, order.p, mol(), pos.p, wpos.p, center.p, e.arrays(),
+        launch(k_gather_atoms<real>, nblk(npad, 128), 128, 0, st, n, npad, order.p, mol(), pos.p, wpos.p, center.p, e.arrays(),
                                                                main ? mom64.p : nullptr, main ? prm64.p : nullptr);
         if (usePme) {
             e.pme.set_stream(st);
             e.pme.bsplines(n, npad, order.p, wpos.p, box, st);
-            k_frac_multipoles<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, e.mom.p, e.mf.p);
+            launch(k_frac_multipoles<real>, nblk(npad, 128), 128, 0, st, npad, box, e.mom.p, e.mf.p);
         }
         CUDA_CHECK(cudaGetLastError());
     }
@@ -646,7 +661,7 @@ struct Context {
         cudaStream_t st = stream;
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
         timer.begin(ST_FIXED_REAL, st);
-        k_fixed_field<real><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tile_ctx(), e.arrays(), e.fieldFx.p);
+        launch(k_fixed_field<real>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tile_ctx(), e.arrays(), e.fieldFx.p);
         timer.end(st);
         if (usePme) {
             timer.begin(ST_PME, st);
@@ -655,7 +670,7 @@ struct Context {
             e.pme.template gather<35>(n, npad, box, e.phiP.p, nullptr, st);
             timer.end(st);
         }
-        k_record_fixed<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, self_coef(), e.fieldFx.p,
+        launch(k_record_fixed<real>, nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
                                                                usePme ? e.phiP.p : nullptr, e.arrays(), e.Efix.p, e.muD.p,
                                                                e.SE.p);
         CUDA_CHECK(cudaGetLastError());
@@ -666,19 +681,20 @@ struct Context {
     void dipole_field(Engine<real>& e, const real* mu, real* E, real* G, const int* skip, int nterm = 4) {
         cudaStream_t st = stream;
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
-        timer.begin(ST_DIPOLE_REAL, st);
+        // the FP64 field of the mixed path's residual refinement is timed on its own
+        timer.begin(mixed && sizeof(real) == 8 ? ST_REFINE_REAL : ST_DIPOLE_REAL, st);
         if (G) {
             CUDA_CHECK(cudaMemsetAsync(e.gradFx.p, 0, 6 * (size_t) npad * 8, st));
-            k_dipole_field<real, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tile_ctx(), e.arrays(), mu, e.fieldFx.p,
+            launch(k_dipole_field<real, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tile_ctx(), e.arrays(), mu, e.fieldFx.p,
                                                                                      e.gradFx.p, skip);
         } else {
-            k_dipole_field<real, false><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tile_ctx(), e.arrays(), mu,
+            launch(k_dipole_field<real, false>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tile_ctx(), e.arrays(), mu,
                                                                                       e.fieldFx.p, nullptr, skip);
         }
         timer.end(st);
         if (usePme) {
             timer.begin(ST_PME, st);
-            k_frac_dipoles<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, mu, e.mfd.p, skip);
+            launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, st, npad, box, mu, e.mfd.p, skip);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, skip, st);
             e.pme.convolve(influence.p, skip, st);
             if (nterm == 4)
@@ -689,7 +705,7 @@ struct Context {
                 e.pme.template gather<35>(n, npad, box, e.phiT.p, skip, st);
             timer.end(st);
         }
-        k_dipole_field_total<real><<<nblk(npad, 128), 128, 0, st>>>(n, npad, box, self_coef(), e.fieldFx.p, e.gradFx.p,
+        launch(k_dipole_field_total<real>, nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p, e.gradFx.p,
                                                                      usePme ? e.phiT.p : nullptr, nterm, mu, E, G, skip);
         CUDA_CHECK(cudaGetLastError());
     }
@@ -701,21 +717,21 @@ struct Context {
                  double* finalMetric) {
         cudaStream_t st = stream;
         const int nb = nblk(npad, 256);
-        k_cg_start<real, xreal><<<nb, 256, 0, st>>>(npad, e.sroot.p, b, x, r, p, partial.p, nb);
-        k_reduce_partials<<<1, 1024, 0, st>>>(nb, 2, partial.p, red.p, nullptr);
-        k_cg_init_scalars<<<1, 1, 0, st>>>(sc.p, red.p, n, target, iter.p, done.p);
+        launch(k_cg_start<real, xreal>, nb, 256, 0, st, npad, e.sroot.p, b, x, r, p, partial.p, nb);
+        launch(k_reduce_partials, 1, 1024, 0, st, nb, 2, partial.p, red.p, nullptr);
+        launch(k_cg_init_scalars, 1, 1, 0, st, sc.p, red.p, n, target, iter.p, done.p);
         CUDA_CHECK(cudaGetLastError());
         int it = 0;
         for (it = 0; it < maxIter; ++it) {
             // q = B p
-            k_apply_sroot<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, e.sroot.p, p, e.sp.p, nullptr, done.p);
+            launch(k_apply_sroot<real>, nblk(npad, 128), 128, 0, st, npad, box, e.sroot.p, p, e.sp.p, nullptr, done.p);
             dipole_field(e, e.sp.p, e.Etmp.p, (real*) nullptr, done.p, 4);
-            k_cg_finish_matvec<real><<<nb, 256, 0, st>>>(npad, e.sroot.p, p, e.Etmp.p, q, partial.p, done.p);
-            k_reduce_partials<<<1, 1024, 0, st>>>(nb, 1, partial.p, sc.p + 1, done.p);
-            k_cg_update<real, xreal><<<nb, 256, 0, st>>>(npad, e.sroot.p, sc.p, p, q, x, r, partial.p, nb, done.p);
-            k_reduce_partials<<<1, 1024, 0, st>>>(nb, 2, partial.p, red.p, done.p);
-            k_cg_scalars<<<1, 1, 0, st>>>(sc.p, red.p, n, target, iter.p, maxIter, done.p);
-            k_cg_direction<real><<<nblk(npad, 128), 128, 0, st>>>(npad, sc.p, r, p, done.p);
+            launch(k_cg_finish_matvec<real>, nb, 256, 0, st, npad, e.sroot.p, p, e.Etmp.p, q, partial.p, done.p);
+            launch(k_reduce_partials, 1, 1024, 0, st, nb, 1, partial.p, sc.p + 1, done.p);
+            launch(k_cg_update<real, xreal>, nb, 256, 0, st, npad, e.sroot.p, sc.p, p, q, x, r, partial.p, nb, done.p);
+            launch(k_reduce_partials, 1, 1024, 0, st, nb, 2, partial.p, red.p, done.p);
+            launch(k_cg_scalars, 1, 1, 0, st, sc.p, red.p, n, target, iter.p, maxIter, done.p);
+            launch(k_cg_direction<real>, nblk(npad, 128), 128, 0, st, npad, sc.p, r, p, done.p);
             CUDA_CHECK(cudaGetLastError());
             const int slot = it % (int) iterEvents.size();
             CUDA_CHECK(cudaMemcpyAsync(hostDone + (slot % 256), done.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -738,7 +754,7 @@ struct Context {
 
     template <typename real>
     void alpha_times(Engine<real>& e, const real* E, real* out) {
-        k_alpha_times<real><<<nblk(npad, 128), 128, 0, stream>>>(npad, e.alab.p, E, out);
+        launch(k_alpha_times<real>, nblk(npad, 128), 128, 0, stream, npad, e.alab.p, E, out);
     }
 
     // Induced dipoles into e.mu (sorted) for the configured polarisation type.
@@ -769,7 +785,7 @@ struct Context {
             }
             CUDA_CHECK(cudaMemsetAsync(e.mu.p, 0, n3 * sizeof(real), st));
             for (int m = 0; m < nPT; ++m)
-                k_axpy<real><<<nblk((long long) n3, 256), 256, 0, st>>>((int) n3, real(cbar[m]), ptMu + m * n3, e.mu.p);
+                launch(k_axpy<real>, nblk((long long) n3, 256), 256, 0, st, (int) n3, real(cbar[m]), ptMu + m * n3, e.mu.p);
             stats.solver_iterations = nPT - 1;
             CUDA_CHECK(cudaGetLastError());
             return;
@@ -782,7 +798,7 @@ struct Context {
         int it = cg_solve<double, double>(e, e.SE.p, y64.p, r64.p, p64.p, q64.p, set.mutual_eps, set.max_iter, &metric);
         stats.solver_iterations = it;
         stats.solver_residual = metric;
-        k_mu_from_y<double, double><<<nblk(npad, 128), 128, 0, stream>>>(npad, e.sroot.p, y64.p, e.mu.p);
+        launch(k_mu_from_y<double, double>, nblk(npad, 128), 128, 0, stream, npad, e.sroot.p, y64.p, e.mu.p);
         if (!(metric < set.mutual_eps)) not_converged(it, metric);
     }
 
@@ -793,7 +809,7 @@ struct Context {
         const size_t n3 = 3 * (size_t) npad;
         // Efix in FP64 for the residual
         CUDA_CHECK(cudaMemsetAsync(Efix64.p, 0, n3 * 8, st));
-        k_axpy_to_double<float><<<nblk((long long) n3, 256), 256, 0, st>>>((int) n3, e.Efix.p, Efix64.p);
+        launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3, e.Efix.p, Efix64.p);
         CUDA_CHECK(cudaMemsetAsync(y64.p, 0, n3 * 8, st));
         CUDA_CHECK(cudaMemcpyAsync(b32.p, e.SE.p, n3 * 4, cudaMemcpyDeviceToDevice, st));
         int total = 0;
@@ -804,12 +820,12 @@ struct Context {
             const int it = cg_solve<float, float>(e, b32.p, x32.p, r32.p, p32.p, q32.p, innerTarget,
                                                   std::max(1, set.max_iter - total), &innerMetric);
             total += it;
-            k_axpy_to_double<float><<<nblk((long long) n3, 256), 256, 0, st>>>((int) n3, x32.p, y64.p);
+            launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3, x32.p, y64.p);
             // FP64 residual res = S (E + T S y) - y
-            k_mu_from_y<double, double><<<nblk(npad, 128), 128, 0, st>>>(npad, d.sroot.p, y64.p, d.mu.p);
+            launch(k_mu_from_y<double, double>, nblk(npad, 128), 128, 0, st, npad, d.sroot.p, y64.p, d.mu.p);
             dipole_field(d, d.mu.p, d.Etmp.p, (double*) nullptr, nullptr, 4);
-            k_refine_residual<<<nb, 256, 0, st>>>(npad, d.sroot.p, Efix64.p, d.Etmp.p, y64.p, res64.p, res32.p, partial.p);
-            k_reduce_partials<<<1, 1024, 0, st>>>(nb, 1, partial.p, red.p, nullptr);
+            launch(k_refine_residual, nb, 256, 0, st, npad, d.sroot.p, Efix64.p, d.Etmp.p, y64.p, res64.p, res32.p, partial.p);
+            launch(k_reduce_partials, 1, 1024, 0, st, nb, 1, partial.p, red.p, nullptr);
             double s2 = 0.0;
             CUDA_CHECK(cudaMemcpyAsync(&s2, red.p, 8, cudaMemcpyDeviceToHost, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
@@ -820,7 +836,7 @@ struct Context {
         }
         stats.solver_iterations = total;
         stats.solver_residual = metric;
-        k_mu_from_y<double, float><<<nblk(npad, 128), 128, 0, st>>>(npad, d.sroot.p, y64.p, e.mu.p);
+        launch(k_mu_from_y<double, float>, nblk(npad, 128), 128, 0, st, npad, d.sroot.p, y64.p, e.mu.p);
         if (!(metric < set.mutual_eps)) not_converged(total, metric);
     }
 
@@ -836,7 +852,7 @@ struct Context {
         if (usePme) {
             // reciprocal potential of the final induced dipoles (35 terms)
             timer.begin(ST_PME, st);
-            k_frac_dipoles<real><<<nblk(npad, 128), 128, 0, st>>>(npad, box, e.mu.p, e.mfd.p, nullptr);
+            launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, st, npad, box, e.mu.p, e.mfd.p, nullptr);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, nullptr, st);
             e.pme.convolve(influence.p, nullptr, st);
             e.pme.template gather<35>(n, npad, box, e.phiD.p, nullptr, st);
@@ -851,13 +867,13 @@ struct Context {
         const TileCtx tc = tile_ctx();
         const AtomArrays<real> aa = e.arrays();
         if (set.polarization_type == MPID_MUTUAL && !exact)
-            k_electrostatics<real, true, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
+            launch(k_electrostatics<real, true, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                              torqueFx.p, energyBlocks.p);
         else if (set.polarization_type == MPID_MUTUAL)
-            k_electrostatics<real, true, false><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
+            launch(k_electrostatics<real, true, false>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
         else
-            k_electrostatics<real, false, true><<<pair_blocks(), 32 * kWarpsPerBlock, 0, st>>>(tc, aa, e.mu.p, forceFx.p,
+            launch(k_electrostatics<real, false, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
         timer.end(st);
         timer.begin(ST_FINISH, st);
@@ -873,29 +889,29 @@ struct Context {
             opt.G = ptG;
         }
         const int nb = nblk(npad, 256);
-        k_recip_self<real><<<nb, 256, 0, st>>>(n, npad, box, set.ewald_alpha, set.polarization_type,
+        launch(k_recip_self<real>, nb, 256, 0, st, n, npad, box, set.ewald_alpha, set.polarization_type,
                                                 usePme ? e.phiP.p : nullptr, e.phiD.p, e.mu.p, e.arrays(), mom64.p, opt,
                                                 forceFx.p, torqueFx.p, energyPartial.p);
-        k_reduce_partials<<<1, 1024, 0, st>>>(nb, 1, energyPartial.p, energyOut.p, nullptr);
-        k_reduce_partials<<<1, 1024, 0, st>>>(eb, 1, energyBlocks.p, energyOut.p + 1, nullptr);
+        launch(k_reduce_partials, 1, 1024, 0, st, nb, 1, energyPartial.p, energyOut.p, nullptr);
+        launch(k_reduce_partials, 1, 1024, 0, st, eb, 1, energyBlocks.p, energyOut.p + 1, nullptr);
         if (nScaled) {
             const int sb = nblk(nScaled, 128);
             const int muIsFloat = sizeof(real) == 4 ? 1 : 0;
             if (set.polarization_type == MPID_MUTUAL)
-                k_scaled_pair_energy<true><<<sb, 128, 0, st>>>(nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad, mom64.p,
+                launch(k_scaled_pair_energy<true>, sb, 128, 0, st, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad, mom64.p,
                                                                prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0,
                                                                set.cutoff, usePme ? set.ewald_alpha : 0.0,
                                                                set.default_thole, scaledPartial.p);
             else
-                k_scaled_pair_energy<false><<<sb, 128, 0, st>>>(nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad, mom64.p,
+                launch(k_scaled_pair_energy<false>, sb, 128, 0, st, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad, mom64.p,
                                                                 prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0,
                                                                 set.cutoff, usePme ? set.ewald_alpha : 0.0,
                                                                 set.default_thole, scaledPartial.p);
-            k_reduce_partials<<<1, 1024, 0, st>>>(sb, 1, scaledPartial.p, energyOut.p + 2, nullptr);
+            launch(k_reduce_partials, 1, 1024, 0, st, sb, 1, scaledPartial.p, energyOut.p + 2, nullptr);
         } else {
             CUDA_CHECK(cudaMemsetAsync(energyOut.p + 2, 0, sizeof(double), st));
         }
-        k_torque_map<<<nblk(n, 128), 128, 0, st>>>(n, npad, pos.p, mol(), e.rank.p, torqueFx.p, forceFx.p);
+        launch(k_torque_map, nblk(n, 128), 128, 0, st, n, npad, pos.p, mol(), e.rank.p, torqueFx.p, forceFx.p);
         timer.end(st);
         CUDA_CHECK(cudaGetLastError());
     }
@@ -908,6 +924,7 @@ struct Context {
         if (!haveParams) throw Error(MPID_ERR_STATE, "mpid_set_multipoles must be called before evaluating");
         CUDA_CHECK(cudaSetDevice(device));
         cudaStream_t st = stream;
+        const long long launches0 = t_launches, library0 = t_library_calls;
         CUDA_CHECK(cudaEventRecord(evStart, st));
         if (d_pos != pos.p) CUDA_CHECK(cudaMemcpyAsync(pos.p, d_pos, 3 * (size_t) n * 8, cudaMemcpyDeviceToDevice, st));
         timer.reset();
@@ -926,7 +943,7 @@ struct Context {
             else
                 solve_dipoles(e, ptMuF.p, ptEF.p, ptGF.p);
             finish(e, ptMuF.p, ptEF.p, ptGF.p);
-            k_forces_out<<<nblk(n, 128), 128, 0, st>>>(n, npad, e.rank.p, forceFx.p, d_forces);
+            launch(k_forces_out, nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, d_forces);
         } else {
             Engine<double>& e = *ed;
             prepare_engine(e, true);
@@ -937,7 +954,7 @@ struct Context {
             else
                 solve_dipoles(e, ptMuD.p, ptED.p, ptGD.p);
             finish(e, ptMuD.p, ptED.p, ptGD.p);
-            k_forces_out<<<nblk(n, 128), 128, 0, st>>>(n, npad, e.rank.p, forceFx.p, d_forces);
+            launch(k_forces_out, nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, d_forces);
         }
         CUDA_CHECK(cudaGetLastError());
         double eparts[3] = {0, 0, 0};  // reciprocal + self, real space, scaled pairs
@@ -952,6 +969,8 @@ struct Context {
         float ms = 0.f;
         CUDA_CHECK(cudaEventElapsedTime(&ms, evStart, evStop));
         stats.ms_total = ms;
+        stats.kernel_launches = (int) (t_launches - launches0);
+        stats.library_calls = (int) (t_library_calls - library0);
         timer.collect();
         for (int s = 0; s < ST_COUNT; ++s) {
             stats.ms_stage[s] = timer.ms[s];
@@ -967,13 +986,13 @@ struct Context {
         if (which < 0 || which > 3) throw Error(MPID_ERR_INVALID, "which must be 0, 1, 2 or 3");
         if (which == 3) {  // permanent field: reuse the induced-dipole output path with mom = 0
             if (mixed)
-                k_dipoles_out<float><<<nblk(n, 128), 128, 0, stream>>>(n, npad, 0, ef->rank.p, ef->mom.p, ef->Efix.p, forcesOut.p);
+                launch(k_dipoles_out<float>, nblk(n, 128), 128, 0, stream, n, npad, 0, ef->rank.p, ef->mom.p, ef->Efix.p, forcesOut.p);
             else
-                k_dipoles_out<double><<<nblk(n, 128), 128, 0, stream>>>(n, npad, 0, ed->rank.p, ed->mom.p, ed->Efix.p, forcesOut.p);
+                launch(k_dipoles_out<double>, nblk(n, 128), 128, 0, stream, n, npad, 0, ed->rank.p, ed->mom.p, ed->Efix.p, forcesOut.p);
         } else if (mixed)
-            k_dipoles_out<float><<<nblk(n, 128), 128, 0, stream>>>(n, npad, which, ef->rank.p, ef->mom.p, ef->mu.p, forcesOut.p);
+            launch(k_dipoles_out<float>, nblk(n, 128), 128, 0, stream, n, npad, which, ef->rank.p, ef->mom.p, ef->mu.p, forcesOut.p);
         else
-            k_dipoles_out<double><<<nblk(n, 128), 128, 0, stream>>>(n, npad, which, ed->rank.p, ed->mom.p, ed->mu.p, forcesOut.p);
+            launch(k_dipoles_out<double>, nblk(n, 128), 128, 0, stream, n, npad, which, ed->rank.p, ed->mom.p, ed->mu.p, forcesOut.p);
         CUDA_CHECK(cudaGetLastError());
         CUDA_CHECK(cudaMemcpyAsync(host, forcesOut.p, 3 * (size_t) n * 8, cudaMemcpyDeviceToHost, stream));
         CUDA_CHECK(cudaStreamSynchronize(stream));
