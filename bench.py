@@ -332,7 +332,7 @@ def main():
             "clocks": clk,
             "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
             "solver": {"iterations": stats["solver_iterations"], "refinement_steps": stats["refinement_steps"],
-                       "residual_debye": stats["solver_residual"], "tile_pairs": stats["num_tile_pairs"]},
+                       "residual_debye": stats["solver_residual"], "max_neighbours": stats["max_neighbours"]},
         }
         line.update(fp64)
         print(json.dumps(line))

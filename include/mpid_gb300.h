@@ -68,7 +68,7 @@ typedef struct {
     int solver_iterations;     /* FP32/FP64 CG iterations (mutual), PT orders (extrapolated) */
     int refinement_steps;      /* FP64 residual evaluations (mixed mutual) */
     double solver_residual;    /* final Debye RMS residual */
-    int num_tile_pairs;
+    int max_neighbours;        /* longest per-atom neighbour list of the last evaluation */
     double ms_total;           /* device time of the last evaluation */
     /* device time (ms) and timed launch groups per stage: 0 sort/tiles/atom set-up,
      * 1 permanent-field pair kernel, 2 PME spread/FFT/convolution/gather, 3 dipole-field

@@ -48,7 +48,7 @@ class Stats(ctypes.Structure):
         ("solver_iterations", ctypes.c_int),
         ("refinement_steps", ctypes.c_int),
         ("solver_residual", ctypes.c_double),
-        ("num_tile_pairs", ctypes.c_int),
+        ("max_neighbours", ctypes.c_int),
         ("ms_total", ctypes.c_double),
         ("ms_stage", ctypes.c_double * 8),
         ("stage_launches", ctypes.c_int * 8),
@@ -211,7 +211,7 @@ class MPIDContext:
         s = Stats()
         self._check(self.lib.mpid_get_stats(self._h, ctypes.byref(s)))
         return dict(solver_iterations=s.solver_iterations, refinement_steps=s.refinement_steps,
-                    solver_residual=s.solver_residual, num_tile_pairs=s.num_tile_pairs, ms_total=s.ms_total,
+                    solver_residual=s.solver_residual, max_neighbours=s.max_neighbours, ms_total=s.ms_total,
                     ms_stage={STAGES[k]: s.ms_stage[k] for k in range(len(STAGES))},
                     stage_launches={STAGES[k]: s.stage_launches[k] for k in range(len(STAGES))},
                     energy_parts=dict(recip_self=s.energy_parts[0], real_space=s.energy_parts[1],

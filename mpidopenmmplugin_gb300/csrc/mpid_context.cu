@@ -276,10 +276,14 @@ struct Context {
     DBuf<char> cubTemp;
     size_t cubBytes = 0;
     DBuf<double> pos, wpos, center, half;
-    DBuf<int2> pairs;
-    DBuf<int> npairs;
-    int pairCapacity = 0;
-    int lastPairs = 0;
+    // neighbour lists (tile lists, then per-atom lists; layouts in mpid_kernels.cuh)
+    int tcap = 0, cap = 0, chunk = 32, nchunks = 1;
+    DBuf<int> tileCount, tileJ, listCount, listTmax, listMax;
+    DBuf<float4> shF;
+    DBuf<double> shD;
+    DBuf<unsigned> list;
+    int lastTiles = 0, lastMaxList = 0;
+    long long listEntries = 0;
     // PME tables
     DBuf<double> modx, mody, modz, influence;
     double lastBox[9] = {0};
@@ -293,9 +297,6 @@ struct Context {
     DBuf<int2> scaledPairs;             // covalently scaled pairs (i < j), original indices
     DBuf<double> scaledScale, scaledPartial;
     int nScaled = 0;
-    DBuf<unsigned long long> pairKeys, pairKeysAlt;
-    DBuf<char> cubTemp2;
-    size_t cubBytes2 = 0;
     DBuf<double> energyPartial, energyOut;
     DBuf<double> forcesOut;
     // solver scratch
@@ -356,14 +357,11 @@ struct Context {
         cub::DeviceRadixSort::SortPairs(nullptr, cubBytes, keys.p, keysAlt.p, order.p, orderAlt.p, n);
         cubTemp.alloc(cubBytes);
         pos.alloc(3 * n); wpos.alloc(3 * n); center.alloc(3 * ntiles); half.alloc(3 * ntiles);
-        npairs.alloc(1);
-        pairCapacity = std::max(1024, std::min(ntiles * (ntiles + 1) / 2, ntiles * 160));
-        pairs.alloc(pairCapacity);
-        pairKeys.alloc(pairCapacity); pairKeysAlt.alloc(pairCapacity);
-        cub::DeviceRadixSort::SortKeys(nullptr, cubBytes2, pairKeys.p, pairKeysAlt.p, pairCapacity);
-        cubTemp2.alloc(cubBytes2);
+        // list capacities from the density (regrown on overflow)
+        tileCount.alloc(ntiles); listCount.alloc(npad); listTmax.alloc(ntiles); listMax.alloc(2);
+        alloc_tile_lists(usePme ? std::min(ntiles, 96) : ntiles);
+        alloc_atom_lists(usePme ? 64 : npad);
         forceFx.alloc(3 * (size_t) npad); torqueFx.alloc(3 * (size_t) npad);
-        energyBlocks.alloc(152 * 64);
         mom64.alloc(20 * (size_t) npad); prm64.alloc(2 * (size_t) n);
         scaledPairs.alloc(1); scaledScale.alloc(1); scaledPartial.alloc(1);
         energyPartial.alloc(nblk(npad, 256)); energyOut.alloc(4);
@@ -562,23 +560,48 @@ struct Context {
         }
     }
 
-    TileCtx tile_ctx() const {
-        TileCtx c;
-        c.pairs = pairs.p;
-        c.npairs = npairs.p;
-        c.center = center.p;
-        c.box = box;
+    void alloc_tile_lists(int c) {
+        tcap = c;
+        tileJ.alloc((size_t) ntiles * tcap);
+        shF.alloc((size_t) ntiles * tcap);
+        shD.alloc((size_t) 3 * ntiles * tcap);
+    }
+    void alloc_atom_lists(int c) {
+        cap = ((c + chunk - 1) / chunk) * chunk;
+        const size_t entries = (size_t) npad * cap;
+        if (entries > ((size_t) 1 << 34)) throw Error(MPID_ERR_INVALID, "neighbour list would exceed 64 GB");
+        list.alloc(entries);
+        listEntries = (long long) entries;
+        energyBlocks.alloc((size_t) ntiles * (cap / chunk));
+    }
+
+    NbrList nbr_list() const {
+        NbrList c;
+        c.ntiles = ntiles;
+        c.tcap = tcap;
+        c.cap = cap;
+        c.chunk = chunk;
+        c.nchunks = nchunks;
+        c.tileJ = tileJ.p;
+        c.shF = shF.p;
+        c.shD = shD.p;
+        c.count = listCount.p;
+        c.tmax = listTmax.p;
+        c.list = list.p;
         c.usePbc = usePme ? 1 : 0;
         c.cutoff = usePme ? set.cutoff : 1e30;
         c.ewald = usePme ? set.ewald_alpha : 0.0;
         c.defaultThole = set.default_thole;
+        c.box = box;
         c.covOff = covOff.p;
         c.covJ = covJ.p;
         c.covS = covS.p;
         return c;
     }
 
-    int pair_blocks() const { return std::max(1, std::min(nblk(std::max(lastPairs, 1), kWarpsPerBlock), 152 * 64)); }
+    // warp tasks (tile, chunk) of the pair kernels
+    int pair_tasks() const { return ntiles * nchunks; }
+    int pair_blocks() const { return std::max(1, nblk(pair_tasks(), kWarpsPerBlock)); }
 
     // Sort, tiles, tile pairs.
     void neighbour_setup() {
@@ -602,40 +625,43 @@ struct Context {
             CUDA_CHECK(cudaStreamSynchronize(st));
         }
         launch(k_tile_bounds, nblk(ntiles, 128), 128, 0, st, n, ntiles, order.p, wpos.p, center.p, half.p);
-        for (int attempt = 0; attempt < 3; ++attempt) {
-            CUDA_CHECK(cudaMemsetAsync(npairs.p, 0, sizeof(int), st));
-            const long long total = (long long) ntiles * (ntiles + 1) / 2;
-            launch(k_tile_pairs, nblk(total, 256), 256, 0, st, ntiles, center.p, half.p, box, usePme ? set.cutoff : 1e30,
-                                                           usePme ? 1 : 0, pairs.p, npairs.p, pairCapacity);
-            CUDA_CHECK(cudaGetLastError());
-            int cnt = 0;
-            CUDA_CHECK(cudaMemcpyAsync(&cnt, npairs.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        const double listCut = usePme ? set.cutoff * (1.0 + 1e-6) + 1e-5 : 1e30;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            CUDA_CHECK(cudaMemsetAsync(listMax.p, 0, sizeof(int), st));
+            launch(k_tile_list, nblk((long long) ntiles * 32, 128), 128, 0, st, ntiles, center.p, half.p, box, listCut,
+                   usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, shD.p, listMax.p);
+            int m = 0;
+            CUDA_CHECK(cudaMemcpyAsync(&m, listMax.p, sizeof(int), cudaMemcpyDeviceToHost, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
-            lastPairs = cnt;
-            if (cnt <= pairCapacity) {
-                sort_pairs(cnt);
-                return;
-            }
-            pairCapacity = (int) (cnt * 1.25) + 1024;  // regrow and rebuild
-            pairs.alloc(pairCapacity);
-            pairKeys.alloc(pairCapacity);
-            pairKeysAlt.alloc(pairCapacity);
-            cub::DeviceRadixSort::SortKeys(nullptr, cubBytes2, pairKeys.p, pairKeysAlt.p, pairCapacity);
-            cubTemp2.alloc(cubBytes2);
+            lastTiles = m;
+            if (m <= tcap) return;
+            alloc_tile_lists(std::min(ntiles, m + m / 4 + 8));
         }
-        throw Error(MPID_ERR_CUDA, "tile pair list overflow");
+        throw Error(MPID_ERR_CUDA, "tile list overflow");
     }
 
-    // Sort the tile-pair list (I, J) so kernels see a reproducible order with each I's
-    // pairs adjacent.
-    void sort_pairs(int cnt) {
-        if (cnt <= 1) return;
+    // Per-atom lists from the sorted offsets of engine e (after prepare_engine).
+    template <typename real>
+    void atom_lists(Engine<real>& e) {
         cudaStream_t st = stream;
-        CUDA_CHECK(cudaMemcpyAsync(pairKeys.p, pairs.p, cnt * sizeof(int2), cudaMemcpyDeviceToDevice, st));
-        // int2 (x = I, y = J) read as a 64-bit key: J in the high word, so sort by (J, I)
-        ++t_library_calls;
-        CUDA_CHECK(cub::DeviceRadixSort::SortKeys(cubTemp2.p, cubBytes2, pairKeys.p, pairKeysAlt.p, cnt, 0, 64, st));
-        CUDA_CHECK(cudaMemcpyAsync(pairs.p, pairKeysAlt.p, cnt * sizeof(int2), cudaMemcpyDeviceToDevice, st));
+        const double listCut = usePme ? set.cutoff * (1.0 + 1e-6) + 1e-5 : 1e30;
+        const float cut2 = usePme ? (float) (listCut * listCut) : 3.0e38f;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            CUDA_CHECK(cudaMemsetAsync(listMax.p + 1, 0, sizeof(int), st));
+            launch(k_atom_list<real>, nblk((long long) ntiles * 32, 128), 128, 0, st, ntiles, npad, e.off.p, e.orig.p, box,
+                   cut2, tcap, tileCount.p, tileJ.p, shF.p, covOff.p, covJ.p, covS.p, cap, listCount.p, listTmax.p, list.p,
+                   listMax.p + 1);
+            int m = 0;
+            CUDA_CHECK(cudaMemcpyAsync(&m, listMax.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            lastMaxList = m;
+            if (m <= cap) {
+                nchunks = std::max(1, (m + chunk - 1) / chunk);
+                return;
+            }
+            alloc_atom_lists(std::min(npad, m + m / 8 + chunk));
+        }
+        throw Error(MPID_ERR_CUDA, "neighbour list overflow");
     }
 
     template <typename real>
@@ -661,7 +687,7 @@ struct Context {
         cudaStream_t st = stream;
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
         timer.begin(ST_FIXED_REAL, st);
-        launch(k_fixed_field<real>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tile_ctx(), e.arrays(), e.fieldFx.p);
+        launch(k_fixed_field<real>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), e.fieldFx.p);
         timer.end(st);
         if (usePme) {
             timer.begin(ST_PME, st);
@@ -685,10 +711,10 @@ struct Context {
         timer.begin(mixed && sizeof(real) == 8 ? ST_REFINE_REAL : ST_DIPOLE_REAL, st);
         if (G) {
             CUDA_CHECK(cudaMemsetAsync(e.gradFx.p, 0, 6 * (size_t) npad * 8, st));
-            launch(k_dipole_field<real, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tile_ctx(), e.arrays(), mu, e.fieldFx.p,
+            launch(k_dipole_field<real, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), mu, e.fieldFx.p,
                                                                                      e.gradFx.p, skip);
         } else {
-            launch(k_dipole_field<real, false>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tile_ctx(), e.arrays(), mu,
+            launch(k_dipole_field<real, false>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), mu,
                                                                                       e.fieldFx.p, nullptr, skip);
         }
         timer.end(st);
@@ -860,11 +886,11 @@ struct Context {
         }
         CUDA_CHECK(cudaMemsetAsync(forceFx.p, 0, 3 * (size_t) npad * 8, st));
         CUDA_CHECK(cudaMemsetAsync(torqueFx.p, 0, 3 * (size_t) npad * 8, st));
-        const int eb = pair_blocks();
+        const int eb = pair_tasks();
         CUDA_CHECK(cudaMemsetAsync(energyBlocks.p, 0, eb * sizeof(double), st));
         timer.begin(ST_PAIR, st);
         const bool exact = (set.flags & MPID_FLAG_EXACT_ANISO_TORQUE) != 0;
-        const TileCtx tc = tile_ctx();
+        const NbrList tc = nbr_list();
         const AtomArrays<real> aa = e.arrays();
         if (set.polarization_type == MPID_MUTUAL && !exact)
             launch(k_electrostatics<real, true, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
@@ -931,10 +957,11 @@ struct Context {
         timer.begin(ST_SETUP, st);
         set_box(hbox);
         neighbour_setup();
-        stats.num_tile_pairs = lastPairs;
+        stats.max_neighbours = lastMaxList;
         if (mixed) {
             Engine<float>& e = *ef;
             prepare_engine(e, true);
+            atom_lists(e);
             if (ed) prepare_engine(*ed, false);
             timer.end(st);
             fixed_field(e);
@@ -947,6 +974,7 @@ struct Context {
         } else {
             Engine<double>& e = *ed;
             prepare_engine(e, true);
+            atom_lists(e);
             timer.end(st);
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL)

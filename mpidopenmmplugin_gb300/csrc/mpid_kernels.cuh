@@ -94,34 +94,67 @@ __global__ void k_tile_bounds(int n, int ntiles, const int* __restrict__ order,
     }
 }
 
-// Candidate tile pairs (I <= J) whose bounding boxes come within the cutoff.  A
-// dimension whose extents plus the cutoff reach half the box is treated as always
-// overlapping, so minimum imaging of the centres can never drop a pair.
-__global__ void k_tile_pairs(int ntiles, const double* __restrict__ center, const double* __restrict__ half,
-                             BoxDev box, double cutoff, int usePbc, int2* __restrict__ pairs, int* __restrict__ count,
-                             int capacity) {
-    long long idx = (long long) blockIdx.x * blockDim.x + threadIdx.x;
-    long long total = (long long) ntiles * (ntiles + 1) / 2;
-    if (idx >= total) return;
-    // invert idx -> (I, J) with I <= J over rows of decreasing length
-    long long I = (long long) ((2.0 * ntiles + 1.0 - sqrt((2.0 * ntiles + 1.0) * (2.0 * ntiles + 1.0) - 8.0 * idx)) / 2.0);
-    while (I > 0 && I * (2LL * ntiles - I + 1) / 2 > idx) --I;
-    while ((I + 1) * (2LL * ntiles - I) / 2 <= idx) ++I;
-    long long J = idx - I * (2LL * ntiles - I + 1) / 2 + I;
-    double d2 = 0.0;
-    for (int k = 0; k < 3; ++k) {
-        double dc = center[3 * J + k] - center[3 * I + k];
-        double ext = half[3 * I + k] + half[3 * J + k];
-        if (usePbc) {
-            if (ext + cutoff >= 0.5 * box.L[k]) continue;
-            dc -= box.L[k] * rint(dc * box.invL[k]);
+// ---------------------------------------------------------------------------
+// Neighbour lists.  Real-space work is organised per 32-atom tile I (one warp):
+//  * tile list: the tiles J whose bounding boxes come within the list cutoff of I's, in
+//    ascending order, with the minimum-image shift of the tile centres (float and double)
+//    and a flag when a dimension is so short against the cutoff that each pair must be
+//    imaged on its own;
+//  * atom lists: for every atom (lane) the atoms j within the list cutoff, both
+//    directions (each pair appears in the lists of both atoms), lane-interleaved
+//    [tile][entry][lane] so that a warp reads 128 contiguous bytes per entry.
+// An entry is (slot << 7) | (flag << 5) | jlane: slot indexes I's tile list, jlane is
+// j's lane in that tile, flag is 0 for covalent scale 1, 1 for scale 0, 2 for any other
+// scale (looked up again by the kernel).  Every lane's entries run over J tiles in
+// ascending order and jlane ascending, so the lists and all sums over them are
+// reproducible.
+
+// One warp per tile I scans all tiles J.  A dimension whose extents plus the cutoff reach
+// half the box always counts as overlapping and marks the pair for per-pair imaging.
+__global__ void k_tile_list(int ntiles, const double* __restrict__ center, const double* __restrict__ half, BoxDev box,
+                            double cutoff, int usePbc, int tcap, int* __restrict__ tileCount, int* __restrict__ tileJ,
+                            float4* __restrict__ shF, double* __restrict__ shD, int* __restrict__ maxTiles) {
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (I >= ntiles) return;
+    int base = 0;
+    for (int J0 = 0; J0 < ntiles; J0 += 32) {
+        const int J = J0 + lane;
+        bool hit = false, wrap = false;
+        double sh[3] = {0.0, 0.0, 0.0};
+        if (J < ntiles) {
+            double d2 = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                double dc = center[3 * J + k] - center[3 * I + k];
+                const double ext = half[3 * I + k] + half[3 * J + k];
+                bool always = false;
+                if (usePbc) {
+                    always = ext + cutoff >= 0.5 * box.L[k];
+                    wrap = wrap || always;
+                    dc -= box.L[k] * rint(dc * box.invL[k]);
+                }
+                sh[k] = dc;
+                const double g = fabs(dc) - ext;
+                if (!always && g > 0) d2 += g * g;
+            }
+            hit = d2 < cutoff * cutoff;
         }
-        double g = fabs(dc) - ext;
-        if (g > 0) d2 += g * g;
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int pos = base + __popc(m & ((1u << lane) - 1u));
+            if (pos < tcap) {
+                const size_t s = (size_t) I * tcap + pos;
+                tileJ[s] = J | (wrap ? (int) 0x80000000 : 0);
+                shF[s] = make_float4((float) sh[0], (float) sh[1], (float) sh[2], 0.f);
+                shD[3 * s] = sh[0];
+                shD[3 * s + 1] = sh[1];
+                shD[3 * s + 2] = sh[2];
+            }
+        }
+        base += __popc(m);
     }
-    if (d2 < cutoff * cutoff) {
-        int slot = atomicAdd(count, 1);
-        if (slot < capacity) pairs[slot] = make_int2((int) I, (int) J);
+    if (lane == 0) {
+        tileCount[I] = min(base, tcap);
+        atomicMax(maxTiles, base);
     }
 }
 
@@ -237,38 +270,145 @@ __device__ __forceinline__ double pair_scale(int oi, int oj, const int* __restri
     return 1.0;
 }
 
-struct TileCtx {
-    const int2* pairs;
-    const int* npairs;
-    const double* center;
-    BoxDev box;
+// Atom lists: one warp per tile I; each lane tests the 32 atoms of every J tile in I's
+// tile list (float arithmetic, cutoff2 already includes a small skin so that both the
+// FP32 and the FP64 kernels, which apply the exact cutoff, see every pair).
+template <typename real>
+__global__ void k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __restrict__ orig, BoxDev box,
+                            float cutoff2, int tcap, const int* __restrict__ tileCount, const int* __restrict__ tileJ,
+                            const float4* __restrict__ shF, const int* __restrict__ covOff, const int* __restrict__ covJ,
+                            const double* __restrict__ covS, int cap, int* __restrict__ count, int* __restrict__ tmax,
+                            unsigned* __restrict__ list, int* __restrict__ maxCount) {
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (I >= ntiles) return;
+    const int si = I * 32 + lane;
+    const float oi[3] = {(float) off[si], (float) off[npad + si], (float) off[2 * npad + si]};
+    const int origI = orig[si];
+    const float L[3] = {(float) box.L[0], (float) box.L[1], (float) box.L[2]};
+    const float iL[3] = {(float) box.invL[0], (float) box.invL[1], (float) box.invL[2]};
+    unsigned* out = list + (size_t) I * cap * 32 + lane;
+    int cnt = 0;
+    const int nt = tileCount[I];
+    for (int s = 0; s < nt; ++s) {
+        const int Jw = tileJ[(size_t) I * tcap + s];
+        const int J = Jw & 0x7fffffff;
+        const bool wrap = Jw < 0;
+        const float4 sh = shF[(size_t) I * tcap + s];
+        const int sj = J * 32 + lane;
+        const float oj0 = (float) off[sj], oj1 = (float) off[npad + sj], oj2 = (float) off[2 * npad + sj];
+        const int origJl = orig[sj];
+        for (int jl = 0; jl < 32; ++jl) {
+            float d[3] = {sh.x + (__shfl_sync(0xffffffffu, oj0, jl) - oi[0]),
+                          sh.y + (__shfl_sync(0xffffffffu, oj1, jl) - oi[1]),
+                          sh.z + (__shfl_sync(0xffffffffu, oj2, jl) - oi[2])};
+            const int oj = __shfl_sync(0xffffffffu, origJl, jl);
+            if (wrap)
+                for (int k = 0; k < 3; ++k) d[k] -= L[k] * rintf(d[k] * iL[k]);
+            const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (origI < 0 || oj < 0 || r2 >= cutoff2 || (J == I && jl == lane)) continue;
+            unsigned flag = 0;
+            for (int k = covOff[origI]; k < covOff[origI + 1]; ++k)
+                if (covJ[k] == oj) {
+                    const double sc = covS[k];
+                    flag = sc == 1.0 ? 0u : (sc == 0.0 ? 1u : 2u);
+                    break;
+                }
+            if (cnt < cap) out[(size_t) cnt * 32] = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
+            ++cnt;
+        }
+    }
+    count[si] = min(cnt, cap);
+    int m = cnt;
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) {
+        tmax[I] = min(m, cap);
+        atomicMax(maxCount, m);
+    }
+}
+
+// Neighbour lists and pair constants as the pair kernels see them.
+struct NbrList {
+    int ntiles, tcap, cap, chunk, nchunks;
+    const int* tileJ;
+    const float4* shF;
+    const double* shD;
+    const int* count;
+    const int* tmax;
+    const unsigned* list;
     int usePbc;
     double cutoff;
     double ewald;
     double defaultThole;
+    BoxDev box;
     const int* covOff;
     const int* covJ;
     const double* covS;
 };
 
-// Displacement R_j - R_i of two sorted atoms from the tile-centre shift and offsets.
-template <typename real>
-__device__ __forceinline__ void tile_shift(const TileCtx& c, int I, int J, real* sh) {
-    for (int k = 0; k < 3; ++k) {
-        double d = c.center[3 * J + k] - c.center[3 * I + k];
-        if (c.usePbc) d -= c.box.L[k] * rint(d * c.box.invL[k]);
-        sh[k] = real(d);
+// Work item of a pair kernel: entries [k0, k0 + chunk) of the lists of tile I.
+struct PairTask {
+    int I, k0, lane, si;
+    __device__ __forceinline__ bool init(const NbrList& nl) {
+        const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        lane = threadIdx.x & 31;
+        I = w / nl.nchunks;
+        k0 = (w - I * nl.nchunks) * nl.chunk;
+        si = I * 32 + lane;
+        return I < nl.ntiles && k0 < nl.tmax[I];
     }
+};
+
+// Precision-specific pieces of the pair loop: the tile shift and the box in `real`.
+template <typename real> struct PairGeom;
+template <> struct PairGeom<float> {
+    float L[3], iL[3], rc2, thole;
+    __device__ __forceinline__ void init(const NbrList& nl) {
+        for (int k = 0; k < 3; ++k) { L[k] = (float) nl.box.L[k]; iL[k] = (float) nl.box.invL[k]; }
+        rc2 = (float) (nl.cutoff * nl.cutoff);
+        thole = (float) nl.defaultThole;
+    }
+    __device__ __forceinline__ void shift(const NbrList& nl, size_t s, float* sh) const {
+        const float4 v = nl.shF[s];
+        sh[0] = v.x; sh[1] = v.y; sh[2] = v.z;
+    }
+};
+template <> struct PairGeom<double> {
+    double L[3], iL[3], rc2, thole;
+    __device__ __forceinline__ void init(const NbrList& nl) {
+        for (int k = 0; k < 3; ++k) { L[k] = nl.box.L[k]; iL[k] = nl.box.invL[k]; }
+        rc2 = nl.cutoff * nl.cutoff;
+        thole = nl.defaultThole;
+    }
+    __device__ __forceinline__ void shift(const NbrList& nl, size_t s, double* sh) const {
+        sh[0] = nl.shD[3 * s]; sh[1] = nl.shD[3 * s + 1]; sh[2] = nl.shD[3 * s + 2];
+    }
+};
+
+// Decode one list entry of lane `si` into j's sorted index, the displacement
+// d = R_j - R_i and r^2; returns false for pairs beyond the cutoff.
+template <typename real>
+__device__ __forceinline__ bool list_pair(const NbrList& nl, const PairGeom<real>& g, const AtomArrays<real>& at, int I,
+                                          int k, int lane, const real* oi, int& sj, unsigned& flag, real* d, real& r2) {
+    const unsigned code = nl.list[((size_t) I * nl.cap + k) * 32 + lane];
+    const size_t s = (size_t) I * nl.tcap + (code >> 7);
+    const int Jw = nl.tileJ[s];
+    sj = (Jw & 0x7fffffff) * 32 + (int) (code & 31u);
+    flag = (code >> 5) & 3u;
+    real sh[3];
+    g.shift(nl, s, sh);
+    const int npad = at.npad;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) d[q] = sh[q] + (at.off[q * npad + sj] - oi[q]);
+    if (Jw < 0)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) d[q] -= g.L[q] * rint(d[q] * g.iL[q]);
+    r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    return !(nl.usePbc && r2 > g.rc2);
 }
 
 template <typename real>
-__device__ __forceinline__ void pair_delta(const TileCtx& c, const real* sh, const real* oi, const real* oj, real* d) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        real x = sh[k] + (oj[k] - oi[k]);
-        if (c.usePbc) x -= real(c.box.L[k]) * rint(x * real(c.box.invL[k]));
-        d[k] = x;
-    }
+__device__ __forceinline__ real list_scale(const NbrList& nl, unsigned flag, int origI, int origJ) {
+    return flag == 0u ? real(1) : (flag == 1u ? real(0) : (real) pair_scale(origI, origJ, nl.covOff, nl.covJ, nl.covS));
 }
 
 constexpr int kWarpsPerBlock = 4;
@@ -278,264 +418,161 @@ constexpr int kWarpsPerBlock = 4;
 // the PME real-space part of MPIDReferenceForce.cpp:2812-2920 / :911-934.
 template <typename real>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_fixed_field(TileCtx c, AtomArrays<real> at, unsigned long long* __restrict__ field) {
-    __shared__ real shOff[kWarpsPerBlock][3][32];
-    __shared__ real shMom[kWarpsPerBlock][20][32];
-    __shared__ typename Vec4<real>::type shPrm[kWarpsPerBlock][32];
-    __shared__ int shOrig[kWarpsPerBlock][32];
-    __shared__ real shAcc[kWarpsPerBlock][3][32];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int np = *c.npairs;
-    const EwaldAlpha<real> ew(c.ewald);
-    const int npad = at.npad;
-    for (int p = blockIdx.x * kWarpsPerBlock + w; p < np; p += gridDim.x * kWarpsPerBlock) {
-        const int2 IJ = c.pairs[p];
-        const int si = IJ.x * 32 + lane, sj = IJ.y * 32 + lane;
-        // i in registers
-        real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
-        LabMoments<real> mi;
-        load_moments(at.mom, npad, si, mi);
-        const typename Vec4<real>::type pi = at.prm[si];
-        const int origI = at.orig[si];
-        // j in shared memory
-        for (int k = 0; k < 3; ++k) shOff[w][k][lane] = at.off[k * npad + sj];
-        for (int k = 0; k < 20; ++k) shMom[w][k][lane] = at.mom[k * npad + sj];
-        shPrm[w][lane] = at.prm[sj];
-        shOrig[w][lane] = at.orig[sj];
-        for (int k = 0; k < 3; ++k) shAcc[w][k][lane] = real(0);
-        __syncwarp();
-        real sh[3];
-        tile_shift(c, IJ.x, IJ.y, sh);
-        real Ei[3] = {real(0), real(0), real(0)};
-        const bool diag = IJ.x == IJ.y;
-        const real rc2 = real(c.cutoff * c.cutoff);
-        for (int k = 0; k < 32; ++k) {
-            const int jl = (lane + k) & 31;
-            const int origJ = shOrig[w][jl];
-            if (origI < 0 || origJ < 0 || (diag && jl <= lane)) continue;
-            real oj[3] = {shOff[w][0][jl], shOff[w][1][jl], shOff[w][2][jl]};
-            real d[3];
-            pair_delta(c, sh, oi, oj, d);
-            const real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-            if (c.usePbc && r2 > rc2) continue;
-            const real r = sqrt(r2);
-            const real scale = (real) pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
-            const typename Vec4<real>::type pj = shPrm[w][jl];
-            const real a = scale == real(0) ? pi.x + pj.x : real(c.defaultThole);
-            PairRadial<real, 0, 4, 0> pr;
-            pair_radial<real, -1, 4, -1>(r, ew, scale, a, pi.y * pj.y, pr);
-            LabMoments<real> mj;
-            mj.q = shMom[w][0][jl];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) mj.d[q] = shMom[w][1 + q][jl];
-#pragma unroll
-            for (int q = 0; q < 6; ++q) mj.Q[q] = shMom[w][4 + q][jl];
-#pragma unroll
-            for (int q = 0; q < 10; ++q) mj.O[q] = shMom[w][10 + q][jl];
-            real sI[3] = {-d[0], -d[1], -d[2]};
-            real e[3];
-            multipole_field(mj, sI, pr.bI, e);
-            Ei[0] += e[0]; Ei[1] += e[1]; Ei[2] += e[2];
-            multipole_field(mi, d, pr.bI, e);
-            shAcc[w][0][jl] += e[0];
-            shAcc[w][1][jl] += e[1];
-            shAcc[w][2][jl] += e[2];
-        }
-        __syncwarp();
-        if (origI >= 0)
-            for (int k = 0; k < 3; ++k) fx_add(field + k * npad + si, Ei[k]);
-        if (shOrig[w][lane] >= 0)
-            for (int k = 0; k < 3; ++k) fx_add(field + k * npad + sj, shAcc[w][k][lane]);
-        __syncwarp();
+k_fixed_field(NbrList nl, AtomArrays<real> at, unsigned long long* __restrict__ field) {
+    PairTask t;
+    if (!t.init(nl)) return;
+    const int npad = at.npad, si = t.si;
+    const int origI = at.orig[si];
+    if (origI < 0) return;
+    const int k1 = min(t.k0 + nl.chunk, nl.count[si]);
+    PairGeom<real> g;
+    g.init(nl);
+    const EwaldAlpha<real> ew(nl.ewald);
+    const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+    const typename Vec4<real>::type pi = at.prm[si];
+    real Ei[3] = {real(0), real(0), real(0)};
+    for (int k = t.k0; k < k1; ++k) {
+        int sj;
+        unsigned flag;
+        real d[3], r2;
+        if (!list_pair(nl, g, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
+        const real r = sqrt(r2);
+        const real scale = list_scale<real>(nl, flag, origI, at.orig[sj]);
+        const typename Vec4<real>::type pj = at.prm[sj];
+        const real a = scale == real(0) ? pi.x + pj.x : g.thole;
+        PairRadial<real, 0, 4, 0> pr;
+        pair_radial<real, -1, 4, -1>(r, ew, scale, a, pi.y * pj.y, pr);
+        LabMoments<real> mj;
+        load_moments(at.mom, npad, sj, mj);
+        const real sI[3] = {-d[0], -d[1], -d[2]};
+        real e[3];
+        multipole_field(mj, sI, pr.bI, e);
+        Ei[0] += e[0]; Ei[1] += e[1]; Ei[2] += e[2];
     }
+    for (int q = 0; q < 3; ++q) fx_add(field + q * npad + si, Ei[q]);
 }
 
 // Real-space field of point dipoles (kernel K_u), optionally with its gradient:
 // MPIDReferenceForce.cpp:4161-4281.  mu is [3][npad] in sorted order.
 template <typename real, bool GRAD>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_dipole_field(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ field,
+k_dipole_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ field,
                unsigned long long* __restrict__ grad, const int* __restrict__ skip) {
-    constexpr int NACC = GRAD ? 9 : 3;
-    __shared__ real shOff[kWarpsPerBlock][3][32];
-    __shared__ real shMu[kWarpsPerBlock][3][32];
-    __shared__ typename Vec4<real>::type shPrm[kWarpsPerBlock][32];
-    __shared__ int shOrig[kWarpsPerBlock][32];
-    __shared__ real shAcc[kWarpsPerBlock][NACC][32];
     if (skip && *skip) return;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int np = *c.npairs;
-    const EwaldAlpha<real> ew(c.ewald);
-    const int npad = at.npad;
-    for (int p = blockIdx.x * kWarpsPerBlock + w; p < np; p += gridDim.x * kWarpsPerBlock) {
-        const int2 IJ = c.pairs[p];
-        const int si = IJ.x * 32 + lane, sj = IJ.y * 32 + lane;
-        real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
-        real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
-        const typename Vec4<real>::type pi = at.prm[si];
-        const int origI = at.orig[si];
-        for (int k = 0; k < 3; ++k) {
-            shOff[w][k][lane] = at.off[k * npad + sj];
-            shMu[w][k][lane] = mu[k * npad + sj];
-        }
-        shPrm[w][lane] = at.prm[sj];
-        shOrig[w][lane] = at.orig[sj];
-        for (int k = 0; k < NACC; ++k) shAcc[w][k][lane] = real(0);
-        __syncwarp();
-        real sh[3];
-        tile_shift(c, IJ.x, IJ.y, sh);
-        real acc[NACC];
+    PairTask t;
+    if (!t.init(nl)) return;
+    const int npad = at.npad, si = t.si;
+    const int origI = at.orig[si];
+    if (origI < 0) return;
+    const int k1 = min(t.k0 + nl.chunk, nl.count[si]);
+    PairGeom<real> g;
+    g.init(nl);
+    const EwaldAlpha<real> ew(nl.ewald);
+    const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+    const typename Vec4<real>::type pi = at.prm[si];
+    constexpr int NACC = GRAD ? 9 : 3;
+    real acc[NACC];
 #pragma unroll
-        for (int k = 0; k < NACC; ++k) acc[k] = real(0);
-        const bool diag = IJ.x == IJ.y;
-        const real rc2 = real(c.cutoff * c.cutoff);
-        for (int k = 0; k < 32; ++k) {
-            const int jl = (lane + k) & 31;
-            const int origJ = shOrig[w][jl];
-            if (origI < 0 || origJ < 0 || (diag && jl <= lane)) continue;
-            real oj[3] = {shOff[w][0][jl], shOff[w][1][jl], shOff[w][2][jl]};
-            real d[3];
-            pair_delta(c, sh, oi, oj, d);
-            const real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-            if (c.usePbc && r2 > rc2) continue;
-            const real r = sqrt(r2);
-            const real scale = (real) pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
-            const typename Vec4<real>::type pj = shPrm[w][jl];
-            const real a = scale == real(0) ? pi.x + pj.x : real(c.defaultThole);
-            PairRadial<real, 0, 0, GRAD ? 3 : 2> pr;
-            pair_radial<real, -1, -1, GRAD ? 3 : 2>(r, ew, real(1), a, pi.y * pj.y, pr);
-            real b[4] = {real(0), pr.bU[1], pr.bU[2], GRAD ? pr.bU[GRAD ? 3 : 2] : real(0)};
-            real uj[3] = {shMu[w][0][jl], shMu[w][1][jl], shMu[w][2][jl]};
-            real sI[3] = {-d[0], -d[1], -d[2]};
-            real e[3], g[6];
-            dipole_field<real, GRAD>(uj, sI, b, e, g);
+    for (int q = 0; q < NACC; ++q) acc[q] = real(0);
+    for (int k = t.k0; k < k1; ++k) {
+        int sj;
+        unsigned flag;
+        real d[3], r2;
+        if (!list_pair(nl, g, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
+        const real r = sqrt(r2);
+        const typename Vec4<real>::type pj = at.prm[sj];
+        const real a = flag == 1u ? pi.x + pj.x : g.thole;  // flag 1: covalent scale 0
+        PairRadial<real, 0, 0, GRAD ? 3 : 2> pr;
+        pair_radial<real, -1, -1, GRAD ? 3 : 2>(r, ew, real(1), a, pi.y * pj.y, pr);
+        const real b[4] = {real(0), pr.bU[1], pr.bU[2], GRAD ? pr.bU[GRAD ? 3 : 2] : real(0)};
+        const real uj[3] = {mu[sj], mu[npad + sj], mu[2 * npad + sj]};
+        const real sI[3] = {-d[0], -d[1], -d[2]};
+        real e[3], gr[6];
+        dipole_field<real, GRAD>(uj, sI, b, e, gr);
 #pragma unroll
-            for (int q = 0; q < 3; ++q) acc[q] += e[q];
-            if (GRAD)
+        for (int q = 0; q < 3; ++q) acc[q] += e[q];
+        if (GRAD)
 #pragma unroll
-                for (int q = 0; q < 6; ++q) acc[3 + q] += g[q];
-            dipole_field<real, GRAD>(ui, d, b, e, g);
-#pragma unroll
-            for (int q = 0; q < 3; ++q) shAcc[w][q][jl] += e[q];
-            if (GRAD)
-#pragma unroll
-                for (int q = 0; q < 6; ++q) shAcc[w][3 + q][jl] += g[q];
-        }
-        __syncwarp();
-        if (origI >= 0) {
-            for (int k = 0; k < 3; ++k) fx_add(field + k * npad + si, acc[k]);
-            if (GRAD)
-                for (int k = 0; k < 6; ++k) fx_add(grad + k * npad + si, acc[3 + k]);
-        }
-        if (shOrig[w][lane] >= 0) {
-            for (int k = 0; k < 3; ++k) fx_add(field + k * npad + sj, shAcc[w][k][lane]);
-            if (GRAD)
-                for (int k = 0; k < 6; ++k) fx_add(grad + k * npad + sj, shAcc[w][3 + k][lane]);
-        }
-        __syncwarp();
+            for (int q = 0; q < 6; ++q) acc[3 + q] += gr[q];
     }
+    for (int q = 0; q < 3; ++q) fx_add(field + q * npad + si, acc[q]);
+    if (GRAD)
+        for (int q = 0; q < 6; ++q) fx_add(grad + q * npad + si, acc[3 + q]);
 }
 
-// Real-space energy, forces and torques (MPIDReferenceForce.cpp:4335-4920).
-// out: force[3][npad], torque[3][npad] fixed point; energy: fixed point scalar.
+// Compensated running sum (TwoSum) for the FP32 pair energies.
+template <typename real>
+struct KahanSum {
+    real s = real(0), c = real(0);
+    __device__ __forceinline__ void add(real x) {
+        const real y = x - c;
+        const real t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double) s - (double) c; }
+};
+
+// Real-space energy, forces and torques (MPIDReferenceForce.cpp:4335-4920).  Each lane
+// evaluates its atom's pairs (both atoms of a pair evaluate it), adds force and torque
+// on its own atom, and counts the energy of pairs with i < j; pairs of covalent scale
+// other than 1 leave their energy to k_scaled_pair_energy.
+// out: force[3][npad], torque[3][npad] fixed point; energy[task] (already x kElectric).
 template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_electrostatics(TileCtx c, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ force,
+k_electrostatics(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ force,
                  unsigned long long* __restrict__ torque, double* __restrict__ energy) {
-    __shared__ real shOff[kWarpsPerBlock][3][32];
-    __shared__ real shMom[kWarpsPerBlock][20][32];
-    __shared__ real shMu[kWarpsPerBlock][3][32];
-    __shared__ typename Vec4<real>::type shPrm[kWarpsPerBlock][32];
-    __shared__ int shOrig[kWarpsPerBlock][32];
-    __shared__ real shAcc[kWarpsPerBlock][6][32];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int np = *c.npairs;
-    const EwaldAlpha<real> ew(c.ewald);
-    const int npad = at.npad;
-    double eLane = 0.0;
-    for (int p = blockIdx.x * kWarpsPerBlock + w; p < np; p += gridDim.x * kWarpsPerBlock) {
-        const int2 IJ = c.pairs[p];
-        const int si = IJ.x * 32 + lane, sj = IJ.y * 32 + lane;
-        real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
-        real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
+    PairTask t;
+    const bool active = t.init(nl);
+    const int npad = at.npad, si = t.si;
+    const int origI = active ? at.orig[si] : -1;
+    KahanSum<real> eSum;
+    if (origI >= 0) {
+        const int k1 = min(t.k0 + nl.chunk, nl.count[si]);
+        PairGeom<real> g;
+        g.init(nl);
+        const EwaldAlpha<real> ew(nl.ewald);
+        const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+        const real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
         LabMoments<real> mi;
         load_moments(at.mom, npad, si, mi);
         const typename Vec4<real>::type pi = at.prm[si];
-        const int origI = at.orig[si];
-        for (int k = 0; k < 3; ++k) {
-            shOff[w][k][lane] = at.off[k * npad + sj];
-            shMu[w][k][lane] = mu[k * npad + sj];
-        }
-        for (int k = 0; k < 20; ++k) shMom[w][k][lane] = at.mom[k * npad + sj];
-        shPrm[w][lane] = at.prm[sj];
-        shOrig[w][lane] = at.orig[sj];
-        for (int k = 0; k < 6; ++k) shAcc[w][k][lane] = real(0);
-        __syncwarp();
-        real sh[3];
-        tile_shift(c, IJ.x, IJ.y, sh);
         real accF[3] = {real(0), real(0), real(0)}, accT[3] = {real(0), real(0), real(0)};
-        const bool diag = IJ.x == IJ.y;
-        const real rc2 = real(c.cutoff * c.cutoff);
-        for (int k = 0; k < 32; ++k) {
-            const int jl = (lane + k) & 31;
-            const int origJ = shOrig[w][jl];
-            if (origI < 0 || origJ < 0 || (diag && jl <= lane)) continue;
-            real oj[3] = {shOff[w][0][jl], shOff[w][1][jl], shOff[w][2][jl]};
-            real d[3];
-            pair_delta(c, sh, oi, oj, d);
-            const real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-            if (c.usePbc && r2 > rc2) continue;
+        for (int k = t.k0; k < k1; ++k) {
+            int sj;
+            unsigned flag;
+            real d[3], r2;
+            if (!list_pair(nl, g, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
             const real r = sqrt(r2);
-            const real scale = (real) pair_scale(origI, origJ, c.covOff, c.covJ, c.covS);
-            const typename Vec4<real>::type pj = shPrm[w][jl];
-            const real a = scale == real(0) ? pi.x + pj.x : real(c.defaultThole);
+            const real scale = list_scale<real>(nl, flag, origI, at.orig[sj]);
+            const typename Vec4<real>::type pj = at.prm[sj];
+            const real a = scale == real(0) ? pi.x + pj.x : g.thole;
             PairRadial<real, 7, 5, MUTUAL ? 3 : 0> pr;
             pair_radial<real, 7, 5, MUTUAL ? 3 : -1>(r, ew, scale, a, pi.y * pj.y, pr);
             LabMoments<real> mj;
-            mj.q = shMom[w][0][jl];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) mj.d[q] = shMom[w][1 + q][jl];
-#pragma unroll
-            for (int q = 0; q < 6; ++q) mj.Q[q] = shMom[w][4 + q][jl];
-#pragma unroll
-            for (int q = 0; q < 10; ++q) mj.O[q] = shMom[w][10 + q][jl];
-            real uj[3] = {shMu[w][0][jl], shMu[w][1][jl], shMu[w][2][jl]};
+            load_moments(at.mom, npad, sj, mj);
+            const real uj[3] = {mu[sj], mu[npad + sj], mu[2 * npad + sj]};
             PairOut<real> po;
-            qi_pair<real, MUTUAL, REF_ANISO_TORQUE>(d, r, mi, mj, ui, uj, pi.z != real(0), pj.z != real(0), pr.bP, pr.bI, pr.bU, po);
-            if (scale == real(1)) eLane += (double) po.energy;  // scaled pairs: k_scaled_pair_energy
+            qi_pair<real, MUTUAL, REF_ANISO_TORQUE>(d, r, mi, mj, ui, uj, pi.z != real(0), pj.z != real(0), pr.bP, pr.bI,
+                                                     pr.bU, po);
+            if (flag == 0u && si < sj) eSum.add(po.energy);
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 accF[q] -= po.fJ[q];
                 accT[q] += po.tI[q];
-                shAcc[w][q][jl] += po.fJ[q];
-                shAcc[w][3 + q][jl] += po.tJ[q];
             }
         }
-        __syncwarp();
         const real E = real(kElectric);
-        if (origI >= 0)
-            for (int k = 0; k < 3; ++k) {
-                fx_add(force + k * npad + si, E * accF[k]);
-                fx_add(torque + k * npad + si, E * accT[k]);
-            }
-        if (shOrig[w][lane] >= 0)
-            for (int k = 0; k < 3; ++k) {
-                fx_add(force + k * npad + sj, E * shAcc[w][k][lane]);
-                fx_add(torque + k * npad + sj, E * shAcc[w][3 + k][lane]);
-            }
-        __syncwarp();
+        for (int q = 0; q < 3; ++q) {
+            fx_add(force + q * npad + si, E * accF[q]);
+            fx_add(torque + q * npad + si, E * accT[q]);
+        }
     }
-    // FP64 energy: warp reduction, then a fixed-order sum of the warps of this block
-    // into energy[blockIdx.x] (the tile-pair list is sorted, so the result is reproducible).
-    __shared__ double shE[kWarpsPerBlock];
-    for (int o = 16; o > 0; o >>= 1) eLane += __shfl_down_sync(0xffffffffu, eLane, o);
-    if (lane == 0) shE[w] = eLane;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double e = 0.0;
-        for (int k = 0; k < kWarpsPerBlock; ++k) e += shE[k];
-        energy[blockIdx.x] = e * kElectric;
-    }
+    // FP64 energy of the task: warp sum, written per task (fixed-order reduction later)
+    double e = eSum.value();
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (t.lane == 0 && w < nl.ntiles * nl.nchunks) energy[w] = e * kElectric;
 }
 
 // Energy of covalently scaled pairs (scale != 1) in FP64.  Their real-space terms remove
