@@ -112,6 +112,28 @@ int mpid_evaluate(mpid_context* ctx, const double* positions, const double* box,
 int mpid_evaluate_device(mpid_context* ctx, const double* d_positions, const double* box, double* d_forces,
                          double* d_energy, void* stream);
 
+/* mpid_evaluate_device without any allocation.  No reference counterpart: the reference
+ * kernel runs inside OpenMM, which owns all memory.  For callers that may not allocate
+ * device memory while they evaluate: code under CUDA stream capture, integrators with a
+ * fixed memory budget, hosts whose own allocator holds the device memory.  The ordinary
+ * call allocates only when its neighbour lists must grow; this one keeps the neighbour
+ * lists and the pair kernel's per-task energies in one static 8 MiB device array per
+ * device and never grows anything.
+ *  - PME only.  Size limit: npad x (longest neighbour list rounded up to 32) <= 1,835,008
+ *    entries (npad = atoms rounded up to 32), e.g. about 5,000 water atoms at a 0.9 nm
+ *    cutoff.  Larger systems, and systems whose tile lists have not been sized by one
+ *    mpid_evaluate_device call, are rejected with MPID_ERR_INVALID before anything is
+ *    written to d_forces; the context stays usable.
+ *  - Nothing in the array needs to start at zero: each call writes the lists and clears
+ *    the energy partials before using them.
+ *  - The first call on a device looks the array up (cudaGetSymbolAddress); make that
+ *    first call before any stream capture.
+ *  - The array is shared by every context of the process on that device: calls must not
+ *    overlap in time on a device, from any thread or stream, or they race on it.
+ * Arguments and results as mpid_evaluate_device. */
+int mpid_evaluate_device_noalloc(mpid_context* ctx, const double* d_positions, const double* box, double* d_forces,
+                                 double* d_energy, void* stream);
+
 /* Dipoles of the last evaluation in caller order, 3n host doubles (e nm):
  * which 0 induced (getInducedDipoles), 1 lab-frame permanent (getLabFramePermanentDipoles),
  * 2 total (getTotalDipoles); mpidKernels.h:79-81.  which 3 returns the permanent

@@ -19,8 +19,8 @@ MPID_FLAG_EXACT_ANISO_TORQUE = 1
 
 # Entry points declared in include/mpid_gb300.h
 C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multipoles", "mpid_set_covalent",
-         "mpid_evaluate", "mpid_evaluate_device", "mpid_get_dipoles", "mpid_get_pme_parameters", "mpid_get_stats",
-         "mpid_last_error"]
+         "mpid_evaluate", "mpid_evaluate_device", "mpid_evaluate_device_noalloc", "mpid_get_dipoles",
+         "mpid_get_pme_parameters", "mpid_get_stats", "mpid_last_error"]
 
 
 class Settings(ctypes.Structure):
@@ -91,6 +91,7 @@ def load_library(build=True):
     lib.mpid_set_covalent.argtypes = [vp, ip, ip]
     lib.mpid_evaluate.argtypes = [vp, dp, dp, dp, dp]
     lib.mpid_evaluate_device.argtypes = [vp, vp, dp, vp, vp, vp]
+    lib.mpid_evaluate_device_noalloc.argtypes = [vp, vp, dp, vp, vp, vp]
     lib.mpid_get_dipoles.argtypes = [vp, ctypes.c_int, dp]
     lib.mpid_get_pme_parameters.argtypes = [vp, dp, ip, ip, ip]
     lib.mpid_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
@@ -181,6 +182,13 @@ class MPIDContext:
         self._check(self.lib.mpid_evaluate_device(self._h, ctypes.c_void_p(d_positions), _dp(b),
                                                   ctypes.c_void_p(d_forces), ctypes.c_void_p(d_energy),
                                                   ctypes.c_void_p(stream)))
+
+    def evaluate_device_noalloc(self, d_positions, box, d_forces, d_energy=0, stream=0):
+        """evaluate_device through the allocation-free entry point (PME, small systems)."""
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        self._check(self.lib.mpid_evaluate_device_noalloc(self._h, ctypes.c_void_p(d_positions), _dp(b),
+                                                          ctypes.c_void_p(d_forces), ctypes.c_void_p(d_energy),
+                                                          ctypes.c_void_p(stream)))
 
     def _dipoles(self, which):
         out = np.zeros((self.n, 3))

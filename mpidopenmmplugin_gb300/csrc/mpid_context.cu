@@ -12,6 +12,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -21,6 +22,27 @@
 #include "mpid_gb300.h"
 #include "mpid_kernels.cuh"
 #include "pme_host.h"
+
+// ---------------------------------------------------------------------------
+// Static scratch of the allocation-free evaluation (mpid_evaluate_device_noalloc).
+// Some callers may not allocate device memory at the moment they evaluate: code being
+// captured into a CUDA graph (cudaMalloc is not a capturable operation), integrators
+// that run under a fixed memory budget, or hosts whose allocator owns the device
+// memory.  The ordinary evaluation allocates only when its neighbour lists outgrow
+// their capacity; the allocation-free variant keeps the per-atom neighbour lists and
+// the pair kernel's per-task energy partials in this fixed array instead and fails
+// with MPID_ERR_INVALID rather than grow.  8 MiB: 1,835,008 list entries (npad x
+// neighbours per atom, e.g. about 5,000 water atoms at a 0.9 nm cutoff) and 131,072
+// FP64 task energies.  The array is one per device and per process, so calls must not
+// overlap in time on a device (from any context, thread or stream): overlapping calls
+// race on it.
+namespace mpid {
+constexpr size_t kNoAllocListEntries = 1835008;
+constexpr size_t kNoAllocTasks = 131072;
+constexpr size_t kNoAllocBytes = kNoAllocListEntries * 4 + kNoAllocTasks * 8;
+constexpr int kNoAllocMaxDevices = 64;
+}  // namespace mpid
+static __device__ __align__(256) unsigned char g_noallocScratch[mpid::kNoAllocBytes];
 
 namespace mpid {
 
@@ -284,6 +306,7 @@ struct Context {
     DBuf<unsigned> list;
     int lastTiles = 0, lastMaxList = 0;
     long long listEntries = 0;
+    bool growForbidden = false;  // set by the allocation-free entry point
     // PME tables
     DBuf<double> modx, mody, modz, influence;
     double lastBox[9] = {0};
@@ -635,6 +658,10 @@ struct Context {
             CUDA_CHECK(cudaStreamSynchronize(st));
             lastTiles = m;
             if (m <= tcap) return;
+            if (growForbidden)
+                throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: the tile lists would have to grow (" +
+                                                  std::to_string(m) + " > " + std::to_string(tcap) +
+                                                  " neighbour tiles); evaluate once with mpid_evaluate_device first");
             alloc_tile_lists(std::min(ntiles, m + m / 4 + 8));
         }
         throw Error(MPID_ERR_CUDA, "tile list overflow");
@@ -659,6 +686,10 @@ struct Context {
                 nchunks = std::max(1, (m + chunk - 1) / chunk);
                 return;
             }
+            if (growForbidden)
+                throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: an atom has " + std::to_string(m) +
+                                                  " neighbours, more than the " + std::to_string(cap) +
+                                                  " that the static scratch holds for this system size");
             alloc_atom_lists(std::min(npad, m + m / 8 + chunk));
         }
         throw Error(MPID_ERR_CUDA, "neighbour list overflow");
@@ -1009,6 +1040,42 @@ struct Context {
         return energy;
     }
 
+    // Evaluation with the neighbour lists and per-task energies in `scratch` (the static
+    // array above, kNoAllocBytes); allocates nothing and never grows a buffer.
+    double evaluate_device_noalloc(const double* d_pos, const double* hbox, double* d_forces, double* d_energy,
+                                   void* scratch) {
+        if (!usePme)
+            throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc supports PME only (the no-cutoff set-up "
+                                          "stages the sort order through host memory)");
+        size_t capUse = (kNoAllocListEntries / (size_t) npad) / chunk * chunk;
+        capUse = std::min(capUse, (kNoAllocTasks / (size_t) ntiles) * chunk);
+        if (capUse < (size_t) chunk)
+            throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: " + std::to_string(n) +
+                                              " atoms do not fit the static scratch (at most " +
+                                              std::to_string(kNoAllocListEntries / chunk) + " atoms)");
+        // Point the list and task-energy buffers at the scratch for this call only.
+        struct Redirect {
+            Context& c;
+            unsigned* listP; size_t listN;
+            double* enP; size_t enN;
+            int cap; long long entries;
+            ~Redirect() {
+                c.list.p = listP; c.list.n = listN;
+                c.energyBlocks.p = enP; c.energyBlocks.n = enN;
+                c.cap = cap; c.listEntries = entries;
+                c.growForbidden = false;
+            }
+        } guard{*this, list.p, list.n, energyBlocks.p, energyBlocks.n, cap, listEntries};
+        list.p = (unsigned*) scratch;
+        list.n = (size_t) npad * capUse;
+        energyBlocks.p = (double*) ((char*) scratch + kNoAllocListEntries * 4);
+        energyBlocks.n = kNoAllocTasks;
+        cap = (int) capUse;
+        listEntries = (long long) list.n;
+        growForbidden = true;
+        return evaluate_device(d_pos, hbox, d_forces, d_energy);
+    }
+
     void get_dipoles(int which, double* host) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
         if (which < 0 || which > 3) throw Error(MPID_ERR_INVALID, "which must be 0, 1, 2 or 3");
@@ -1127,6 +1194,36 @@ int mpid_evaluate_device(mpid_context* ctx, const double* d_positions, const dou
     if (!ctx || !d_positions || !box || !d_forces) throw Error(MPID_ERR_INVALID, "null argument");
     ctx->ctx.stream = (cudaStream_t) stream;
     ctx->ctx.evaluate_device(d_positions, box, d_forces, d_energy);
+    return MPID_OK;
+    MPID_API_END
+}
+
+// Device address of the static scratch on the current device, looked up once per device
+// (the first call on a device must not run under stream capture).
+static std::mutex g_noallocMutex;
+static void* g_noallocPtr[mpid::kNoAllocMaxDevices] = {};
+
+static void* noalloc_scratch(int device) {
+    if (device < 0 || device >= mpid::kNoAllocMaxDevices) throw Error(MPID_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (!g_noallocPtr[device]) {
+        CUDA_CHECK(cudaSetDevice(device));
+        void* p = nullptr;
+        const cudaError_t rc = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (rc != cudaSuccess)
+            throw Error(MPID_ERR_CUDA, std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(rc));
+        g_noallocPtr[device] = p;
+    }
+    return g_noallocPtr[device];
+}
+
+int mpid_evaluate_device_noalloc(mpid_context* ctx, const double* d_positions, const double* box, double* d_forces,
+                                 double* d_energy, void* stream) {
+    MPID_API_BEGIN
+    if (!ctx || !d_positions || !box || !d_forces) throw Error(MPID_ERR_INVALID, "null argument");
+    void* scratch = noalloc_scratch(ctx->ctx.device);
+    ctx->ctx.stream = (cudaStream_t) stream;
+    ctx->ctx.evaluate_device_noalloc(d_positions, box, d_forces, d_energy, scratch);
     return MPID_OK;
     MPID_API_END
 }
