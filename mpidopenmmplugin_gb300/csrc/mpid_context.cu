@@ -299,8 +299,8 @@ struct Context {
     size_t cubBytes = 0;
     DBuf<double> pos, wpos, center, half;
     // neighbour lists (tile lists, then per-atom lists; layouts in mpid_kernels.cuh)
-    int tcap = 0, cap = 0, chunk = 32, nchunks = 1;
-    DBuf<int> tileCount, tileJ, listCount, listTmax, listMax;
+    int tcap = 0, cap = 0, chunk = 32, nchunksL = 1, nchunksS = 0;
+    DBuf<int> tileCount, tileJ, countL, countS, tmaxL, tmaxS, listMax;
     DBuf<float4> shF;
     DBuf<double> shD;
     DBuf<unsigned> list;
@@ -381,7 +381,8 @@ struct Context {
         cubTemp.alloc(cubBytes);
         pos.alloc(3 * n); wpos.alloc(3 * n); center.alloc(3 * ntiles); half.alloc(3 * ntiles);
         // list capacities from the density (regrown on overflow)
-        tileCount.alloc(ntiles); listCount.alloc(npad); listTmax.alloc(ntiles); listMax.alloc(2);
+        tileCount.alloc(ntiles); countL.alloc(npad); countS.alloc(npad); tmaxL.alloc(ntiles); tmaxS.alloc(ntiles);
+        listMax.alloc(4);
         alloc_tile_lists(usePme ? std::min(ntiles, 96) : ntiles);
         alloc_atom_lists(usePme ? 64 : npad);
         forceFx.alloc(3 * (size_t) npad); torqueFx.alloc(3 * (size_t) npad);
@@ -595,7 +596,20 @@ struct Context {
         if (entries > ((size_t) 1 << 34)) throw Error(MPID_ERR_INVALID, "neighbour list would exceed 64 GB");
         list.alloc(entries);
         listEntries = (long long) entries;
-        energyBlocks.alloc((size_t) ntiles * (cap / chunk));
+        energyBlocks.alloc((size_t) ntiles * (cap / chunk + 2));
+    }
+
+    template <typename real>
+    PairConsts<real> pair_consts_host() const {
+        PairConsts<real> c;
+        for (int k = 0; k < 3; ++k) {
+            c.L[k] = (real) box.L[k];
+            c.iL[k] = (real) box.invL[k];
+        }
+        c.rc2 = usePme ? (real) (set.cutoff * set.cutoff) : (real) 3.0e38f;
+        c.thole = (real) set.default_thole;
+        c.ew = EwaldAlpha<real>(usePme ? set.ewald_alpha : 0.0);
+        return c;
     }
 
     NbrList nbr_list() const {
@@ -604,18 +618,19 @@ struct Context {
         c.tcap = tcap;
         c.cap = cap;
         c.chunk = chunk;
-        c.nchunks = nchunks;
+        c.nchunksL = nchunksL;
+        c.nchunksS = nchunksS;
         c.tileJ = tileJ.p;
         c.shF = shF.p;
         c.shD = shD.p;
-        c.count = listCount.p;
-        c.tmax = listTmax.p;
+        c.countL = countL.p;
+        c.countS = countS.p;
+        c.tmaxL = tmaxL.p;
+        c.tmaxS = tmaxS.p;
         c.list = list.p;
         c.usePbc = usePme ? 1 : 0;
-        c.cutoff = usePme ? set.cutoff : 1e30;
-        c.ewald = usePme ? set.ewald_alpha : 0.0;
-        c.defaultThole = set.default_thole;
-        c.box = box;
+        c.cf = pair_consts_host<float>();
+        c.cd = pair_consts_host<double>();
         c.covOff = covOff.p;
         c.covJ = covJ.p;
         c.covS = covS.p;
@@ -623,7 +638,7 @@ struct Context {
     }
 
     // warp tasks (tile, chunk) of the pair kernels
-    int pair_tasks() const { return ntiles * nchunks; }
+    int pair_tasks() const { return ntiles * (nchunksL + nchunksS); }
     int pair_blocks() const { return std::max(1, nblk(pair_tasks(), kWarpsPerBlock)); }
 
     // Sort, tiles, tile pairs.
@@ -673,24 +688,28 @@ struct Context {
         cudaStream_t st = stream;
         const double listCut = usePme ? set.cutoff * (1.0 + 1e-6) + 1e-5 : 1e30;
         const float cut2 = usePme ? (float) (listCut * listCut) : 3.0e38f;
+        // erfc / quadrature segment boundary: alpha r = kQuadX
+        const float quadR2 = usePme ? (float) std::pow(Prec<float>::kQuadX / set.ewald_alpha, 2) : 0.f;
         for (int attempt = 0; attempt < 2; ++attempt) {
-            CUDA_CHECK(cudaMemsetAsync(listMax.p + 1, 0, sizeof(int), st));
+            CUDA_CHECK(cudaMemsetAsync(listMax.p + 1, 0, 3 * sizeof(int), st));
             launch(k_atom_list<real>, nblk((long long) ntiles * 32, 128), 128, 0, st, ntiles, npad, e.off.p, e.orig.p, box,
-                   cut2, tcap, tileCount.p, tileJ.p, shF.p, covOff.p, covJ.p, covS.p, cap, listCount.p, listTmax.p, list.p,
-                   listMax.p + 1);
-            int m = 0;
-            CUDA_CHECK(cudaMemcpyAsync(&m, listMax.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+                   cut2, quadR2, usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, covOff.p, covJ.p, covS.p, cap,
+                   countL.p, countS.p, tmaxL.p, tmaxS.p, list.p, listMax.p + 1);
+            int m[3] = {0, 0, 0};
+            CUDA_CHECK(cudaMemcpyAsync(m, listMax.p + 1, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
-            lastMaxList = m;
-            if (m <= cap) {
-                nchunks = std::max(1, (m + chunk - 1) / chunk);
+            lastMaxList = m[0];
+            if (m[0] <= cap) {
+                nchunksL = (m[1] + chunk - 1) / chunk;
+                nchunksS = (m[2] + chunk - 1) / chunk;
+                if (nchunksL + nchunksS == 0) nchunksL = 1;
                 return;
             }
             if (growForbidden)
-                throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: an atom has " + std::to_string(m) +
+                throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: an atom has " + std::to_string(m[0]) +
                                                   " neighbours, more than the " + std::to_string(cap) +
                                                   " that the static scratch holds for this system size");
-            alloc_atom_lists(std::min(npad, m + m / 8 + chunk));
+            alloc_atom_lists(std::min(npad, m[0] + m[0] / 8 + chunk));
         }
         throw Error(MPID_ERR_CUDA, "neighbour list overflow");
     }
@@ -1048,7 +1067,8 @@ struct Context {
             throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc supports PME only (the no-cutoff set-up "
                                           "stages the sort order through host memory)");
         size_t capUse = (kNoAllocListEntries / (size_t) npad) / chunk * chunk;
-        capUse = std::min(capUse, (kNoAllocTasks / (size_t) ntiles) * chunk);
+        const size_t perTile = kNoAllocTasks / (size_t) ntiles;  // work items per tile the array holds
+        capUse = std::min(capUse, perTile >= 2 ? (perTile - 2) * chunk : 0);
         if (capUse < (size_t) chunk)
             throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: " + std::to_string(n) +
                                               " atoms do not fit the static scratch (at most " +

@@ -270,15 +270,23 @@ __device__ __forceinline__ double pair_scale(int oi, int oj, const int* __restri
     return 1.0;
 }
 
+// Flag of a covalent scale as stored in list entries.
+__device__ __forceinline__ unsigned scale_flag(double sc) { return sc == 1.0 ? 0u : (sc == 0.0 ? 1u : 2u); }
+
 // Atom lists: one warp per tile I; each lane tests the 32 atoms of every J tile in I's
-// tile list (float arithmetic, cutoff2 already includes a small skin so that both the
-// FP32 and the FP64 kernels, which apply the exact cutoff, see every pair).
+// tile list (float arithmetic; cutoff2 includes a small skin so that both the FP32 and
+// the FP64 kernels, which apply the exact cutoff, see every pair).  Each lane's list has
+// two segments so that the pair kernels never mix the two radial branches in a warp:
+// the erfc segment grows from the front (count nL), the quadrature segment (alpha r
+// below the threshold, r2 < quadR2, or covalent scale 0 under PME) from the back (nS).
 template <typename real>
 __global__ void k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __restrict__ orig, BoxDev box,
-                            float cutoff2, int tcap, const int* __restrict__ tileCount, const int* __restrict__ tileJ,
-                            const float4* __restrict__ shF, const int* __restrict__ covOff, const int* __restrict__ covJ,
-                            const double* __restrict__ covS, int cap, int* __restrict__ count, int* __restrict__ tmax,
-                            unsigned* __restrict__ list, int* __restrict__ maxCount) {
+                            float cutoff2, float quadR2, int usePme, int tcap, const int* __restrict__ tileCount,
+                            const int* __restrict__ tileJ, const float4* __restrict__ shF, const int* __restrict__ covOff,
+                            const int* __restrict__ covJ, const double* __restrict__ covS, int cap,
+                            int* __restrict__ countL, int* __restrict__ countS, int* __restrict__ tmaxL,
+                            int* __restrict__ tmaxS, unsigned* __restrict__ list, int* __restrict__ maxCounts) {
+    constexpr int kCache = 8;
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (I >= ntiles) return;
     const int si = I * 32 + lane;
@@ -286,8 +294,19 @@ __global__ void k_atom_list(int ntiles, int npad, const real* __restrict__ off, 
     const int origI = orig[si];
     const float L[3] = {(float) box.L[0], (float) box.L[1], (float) box.L[2]};
     const float iL[3] = {(float) box.invL[0], (float) box.invL[1], (float) box.invL[2]};
+    // covalent partners of this atom: the first kCache in registers
+    int cb = 0, ce = 0;
+    if (origI >= 0) { cb = covOff[origI]; ce = covOff[origI + 1]; }
+    const int ncached = min(ce - cb, kCache);
+    int pJ[kCache];
+    unsigned pF[kCache];
+#pragma unroll
+    for (int k = 0; k < kCache; ++k) {
+        pJ[k] = k < ncached ? covJ[cb + k] : -1;
+        pF[k] = k < ncached ? scale_flag(covS[cb + k]) : 0u;
+    }
     unsigned* out = list + (size_t) I * cap * 32 + lane;
-    int cnt = 0;
+    int nL = 0, nS = 0;
     const int nt = tileCount[I];
     for (int s = 0; s < nt; ++s) {
         const int Jw = tileJ[(size_t) I * tcap + s];
@@ -307,103 +326,126 @@ __global__ void k_atom_list(int ntiles, int npad, const real* __restrict__ off, 
             const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
             if (origI < 0 || oj < 0 || r2 >= cutoff2 || (J == I && jl == lane)) continue;
             unsigned flag = 0;
-            for (int k = covOff[origI]; k < covOff[origI + 1]; ++k)
-                if (covJ[k] == oj) {
-                    const double sc = covS[k];
-                    flag = sc == 1.0 ? 0u : (sc == 0.0 ? 1u : 2u);
-                    break;
-                }
-            if (cnt < cap) out[(size_t) cnt * 32] = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
-            ++cnt;
+#pragma unroll
+            for (int k = 0; k < kCache; ++k)
+                if (pJ[k] == oj) flag = pF[k];
+            if (ce - cb > kCache)
+                for (int k = cb + kCache; k < ce; ++k)
+                    if (covJ[k] == oj) {
+                        flag = scale_flag(covS[k]);
+                        break;
+                    }
+            const unsigned code = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
+            const bool quad = usePme && (r2 < quadR2 || flag == 1u);
+            if (nL + nS < cap) out[(size_t) (quad ? cap - 1 - nS : nL) * 32] = code;
+            if (quad) ++nS; else ++nL;
         }
     }
-    count[si] = min(cnt, cap);
-    int m = cnt;
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    countL[si] = nL;
+    countS[si] = nS;
+    int mt = nL + nS, ml = nL, ms = nS;
+    for (int o = 16; o > 0; o >>= 1) {
+        mt = max(mt, __shfl_xor_sync(0xffffffffu, mt, o));
+        ml = max(ml, __shfl_xor_sync(0xffffffffu, ml, o));
+        ms = max(ms, __shfl_xor_sync(0xffffffffu, ms, o));
+    }
     if (lane == 0) {
-        tmax[I] = min(m, cap);
-        atomicMax(maxCount, m);
+        tmaxL[I] = ml;
+        tmaxS[I] = ms;
+        atomicMax(maxCounts, mt);
+        atomicMax(maxCounts + 1, ml);
+        atomicMax(maxCounts + 2, ms);
     }
 }
 
+// Pair constants of one arithmetic type, computed on the host (no FP64 in FP32 loops).
+template <typename real>
+struct PairConsts {
+    real L[3], iL[3];
+    real rc2;       // exact cutoff squared
+    real thole;     // default Thole width
+    EwaldAlpha<real> ew;
+};
+
 // Neighbour lists and pair constants as the pair kernels see them.
 struct NbrList {
-    int ntiles, tcap, cap, chunk, nchunks;
+    int ntiles, tcap, cap, chunk;
+    int nchunksL, nchunksS;   // work items per tile over the erfc / quadrature segments
     const int* tileJ;
     const float4* shF;
     const double* shD;
-    const int* count;
-    const int* tmax;
+    const int* countL;
+    const int* countS;
+    const int* tmaxL;
+    const int* tmaxS;
     const unsigned* list;
     int usePbc;
-    double cutoff;
-    double ewald;
-    double defaultThole;
-    BoxDev box;
+    PairConsts<float> cf;
+    PairConsts<double> cd;
     const int* covOff;
     const int* covJ;
     const double* covS;
 };
 
-// Work item of a pair kernel: entries [k0, k0 + chunk) of the lists of tile I.
+template <typename real> __device__ __forceinline__ const PairConsts<real>& pair_consts(const NbrList& nl);
+template <> __device__ __forceinline__ const PairConsts<float>& pair_consts<float>(const NbrList& nl) { return nl.cf; }
+template <> __device__ __forceinline__ const PairConsts<double>& pair_consts<double>(const NbrList& nl) { return nl.cd; }
+
+// Work item of a pair kernel: entries [k0, k0 + chunk) of one segment of the lists of
+// tile I.  quad is uniform over the warp.
 struct PairTask {
-    int I, k0, lane, si;
+    int I, k0, k1, lane, si;
+    bool quad;
+    __device__ __forceinline__ int tasks(const NbrList& nl) const { return nl.ntiles * (nl.nchunksL + nl.nchunksS); }
     __device__ __forceinline__ bool init(const NbrList& nl) {
         const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        const int nch = nl.nchunksL + nl.nchunksS;
         lane = threadIdx.x & 31;
-        I = w / nl.nchunks;
-        k0 = (w - I * nl.nchunks) * nl.chunk;
+        I = w / nch;
+        const int c = w - I * nch;
+        quad = c >= nl.nchunksL;
+        k0 = (quad ? c - nl.nchunksL : c) * nl.chunk;
         si = I * 32 + lane;
-        return I < nl.ntiles && k0 < nl.tmax[I];
+        if (I >= nl.ntiles || k0 >= (quad ? nl.tmaxS[I] : nl.tmaxL[I])) return false;
+        k1 = min(k0 + nl.chunk, quad ? nl.countS[si] : nl.countL[si]);
+        return true;
     }
 };
 
-// Precision-specific pieces of the pair loop: the tile shift and the box in `real`.
-template <typename real> struct PairGeom;
-template <> struct PairGeom<float> {
-    float L[3], iL[3], rc2, thole;
-    __device__ __forceinline__ void init(const NbrList& nl) {
-        for (int k = 0; k < 3; ++k) { L[k] = (float) nl.box.L[k]; iL[k] = (float) nl.box.invL[k]; }
-        rc2 = (float) (nl.cutoff * nl.cutoff);
-        thole = (float) nl.defaultThole;
-    }
-    __device__ __forceinline__ void shift(const NbrList& nl, size_t s, float* sh) const {
-        const float4 v = nl.shF[s];
-        sh[0] = v.x; sh[1] = v.y; sh[2] = v.z;
-    }
-};
-template <> struct PairGeom<double> {
-    double L[3], iL[3], rc2, thole;
-    __device__ __forceinline__ void init(const NbrList& nl) {
-        for (int k = 0; k < 3; ++k) { L[k] = nl.box.L[k]; iL[k] = nl.box.invL[k]; }
-        rc2 = nl.cutoff * nl.cutoff;
-        thole = nl.defaultThole;
-    }
-    __device__ __forceinline__ void shift(const NbrList& nl, size_t s, double* sh) const {
-        sh[0] = nl.shD[3 * s]; sh[1] = nl.shD[3 * s + 1]; sh[2] = nl.shD[3 * s + 2];
-    }
-};
-
-// Decode one list entry of lane `si` into j's sorted index, the displacement
-// d = R_j - R_i and r^2; returns false for pairs beyond the cutoff.
 template <typename real>
-__device__ __forceinline__ bool list_pair(const NbrList& nl, const PairGeom<real>& g, const AtomArrays<real>& at, int I,
-                                          int k, int lane, const real* oi, int& sj, unsigned& flag, real* d, real& r2) {
-    const unsigned code = nl.list[((size_t) I * nl.cap + k) * 32 + lane];
+__device__ __forceinline__ void tile_shift(const NbrList& nl, size_t s, real* sh);
+template <>
+__device__ __forceinline__ void tile_shift<float>(const NbrList& nl, size_t s, float* sh) {
+    const float4 v = nl.shF[s];
+    sh[0] = v.x; sh[1] = v.y; sh[2] = v.z;
+}
+template <>
+__device__ __forceinline__ void tile_shift<double>(const NbrList& nl, size_t s, double* sh) {
+    sh[0] = nl.shD[3 * s]; sh[1] = nl.shD[3 * s + 1]; sh[2] = nl.shD[3 * s + 2];
+}
+
+// Decode entry k of lane `lane` in segment QUAD of tile I into j's sorted index, the
+// displacement d = R_j - R_i and r^2; returns false for pairs beyond the cutoff.
+template <typename real, bool QUAD>
+__device__ __forceinline__ bool list_pair(const NbrList& nl, const PairConsts<real>& pc, const AtomArrays<real>& at,
+                                          int I, int k, int lane, const real* oi, int& sj, unsigned& flag, real* d,
+                                          real& r2) {
+    const int pos = QUAD ? nl.cap - 1 - k : k;
+    const unsigned code = nl.list[((size_t) I * nl.cap + pos) * 32 + lane];
     const size_t s = (size_t) I * nl.tcap + (code >> 7);
     const int Jw = nl.tileJ[s];
     sj = (Jw & 0x7fffffff) * 32 + (int) (code & 31u);
     flag = (code >> 5) & 3u;
     real sh[3];
-    g.shift(nl, s, sh);
+    tile_shift<real>(nl, s, sh);
     const int npad = at.npad;
 #pragma unroll
     for (int q = 0; q < 3; ++q) d[q] = sh[q] + (at.off[q * npad + sj] - oi[q]);
     if (Jw < 0)
 #pragma unroll
-        for (int q = 0; q < 3; ++q) d[q] -= g.L[q] * rint(d[q] * g.iL[q]);
+        for (int q = 0; q < 3; ++q) d[q] -= pc.L[q] * rint(d[q] * pc.iL[q]);
     r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-    return !(nl.usePbc && r2 > g.rc2);
+    return !(nl.usePbc && r2 > pc.rc2);
 }
 
 template <typename real>
@@ -416,32 +458,24 @@ constexpr int kWarpsPerBlock = 4;
 // ---------------------------------------------------------------------------
 // Real-space permanent field at every atom (kernel K_i with the pair's covalent scale):
 // the PME real-space part of MPIDReferenceForce.cpp:2812-2920 / :911-934.
-template <typename real>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_fixed_field(NbrList nl, AtomArrays<real> at, unsigned long long* __restrict__ field) {
-    PairTask t;
-    if (!t.init(nl)) return;
+template <typename real, bool QUAD>
+__device__ __forceinline__ void fixed_field_loop(const NbrList& nl, const AtomArrays<real>& at, const PairTask& t,
+                                                 int origI, real* Ei) {
+    const PairConsts<real>& pc = pair_consts<real>(nl);
     const int npad = at.npad, si = t.si;
-    const int origI = at.orig[si];
-    if (origI < 0) return;
-    const int k1 = min(t.k0 + nl.chunk, nl.count[si]);
-    PairGeom<real> g;
-    g.init(nl);
-    const EwaldAlpha<real> ew(nl.ewald);
     const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
     const typename Vec4<real>::type pi = at.prm[si];
-    real Ei[3] = {real(0), real(0), real(0)};
-    for (int k = t.k0; k < k1; ++k) {
+    for (int k = t.k0; k < t.k1; ++k) {
         int sj;
         unsigned flag;
         real d[3], r2;
-        if (!list_pair(nl, g, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
+        if (!list_pair<real, QUAD>(nl, pc, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
         const real r = sqrt(r2);
         const real scale = list_scale<real>(nl, flag, origI, at.orig[sj]);
         const typename Vec4<real>::type pj = at.prm[sj];
-        const real a = scale == real(0) ? pi.x + pj.x : g.thole;
+        const real a = scale == real(0) ? pi.x + pj.x : pc.thole;
         PairRadial<real, 0, 4, 0> pr;
-        pair_radial<real, -1, 4, -1>(r, ew, scale, a, pi.y * pj.y, pr);
+        pair_radial_branch<real, -1, 4, -1, QUAD>(r, pc.ew, scale, a, pi.y * pj.y, pr);
         LabMoments<real> mj;
         load_moments(at.mom, npad, sj, mj);
         const real sI[3] = {-d[0], -d[1], -d[2]};
@@ -449,41 +483,42 @@ k_fixed_field(NbrList nl, AtomArrays<real> at, unsigned long long* __restrict__ 
         multipole_field(mj, sI, pr.bI, e);
         Ei[0] += e[0]; Ei[1] += e[1]; Ei[2] += e[2];
     }
-    for (int q = 0; q < 3; ++q) fx_add(field + q * npad + si, Ei[q]);
+}
+
+template <typename real>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_fixed_field(NbrList nl, AtomArrays<real> at, unsigned long long* __restrict__ field) {
+    PairTask t;
+    if (!t.init(nl)) return;
+    const int origI = at.orig[t.si];
+    if (origI < 0) return;
+    real Ei[3] = {real(0), real(0), real(0)};
+    if (t.quad)
+        fixed_field_loop<real, true>(nl, at, t, origI, Ei);
+    else
+        fixed_field_loop<real, false>(nl, at, t, origI, Ei);
+    for (int q = 0; q < 3; ++q) fx_add(field + q * at.npad + t.si, Ei[q]);
 }
 
 // Real-space field of point dipoles (kernel K_u), optionally with its gradient:
 // MPIDReferenceForce.cpp:4161-4281.  mu is [3][npad] in sorted order.
-template <typename real, bool GRAD>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_dipole_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ field,
-               unsigned long long* __restrict__ grad, const int* __restrict__ skip) {
-    if (skip && *skip) return;
-    PairTask t;
-    if (!t.init(nl)) return;
+template <typename real, bool GRAD, bool QUAD>
+__device__ __forceinline__ void dipole_field_loop(const NbrList& nl, const AtomArrays<real>& at, const real* mu,
+                                                  const PairTask& t, real* acc) {
+    const PairConsts<real>& pc = pair_consts<real>(nl);
     const int npad = at.npad, si = t.si;
-    const int origI = at.orig[si];
-    if (origI < 0) return;
-    const int k1 = min(t.k0 + nl.chunk, nl.count[si]);
-    PairGeom<real> g;
-    g.init(nl);
-    const EwaldAlpha<real> ew(nl.ewald);
     const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
     const typename Vec4<real>::type pi = at.prm[si];
-    constexpr int NACC = GRAD ? 9 : 3;
-    real acc[NACC];
-#pragma unroll
-    for (int q = 0; q < NACC; ++q) acc[q] = real(0);
-    for (int k = t.k0; k < k1; ++k) {
+    for (int k = t.k0; k < t.k1; ++k) {
         int sj;
         unsigned flag;
         real d[3], r2;
-        if (!list_pair(nl, g, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
+        if (!list_pair<real, QUAD>(nl, pc, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
         const real r = sqrt(r2);
         const typename Vec4<real>::type pj = at.prm[sj];
-        const real a = flag == 1u ? pi.x + pj.x : g.thole;  // flag 1: covalent scale 0
+        const real a = flag == 1u ? pi.x + pj.x : pc.thole;  // flag 1: covalent scale 0
         PairRadial<real, 0, 0, GRAD ? 3 : 2> pr;
-        pair_radial<real, -1, -1, GRAD ? 3 : 2>(r, ew, real(1), a, pi.y * pj.y, pr);
+        pair_radial_branch<real, -1, -1, GRAD ? 3 : 2, QUAD>(r, pc.ew, real(1), a, pi.y * pj.y, pr);
         const real b[4] = {real(0), pr.bU[1], pr.bU[2], GRAD ? pr.bU[GRAD ? 3 : 2] : real(0)};
         const real uj[3] = {mu[sj], mu[npad + sj], mu[2 * npad + sj]};
         const real sI[3] = {-d[0], -d[1], -d[2]};
@@ -495,9 +530,28 @@ k_dipole_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, uns
 #pragma unroll
             for (int q = 0; q < 6; ++q) acc[3 + q] += gr[q];
     }
-    for (int q = 0; q < 3; ++q) fx_add(field + q * npad + si, acc[q]);
+}
+
+template <typename real, bool GRAD>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_dipole_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ field,
+               unsigned long long* __restrict__ grad, const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    PairTask t;
+    if (!t.init(nl)) return;
+    if (at.orig[t.si] < 0) return;
+    constexpr int NACC = GRAD ? 9 : 3;
+    real acc[NACC];
+#pragma unroll
+    for (int q = 0; q < NACC; ++q) acc[q] = real(0);
+    if (t.quad)
+        dipole_field_loop<real, GRAD, true>(nl, at, mu, t, acc);
+    else
+        dipole_field_loop<real, GRAD, false>(nl, at, mu, t, acc);
+    const int npad = at.npad;
+    for (int q = 0; q < 3; ++q) fx_add(field + q * npad + t.si, acc[q]);
     if (GRAD)
-        for (int q = 0; q < 6; ++q) fx_add(grad + q * npad + si, acc[3 + q]);
+        for (int q = 0; q < 6; ++q) fx_add(grad + q * npad + t.si, acc[3 + q]);
 }
 
 // Compensated running sum (TwoSum) for the FP32 pair energies.
@@ -517,6 +571,43 @@ struct KahanSum {
 // evaluates its atom's pairs (both atoms of a pair evaluate it), adds force and torque
 // on its own atom, and counts the energy of pairs with i < j; pairs of covalent scale
 // other than 1 leave their energy to k_scaled_pair_energy.
+template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE, bool QUAD>
+__device__ __forceinline__ void electrostatics_loop(const NbrList& nl, const AtomArrays<real>& at, const real* mu,
+                                                    const PairTask& t, int origI, real* accF, real* accT,
+                                                    KahanSum<real>& eSum) {
+    const PairConsts<real>& pc = pair_consts<real>(nl);
+    const int npad = at.npad, si = t.si;
+    const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+    const real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
+    LabMoments<real> mi;
+    load_moments(at.mom, npad, si, mi);
+    const typename Vec4<real>::type pi = at.prm[si];
+    for (int k = t.k0; k < t.k1; ++k) {
+        int sj;
+        unsigned flag;
+        real d[3], r2;
+        if (!list_pair<real, QUAD>(nl, pc, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
+        const real r = sqrt(r2);
+        const real scale = list_scale<real>(nl, flag, origI, at.orig[sj]);
+        const typename Vec4<real>::type pj = at.prm[sj];
+        const real a = scale == real(0) ? pi.x + pj.x : pc.thole;
+        PairRadial<real, 7, 5, MUTUAL ? 3 : 0> pr;
+        pair_radial_branch<real, 7, 5, MUTUAL ? 3 : -1, QUAD>(r, pc.ew, scale, a, pi.y * pj.y, pr);
+        LabMoments<real> mj;
+        load_moments(at.mom, npad, sj, mj);
+        const real uj[3] = {mu[sj], mu[npad + sj], mu[2 * npad + sj]};
+        PairOut<real> po;
+        qi_pair<real, MUTUAL, REF_ANISO_TORQUE>(d, r, mi, mj, ui, uj, pi.z != real(0), pj.z != real(0), pr.bP, pr.bI,
+                                                 pr.bU, po);
+        if (flag == 0u && si < sj) eSum.add(po.energy);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            accF[q] -= po.fJ[q];
+            accT[q] += po.tI[q];
+        }
+    }
+}
+
 // out: force[3][npad], torque[3][npad] fixed point; energy[task] (already x kElectric).
 template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
@@ -528,51 +619,22 @@ k_electrostatics(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, u
     const int origI = active ? at.orig[si] : -1;
     KahanSum<real> eSum;
     if (origI >= 0) {
-        const int k1 = min(t.k0 + nl.chunk, nl.count[si]);
-        PairGeom<real> g;
-        g.init(nl);
-        const EwaldAlpha<real> ew(nl.ewald);
-        const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
-        const real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
-        LabMoments<real> mi;
-        load_moments(at.mom, npad, si, mi);
-        const typename Vec4<real>::type pi = at.prm[si];
         real accF[3] = {real(0), real(0), real(0)}, accT[3] = {real(0), real(0), real(0)};
-        for (int k = t.k0; k < k1; ++k) {
-            int sj;
-            unsigned flag;
-            real d[3], r2;
-            if (!list_pair(nl, g, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
-            const real r = sqrt(r2);
-            const real scale = list_scale<real>(nl, flag, origI, at.orig[sj]);
-            const typename Vec4<real>::type pj = at.prm[sj];
-            const real a = scale == real(0) ? pi.x + pj.x : g.thole;
-            PairRadial<real, 7, 5, MUTUAL ? 3 : 0> pr;
-            pair_radial<real, 7, 5, MUTUAL ? 3 : -1>(r, ew, scale, a, pi.y * pj.y, pr);
-            LabMoments<real> mj;
-            load_moments(at.mom, npad, sj, mj);
-            const real uj[3] = {mu[sj], mu[npad + sj], mu[2 * npad + sj]};
-            PairOut<real> po;
-            qi_pair<real, MUTUAL, REF_ANISO_TORQUE>(d, r, mi, mj, ui, uj, pi.z != real(0), pj.z != real(0), pr.bP, pr.bI,
-                                                     pr.bU, po);
-            if (flag == 0u && si < sj) eSum.add(po.energy);
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                accF[q] -= po.fJ[q];
-                accT[q] += po.tI[q];
-            }
-        }
+        if (t.quad)
+            electrostatics_loop<real, MUTUAL, REF_ANISO_TORQUE, true>(nl, at, mu, t, origI, accF, accT, eSum);
+        else
+            electrostatics_loop<real, MUTUAL, REF_ANISO_TORQUE, false>(nl, at, mu, t, origI, accF, accT, eSum);
         const real E = real(kElectric);
         for (int q = 0; q < 3; ++q) {
             fx_add(force + q * npad + si, E * accF[q]);
             fx_add(torque + q * npad + si, E * accT[q]);
         }
     }
-    // FP64 energy of the task: warp sum, written per task (fixed-order reduction later)
+    // FP64 energy of the work item: warp sum, written per item (fixed-order reduction later)
     double e = eSum.value();
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (t.lane == 0 && w < nl.ntiles * nl.nchunks) energy[w] = e * kElectric;
+    if (t.lane == 0 && w < t.tasks(nl)) energy[w] = e * kElectric;
 }
 
 // Energy of covalently scaled pairs (scale != 1) in FP64.  Their real-space terms remove

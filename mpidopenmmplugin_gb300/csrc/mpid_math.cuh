@@ -89,6 +89,7 @@ struct EwaldAlpha {
     real hi, lo;        // alpha
     real pre_hi, pre_lo;  // 2 alpha / sqrt(pi)
     real a2x2;          // 2 alpha^2
+    MPID_HD EwaldAlpha() : hi(0), lo(0), pre_hi(0), pre_lo(0), a2x2(0) {}
     MPID_HD explicit EwaldAlpha(double a) {
         hi = real(a);
         lo = real(a - double(hi));
@@ -218,9 +219,13 @@ struct PairRadial {
     real bU[NU + 1];
 };
 
-// Compute the requested radial arrays.  NP/NI/NU < 0 disables a kernel.
-template <typename real, int NP, int NI, int NU>
-MPID_HD void pair_radial(real r, const EwaldAlpha<real>& alpha, real scale, real tholeA, real dampProd, PairRadial<real, (NP > 0 ? NP : 0), (NI > 0 ? NI : 0), (NU > 0 ? NU : 0)>& out) {
+// Compute the requested radial arrays.  NP/NI/NU < 0 disables a kernel.  QUAD selects
+// the branch at compile time: true integrates the erf part by quadrature (needed where
+// erf(alpha r)/r must not be formed as a difference: alpha r below the threshold, or
+// covalent scale 0), false uses the erfc recursion.  pair_radial picks by alpha r.
+template <typename real, int NP, int NI, int NU, bool QUAD>
+MPID_HD void pair_radial_branch(real r, const EwaldAlpha<real>& alpha, real scale, real tholeA, real dampProd,
+                                PairRadial<real, (NP > 0 ? NP : 0), (NI > 0 ? NI : 0), (NU > 0 ? NU : 0)>& out) {
     constexpr int NMAX = (NP > NI ? (NP > NU ? NP : NU) : (NI > NU ? NI : NU));
     const real rinv = real(1) / r;
     const real rinv2 = rinv * rinv;
@@ -239,8 +244,7 @@ MPID_HD void pair_radial(real r, const EwaldAlpha<real>& alpha, real scale, real
             thole_lambdas<real, NT>(sT, lam, oneMinus);
         }
     }
-    const real x = alpha.times(r);
-    if (x < real(Prec<real>::kQuadX)) {
+    if (QUAD) {
         real bF[NMAX + 1];
         erf_part_quadrature<real, NMAX>(r, alpha, bF);
         if (NP >= 0) {
@@ -273,6 +277,22 @@ MPID_HD void pair_radial(real r, const EwaldAlpha<real>& alpha, real scale, real
             for (int n = 1; n <= NU; ++n) out.bU[n] = bE[n] - oneMinus[n] * bB[n];
         }
     }
+}
+
+// True where the quadrature branch is required: alpha r below the threshold, or a
+// covalent scale of 0 (the kernel is then -erf(alpha r)/r at any distance).
+template <typename real>
+MPID_HD bool radial_needs_quadrature(real r, const EwaldAlpha<real>& alpha, real scale) {
+    return alpha.times(r) < real(Prec<real>::kQuadX) || scale == real(0);
+}
+
+template <typename real, int NP, int NI, int NU>
+MPID_HD void pair_radial(real r, const EwaldAlpha<real>& alpha, real scale, real tholeA, real dampProd,
+                         PairRadial<real, (NP > 0 ? NP : 0), (NI > 0 ? NI : 0), (NU > 0 ? NU : 0)>& out) {
+    if (alpha.times(r) < real(Prec<real>::kQuadX))
+        pair_radial_branch<real, NP, NI, NU, true>(r, alpha, scale, tholeA, dampProd, out);
+    else
+        pair_radial_branch<real, NP, NI, NU, false>(r, alpha, scale, tholeA, dampProd, out);
 }
 
 // ---------------------------------------------------------------------------
