@@ -9,7 +9,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libmpid_gb300.so")
 SOURCES = ["mpid_context.cu"]
-DEPS = ["mpid_context.cu", "mpid_kernels.cuh", "mpid_math.cuh", "qi_tables.cuh", "pme_host.h"]
+DEPS = ["mpid_context.cu", "mpid_kernels.cuh", "mpid_math.cuh", "qi_tables.cuh", "pme_host.h", "df64.cuh",
+        "radial_tables.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -22,6 +22,7 @@
 #include "mpid_gb300.h"
 #include "mpid_kernels.cuh"
 #include "pme_host.h"
+#include "radial_tables.h"
 
 // ---------------------------------------------------------------------------
 // Static scratch of the allocation-free evaluation (mpid_evaluate_device_noalloc).
@@ -300,9 +301,14 @@ struct Context {
     DBuf<double> pos, wpos, center, half;
     // neighbour lists (tile lists, then per-atom lists; layouts in mpid_kernels.cuh)
     int tcap = 0, cap = 0, chunk = 32, nchunksL = 1, nchunksS = 0;
-    DBuf<int> tileCount, tileJ, countL, countS, tmaxL, tmaxS, listMax;
+    DBuf<int> tileCount, tileJ, countL, countS, loL, loS, tmaxL, tmaxS, listMax;
     DBuf<float4> shF;
     DBuf<double> shD;
+    DBuf<float2> shDF;
+    // double-float inputs and Ewald tables of the mixed path's residual field
+    DBuf<float2> offDF, muDF, tholeDF, dampDF;
+    DBuf<float> tabG, tabGc, tabH, tabHc;
+    RadialTableHost tabGh, tabHh;
     DBuf<unsigned> list;
     int lastTiles = 0, lastMaxList = 0;
     long long listEntries = 0;
@@ -381,7 +387,8 @@ struct Context {
         cubTemp.alloc(cubBytes);
         pos.alloc(3 * n); wpos.alloc(3 * n); center.alloc(3 * ntiles); half.alloc(3 * ntiles);
         // list capacities from the density (regrown on overflow)
-        tileCount.alloc(ntiles); countL.alloc(npad); countS.alloc(npad); tmaxL.alloc(ntiles); tmaxS.alloc(ntiles);
+        tileCount.alloc(ntiles); countL.alloc(npad); countS.alloc(npad); loL.alloc(npad); loS.alloc(npad);
+        tmaxL.alloc(ntiles); tmaxS.alloc(ntiles);
         listMax.alloc(4);
         alloc_tile_lists(usePme ? std::min(ntiles, 96) : ntiles);
         alloc_atom_lists(usePme ? 64 : npad);
@@ -408,6 +415,15 @@ struct Context {
             if (s.polarization_type == MPID_MUTUAL) {
                 ed.reset(new Engine<double>());  // FP64 residual of the refinement loop
                 ed->init(n, npad, usePme, s.pme_order, s.grid);
+                offDF.alloc(3 * (size_t) npad); muDF.alloc(3 * (size_t) npad);
+                tholeDF.alloc(npad); dampDF.alloc(npad);
+                if (usePme) {
+                    const double rq = Prec<float>::kQuadX / s.ewald_alpha;
+                    const double rL = s.cutoff * (1.0 + 1e-6) + 1e-5;
+                    build_ewald_tables(s.ewald_alpha, rq, rL, 32, 7, tabGh, tabHh);
+                    upload(tabG, tabGh.coef); upload(tabGc, tabGh.centre);
+                    upload(tabH, tabHh.coef); upload(tabHc, tabHh.centre);
+                }
             }
         } else {
             ed.reset(new Engine<double>());
@@ -589,6 +605,7 @@ struct Context {
         tileJ.alloc((size_t) ntiles * tcap);
         shF.alloc((size_t) ntiles * tcap);
         shD.alloc((size_t) 3 * ntiles * tcap);
+        shDF.alloc((size_t) 3 * ntiles * tcap);
     }
     void alloc_atom_lists(int c) {
         cap = ((c + chunk - 1) / chunk) * chunk;
@@ -597,6 +614,39 @@ struct Context {
         list.alloc(entries);
         listEntries = (long long) entries;
         energyBlocks.alloc((size_t) ntiles * (cap / chunk + 2));
+    }
+
+    static void upload(DBuf<float>& d, const std::vector<float>& h) {
+        d.alloc(h.size());
+        CUDA_CHECK(cudaMemcpy(d.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+
+    DfRadial df_radial() const {
+        DfRadial R;
+        R.Gcoef = tabG.p; R.Gcentre = tabGc.p; R.Hcoef = tabH.p; R.Hcentre = tabHc.p;
+        R.Gr0 = tabGh.r0; R.Ginvh = tabGh.invh; R.GK = tabGh.K;
+        R.Hr0 = tabHh.r0; R.Hinvh = tabHh.invh; R.HK = tabHh.K;
+        R.usePme = usePme ? 1 : 0;
+        R.rc2 = usePme ? (float) (set.cutoff * set.cutoff) : 3.0e38f;
+        for (int k = 0; k < 3; ++k) {
+            R.L[k] = (float) box.L[k];
+            R.iL[k] = (float) box.invL[k];
+            const dfloat v = df_from_double(box.L[k]);
+            R.Ldf[k] = make_float2(v.hi, v.lo);
+        }
+        const dfloat th = df_from_double(set.default_thole);
+        R.tholeDefault = make_float2(th.hi, th.lo);
+        return R;
+    }
+
+    DfAtoms df_atoms() const {
+        DfAtoms A;
+        A.npad = npad;
+        A.off = offDF.p;
+        A.mu = muDF.p;
+        A.thole = tholeDF.p;
+        A.damp = dampDF.p;
+        return A;
     }
 
     template <typename real>
@@ -623,8 +673,11 @@ struct Context {
         c.tileJ = tileJ.p;
         c.shF = shF.p;
         c.shD = shD.p;
+        c.shDF = shDF.p;
         c.countL = countL.p;
         c.countS = countS.p;
+        c.loL = loL.p;
+        c.loS = loS.p;
         c.tmaxL = tmaxL.p;
         c.tmaxS = tmaxS.p;
         c.list = list.p;
@@ -667,7 +720,7 @@ struct Context {
         for (int attempt = 0; attempt < 2; ++attempt) {
             CUDA_CHECK(cudaMemsetAsync(listMax.p, 0, sizeof(int), st));
             launch(k_tile_list, nblk((long long) ntiles * 32, 128), 128, 0, st, ntiles, center.p, half.p, box, listCut,
-                   usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, shD.p, listMax.p);
+                   usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, shD.p, shDF.p, listMax.p);
             int m = 0;
             CUDA_CHECK(cudaMemcpyAsync(&m, listMax.p, sizeof(int), cudaMemcpyDeviceToHost, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
@@ -694,7 +747,7 @@ struct Context {
             CUDA_CHECK(cudaMemsetAsync(listMax.p + 1, 0, 3 * sizeof(int), st));
             launch(k_atom_list<real>, nblk((long long) ntiles * 32, 128), 128, 0, st, ntiles, npad, e.off.p, e.orig.p, box,
                    cut2, quadR2, usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, covOff.p, covJ.p, covS.p, cap,
-                   countL.p, countS.p, tmaxL.p, tmaxS.p, list.p, listMax.p + 1);
+                   countL.p, countS.p, loL.p, loS.p, tmaxL.p, tmaxS.p, list.p, listMax.p + 1);
             int m[3] = {0, 0, 0};
             CUDA_CHECK(cudaMemcpyAsync(m, listMax.p + 1, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
@@ -759,12 +812,17 @@ struct Context {
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
         // the FP64 field of the mixed path's residual refinement is timed on its own
         timer.begin(mixed && sizeof(real) == 8 ? ST_REFINE_REAL : ST_DIPOLE_REAL, st);
-        if (G) {
+        if (mixed && sizeof(real) == 8) {
+            // residual refinement: real-space part in double-float on the FP32 pipes
+            launch(k_to_df, nblk(3LL * npad, 256), 256, 0, st, 3 * npad, (const double*) mu, muDF.p);
+            launch(k_dipole_field_df, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), df_radial(), df_atoms(),
+                   (const int*) e.orig.p, e.fieldFx.p);
+        } else if (G) {
             CUDA_CHECK(cudaMemsetAsync(e.gradFx.p, 0, 6 * (size_t) npad * 8, st));
-            launch(k_dipole_field<real, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), mu, e.fieldFx.p,
+            launch(k_dipole_field<real, true, sizeof(real) == 8>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), mu, e.fieldFx.p,
                                                                                      e.gradFx.p, skip);
         } else {
-            launch(k_dipole_field<real, false>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), mu,
+            launch(k_dipole_field<real, false, sizeof(real) == 8>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), mu,
                                                                                       e.fieldFx.p, nullptr, skip);
         }
         timer.end(st);
@@ -1012,7 +1070,10 @@ struct Context {
             Engine<float>& e = *ef;
             prepare_engine(e, true);
             atom_lists(e);
-            if (ed) prepare_engine(*ed, false);
+            if (ed) {
+                prepare_engine(*ed, false);
+                launch(k_df_atoms, nblk(npad, 128), 128, 0, st, npad, ed->off.p, ed->prm.p, offDF.p, tholeDF.p, dampDF.p);
+            }
             timer.end(st);
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL)

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "mpid_math.cuh"
+#include "df64.cuh"
 
 namespace mpid {
 
@@ -113,7 +114,8 @@ __global__ void k_tile_bounds(int n, int ntiles, const int* __restrict__ order,
 // half the box always counts as overlapping and marks the pair for per-pair imaging.
 __global__ void k_tile_list(int ntiles, const double* __restrict__ center, const double* __restrict__ half, BoxDev box,
                             double cutoff, int usePbc, int tcap, int* __restrict__ tileCount, int* __restrict__ tileJ,
-                            float4* __restrict__ shF, double* __restrict__ shD, int* __restrict__ maxTiles) {
+                            float4* __restrict__ shF, double* __restrict__ shD, float2* __restrict__ shDF,
+                            int* __restrict__ maxTiles) {
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (I >= ntiles) return;
     int base = 0;
@@ -145,9 +147,11 @@ __global__ void k_tile_list(int ntiles, const double* __restrict__ center, const
                 const size_t s = (size_t) I * tcap + pos;
                 tileJ[s] = J | (wrap ? (int) 0x80000000 : 0);
                 shF[s] = make_float4((float) sh[0], (float) sh[1], (float) sh[2], 0.f);
-                shD[3 * s] = sh[0];
-                shD[3 * s + 1] = sh[1];
-                shD[3 * s + 2] = sh[2];
+                for (int k = 0; k < 3; ++k) {
+                    shD[3 * s + k] = sh[k];
+                    const dfloat v = df_from_double(sh[k]);
+                    shDF[3 * s + k] = make_float2(v.hi, v.lo);
+                }
             }
         }
         base += __popc(m);
@@ -284,8 +288,9 @@ __global__ void k_atom_list(int ntiles, int npad, const real* __restrict__ off, 
                             float cutoff2, float quadR2, int usePme, int tcap, const int* __restrict__ tileCount,
                             const int* __restrict__ tileJ, const float4* __restrict__ shF, const int* __restrict__ covOff,
                             const int* __restrict__ covJ, const double* __restrict__ covS, int cap,
-                            int* __restrict__ countL, int* __restrict__ countS, int* __restrict__ tmaxL,
-                            int* __restrict__ tmaxS, unsigned* __restrict__ list, int* __restrict__ maxCounts) {
+                            int* __restrict__ countL, int* __restrict__ countS, int* __restrict__ loL,
+                            int* __restrict__ loS, int* __restrict__ tmaxL, int* __restrict__ tmaxS,
+                            unsigned* __restrict__ list, int* __restrict__ maxCounts) {
     constexpr int kCache = 8;
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (I >= ntiles) return;
@@ -306,7 +311,7 @@ __global__ void k_atom_list(int ntiles, int npad, const real* __restrict__ off, 
         pF[k] = k < ncached ? scale_flag(covS[cb + k]) : 0u;
     }
     unsigned* out = list + (size_t) I * cap * 32 + lane;
-    int nL = 0, nS = 0;
+    int nL = 0, nS = 0, lowL = 0, lowS = 0;  // lowX: entries with j < i (a prefix: j ascends)
     const int nt = tileCount[I];
     for (int s = 0; s < nt; ++s) {
         const int Jw = tileJ[(size_t) I * tcap + s];
@@ -338,11 +343,14 @@ __global__ void k_atom_list(int ntiles, int npad, const real* __restrict__ off, 
             const unsigned code = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
             const bool quad = usePme && (r2 < quadR2 || flag == 1u);
             if (nL + nS < cap) out[(size_t) (quad ? cap - 1 - nS : nL) * 32] = code;
-            if (quad) ++nS; else ++nL;
+            const bool low = J * 32 + jl < si;
+            if (quad) { ++nS; lowS += low; } else { ++nL; lowL += low; }
         }
     }
     countL[si] = nL;
     countS[si] = nS;
+    loL[si] = lowL;
+    loS[si] = lowS;
     int mt = nL + nS, ml = nL, ms = nS;
     for (int o = 16; o > 0; o >>= 1) {
         mt = max(mt, __shfl_xor_sync(0xffffffffu, mt, o));
@@ -374,8 +382,11 @@ struct NbrList {
     const int* tileJ;
     const float4* shF;
     const double* shD;
+    const float2* shDF;       // the same shifts as double-float
     const int* countL;
     const int* countS;
+    const int* loL;           // entries with j < i at the head of each segment
+    const int* loS;
     const int* tmaxL;
     const int* tmaxS;
     const unsigned* list;
@@ -502,14 +513,19 @@ k_fixed_field(NbrList nl, AtomArrays<real> at, unsigned long long* __restrict__ 
 
 // Real-space field of point dipoles (kernel K_u), optionally with its gradient:
 // MPIDReferenceForce.cpp:4161-4281.  mu is [3][npad] in sorted order.
-template <typename real, bool GRAD, bool QUAD>
+// HALF: only the pairs with j > i, whose field at j is added with fixed-point atomics
+// (half the pair evaluations; used by the FP64 kernels, where arithmetic dominates).
+template <typename real, bool GRAD, bool QUAD, bool HALF>
 __device__ __forceinline__ void dipole_field_loop(const NbrList& nl, const AtomArrays<real>& at, const real* mu,
-                                                  const PairTask& t, real* acc) {
+                                                  const PairTask& t, real* acc, unsigned long long* field,
+                                                  unsigned long long* grad) {
     const PairConsts<real>& pc = pair_consts<real>(nl);
     const int npad = at.npad, si = t.si;
     const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+    const real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
     const typename Vec4<real>::type pi = at.prm[si];
-    for (int k = t.k0; k < t.k1; ++k) {
+    const int kb = HALF ? max(t.k0, QUAD ? nl.loS[si] : nl.loL[si]) : t.k0;
+    for (int k = kb; k < t.k1; ++k) {
         int sj;
         unsigned flag;
         real d[3], r2;
@@ -529,10 +545,16 @@ __device__ __forceinline__ void dipole_field_loop(const NbrList& nl, const AtomA
         if (GRAD)
 #pragma unroll
             for (int q = 0; q < 6; ++q) acc[3 + q] += gr[q];
+        if (HALF) {
+            dipole_field<real, GRAD>(ui, d, b, e, gr);
+            for (int q = 0; q < 3; ++q) fx_add(field + q * npad + sj, e[q]);
+            if (GRAD)
+                for (int q = 0; q < 6; ++q) fx_add(grad + q * npad + sj, gr[q]);
+        }
     }
 }
 
-template <typename real, bool GRAD>
+template <typename real, bool GRAD, bool HALF>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 k_dipole_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ field,
                unsigned long long* __restrict__ grad, const int* __restrict__ skip) {
@@ -545,13 +567,163 @@ k_dipole_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, uns
 #pragma unroll
     for (int q = 0; q < NACC; ++q) acc[q] = real(0);
     if (t.quad)
-        dipole_field_loop<real, GRAD, true>(nl, at, mu, t, acc);
+        dipole_field_loop<real, GRAD, true, HALF>(nl, at, mu, t, acc, field, grad);
     else
-        dipole_field_loop<real, GRAD, false>(nl, at, mu, t, acc);
+        dipole_field_loop<real, GRAD, false, HALF>(nl, at, mu, t, acc, field, grad);
     const int npad = at.npad;
     for (int q = 0; q < 3; ++q) fx_add(field + q * npad + t.si, acc[q]);
     if (GRAD)
         for (int q = 0; q < 6; ++q) fx_add(grad + q * npad + t.si, acc[3 + q]);
+}
+
+// ---------------------------------------------------------------------------
+// Residual field of the mixed path's refinement in double-float arithmetic: the
+// real-space T.mu of k_dipole_field<double> (MPIDReferenceForce.cpp:4161-4281) to
+// ~1e-14 relative, on the FP32 pipes.  The Ewald parts of b_1, b_2 come from the tables
+// of radial_tables.h; Thole factors and geometry are computed in df.  Pairs j > i only,
+// with the field at j added by fixed-point atomics.
+
+// Per-atom df inputs: offsets [3][npad] from the FP64 engine, dipoles [3][npad], Thole
+// width and damping factor [npad].
+struct DfAtoms {
+    int npad;
+    const float2* off;
+    const float2* mu;
+    const float2* thole;
+    const float2* damp;
+};
+
+struct DfRadial {
+    const float* Gcoef;
+    const float* Gcentre;
+    const float* Hcoef;
+    const float* Hcentre;
+    float Gr0, Ginvh, Hr0, Hinvh;
+    int GK, HK;
+    int usePme;
+    float rc2;
+    float L[3], iL[3];
+    float2 Ldf[3];
+    float2 tholeDefault;
+};
+
+__device__ __forceinline__ dfloat df_load(const float2* p, int i) {
+    const float2 v = p[i];
+    return df_make(v.x, v.y);
+}
+
+__device__ __forceinline__ void fx_add_df(unsigned long long* p, dfloat v) {
+    const long long a = __float2ll_rn(v.hi * 4294967296.0f) + __float2ll_rn(v.lo * 4294967296.0f);
+    atomicAdd(p, (unsigned long long) a);
+}
+
+// float2 copies of FP64 arrays
+__global__ void k_to_df(int count, const double* __restrict__ src, float2* __restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const dfloat v = df_from_double(src[i]);
+    dst[i] = make_float2(v.hi, v.lo);
+}
+
+// df offsets, Thole widths and damping factors of the FP64 engine's atoms
+__global__ void k_df_atoms(int npad, const double* __restrict__ off, const double4* __restrict__ prm,
+                           float2* __restrict__ offDF, float2* __restrict__ tholeDF, float2* __restrict__ dampDF) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    for (int k = 0; k < 3; ++k) {
+        const dfloat v = df_from_double(off[k * npad + i]);
+        offDF[k * npad + i] = make_float2(v.hi, v.lo);
+    }
+    const double4 p = prm[i];
+    const dfloat t = df_from_double(p.x), d = df_from_double(p.y);
+    tholeDF[i] = make_float2(t.hi, t.lo);
+    dampDF[i] = make_float2(d.hi, d.lo);
+}
+
+template <bool QUAD>
+__device__ __forceinline__ void df_field_loop(const NbrList& nl, const DfRadial& R, const DfAtoms& A, const PairTask& t,
+                                              dfloat* acc, unsigned long long* field) {
+    const int npad = A.npad, si = t.si;
+    const dfloat oi[3] = {df_load(A.off, si), df_load(A.off, npad + si), df_load(A.off, 2 * npad + si)};
+    const dfloat ui[3] = {df_load(A.mu, si), df_load(A.mu, npad + si), df_load(A.mu, 2 * npad + si)};
+    const dfloat thi = df_load(A.thole, si), dpi = df_load(A.damp, si);
+    const dfloat one = df_from_float(1.f);
+    const dfloat third = df_make(0.333333343f, -9.93410776e-09f);  // 1/3
+    const int kb = max(t.k0, QUAD ? nl.loS[si] : nl.loL[si]);
+    for (int k = kb; k < t.k1; ++k) {
+        const int pos = QUAD ? nl.cap - 1 - k : k;
+        const unsigned code = nl.list[((size_t) t.I * nl.cap + pos) * 32 + t.lane];
+        const size_t s = (size_t) t.I * nl.tcap + (code >> 7);
+        const int Jw = nl.tileJ[s];
+        const int sj = (Jw & 0x7fffffff) * 32 + (int) (code & 31u);
+        const unsigned flag = (code >> 5) & 3u;
+        dfloat d[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) d[q] = df_add(df_sub(df_load(A.off, q * npad + sj), oi[q]), df_load(nl.shDF, 3 * s + q));
+        if (Jw < 0)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float m = rintf(d[q].hi * R.iL[q]);
+                d[q] = df_sub(d[q], df_mul(df_make(R.Ldf[q].x, R.Ldf[q].y), m));
+            }
+        const dfloat r2 = df_add(df_add(df_mul(d[0], d[0]), df_mul(d[1], d[1])), df_mul(d[2], d[2]));
+        if (R.usePme && r2.hi > R.rc2) continue;
+        const dfloat r = df_sqrt(r2);
+        const dfloat rinv = df_recip(r);
+        const dfloat rinv2 = df_mul(rinv, rinv);
+        const dfloat bB1 = df_mul(rinv, rinv2);        // 1/r^3
+        const dfloat r5inv = df_mul(bB1, rinv2);       // 1/r^5
+        // Thole: oneMinus_n = e^-s P_n(s), P_1 = 1 + s + s^2/2, P_2 = P_1 + s^3/6
+        dfloat om1 = df_from_float(0.f), om2 = df_from_float(0.f);
+        const dfloat dd = df_mul(dpi, df_load(A.damp, sj));
+        if (dd.hi > 0.f) {
+            const dfloat a = flag == 1u ? df_add(thi, df_load(A.thole, sj)) : df_make(R.tholeDefault.x, R.tholeDefault.y);
+            const dfloat sT = df_div(df_mul(a, r), dd);
+            if (sT.hi < 50.f) {
+                const dfloat e = df_exp_neg(sT);
+                const dfloat s2h = df_mul(df_mul(sT, sT), 0.5f);
+                const dfloat P1 = df_add(df_add(sT, 1.f), s2h);
+                const dfloat P2 = df_add(P1, df_mul(df_mul(s2h, sT), third));
+                om1 = df_mul(e, P1);
+                om2 = df_mul(e, P2);
+            }
+        }
+        dfloat b1, b2;
+        if (QUAD) {
+            dfloat H1, H2;
+            df_table_eval<7>(R.Hcoef, R.Hcentre, R.Hr0, R.Hinvh, R.HK, r, H1, H2);
+            b1 = df_sub(df_mul(df_sub(one, om1), bB1), H1);
+            b2 = df_sub(df_mul(df_mul(df_sub(one, om2), r5inv), 3.f), H2);
+        } else {
+            dfloat G1 = df_from_float(1.f), G2 = df_from_float(3.f);  // no Ewald part without PME
+            if (R.usePme) df_table_eval<7>(R.Gcoef, R.Gcentre, R.Gr0, R.Ginvh, R.GK, r, G1, G2);
+            b1 = df_mul(df_sub(G1, om1), bB1);
+            b2 = df_mul(df_sub(G2, df_mul(om2, 3.f)), r5inv);
+        }
+        // field at i from mu_j and at j from mu_i: E = -b1 mu + b2 (mu.d) d
+        const dfloat uj[3] = {df_load(A.mu, sj), df_load(A.mu, npad + sj), df_load(A.mu, 2 * npad + sj)};
+        const dfloat mjd = df_add(df_add(df_mul(uj[0], d[0]), df_mul(uj[1], d[1])), df_mul(uj[2], d[2]));
+        const dfloat mid = df_add(df_add(df_mul(ui[0], d[0]), df_mul(ui[1], d[1])), df_mul(ui[2], d[2]));
+        const dfloat b2mj = df_mul(b2, mjd), b2mi = df_mul(b2, mid);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            acc[q] = df_add(acc[q], df_sub(df_mul(b2mj, d[q]), df_mul(b1, uj[q])));
+            fx_add_df(field + q * npad + sj, df_sub(df_mul(b2mi, d[q]), df_mul(b1, ui[q])));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_dipole_field_df(NbrList nl, DfRadial R, DfAtoms A, const int* __restrict__ orig, unsigned long long* __restrict__ field) {
+    PairTask t;
+    if (!t.init(nl)) return;
+    if (orig[t.si] < 0) return;
+    dfloat acc[3] = {df_from_float(0.f), df_from_float(0.f), df_from_float(0.f)};
+    if (t.quad)
+        df_field_loop<true>(nl, R, A, t, acc, field);
+    else
+        df_field_loop<false>(nl, R, A, t, acc, field);
+    for (int q = 0; q < 3; ++q) fx_add_df(field + q * A.npad + t.si, acc[q]);
 }
 
 // Compensated running sum (TwoSum) for the FP32 pair energies.

@@ -112,3 +112,23 @@ def test_synthetic_multipoles_are_traceless():
     r = np.sqrt((d ** 2).sum(-1))
     np.fill_diagonal(r, 10)
     assert r.min() >= 0.26 - 1e-9
+
+
+@pytest.mark.parametrize("alpha,cutoff", [(3.4, 0.9), (3.5, 0.8), (4.0, 0.7)])
+def test_double_float_residual_arithmetic(tmp_path, alpha, cutoff):
+    """The df arithmetic and Ewald tables of the residual field (df64.cuh,
+    radial_tables.h) against long double: tables, exp(-s), division and square root
+    to ~1e-14 relative."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    csrc = os.path.join(ROOT, "mpidopenmmplugin_gb300", "csrc")
+    exe = str(tmp_path / "df_check")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I", csrc, os.path.join(csrc, "df_check.cpp"), "-o", exe], check=True)
+    out = subprocess.run([exe, str(alpha), str(cutoff)], check=True, capture_output=True, text=True).stdout
+    errs = {k: float(v) for k, v in (line.split() for line in out.strip().splitlines())}
+    assert set(errs) == {"erfc_table", "erf_table", "exp_neg", "div", "sqrt"}
+    for name, e in errs.items():
+        assert e < 1e-13, (name, e)
