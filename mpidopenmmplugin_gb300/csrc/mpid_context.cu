@@ -331,6 +331,7 @@ struct Context {
     // solver scratch
     DBuf<double> partial, red, sc;
     DBuf<int> iter, done;
+    DBuf<unsigned> counters;  // last-block counters of the fused CG reductions
     DBuf<float> r32, p32, q32, x32, b32;
     DBuf<double> r64, p64, q64, y64, b64, res64, Efix64;
     DBuf<float> res32;
@@ -399,6 +400,8 @@ struct Context {
         forcesOut.alloc(3 * (size_t) n);
         partial.alloc(2 * (size_t) nblk(npad, 256)); red.alloc(4); sc.alloc(8);
         iter.alloc(1); done.alloc(1);
+        counters.alloc(2);
+        CUDA_CHECK(cudaMemset(counters.p, 0, 2 * sizeof(unsigned)));
         CUDA_CHECK(cudaMallocHost(&hostDone, 256 * sizeof(int)));
         CUDA_CHECK(cudaEventCreate(&evStart));
         CUDA_CHECK(cudaEventCreate(&evStop));
@@ -844,6 +847,30 @@ struct Context {
         CUDA_CHECK(cudaGetLastError());
     }
 
+    // One CG operator application: (p = r + beta p unless first), sp = S p, E = T sp
+    // (real space, reciprocal, self), q = p - S E and p.q into sc[1].
+    template <typename real>
+    void cg_matvec(Engine<real>& e, const real* r, real* p, real* q, bool first) {
+        cudaStream_t st = stream;
+        const int nb = nblk(npad, 256);
+        launch(k_cg_direction_sroot<real>, nblk(npad, 128), 128, 0, st, npad, box, e.sroot.p, sc.p, first ? 1 : 0, r,
+               p, e.sp.p, usePme ? e.mfd.p : (real*) nullptr, done.p);
+        timer.begin(ST_DIPOLE_REAL, st);
+        launch(k_dipole_field<real, false, sizeof(real) == 8>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+               e.arrays(), (const real*) e.sp.p, e.fieldFx.p, (unsigned long long*) nullptr, (const int*) done.p);
+        timer.end(st);
+        if (usePme) {
+            timer.begin(ST_PME, st);
+            e.pme.template spread<4>(n, npad, box, e.mfd.p, done.p, st);
+            e.pme.convolve(influence.p, done.p, st);
+            e.pme.template gather<4>(n, npad, box, e.phiT.p, done.p, st);
+            timer.end(st);
+        }
+        launch(k_cg_matvec_finish<real>, nb, 256, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
+               usePme ? (const real*) e.phiT.p : (const real*) nullptr, (const real*) e.sroot.p, (const real*) p,
+               (const real*) e.sp.p, q, partial.p, counters.p, sc.p, (const int*) done.p);
+    }
+
     // Preconditioned CG on B y = b, B = I - S T S, in precision `real`; x accumulates in xreal.
     // Convergence: 48.033324 sqrt(|S r|^2/n) < target.  Returns iterations used.
     template <typename real, typename xreal>
@@ -854,18 +881,14 @@ struct Context {
         launch(k_cg_start<real, xreal>, nb, 256, 0, st, npad, e.sroot.p, b, x, r, p, partial.p, nb);
         launch(k_reduce_partials, 1, 1024, 0, st, nb, 2, partial.p, red.p, nullptr);
         launch(k_cg_init_scalars, 1, 1, 0, st, sc.p, red.p, n, target, iter.p, done.p);
+        CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));  // cleared again by each matvec
         CUDA_CHECK(cudaGetLastError());
         int it = 0;
         for (it = 0; it < maxIter; ++it) {
-            // q = B p
-            launch(k_apply_sroot<real>, nblk(npad, 128), 128, 0, st, npad, box, e.sroot.p, p, e.sp.p, nullptr, done.p);
-            dipole_field(e, e.sp.p, e.Etmp.p, (real*) nullptr, done.p, 4);
-            launch(k_cg_finish_matvec<real>, nb, 256, 0, st, npad, e.sroot.p, p, e.Etmp.p, q, partial.p, done.p);
-            launch(k_reduce_partials, 1, 1024, 0, st, nb, 1, partial.p, sc.p + 1, done.p);
-            launch(k_cg_update<real, xreal>, nb, 256, 0, st, npad, e.sroot.p, sc.p, p, q, x, r, partial.p, nb, done.p);
-            launch(k_reduce_partials, 1, 1024, 0, st, nb, 2, partial.p, red.p, done.p);
-            launch(k_cg_scalars, 1, 1, 0, st, sc.p, red.p, n, target, iter.p, maxIter, done.p);
-            launch(k_cg_direction<real>, nblk(npad, 128), 128, 0, st, npad, sc.p, r, p, done.p);
+            // q = B p = p - S T S p, p.q, then the update and the scalars
+            cg_matvec(e, (const real*) r, p, q, it == 0);
+            launch(k_cg_update_scalars<real, xreal>, nb, 256, 0, st, n, npad, e.sroot.p, sc.p, p, q, x, r, partial.p,
+                   counters.p + 1, target, iter.p, maxIter, done.p);
             CUDA_CHECK(cudaGetLastError());
             const int slot = it % (int) iterEvents.size();
             CUDA_CHECK(cudaMemcpyAsync(hostDone + (slot % 256), done.p, sizeof(int), cudaMemcpyDeviceToHost, st));

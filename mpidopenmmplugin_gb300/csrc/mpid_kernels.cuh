@@ -1340,6 +1340,162 @@ __global__ void k_cg_init_scalars(double* __restrict__ sc, const double* __restr
     *done = (sc[6] < target) ? 1 : 0;
 }
 
+// ---------------------------------------------------------------------------
+// Fused CG iteration kernels.  Each reduction writes per-block partials and the last
+// block to finish sums them in block order (deterministic) and updates the scalars, so
+// an iteration needs no separate reduction launches.  `counter` returns to 0 after use.
+
+// Block sum of v (blockDim.x == 256) into red[0].
+__device__ __forceinline__ double block_sum_256(double v, double* red) {
+    __syncthreads();  // red may still be read from the previous sum
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    return red[0];
+}
+
+// True in exactly one block: the last of gridDim.x blocks to pass this point (after
+// each block has published its partials).
+__device__ __forceinline__ bool last_block(unsigned* counter) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    return last;
+}
+
+// Fixed-order sum of partial[0..nblocks) by one block of 256 threads.
+__device__ __forceinline__ double sum_partials_256(const double* partial, int nblocks, double* red) {
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += 256) acc += ((volatile const double*) partial)[b];
+    return block_sum_256(acc, red);
+}
+
+// Start of an iteration: p = r + beta p (not on the first), sp = S p and the fractional
+// dipoles of sp for the reciprocal-space spread.
+template <typename real>
+__global__ void k_cg_direction_sroot(int npad, BoxDev box, const real* __restrict__ S, const double* __restrict__ sc,
+                                     int first, const real* __restrict__ r, real* __restrict__ p, real* __restrict__ sp,
+                                     real* __restrict__ mfd, const int* __restrict__ skip) {
+    if (*skip) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    real v[3];
+    if (first) {
+        for (int c = 0; c < 3; ++c) v[c] = p[c * npad + s];
+    } else {
+        const double b = sc[5];
+        for (int c = 0; c < 3; ++c) {
+            v[c] = real((double) r[c * npad + s] + b * (double) p[c * npad + s]);
+            p[c * npad + s] = v[c];
+        }
+    }
+    real o[3];
+    sym_mul(S, npad, s, v, o);
+    for (int c = 0; c < 3; ++c) sp[c * npad + s] = o[c];
+    if (mfd) {
+        mfd[s] = real(0);
+        for (int j = 0; j < 3; ++j)
+            mfd[(1 + j) * npad + s] = real(box.A[j][0]) * o[0] + real(box.A[j][1]) * o[1] + real(box.A[j][2]) * o[2];
+    }
+}
+
+// E = T sp (real space from the fixed-point accumulator, which is cleared here, plus
+// reciprocal and self terms), q = p - S E, and sc[1] = p.q.
+template <typename real>
+__global__ void __launch_bounds__(256)
+k_cg_matvec_finish(int n, int npad, BoxDev box, double selfCoef, unsigned long long* __restrict__ fx,
+                   const real* __restrict__ phi, const real* __restrict__ S, const real* __restrict__ p,
+                   const real* __restrict__ sp, real* __restrict__ q, double* __restrict__ partial,
+                   unsigned* __restrict__ counter, double* __restrict__ sc, const int* __restrict__ skip) {
+    __shared__ double red[256];
+    if (*skip) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (s < npad) {
+        real e[3];
+        for (int c = 0; c < 3; ++c) {
+            double v = 0.0;
+            if (s < n) {
+                v = fx_get(fx, c * npad + s) + selfCoef * (double) sp[c * npad + s];
+                if (phi) v -= box.A[0][c] * (double) phi[npad + s] + box.A[1][c] * (double) phi[2 * npad + s] +
+                              box.A[2][c] * (double) phi[3 * npad + s];
+            }
+            fx[c * npad + s] = 0ull;
+            e[c] = real(v);
+        }
+        real se[3];
+        sym_mul(S, npad, s, e, se);
+        for (int c = 0; c < 3; ++c) {
+            const real pv = p[c * npad + s];
+            const real qv = pv - se[c];
+            q[c * npad + s] = qv;
+            acc += (double) pv * (double) qv;
+        }
+    }
+    const double b = block_sum_256(acc, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = b;
+    if (last_block(counter)) {
+        const double pq = sum_partials_256(partial, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            sc[1] = pq;
+            *counter = 0u;
+        }
+    }
+}
+
+// x += a p, r -= a q (a = rr / pq); then beta, the convergence test
+// 48.033324 sqrt(|S r|^2 / n) < target (MPIDReferenceForce.cpp:1219) and the iteration
+// limit; done = 1 stops the loop.  sc: 0 rr, 1 pq, 2 rr_new, 3 |S r|^2, 5 beta, 6 metric.
+template <typename real, typename xreal>
+__global__ void __launch_bounds__(256)
+k_cg_update_scalars(int n, int npad, const real* __restrict__ S, double* __restrict__ sc, const real* __restrict__ p,
+                    const real* __restrict__ q, xreal* __restrict__ x, real* __restrict__ r, double* __restrict__ partial,
+                    unsigned* __restrict__ counter, double target, int* __restrict__ iter, int maxIter,
+                    int* __restrict__ done) {
+    __shared__ double red[256];
+    if (*done) return;
+    const double a = sc[0] / sc[1];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, sr = 0.0;
+    if (s < npad) {
+        real rv[3];
+        for (int c = 0; c < 3; ++c) {
+            x[c * npad + s] += xreal(a * (double) p[c * npad + s]);
+            rv[c] = real((double) r[c * npad + s] - a * (double) q[c * npad + s]);
+            r[c * npad + s] = rv[c];
+            rr += (double) rv[c] * (double) rv[c];
+        }
+        real z[3];
+        sym_mul(S, npad, s, rv, z);
+        sr = (double) z[0] * z[0] + (double) z[1] * z[1] + (double) z[2] * z[2];
+    }
+    const double b0 = block_sum_256(rr, red);
+    const double b1 = block_sum_256(sr, red);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = b0;
+        partial[gridDim.x + blockIdx.x] = b1;
+    }
+    if (last_block(counter)) {
+        const double rrNew = sum_partials_256(partial, gridDim.x, red);
+        const double srNew = sum_partials_256(partial + gridDim.x, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            sc[2] = rrNew;
+            sc[3] = srNew;
+            sc[5] = rrNew / sc[0];
+            sc[0] = rrNew;
+            sc[6] = 48.033324 * sqrt(srNew / n);
+            *iter += 1;
+            if (sc[6] < target || *iter >= maxIter || !(sc[6] == sc[6])) *done = 1;
+            *counter = 0u;
+        }
+    }
+}
+
 // mu = S y (sorted), in the precision of the pair kernels.
 template <typename xreal, typename real>
 __global__ void k_mu_from_y(int npad, const xreal* __restrict__ S, const xreal* __restrict__ y, real* __restrict__ mu) {
