@@ -339,6 +339,8 @@ struct Context {
     DBuf<float> ptMuF, ptEF, ptGF;
     DBuf<double> ptMuD, ptED, ptGD;
     int* hostDone = nullptr;
+    int* hostMax = nullptr;        // list maxima (pinned)
+    cudaEvent_t evLists = nullptr;
     std::vector<cudaEvent_t> iterEvents;
     cudaEvent_t evStart = nullptr, evStop = nullptr;
     mpid_stats stats{};
@@ -349,6 +351,8 @@ struct Context {
     ~Context() {
         timer.destroy();
         if (hostDone) cudaFreeHost(hostDone);
+        if (hostMax) cudaFreeHost(hostMax);
+        if (evLists) cudaEventDestroy(evLists);
         for (auto e : iterEvents) cudaEventDestroy(e);
         if (evStart) cudaEventDestroy(evStart);
         if (evStop) cudaEventDestroy(evStop);
@@ -403,6 +407,8 @@ struct Context {
         counters.alloc(2);
         CUDA_CHECK(cudaMemset(counters.p, 0, 2 * sizeof(unsigned)));
         CUDA_CHECK(cudaMallocHost(&hostDone, 256 * sizeof(int)));
+        CUDA_CHECK(cudaMallocHost(&hostMax, 4 * sizeof(int)));
+        CUDA_CHECK(cudaEventCreateWithFlags(&evLists, cudaEventDisableTiming));
         CUDA_CHECK(cudaEventCreate(&evStart));
         CUDA_CHECK(cudaEventCreate(&evStop));
         timer.init();
@@ -697,8 +703,8 @@ struct Context {
     int pair_tasks() const { return ntiles * (nchunksL + nchunksS); }
     int pair_blocks() const { return std::max(1, nblk(pair_tasks(), kWarpsPerBlock)); }
 
-    // Sort, tiles, tile pairs.
-    void neighbour_setup() {
+    // Spatial sort (PME) or caller order (no cutoff), then tile centres and extents.
+    void sort_and_tiles() {
         cudaStream_t st = stream;
         if (usePme) {
             // columns about (32 / density)^(1/3) wide
@@ -712,60 +718,60 @@ struct Context {
                                                         64, st));
         } else {
             // No periodic box: keep the caller's order (all pairs interact).
-            std::vector<int> k(n);
-            for (int i = 0; i < n; ++i) k[i] = i;
-            CUDA_CHECK(cudaMemcpyAsync(order.p, k.data(), n * 4, cudaMemcpyHostToDevice, st));
-            CUDA_CHECK(cudaMemcpyAsync(wpos.p, pos.p, 3 * n * 8, cudaMemcpyDeviceToDevice, st));
-            CUDA_CHECK(cudaStreamSynchronize(st));
+            launch(k_identity_order, nblk(n, 256), 256, 0, st, n, (const double*) pos.p, order.p, wpos.p);
         }
         launch(k_tile_bounds, nblk(ntiles, 128), 128, 0, st, n, ntiles, order.p, wpos.p, center.p, half.p);
-        const double listCut = usePme ? set.cutoff * (1.0 + 1e-6) + 1e-5 : 1e30;
-        for (int attempt = 0; attempt < 2; ++attempt) {
-            CUDA_CHECK(cudaMemsetAsync(listMax.p, 0, sizeof(int), st));
-            launch(k_tile_list, nblk((long long) ntiles * 32, 128), 128, 0, st, ntiles, center.p, half.p, box, listCut,
-                   usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, shD.p, shDF.p, listMax.p);
-            int m = 0;
-            CUDA_CHECK(cudaMemcpyAsync(&m, listMax.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-            CUDA_CHECK(cudaStreamSynchronize(st));
-            lastTiles = m;
-            if (m <= tcap) return;
-            if (growForbidden)
-                throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: the tile lists would have to grow (" +
-                                                  std::to_string(m) + " > " + std::to_string(tcap) +
-                                                  " neighbour tiles); evaluate once with mpid_evaluate_device first");
-            alloc_tile_lists(std::min(ntiles, m + m / 4 + 8));
-        }
-        throw Error(MPID_ERR_CUDA, "tile list overflow");
     }
 
-    // Per-atom lists from the sorted offsets of engine e (after prepare_engine).
+    double list_cutoff() const { return usePme ? set.cutoff * (1.0 + 1e-6) + 1e-5 : 1e30; }
+
+    // Tile lists and per-atom lists from the sorted offsets of engine e; the list maxima
+    // go to pinned host memory, read by finish_lists.
     template <typename real>
-    void atom_lists(Engine<real>& e) {
+    void launch_lists(Engine<real>& e) {
         cudaStream_t st = stream;
-        const double listCut = usePme ? set.cutoff * (1.0 + 1e-6) + 1e-5 : 1e30;
+        const double listCut = list_cutoff();
         const float cut2 = usePme ? (float) (listCut * listCut) : 3.0e38f;
         // erfc / quadrature segment boundary: alpha r = kQuadX
         const float quadR2 = usePme ? (float) std::pow(Prec<float>::kQuadX / set.ewald_alpha, 2) : 0.f;
-        for (int attempt = 0; attempt < 2; ++attempt) {
-            CUDA_CHECK(cudaMemsetAsync(listMax.p + 1, 0, 3 * sizeof(int), st));
-            launch(k_atom_list<real>, nblk((long long) ntiles * 32, 128), 128, 0, st, ntiles, npad, e.off.p, e.orig.p, box,
-                   cut2, quadR2, usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, covOff.p, covJ.p, covS.p, cap,
-                   countL.p, countS.p, loL.p, loS.p, tmaxL.p, tmaxS.p, list.p, listMax.p + 1);
-            int m[3] = {0, 0, 0};
-            CUDA_CHECK(cudaMemcpyAsync(m, listMax.p + 1, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
-            CUDA_CHECK(cudaStreamSynchronize(st));
-            lastMaxList = m[0];
-            if (m[0] <= cap) {
-                nchunksL = (m[1] + chunk - 1) / chunk;
-                nchunksS = (m[2] + chunk - 1) / chunk;
+        CUDA_CHECK(cudaMemsetAsync(listMax.p, 0, 4 * sizeof(int), st));
+        launch(k_tile_list, nblk((long long) ntiles * 32, 128), 128, 0, st, ntiles, center.p, half.p, box, listCut,
+               usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, shD.p, shDF.p, listMax.p);
+        launch(k_atom_list<real>, ntiles, 32 * kListWarps, 0, st, ntiles, npad, (const real*) e.off.p,
+               (const int*) e.orig.p, box, cut2, quadR2, usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, covOff.p,
+               covJ.p, covS.p, cap, countL.p, countS.p, loL.p, loS.p, tmaxL.p, tmaxS.p, list.p, listMax.p + 1);
+        CUDA_CHECK(cudaMemcpyAsync(hostMax, listMax.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaEventRecord(evLists, st));
+    }
+
+    // Waits for the list maxima (work queued after launch_lists keeps the GPU busy), grows
+    // and rebuilds on overflow, and sizes the pair kernels' work items.
+    template <typename real>
+    void finish_lists(Engine<real>& e) {
+        for (int attempt = 0; attempt < 3; ++attempt) {
+            CUDA_CHECK(cudaEventSynchronize(evLists));
+            const int mTiles = hostMax[0], mTotal = hostMax[1], mL = hostMax[2], mS = hostMax[3];
+            lastTiles = mTiles;
+            lastMaxList = mTotal;
+            if (mTiles <= tcap && mTotal <= cap) {
+                nchunksL = (mL + chunk - 1) / chunk;
+                nchunksS = (mS + chunk - 1) / chunk;
                 if (nchunksL + nchunksS == 0) nchunksL = 1;
                 return;
             }
-            if (growForbidden)
-                throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: an atom has " + std::to_string(m[0]) +
+            if (growForbidden) {
+                if (mTiles > tcap)
+                    throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: the tile lists would have to grow (" +
+                                                      std::to_string(mTiles) + " > " + std::to_string(tcap) +
+                                                      " neighbour tiles); evaluate once with mpid_evaluate_device first");
+                throw Error(MPID_ERR_INVALID, "mpid_evaluate_device_noalloc: an atom has " + std::to_string(mTotal) +
                                                   " neighbours, more than the " + std::to_string(cap) +
                                                   " that the static scratch holds for this system size");
-            alloc_atom_lists(std::min(npad, m[0] + m[0] / 8 + chunk));
+            }
+            if (mTiles > tcap) alloc_tile_lists(std::min(ntiles, mTiles + mTiles / 4 + 8));
+            // with a truncated tile list the atom counts are low: size from the worst case
+            if (mTotal > cap || mTiles > tcap) alloc_atom_lists(std::min(npad, std::max(mTotal + mTotal / 8 + chunk, cap)));
+            launch_lists(e);
         }
         throw Error(MPID_ERR_CUDA, "neighbour list overflow");
     }
@@ -1087,16 +1093,17 @@ struct Context {
         timer.reset();
         timer.begin(ST_SETUP, st);
         set_box(hbox);
-        neighbour_setup();
-        stats.max_neighbours = lastMaxList;
+        sort_and_tiles();
         if (mixed) {
             Engine<float>& e = *ef;
             prepare_engine(e, true);
-            atom_lists(e);
+            launch_lists(e);
             if (ed) {
                 prepare_engine(*ed, false);
                 launch(k_df_atoms, nblk(npad, 128), 128, 0, st, npad, ed->off.p, ed->prm.p, offDF.p, tholeDF.p, dampDF.p);
             }
+            finish_lists(e);
+            stats.max_neighbours = lastMaxList;
             timer.end(st);
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL)
@@ -1108,7 +1115,9 @@ struct Context {
         } else {
             Engine<double>& e = *ed;
             prepare_engine(e, true);
-            atom_lists(e);
+            launch_lists(e);
+            finish_lists(e);
+            stats.max_neighbours = lastMaxList;
             timer.end(st);
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL)

@@ -74,6 +74,15 @@ __global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, i
     vals[i] = i;
 }
 
+// No-cutoff systems keep the caller's order.
+__global__ void k_identity_order(int n, const double* __restrict__ pos, int* __restrict__ order,
+                                 double* __restrict__ wpos) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    order[i] = i;
+    for (int k = 0; k < 3; ++k) wpos[3 * i + k] = pos[3 * i + k];
+}
+
 // Tile centres and half extents from the wrapped positions of the sorted atoms.
 __global__ void k_tile_bounds(int n, int ntiles, const int* __restrict__ order,
                               const double* __restrict__ wpos, double* __restrict__ center,
@@ -277,22 +286,28 @@ __device__ __forceinline__ double pair_scale(int oi, int oj, const int* __restri
 // Flag of a covalent scale as stored in list entries.
 __device__ __forceinline__ unsigned scale_flag(double sc) { return sc == 1.0 ? 0u : (sc == 0.0 ? 1u : 2u); }
 
-// Atom lists: one warp per tile I; each lane tests the 32 atoms of every J tile in I's
-// tile list (float arithmetic; cutoff2 includes a small skin so that both the FP32 and
-// the FP64 kernels, which apply the exact cutoff, see every pair).  Each lane's list has
-// two segments so that the pair kernels never mix the two radial branches in a warp:
-// the erfc segment grows from the front (count nL), the quadrature segment (alpha r
-// below the threshold, r2 < quadR2, or covalent scale 0 under PME) from the back (nS).
+// Atom lists: one block of kListWarps warps per tile I; warp w scans a contiguous range
+// of I's tile list, each lane testing the 32 atoms of every J tile in the range (float
+// arithmetic; cutoff2 includes a small skin so that both the FP32 and the FP64 kernels,
+// which apply the exact cutoff, see every pair).  Each lane's list has two segments so
+// that the pair kernels never mix the two radial branches in a warp: the erfc segment
+// grows from the front (count nL), the quadrature segment (alpha r below the threshold,
+// r2 < quadR2, or covalent scale 0 under PME) from the back (nS).  A first pass counts
+// per warp, a second writes at the lane's running offset, so the entries of every lane
+// are in ascending J order (and ascending j).
+constexpr int kListWarps = 8;
+
 template <typename real>
-__global__ void k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __restrict__ orig, BoxDev box,
-                            float cutoff2, float quadR2, int usePme, int tcap, const int* __restrict__ tileCount,
-                            const int* __restrict__ tileJ, const float4* __restrict__ shF, const int* __restrict__ covOff,
-                            const int* __restrict__ covJ, const double* __restrict__ covS, int cap,
-                            int* __restrict__ countL, int* __restrict__ countS, int* __restrict__ loL,
-                            int* __restrict__ loS, int* __restrict__ tmaxL, int* __restrict__ tmaxS,
-                            unsigned* __restrict__ list, int* __restrict__ maxCounts) {
+__global__ void __launch_bounds__(32 * kListWarps)
+k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __restrict__ orig, BoxDev box,
+            float cutoff2, float quadR2, int usePme, int tcap, const int* __restrict__ tileCount,
+            const int* __restrict__ tileJ, const float4* __restrict__ shF, const int* __restrict__ covOff,
+            const int* __restrict__ covJ, const double* __restrict__ covS, int cap, int* __restrict__ countL,
+            int* __restrict__ countS, int* __restrict__ loL, int* __restrict__ loS, int* __restrict__ tmaxL,
+            int* __restrict__ tmaxS, unsigned* __restrict__ list, int* __restrict__ maxCounts) {
     constexpr int kCache = 8;
-    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    __shared__ int cnt[kListWarps][4][32];  // nL, nS, lowL, lowS per warp and lane
+    const int I = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (I >= ntiles) return;
     const int si = I * 32 + lane;
     const float oi[3] = {(float) off[si], (float) off[npad + si], (float) off[2 * npad + si]};
@@ -310,59 +325,89 @@ __global__ void k_atom_list(int ntiles, int npad, const real* __restrict__ off, 
         pJ[k] = k < ncached ? covJ[cb + k] : -1;
         pF[k] = k < ncached ? scale_flag(covS[cb + k]) : 0u;
     }
-    unsigned* out = list + (size_t) I * cap * 32 + lane;
-    int nL = 0, nS = 0, lowL = 0, lowS = 0;  // lowX: entries with j < i (a prefix: j ascends)
     const int nt = tileCount[I];
-    for (int s = 0; s < nt; ++s) {
-        const int Jw = tileJ[(size_t) I * tcap + s];
-        const int J = Jw & 0x7fffffff;
-        const bool wrap = Jw < 0;
-        const float4 sh = shF[(size_t) I * tcap + s];
-        const int sj = J * 32 + lane;
-        const float oj0 = (float) off[sj], oj1 = (float) off[npad + sj], oj2 = (float) off[2 * npad + sj];
-        const int origJl = orig[sj];
-        for (int jl = 0; jl < 32; ++jl) {
-            float d[3] = {sh.x + (__shfl_sync(0xffffffffu, oj0, jl) - oi[0]),
-                          sh.y + (__shfl_sync(0xffffffffu, oj1, jl) - oi[1]),
-                          sh.z + (__shfl_sync(0xffffffffu, oj2, jl) - oi[2])};
-            const int oj = __shfl_sync(0xffffffffu, origJl, jl);
-            if (wrap)
-                for (int k = 0; k < 3; ++k) d[k] -= L[k] * rintf(d[k] * iL[k]);
-            const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-            if (origI < 0 || oj < 0 || r2 >= cutoff2 || (J == I && jl == lane)) continue;
-            unsigned flag = 0;
+    const int s0 = (w * nt) / kListWarps, s1 = ((w + 1) * nt) / kListWarps;
+    unsigned* out = list + (size_t) I * cap * 32 + lane;
+    int baseL = 0, baseS = 0;
+    bool fits = true;
+    for (int pass = 0; pass < 2; ++pass) {
+        int nL = 0, nS = 0, lowL = 0, lowS = 0;
+        for (int s = s0; s < s1; ++s) {
+            const int Jw = tileJ[(size_t) I * tcap + s];
+            const int J = Jw & 0x7fffffff;
+            const bool wrap = Jw < 0;
+            const float4 sh = shF[(size_t) I * tcap + s];
+            const int sj = J * 32 + lane;
+            const float oj0 = (float) off[sj], oj1 = (float) off[npad + sj], oj2 = (float) off[2 * npad + sj];
+            const int origJl = orig[sj];
+            for (int jl = 0; jl < 32; ++jl) {
+                float d[3] = {sh.x + (__shfl_sync(0xffffffffu, oj0, jl) - oi[0]),
+                              sh.y + (__shfl_sync(0xffffffffu, oj1, jl) - oi[1]),
+                              sh.z + (__shfl_sync(0xffffffffu, oj2, jl) - oi[2])};
+                const int oj = __shfl_sync(0xffffffffu, origJl, jl);
+                if (wrap)
+                    for (int k = 0; k < 3; ++k) d[k] -= L[k] * rintf(d[k] * iL[k]);
+                const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                if (origI < 0 || oj < 0 || r2 >= cutoff2 || (J == I && jl == lane)) continue;
+                unsigned flag = 0;
 #pragma unroll
-            for (int k = 0; k < kCache; ++k)
-                if (pJ[k] == oj) flag = pF[k];
-            if (ce - cb > kCache)
-                for (int k = cb + kCache; k < ce; ++k)
-                    if (covJ[k] == oj) {
-                        flag = scale_flag(covS[k]);
-                        break;
-                    }
-            const unsigned code = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
-            const bool quad = usePme && (r2 < quadR2 || flag == 1u);
-            if (nL + nS < cap) out[(size_t) (quad ? cap - 1 - nS : nL) * 32] = code;
-            const bool low = J * 32 + jl < si;
-            if (quad) { ++nS; lowS += low; } else { ++nL; lowL += low; }
+                for (int k = 0; k < kCache; ++k)
+                    if (pJ[k] == oj) flag = pF[k];
+                if (ce - cb > kCache)
+                    for (int k = cb + kCache; k < ce; ++k)
+                        if (covJ[k] == oj) {
+                            flag = scale_flag(covS[k]);
+                            break;
+                        }
+                const bool quad = usePme && (r2 < quadR2 || flag == 1u);
+                if (pass == 1 && fits) {
+                    const unsigned code = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
+                    out[(size_t) (quad ? cap - 1 - (baseS + nS) : baseL + nL) * 32] = code;
+                }
+                const int low = J * 32 + jl < si;
+                if (quad) { ++nS; lowS += low; } else { ++nL; lowL += low; }
+            }
+        }
+        if (pass == 0) {
+            cnt[w][0][lane] = nL;
+            cnt[w][1][lane] = nS;
+            cnt[w][2][lane] = lowL;
+            cnt[w][3][lane] = lowS;
+            __syncthreads();
+            int tL = 0, tS = 0;
+            for (int v = 0; v < kListWarps; ++v) {
+                if (v == w) { baseL = tL; baseS = tS; }
+                tL += cnt[v][0][lane];
+                tS += cnt[v][1][lane];
+            }
+            fits = tL + tS <= cap;
         }
     }
-    countL[si] = nL;
-    countS[si] = nS;
-    loL[si] = lowL;
-    loS[si] = lowS;
-    int mt = nL + nS, ml = nL, ms = nS;
-    for (int o = 16; o > 0; o >>= 1) {
-        mt = max(mt, __shfl_xor_sync(0xffffffffu, mt, o));
-        ml = max(ml, __shfl_xor_sync(0xffffffffu, ml, o));
-        ms = max(ms, __shfl_xor_sync(0xffffffffu, ms, o));
-    }
-    if (lane == 0) {
-        tmaxL[I] = ml;
-        tmaxS[I] = ms;
-        atomicMax(maxCounts, mt);
-        atomicMax(maxCounts + 1, ml);
-        atomicMax(maxCounts + 2, ms);
+    if (w == 0) {
+        int nL = 0, nS = 0, lowL = 0, lowS = 0;
+        for (int v = 0; v < kListWarps; ++v) {
+            nL += cnt[v][0][lane];
+            nS += cnt[v][1][lane];
+            lowL += cnt[v][2][lane];
+            lowS += cnt[v][3][lane];
+        }
+        countL[si] = nL;
+        countS[si] = nS;
+        loL[si] = lowL;
+        loS[si] = lowS;
+        int mt = nL + nS, ml = nL, ms = nS;
+        for (int o = 16; o > 0; o >>= 1) {
+            mt = max(mt, __shfl_xor_sync(0xffffffffu, mt, o));
+            ml = max(ml, __shfl_xor_sync(0xffffffffu, ml, o));
+            ms = max(ms, __shfl_xor_sync(0xffffffffu, ms, o));
+        }
+        if (lane == 0) {
+            tmaxL[I] = ml;
+            tmaxS[I] = ms;
+            atomicMax(maxCounts, mt);
+            atomicMax(maxCounts + 1, ml);
+            atomicMax(maxCounts + 2, ms);
+        }
     }
 }
 
