@@ -307,6 +307,7 @@ struct Context {
     DBuf<float2> shDF;
     // double-float inputs and Ewald tables of the mixed path's residual field
     DBuf<float2> offDF, muDF, tholeDF, dampDF;
+    DBuf<float4> pack0, pack1;  // packed operands of the FP32 CG pair kernel
     DBuf<float> tabG, tabGc, tabH, tabHc;
     RadialTableHost tabGh, tabHh;
     DBuf<unsigned> list;
@@ -418,6 +419,7 @@ struct Context {
         if (mixed) {
             ef.reset(new Engine<float>());
             ef->init(n, npad, usePme, s.pme_order, s.grid);
+            pack0.alloc(npad); pack1.alloc(npad);
             r32.alloc(3 * (size_t) npad); p32.alloc(3 * (size_t) npad); q32.alloc(3 * (size_t) npad);
             x32.alloc(3 * (size_t) npad); b32.alloc(3 * (size_t) npad); res32.alloc(3 * (size_t) npad);
             if (nPT) { ptMuF.alloc((size_t) nPT * 3 * npad); ptEF.alloc((size_t) nPT * 3 * npad); ptGF.alloc((size_t) nPT * 6 * npad); }
@@ -859,11 +861,17 @@ struct Context {
     void cg_matvec(Engine<real>& e, const real* r, real* p, real* q, bool first) {
         cudaStream_t st = stream;
         const int nb = nblk(npad, 256);
+        const bool packed = sizeof(real) == 4;  // FP32: packed-operand pair kernel
         launch(k_cg_direction_sroot<real>, nblk(npad, 128), 128, 0, st, npad, box, e.sroot.p, sc.p, first ? 1 : 0, r,
-               p, e.sp.p, usePme ? e.mfd.p : (real*) nullptr, done.p);
+               p, e.sp.p, usePme ? e.mfd.p : (real*) nullptr, (const typename Vec4<real>::type*) e.prm.p,
+               packed ? (typename Vec4<real>::type*) pack1.p : nullptr, done.p);
         timer.begin(ST_DIPOLE_REAL, st);
-        launch(k_dipole_field<real, false, sizeof(real) == 8>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(),
-               e.arrays(), (const real*) e.sp.p, e.fieldFx.p, (unsigned long long*) nullptr, (const int*) done.p);
+        if (packed)
+            launch(k_dipole_field_packed, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), (const float4*) pack0.p,
+                   (const float4*) pack1.p, npad, (const int*) e.orig.p, e.fieldFx.p, (const int*) done.p);
+        else
+            launch(k_dipole_field<real, false, sizeof(real) == 8>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+                   e.arrays(), (const real*) e.sp.p, e.fieldFx.p, (unsigned long long*) nullptr, (const int*) done.p);
         timer.end(st);
         if (usePme) {
             timer.begin(ST_PME, st);
@@ -1097,6 +1105,8 @@ struct Context {
         if (mixed) {
             Engine<float>& e = *ef;
             prepare_engine(e, true);
+            launch(k_pack_atoms, nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
+                   pack0.p);
             launch_lists(e);
             if (ed) {
                 prepare_engine(*ed, false);

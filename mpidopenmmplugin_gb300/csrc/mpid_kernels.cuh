@@ -155,7 +155,8 @@ __global__ void k_tile_list(int ntiles, const double* __restrict__ center, const
             if (pos < tcap) {
                 const size_t s = (size_t) I * tcap + pos;
                 tileJ[s] = J | (wrap ? (int) 0x80000000 : 0);
-                shF[s] = make_float4((float) sh[0], (float) sh[1], (float) sh[2], 0.f);
+                shF[s] = make_float4((float) sh[0], (float) sh[1], (float) sh[2],
+                                     __int_as_float(J | (wrap ? (int) 0x80000000 : 0)));
                 for (int k = 0; k < 3; ++k) {
                     shD[3 * s + k] = sh[k];
                     const dfloat v = df_from_double(sh[k]);
@@ -619,6 +620,66 @@ k_dipole_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, uns
     for (int q = 0; q < 3; ++q) fx_add(field + q * npad + t.si, acc[q]);
     if (GRAD)
         for (int q = 0; q < 6; ++q) fx_add(grad + q * npad + t.si, acc[3 + q]);
+}
+
+// FP32 T.mu of the CG iterations with packed operands: per pair one 16-byte load of the
+// tile slot (shift, J in .w), and two of atom j: A0 = (offset, Thole width) and
+// A1 = (dipole, damping factor).  Same arithmetic as k_dipole_field<float, false>.
+template <bool QUAD>
+__device__ __forceinline__ void dipole_field_packed_loop(const NbrList& nl, const float4* __restrict__ A0,
+                                                         const float4* __restrict__ A1, const PairTask& t, float* acc) {
+    const PairConsts<float>& pc = nl.cf;
+    const float4 ai = A0[t.si], bi = A1[t.si];
+    for (int k = t.k0; k < t.k1; ++k) {
+        const int pos = QUAD ? nl.cap - 1 - k : k;
+        const unsigned code = nl.list[((size_t) t.I * nl.cap + pos) * 32 + t.lane];
+        const float4 sh = nl.shF[(size_t) t.I * nl.tcap + (code >> 7)];
+        const int Jw = __float_as_int(sh.w);
+        const int sj = (Jw & 0x7fffffff) * 32 + (int) (code & 31u);
+        const float4 aj = A0[sj], bj = A1[sj];
+        float d[3] = {sh.x + (aj.x - ai.x), sh.y + (aj.y - ai.y), sh.z + (aj.z - ai.z)};
+        if (Jw < 0)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) d[q] -= pc.L[q] * rintf(d[q] * pc.iL[q]);
+        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (nl.usePbc && r2 > pc.rc2) continue;
+        const float r = sqrtf(r2);
+        const unsigned flag = (code >> 5) & 3u;
+        const float a = flag == 1u ? ai.w + aj.w : pc.thole;  // flag 1: covalent scale 0
+        PairRadial<float, 0, 0, 2> pr;
+        pair_radial_branch<float, -1, -1, 2, QUAD>(r, pc.ew, 1.f, a, bi.w * bj.w, pr);
+        const float b[4] = {0.f, pr.bU[1], pr.bU[2], 0.f};
+        const float uj[3] = {bj.x, bj.y, bj.z};
+        const float sI[3] = {-d[0], -d[1], -d[2]};
+        float e[3], gr[6];
+        dipole_field<float, false>(uj, sI, b, e, gr);
+        acc[0] += e[0];
+        acc[1] += e[1];
+        acc[2] += e[2];
+    }
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_dipole_field_packed(NbrList nl, const float4* __restrict__ A0, const float4* __restrict__ A1, int npad,
+                      const int* __restrict__ orig, unsigned long long* __restrict__ field, const int* __restrict__ skip) {
+    if (*skip) return;
+    PairTask t;
+    if (!t.init(nl)) return;
+    if (orig[t.si] < 0) return;
+    float acc[3] = {0.f, 0.f, 0.f};
+    if (t.quad)
+        dipole_field_packed_loop<true>(nl, A0, A1, t, acc);
+    else
+        dipole_field_packed_loop<false>(nl, A0, A1, t, acc);
+    for (int q = 0; q < 3; ++q) fx_add(field + q * npad + t.si, acc[q]);
+}
+
+// A0 = (offset, Thole width) of the float engine's atoms.
+__global__ void k_pack_atoms(int npad, const float* __restrict__ off, const float4* __restrict__ prm,
+                             float4* __restrict__ A0) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npad) return;
+    A0[s] = make_float4(off[s], off[npad + s], off[2 * npad + s], prm[s].x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1425,7 +1486,8 @@ __device__ __forceinline__ double sum_partials_256(const double* partial, int nb
 template <typename real>
 __global__ void k_cg_direction_sroot(int npad, BoxDev box, const real* __restrict__ S, const double* __restrict__ sc,
                                      int first, const real* __restrict__ r, real* __restrict__ p, real* __restrict__ sp,
-                                     real* __restrict__ mfd, const int* __restrict__ skip) {
+                                     real* __restrict__ mfd, const typename Vec4<real>::type* __restrict__ prm,
+                                     typename Vec4<real>::type* __restrict__ A1, const int* __restrict__ skip) {
     if (*skip) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= npad) return;
@@ -1442,6 +1504,7 @@ __global__ void k_cg_direction_sroot(int npad, BoxDev box, const real* __restric
     real o[3];
     sym_mul(S, npad, s, v, o);
     for (int c = 0; c < 3; ++c) sp[c * npad + s] = o[c];
+    if (A1) A1[s] = Vec4<real>::make(o[0], o[1], o[2], prm[s].y);
     if (mfd) {
         mfd[s] = real(0);
         for (int j = 0; j < 3; ++j)
