@@ -786,7 +786,8 @@ struct Context {
         if (usePme) {
             e.pme.set_stream(st);
             e.pme.bsplines(n, npad, order.p, wpos.p, box, st);
-            launch(k_frac_multipoles<real>, nblk(npad, 128), 128, 0, st, npad, box, e.mom.p, e.mf.p);
+            // the refinement engine spreads induced dipoles only
+            if (main) launch(k_frac_multipoles<real>, nblk(npad, 128), 128, 0, st, npad, box, e.mom.p, e.mf.p);
         }
         CUDA_CHECK(cudaGetLastError());
     }

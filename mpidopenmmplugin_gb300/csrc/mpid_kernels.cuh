@@ -127,27 +127,38 @@ __global__ void k_tile_list(int ntiles, const double* __restrict__ center, const
                             int* __restrict__ maxTiles) {
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (I >= ntiles) return;
+    const float cI[3] = {(float) center[3 * I], (float) center[3 * I + 1], (float) center[3 * I + 2]};
+    const float hI[3] = {(float) half[3 * I], (float) half[3 * I + 1], (float) half[3 * I + 2]};
     int base = 0;
     for (int J0 = 0; J0 < ntiles; J0 += 32) {
         const int J = J0 + lane;
         bool hit = false, wrap = false;
         double sh[3] = {0.0, 0.0, 0.0};
         if (J < ntiles) {
-            double d2 = 0.0;
+            // bounding-box test in float with a margin far above its rounding
+            const float cut = (float) cutoff * 1.0001f + 1e-4f;
+            float d2 = 0.f;
             for (int k = 0; k < 3; ++k) {
-                double dc = center[3 * J + k] - center[3 * I + k];
-                const double ext = half[3 * I + k] + half[3 * J + k];
+                const float Lk = (float) box.L[k];
+                float dc = cI[k] - (float) center[3 * J + k];
+                dc = -dc;
+                const float ext = hI[k] + (float) half[3 * J + k];
                 bool always = false;
                 if (usePbc) {
-                    always = ext + cutoff >= 0.5 * box.L[k];
+                    always = ext + cut >= 0.5f * Lk;
                     wrap = wrap || always;
-                    dc -= box.L[k] * rint(dc * box.invL[k]);
+                    dc -= Lk * rintf(dc * (float) box.invL[k]);
                 }
-                sh[k] = dc;
-                const double g = fabs(dc) - ext;
-                if (!always && g > 0) d2 += g * g;
+                const float g = fabsf(dc) - ext;
+                if (!always && g > 0.f) d2 += g * g;
             }
-            hit = d2 < cutoff * cutoff;
+            hit = d2 < cut * cut;
+            if (hit)  // minimum-image shift of the centres in FP64
+                for (int k = 0; k < 3; ++k) {
+                    double dc = center[3 * J + k] - center[3 * I + k];
+                    if (usePbc) dc -= box.L[k] * rint(dc * box.invL[k]);
+                    sh[k] = dc;
+                }
         }
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (hit) {
@@ -454,14 +465,16 @@ struct PairTask {
     int I, k0, k1, lane, si;
     bool quad;
     __device__ __forceinline__ int tasks(const NbrList& nl) const { return nl.ntiles * (nl.nchunksL + nl.nchunksS); }
+    // Work items: all erfc-segment items (tile-major), then all quadrature-segment items,
+    // so that resident warps mostly run the same branch of the code.
     __device__ __forceinline__ bool init(const NbrList& nl) {
         const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-        const int nch = nl.nchunksL + nl.nchunksS;
+        const int nLong = nl.ntiles * nl.nchunksL;
         lane = threadIdx.x & 31;
-        I = w / nch;
-        const int c = w - I * nch;
-        quad = c >= nl.nchunksL;
-        k0 = (quad ? c - nl.nchunksL : c) * nl.chunk;
+        quad = w >= nLong;
+        const int wq = quad ? w - nLong : w, nch = quad ? nl.nchunksS : nl.nchunksL;
+        I = nch > 0 ? wq / nch : nl.ntiles;
+        k0 = (wq - I * nch) * nl.chunk;
         si = I * 32 + lane;
         if (I >= nl.ntiles || k0 >= (quad ? nl.tmaxS[I] : nl.tmaxL[I])) return false;
         k1 = min(k0 + nl.chunk, quad ? nl.countS[si] : nl.countL[si]);
@@ -888,7 +901,7 @@ __device__ __forceinline__ void electrostatics_loop(const NbrList& nl, const Ato
 
 // out: force[3][npad], torque[3][npad] fixed point; energy[task] (already x kElectric).
 template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, sizeof(real) == 4 ? 4 : 1)
 k_electrostatics(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ force,
                  unsigned long long* __restrict__ torque, double* __restrict__ energy) {
     PairTask t;
@@ -1451,16 +1464,19 @@ __global__ void k_cg_init_scalars(double* __restrict__ sc, const double* __restr
 // block to finish sums them in block order (deterministic) and updates the scalars, so
 // an iteration needs no separate reduction launches.  `counter` returns to 0 after use.
 
-// Block sum of v (blockDim.x == 256) into red[0].
+// Block sum of v over 256 threads (fixed order: warp shuffles, then the 8 warp sums);
+// the result is valid in thread 0.
 __device__ __forceinline__ double block_sum_256(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     __syncthreads();  // red may still be read from the previous sum
-    red[threadIdx.x] = v;
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < 8 ? red[threadIdx.x] : 0.0;
+        for (int o = 4; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
     }
-    return red[0];
+    return t;
 }
 
 // True in exactly one block: the last of gridDim.x blocks to pass this point (after
@@ -1698,28 +1714,31 @@ __global__ void k_recip_self(int n, int npad, BoxDev box, double alpha, int polT
             frac_multipole(m, A, Mf);
             real muf[3];
             for (int j = 0; j < 3; ++j) muf[j] = A[j][0] * ui[0] + A[j][1] * ui[1] + A[j][2] * ui[2];
-            auto PP = [&](int t, int u, int v) { return (double) phiP[hermite_index(t, u, v) * npad + s]; };
-            auto PD = [&](int t, int u, int v) { return (double) phiD[hermite_index(t, u, v) * npad + s]; };
-            double ef = 0.0, ei = 0.0, f[3] = {0, 0, 0};
+            // energy contractions in FP64, force contractions in the kernel precision
+            auto PP = [&](int t, int u, int v) { return phiP[hermite_index(t, u, v) * npad + s]; };
+            auto PD = [&](int t, int u, int v) { return phiD[hermite_index(t, u, v) * npad + s]; };
+            double ef = 0.0, ei = 0.0;
+            real f[3] = {real(0), real(0), real(0)};
             for (int k = 0; k < 20; ++k) {
                 int t, u, v;
                 hermite_tuv(k, t, u, v);
-                ef += (double) Mf[k] * PP(t, u, v);
-                f[0] += (double) Mf[k] * (PP(t + 1, u, v) + PD(t + 1, u, v));
-                f[1] += (double) Mf[k] * (PP(t, u + 1, v) + PD(t, u + 1, v));
-                f[2] += (double) Mf[k] * (PP(t, u, v + 1) + PD(t, u, v + 1));
+                ef += (double) Mf[k] * (double) PP(t, u, v);
+                f[0] += Mf[k] * (PP(t + 1, u, v) + PD(t + 1, u, v));
+                f[1] += Mf[k] * (PP(t, u + 1, v) + PD(t, u + 1, v));
+                f[2] += Mf[k] * (PP(t, u, v + 1) + PD(t, u, v + 1));
             }
             for (int k = 0; k < 3; ++k) {
                 const int t = k == 0, u = k == 1, v = k == 2;
-                ei += (double) muf[k] * PP(t, u, v);
-                double g0 = PP(t + 1, u, v), g1 = PP(t, u + 1, v), g2 = PP(t, u, v + 1);
+                ei += (double) muf[k] * (double) PP(t, u, v);
+                real g0 = PP(t + 1, u, v), g1 = PP(t, u + 1, v), g2 = PP(t, u, v + 1);
                 if (polType == 0) { g0 += PD(t + 1, u, v); g1 += PD(t, u + 1, v); g2 += PD(t, u, v + 1); }
-                f[0] += (double) muf[k] * g0;
-                f[1] += (double) muf[k] * g1;
-                f[2] += (double) muf[k] * g2;
+                f[0] += muf[k] * g0;
+                f[1] += muf[k] * g1;
+                f[2] += muf[k] * g2;
             }
             eAcc += 0.5 * kElectric * (ef + ei);
-            for (int c = 0; c < 3; ++c) F[c] -= kElectric * (box.A[0][c] * f[0] + box.A[1][c] * f[1] + box.A[2][c] * f[2]);
+            for (int c = 0; c < 3; ++c)
+                F[c] -= kElectric * (double) (A[0][c] * f[0] + A[1][c] * f[1] + A[2][c] * f[2]);
             // torques from the permanent and induced reciprocal potentials
             real P0, P1[3], P2[3][3], P3[3][3][3], tau[3], dtot[3];
             for (int c = 0; c < 3; ++c) dtot[c] = m.d[c] + (aniso ? ui[c] : real(0));
