@@ -40,6 +40,9 @@ extern "C" {
 /* mpid_settings.flags */
 #define MPID_FLAG_EXACT_ANISO_TORQUE 1u  /* use the energy-consistent induced-induced torque on
                                             anisotropic atoms instead of the reference's */
+#define MPID_FLAG_NEAR_FIELD_PCG 2u      /* mutual solver preconditioned with the near-field dipole
+                                            coupling (fewer iterations for strongly coupled systems;
+                                            on water it saves one iteration and costs more) */
 
 typedef struct mpid_context mpid_context;
 

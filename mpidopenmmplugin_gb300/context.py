@@ -16,6 +16,7 @@ from .force import MPIDError, MPIDForce
 MPID_PRECISION_MIXED = 0
 MPID_PRECISION_DOUBLE = 1
 MPID_FLAG_EXACT_ANISO_TORQUE = 1
+MPID_FLAG_NEAR_FIELD_PCG = 2
 
 # Entry points declared in include/mpid_gb300.h
 C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multipoles", "mpid_set_covalent",
@@ -120,7 +121,7 @@ class MPIDContext:
     """
 
     def __init__(self, force: MPIDForce, num_particles=None, device=0, precision="mixed",
-                 exact_aniso_torque=False, box=None):
+                 exact_aniso_torque=False, box=None, preconditioner=False):
         self.lib = load_library()
         n = force.getNumMultipoles() if num_particles is None else int(num_particles)
         force.validate(n, box)
@@ -144,7 +145,8 @@ class MPIDContext:
         s.default_thole = force.getDefaultTholeWidth()
         s.scale14 = force.get14ScaleFactor()
         s.precision = {"mixed": MPID_PRECISION_MIXED, "double": MPID_PRECISION_DOUBLE}[precision]
-        s.flags = MPID_FLAG_EXACT_ANISO_TORQUE if exact_aniso_torque else 0
+        s.flags = ((MPID_FLAG_EXACT_ANISO_TORQUE if exact_aniso_torque else 0) |
+                   (MPID_FLAG_NEAR_FIELD_PCG if preconditioner else 0))
         self.n = n
         self.precision = precision
         self._h = ctypes.c_void_p()

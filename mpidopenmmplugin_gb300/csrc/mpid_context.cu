@@ -189,6 +189,8 @@ struct Engine {
     DBuf<real> phiP, phiD, phiT;              // [35][npad] each; phiT scratch
     DBuf<unsigned long long> fieldFx, gradFx;  // [3][npad], [6][npad]
     DBuf<real> Efix, muD, SE, mu, Etmp, Gtmp, sp;
+    DBuf<real> zc;                             // preconditioned residual of the mutual CG
+    DBuf<unsigned long long> precFx;           // [3][npad] near-field preconditioner field
     PmeStage<real> pme;
     bool usePme = false;
 
@@ -224,6 +226,8 @@ struct Engine {
         Etmp.alloc(3 * (size_t) npad);
         Gtmp.alloc(6 * (size_t) npad);
         sp.alloc(3 * (size_t) npad);
+        zc.alloc(3 * (size_t) npad);
+        precFx.alloc(3 * (size_t) npad);
         if (usePme) pme.init(order, grid[0], grid[1], grid[2], npad);
     }
 };
@@ -405,8 +409,8 @@ struct Context {
         forcesOut.alloc(3 * (size_t) n);
         partial.alloc(2 * (size_t) nblk(npad, 256)); red.alloc(4); sc.alloc(8);
         iter.alloc(1); done.alloc(1);
-        counters.alloc(2);
-        CUDA_CHECK(cudaMemset(counters.p, 0, 2 * sizeof(unsigned)));
+        counters.alloc(3);
+        CUDA_CHECK(cudaMemset(counters.p, 0, 3 * sizeof(unsigned)));
         CUDA_CHECK(cudaMallocHost(&hostDone, 256 * sizeof(int)));
         CUDA_CHECK(cudaMallocHost(&hostMax, 4 * sizeof(int)));
         CUDA_CHECK(cudaEventCreateWithFlags(&evLists, cudaEventDisableTiming));
@@ -886,6 +890,17 @@ struct Context {
                (const real*) e.sp.p, q, partial.p, counters.p, sc.p, (const int*) done.p);
     }
 
+    // z = P r with the near-field preconditioner (first: also p = z, sc[0] = r.z).
+    template <typename real>
+    void precondition(Engine<real>& e, const real* r, real* p, bool first) {
+        cudaStream_t st = stream;
+        if (nchunksS > 0)
+            launch(k_precond_field<real>, std::max(1, nblk(ntiles * nchunksS, kWarpsPerBlock)), 32 * kWarpsPerBlock, 0, st,
+                   nbr_list(), e.arrays(), r, e.precFx.p, (const int*) done.p);
+        launch(k_precond_finish<real>, nblk(npad, 256), 256, 0, st, n, npad, (const real*) e.sroot.p, e.precFx.p, r, e.zc.p,
+               p, first ? 1 : 0, partial.p, counters.p + 2, sc.p, (const int*) done.p);
+    }
+
     // Preconditioned CG on B y = b, B = I - S T S, in precision `real`; x accumulates in xreal.
     // Convergence: 48.033324 sqrt(|S r|^2/n) < target.  Returns iterations used.
     template <typename real, typename xreal>
@@ -897,13 +912,19 @@ struct Context {
         launch(k_reduce_partials, 1, 1024, 0, st, nb, 2, partial.p, red.p, nullptr);
         launch(k_cg_init_scalars, 1, 1, 0, st, sc.p, red.p, n, target, iter.p, done.p);
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));  // cleared again by each matvec
+        const bool pcg = (set.flags & MPID_FLAG_NEAR_FIELD_PCG) != 0;
+        if (pcg) {
+            CUDA_CHECK(cudaMemsetAsync(e.precFx.p, 0, 3 * (size_t) npad * 8, st));  // cleared by each application
+            precondition(e, r, p, true);
+        }
         CUDA_CHECK(cudaGetLastError());
         int it = 0;
         for (it = 0; it < maxIter; ++it) {
-            // q = B p = p - S T S p, p.q, then the update and the scalars
-            cg_matvec(e, (const real*) r, p, q, it == 0);
+            // q = B p = p - S T S p, p.q, then the update and the scalars (PCG: p from z = P r)
+            cg_matvec(e, pcg ? (const real*) e.zc.p : (const real*) r, p, q, it == 0);
             launch(k_cg_update_scalars<real, xreal>, nb, 256, 0, st, n, npad, e.sroot.p, sc.p, p, q, x, r, partial.p,
-                   counters.p + 1, target, iter.p, maxIter, done.p);
+                   counters.p + 1, target, iter.p, maxIter, done.p, pcg ? 1 : 0);
+            if (pcg) precondition(e, r, p, false);
             CUDA_CHECK(cudaGetLastError());
             const int slot = it % (int) iterEvents.size();
             CUDA_CHECK(cudaMemcpyAsync(hostDone + (slot % 256), done.p, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -1580,7 +1580,7 @@ __global__ void __launch_bounds__(256)
 k_cg_update_scalars(int n, int npad, const real* __restrict__ S, double* __restrict__ sc, const real* __restrict__ p,
                     const real* __restrict__ q, xreal* __restrict__ x, real* __restrict__ r, double* __restrict__ partial,
                     unsigned* __restrict__ counter, double target, int* __restrict__ iter, int maxIter,
-                    int* __restrict__ done) {
+                    int* __restrict__ done, int pcg) {
     __shared__ double red[256];
     if (*done) return;
     const double a = sc[0] / sc[1];
@@ -1610,11 +1610,105 @@ k_cg_update_scalars(int n, int npad, const real* __restrict__ S, double* __restr
         if (threadIdx.x == 0) {
             sc[2] = rrNew;
             sc[3] = srNew;
-            sc[5] = rrNew / sc[0];
-            sc[0] = rrNew;
+            if (!pcg) {  // plain CG: beta from r.r; PCG takes it from k_precond_finish
+                sc[5] = rrNew / sc[0];
+                sc[0] = rrNew;
+            }
             sc[6] = 48.033324 * sqrt(srNew / n);
             *iter += 1;
             if (sc[6] < target || *iter >= maxIter || !(sc[6] == sc[6])) *done = 1;
+            *counter = 0u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Near-field preconditioner of the mutual CG: P = I + S T_n S, T_n the bare
+// Thole-damped dipole field (b_1 = lambda_3 / r^3, b_2 = 3 lambda_5 / r^5) over the
+// quadrature segment of the lists (alpha r < 1.5 and covalent pairs), where the
+// coupling of induced dipoles is strongest.  P is a first-order approximation of
+// B^-1 = (I - S T S)^-1 and costs one pass over about an eighth of the pairs.
+
+// w_i = T_n v over atom i's near pairs, v_j = S_j r_j (fixed-point accumulation).
+template <typename real>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_precond_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ r, unsigned long long* __restrict__ w,
+                const int* __restrict__ skip) {
+    if (*skip) return;
+    const int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (nl.nchunksS == 0) return;
+    const int I = wi / nl.nchunksS;
+    const int k0 = (wi - I * nl.nchunksS) * nl.chunk;
+    if (I >= nl.ntiles || k0 >= nl.tmaxS[I]) return;
+    const int si = I * 32 + lane, npad = at.npad;
+    if (at.orig[si] < 0) return;
+    const int k1 = min(k0 + nl.chunk, nl.countS[si]);
+    const PairConsts<real>& pc = pair_consts<real>(nl);
+    const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+    const typename Vec4<real>::type pi = at.prm[si];
+    real acc[3] = {real(0), real(0), real(0)};
+    for (int k = k0; k < k1; ++k) {
+        int sj;
+        unsigned flag;
+        real d[3], r2;
+        if (!list_pair<real, true>(nl, pc, at, I, k, lane, oi, sj, flag, d, r2)) continue;
+        const typename Vec4<real>::type pj = at.prm[sj];
+        const real dd = pi.y * pj.y;
+        real lam[3] = {real(1), real(1), real(1)}, om[3];
+        const real rr = sqrt(r2);
+        if (dd > real(0)) {
+            const real sT = (flag == 1u ? pi.x + pj.x : pc.thole) * rr / dd;
+            if (sT < real(50)) thole_lambdas<real, 2>(sT, lam, om);
+        }
+        const real rinv2 = real(1) / r2;
+        const real r3inv = rinv2 / rr;
+        const real b1 = lam[1] * r3inv;
+        const real b2 = real(3) * lam[2] * r3inv * rinv2;
+        const real rj[3] = {r[sj], r[npad + sj], r[2 * npad + sj]};
+        real v[3];
+        sym_mul(at.sroot, npad, sj, rj, v);
+        const real vd = v[0] * d[0] + v[1] * d[1] + v[2] * d[2];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) acc[q] += b2 * vd * d[q] - b1 * v[q];
+    }
+    for (int q = 0; q < 3; ++q) fx_add(w + q * npad + si, acc[q]);
+}
+
+// z = r + S w (w read and cleared), r.z; on the first application also p = z and
+// sc[0] = r.z, afterwards sc[5] = beta = (r.z)_new / (r.z)_old and sc[0] = (r.z)_new.
+template <typename real>
+__global__ void __launch_bounds__(256)
+k_precond_finish(int n, int npad, const real* __restrict__ S, unsigned long long* __restrict__ wfx,
+                 const real* __restrict__ r, real* __restrict__ z, real* __restrict__ p, int first,
+                 double* __restrict__ partial, unsigned* __restrict__ counter, double* __restrict__ sc,
+                 const int* __restrict__ skip) {
+    __shared__ double red[256];
+    if (*skip) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (s < npad) {
+        real wv[3];
+        for (int c = 0; c < 3; ++c) {
+            wv[c] = s < n ? real(fx_get(wfx, c * npad + s)) : real(0);
+            wfx[c * npad + s] = 0ull;
+        }
+        real sw[3];
+        sym_mul(S, npad, s, wv, sw);
+        for (int c = 0; c < 3; ++c) {
+            const real rv = r[c * npad + s];
+            const real zv = rv + sw[c];
+            z[c * npad + s] = zv;
+            if (first) p[c * npad + s] = zv;
+            acc += (double) rv * (double) zv;
+        }
+    }
+    const double b = block_sum_256(acc, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = b;
+    if (last_block(counter)) {
+        const double rz = sum_partials_256(partial, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            if (!first) sc[5] = rz / sc[0];
+            sc[0] = rz;
             *counter = 0u;
         }
     }

@@ -163,3 +163,21 @@ def test_validation_errors_on_device():
     ctx = MPIDContext(f, precision="double")
     with pytest.raises(Exception, match="did not converge"):
         ctx.evaluate(pos, box)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "double"])
+def test_preconditioned_cg_matches_plain_cg(precision):
+    """The near-field preconditioner changes the path to the solution, not the solution:
+    PCG and plain CG agree within the solver tolerance (1e-7 D) on the 24,000-atom box."""
+    f, pos, box = synthetic.workload("water24k", polarization=MPIDForce.Mutual)
+    a = MPIDContext(f, precision=precision, preconditioner=True)
+    ea, fa = a.evaluate(pos, box)
+    b = MPIDContext(f, precision=precision)
+    eb, fb = b.evaluate(pos, box)
+    sa, sb = a.stats(), b.stats()
+    print("%s: PCG %d iterations (%d refinements), CG %d iterations (%d refinements)" %
+          (precision, sa["solver_iterations"], sa["refinement_steps"], sb["solver_iterations"], sb["refinement_steps"]))
+    assert sa["solver_residual"] < 1e-7 and sb["solver_residual"] < 1e-7
+    assert abs(ea - eb) / abs(eb) < 1e-7
+    assert helpers.rel_rms(fa, fb) < 2e-6
+    assert helpers.rel_rms(a.getInducedDipoles(), b.getInducedDipoles()) < 2e-6
