@@ -287,6 +287,19 @@ struct Context {
     int n = 0, npad = 0, ntiles = 0;
     bool usePme = false, mixed = true;
     cudaStream_t stream = nullptr;
+    // Side stream for the reciprocal-space (PME) chains, which run concurrently with the
+    // real-space pair kernel on the main stream: fork_pme makes the side stream wait for
+    // the main stream's work so far, join_pme makes the main stream wait for the side.
+    cudaStream_t pmeStream = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
+    void fork_pme() {
+        CUDA_CHECK(cudaEventRecord(evFork, stream));
+        CUDA_CHECK(cudaStreamWaitEvent(pmeStream, evFork, 0));
+    }
+    void join_pme() {
+        CUDA_CHECK(cudaEventRecord(evJoin, pmeStream));
+        CUDA_CHECK(cudaStreamWaitEvent(stream, evJoin, 0));
+    }
     bool ownStream = false;
 
     // parameters (device, original order)
@@ -356,6 +369,9 @@ struct Context {
     ~Context() {
         timer.destroy();
         if (hostDone) cudaFreeHost(hostDone);
+        if (evFork) cudaEventDestroy(evFork);
+        if (evJoin) cudaEventDestroy(evJoin);
+        if (pmeStream) cudaStreamDestroy(pmeStream);
         if (hostMax) cudaFreeHost(hostMax);
         if (evLists) cudaEventDestroy(evLists);
         for (auto e : iterEvents) cudaEventDestroy(e);
@@ -411,6 +427,9 @@ struct Context {
         iter.alloc(1); done.alloc(1);
         counters.alloc(3);
         CUDA_CHECK(cudaMemset(counters.p, 0, 3 * sizeof(unsigned)));
+        CUDA_CHECK(cudaStreamCreateWithFlags(&pmeStream, cudaStreamNonBlocking));
+        CUDA_CHECK(cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming));
+        CUDA_CHECK(cudaEventCreateWithFlags(&evJoin, cudaEventDisableTiming));
         CUDA_CHECK(cudaMallocHost(&hostDone, 256 * sizeof(int)));
         CUDA_CHECK(cudaMallocHost(&hostMax, 4 * sizeof(int)));
         CUDA_CHECK(cudaEventCreateWithFlags(&evLists, cudaEventDisableTiming));
@@ -788,7 +807,7 @@ struct Context {
         launch(k_gather_atoms<real>, nblk(npad, 128), 128, 0, st, n, npad, order.p, mol(), pos.p, wpos.p, center.p, e.arrays(),
                                                                main ? mom64.p : nullptr, main ? prm64.p : nullptr);
         if (usePme) {
-            e.pme.set_stream(st);
+            e.pme.set_stream(pmeStream);
             e.pme.bsplines(n, npad, order.p, wpos.p, box, st);
             // the refinement engine spreads induced dipoles only
             if (main) launch(k_frac_multipoles<real>, nblk(npad, 128), 128, 0, st, npad, box, e.mom.p, e.mf.p);
@@ -805,16 +824,19 @@ struct Context {
     void fixed_field(Engine<real>& e) {
         cudaStream_t st = stream;
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
+        if (usePme) {
+            fork_pme();
+            cudaStream_t ps = pmeStream;
+            timer.begin(ST_PME, ps);
+            e.pme.template spread<20>(n, npad, box, e.mf.p, nullptr, ps);
+            e.pme.convolve(influence.p, nullptr, ps);
+            e.pme.template gather<35>(n, npad, box, e.phiP.p, nullptr, ps);
+            timer.end(ps);
+        }
         timer.begin(ST_FIXED_REAL, st);
         launch(k_fixed_field<real>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), e.fieldFx.p);
         timer.end(st);
-        if (usePme) {
-            timer.begin(ST_PME, st);
-            e.pme.template spread<20>(n, npad, box, e.mf.p, nullptr, st);
-            e.pme.convolve(influence.p, nullptr, st);
-            e.pme.template gather<35>(n, npad, box, e.phiP.p, nullptr, st);
-            timer.end(st);
-        }
+        if (usePme) join_pme();
         launch(k_record_fixed<real>, nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
                                                                usePme ? e.phiP.p : nullptr, e.arrays(), e.Efix.p, e.muD.p,
                                                                e.SE.p);
@@ -826,6 +848,21 @@ struct Context {
     void dipole_field(Engine<real>& e, const real* mu, real* E, real* G, const int* skip, int nterm = 4) {
         cudaStream_t st = stream;
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
+        if (usePme) {
+            fork_pme();
+            cudaStream_t ps = pmeStream;
+            timer.begin(ST_PME, ps);
+            launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, ps, npad, box, mu, e.mfd.p, skip);
+            e.pme.template spread<4>(n, npad, box, e.mfd.p, skip, ps);
+            e.pme.convolve(influence.p, skip, ps);
+            if (nterm == 4)
+                e.pme.template gather<4>(n, npad, box, e.phiT.p, skip, ps);
+            else if (nterm == 10)
+                e.pme.template gather<10>(n, npad, box, e.phiT.p, skip, ps);
+            else
+                e.pme.template gather<35>(n, npad, box, e.phiT.p, skip, ps);
+            timer.end(ps);
+        }
         // the FP64 field of the mixed path's residual refinement is timed on its own
         timer.begin(mixed && sizeof(real) == 8 ? ST_REFINE_REAL : ST_DIPOLE_REAL, st);
         if (mixed && sizeof(real) == 8) {
@@ -842,19 +879,7 @@ struct Context {
                                                                                       e.fieldFx.p, nullptr, skip);
         }
         timer.end(st);
-        if (usePme) {
-            timer.begin(ST_PME, st);
-            launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, st, npad, box, mu, e.mfd.p, skip);
-            e.pme.template spread<4>(n, npad, box, e.mfd.p, skip, st);
-            e.pme.convolve(influence.p, skip, st);
-            if (nterm == 4)
-                e.pme.template gather<4>(n, npad, box, e.phiT.p, skip, st);
-            else if (nterm == 10)
-                e.pme.template gather<10>(n, npad, box, e.phiT.p, skip, st);
-            else
-                e.pme.template gather<35>(n, npad, box, e.phiT.p, skip, st);
-            timer.end(st);
-        }
+        if (usePme) join_pme();
         launch(k_dipole_field_total<real>, nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p, e.gradFx.p,
                                                                      usePme ? e.phiT.p : nullptr, nterm, mu, E, G, skip);
         CUDA_CHECK(cudaGetLastError());
@@ -870,6 +895,15 @@ struct Context {
         launch(k_cg_direction_sroot<real>, nblk(npad, 128), 128, 0, st, npad, box, e.sroot.p, sc.p, first ? 1 : 0, r,
                p, e.sp.p, usePme ? e.mfd.p : (real*) nullptr, (const typename Vec4<real>::type*) e.prm.p,
                packed ? (typename Vec4<real>::type*) pack1.p : nullptr, done.p);
+        if (usePme) {
+            fork_pme();
+            cudaStream_t ps = pmeStream;
+            timer.begin(ST_PME, ps);
+            e.pme.template spread<4>(n, npad, box, e.mfd.p, done.p, ps);
+            e.pme.convolve(influence.p, done.p, ps);
+            e.pme.template gather<4>(n, npad, box, e.phiT.p, done.p, ps);
+            timer.end(ps);
+        }
         timer.begin(ST_DIPOLE_REAL, st);
         if (packed)
             launch(k_dipole_field_packed, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), (const float4*) pack0.p,
@@ -878,13 +912,7 @@ struct Context {
             launch(k_dipole_field<real, false, sizeof(real) == 8>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(),
                    e.arrays(), (const real*) e.sp.p, e.fieldFx.p, (unsigned long long*) nullptr, (const int*) done.p);
         timer.end(st);
-        if (usePme) {
-            timer.begin(ST_PME, st);
-            e.pme.template spread<4>(n, npad, box, e.mfd.p, done.p, st);
-            e.pme.convolve(influence.p, done.p, st);
-            e.pme.template gather<4>(n, npad, box, e.phiT.p, done.p, st);
-            timer.end(st);
-        }
+        if (usePme) join_pme();
         launch(k_cg_matvec_finish<real>, nb, 256, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
                usePme ? (const real*) e.phiT.p : (const real*) nullptr, (const real*) e.sroot.p, (const real*) p,
                (const real*) e.sp.p, q, partial.p, counters.p, sc.p, (const int*) done.p);
@@ -1043,13 +1071,16 @@ struct Context {
     void finish(Engine<real>& e, real* ptMu, real* ptE, real* ptG) {
         cudaStream_t st = stream;
         if (usePme) {
-            // reciprocal potential of the final induced dipoles (35 terms)
-            timer.begin(ST_PME, st);
-            launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, st, npad, box, e.mu.p, e.mfd.p, nullptr);
-            e.pme.template spread<4>(n, npad, box, e.mfd.p, nullptr, st);
-            e.pme.convolve(influence.p, nullptr, st);
-            e.pme.template gather<35>(n, npad, box, e.phiD.p, nullptr, st);
-            timer.end(st);
+            // reciprocal potential of the final induced dipoles (35 terms), on the side
+            // stream while the energy/force pair kernel runs
+            fork_pme();
+            cudaStream_t ps = pmeStream;
+            timer.begin(ST_PME, ps);
+            launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, ps, npad, box, e.mu.p, e.mfd.p, nullptr);
+            e.pme.template spread<4>(n, npad, box, e.mfd.p, nullptr, ps);
+            e.pme.convolve(influence.p, nullptr, ps);
+            e.pme.template gather<35>(n, npad, box, e.phiD.p, nullptr, ps);
+            timer.end(ps);
         }
         CUDA_CHECK(cudaMemsetAsync(forceFx.p, 0, 3 * (size_t) npad * 8, st));
         CUDA_CHECK(cudaMemsetAsync(torqueFx.p, 0, 3 * (size_t) npad * 8, st));
@@ -1069,6 +1100,7 @@ struct Context {
             launch(k_electrostatics<real, false, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
         timer.end(st);
+        if (usePme) join_pme();
         timer.begin(ST_FINISH, st);
         OptArgs opt{};
         if (set.polarization_type == MPID_EXTRAPOLATED) {
