@@ -53,6 +53,7 @@ static inline CF m_sqrt(CF x) { ++g.special; return mk(std::sqrt(x.v)); }
 static inline CF m_erfc(CF x) { ++g.special; return mk(std::erfc(x.v)); }
 static inline CF m_fabs(CF x) { return mk(std::fabs(x.v)); }
 static inline CF m_copysign(CF a, CF b) { return mk(std::copysign(a.v, b.v)); }
+static inline CF m_fma(CF a, CF b, CF c) { g.mul++; g.add++; return mk(std::fma(a.v, b.v, c.v)); }
 }  // namespace mpid
 static inline CF sqrt(CF x) { ++g.special; return mk(std::sqrt(x.v)); }
 
@@ -62,6 +63,7 @@ namespace mpid {
 template <> struct Prec<CF> {
     static constexpr float kQuadX = 1.5f;
     static constexpr int kQuadNodes = 8;
+    static constexpr int kBoysTerms = 16;
 };
 }  // namespace mpid
 

@@ -31,13 +31,16 @@ constexpr double kSqrtPi = 1.7724538509055160273;
 
 template <typename real> struct Prec;
 template <> struct Prec<float> {
-    // Below this alpha*r the erf part of the kernels is integrated by quadrature.
+    // Below this alpha*r the erf part of the kernels comes from the Boys function series
+    // (the erfc recursion above it).
     static constexpr float kQuadX = 1.5f;
     static constexpr int kQuadNodes = 8;
+    static constexpr int kBoysTerms = 16;   // series truncation < 3e-11 relative at (alpha r)^2 <= 2.25
 };
 template <> struct Prec<double> {
     static constexpr double kQuadX = 1.5;
     static constexpr int kQuadNodes = 14;
+    static constexpr int kBoysTerms = 26;   // < 1e-16
 };
 
 MPID_HD float m_exp(float x) { return expf(x); }
@@ -50,6 +53,9 @@ MPID_HD float m_fabs(float x) { return fabsf(x); }
 MPID_HD double m_fabs(double x) { return fabs(x); }
 MPID_HD float m_copysign(float a, float b) { return copysignf(a, b); }
 MPID_HD double m_copysign(double a, double b) { return copysign(a, b); }
+// a * b + c with one rounding (keeps the low parts of split constants effective)
+MPID_HD float m_fma(float a, float b, float c) { return fmaf(a, b, c); }
+MPID_HD double m_fma(double a, double b, double c) { return fma(a, b, c); }
 
 // ---------------------------------------------------------------------------
 // Gauss-Legendre nodes/weights on [0, 1] (8 and 14 points), used to integrate
@@ -88,8 +94,8 @@ template <typename real>
 struct EwaldAlpha {
     real hi, lo;        // alpha
     real pre_hi, pre_lo;  // 2 alpha / sqrt(pi)
-    real a2x2;          // 2 alpha^2
-    MPID_HD EwaldAlpha() : hi(0), lo(0), pre_hi(0), pre_lo(0), a2x2(0) {}
+    real a2x2, a2x2_lo;   // 2 alpha^2
+    MPID_HD EwaldAlpha() : hi(0), lo(0), pre_hi(0), pre_lo(0), a2x2(0), a2x2_lo(0) {}
     MPID_HD explicit EwaldAlpha(double a) {
         hi = real(a);
         lo = real(a - double(hi));
@@ -97,8 +103,13 @@ struct EwaldAlpha {
         pre_hi = real(p);
         pre_lo = real(p - double(pre_hi));
         a2x2 = real(2.0 * a * a);
+        a2x2_lo = real(2.0 * a * a - double(a2x2));
     }
-    MPID_HD real times(real r) const { return hi * r + lo * r; }
+    MPID_HD real times(real r) const { return m_fma(hi, r, lo * r); }
+    // v * 2 alpha^2 without the rounding of 2 alpha^2
+    MPID_HD real times_a2x2(real v) const { return m_fma(a2x2, v, a2x2_lo * v); }
+    // v * 2 alpha / sqrt(pi) without the rounding of the constant
+    MPID_HD real times_pre(real v) const { return m_fma(pre_hi, v, pre_lo * v); }
 };
 
 // b_n (n = 0..NMAX) of erf(alpha r)/r for alpha r below the quadrature threshold.
@@ -125,8 +136,55 @@ MPID_HD void erf_part_quadrature(real r, const EwaldAlpha<real>& al, real* bF) {
     real scale = real(1);
 #pragma unroll
     for (int n = 0; n <= NMAX; ++n) {
-        bF[n] = (al.pre_hi * acc[n] + al.pre_lo * acc[n]) * scale;
-        scale *= al.a2x2;
+        bF[n] = al.times_pre(acc[n]) * scale;
+        scale = al.times_a2x2(scale);
+    }
+}
+
+// 1/m as an unevaluated sum hi + lo of the arithmetic type (so that products with it
+// carry no systematic rounding of the constant).
+template <typename real>
+struct InvOdd {
+    real hi, lo;
+    MPID_HD explicit InvOdd(int m) {
+        const double v = 1.0 / (double) m;
+        hi = real(v);
+        lo = real(v - (double) hi);
+    }
+    MPID_HD real times(real x) const { return m_fma(hi, x, lo * x); }
+};
+
+// b_n (n = 0..NMAX) of erf(alpha r)/r through the Boys function
+//   F_n(T) = int_0^1 v^(2n) exp(-T v^2) dv,  T = (alpha r)^2:
+//   b_n = 2^(n+1) alpha^(2n+1) / sqrt(pi) F_n(T).
+// F_NMAX from the series exp(-T) sum_k (2T)^k / ((2N+1)(2N+3)...(2N+2k+1)), whose terms
+// are all positive; lower orders by the stable downward recursion
+//   F_(n-1) = (2T F_n + exp(-T)) / (2n - 1).
+// No cancellation and no deterministic quadrature error (used for alpha r < 1.5, where
+// the series has converged to the working precision after Prec::kBoysTerms terms).
+template <typename real, int NMAX>
+MPID_HD void erf_part_boys(real r, const EwaldAlpha<real>& al, real* bF) {
+    constexpr int K = Prec<real>::kBoysTerms;
+    const real x = al.times(r);
+    const real T = x * x, twoT = T + T;
+    const real ex = m_exp(-T);
+    real term = InvOdd<real>(2 * NMAX + 1).times(real(1));
+    real sum = term;
+#pragma unroll
+    for (int k = 1; k < K; ++k) {
+        term = InvOdd<real>(2 * NMAX + 2 * k + 1).times(term * twoT);
+        sum += term;
+    }
+    real F[NMAX + 1];
+    F[NMAX] = ex * sum;
+#pragma unroll
+    for (int n = NMAX; n >= 1; --n) F[n - 1] = InvOdd<real>(2 * n - 1).times(twoT * F[n] + ex);
+    // prefactor 2^(n+1) alpha^(2n+1) / sqrt(pi): (2 alpha / sqrt(pi)) (2 alpha^2)^n
+    real scale = real(1);
+#pragma unroll
+    for (int n = 0; n <= NMAX; ++n) {
+        bF[n] = al.times_pre(F[n]) * scale;
+        scale = al.times_a2x2(scale);
     }
 }
 
@@ -137,11 +195,11 @@ MPID_HD void erfc_part(real r, real rinv2, const EwaldAlpha<real>& al, real* bE)
     const real ex = m_exp(-ar * ar);
     bE[0] = m_erfc(ar) / r;
     // c_n = (2 alpha^2)^n / (alpha sqrt(pi)) * exp(-alpha^2 r^2), starting at n = 1
-    real c = (al.pre_hi + al.pre_lo) * ex;
+    real c = al.times_pre(ex);
 #pragma unroll
     for (int n = 1; n <= NMAX; ++n) {
         bE[n] = (real(2 * n - 1) * bE[n - 1] + c) * rinv2;
-        c *= al.a2x2;
+        c = al.times_a2x2(c);
     }
 }
 
@@ -246,10 +304,21 @@ MPID_HD void pair_radial_branch(real r, const EwaldAlpha<real>& alpha, real scal
     }
     if (QUAD) {
         real bF[NMAX + 1];
-        erf_part_quadrature<real, NMAX>(r, alpha, bF);
+        erf_part_boys<real, NMAX>(r, alpha, bF);
         if (NP >= 0) {
+            // K_p = (s - erf)/r: for s = 1 it is erfc(alpha r)/r, whose upward recursion has
+            // no cancellation, while 1/r - erf(alpha r)/r would amplify the relative error
+            // of the erf part by erf/erfc (up to ~30 near the branch threshold)
+            constexpr int NPP = NP > 0 ? NP : 0;
+            if (scale == real(1)) {
+                real bE[NMAX + 1];
+                erfc_part<real, NMAX>(r, rinv2, alpha, bE);
 #pragma unroll
-            for (int n = 0; n <= (NP > 0 ? NP : 0); ++n) out.bP[n] = scale * bB[n] - bF[n];
+                for (int n = 0; n <= NPP; ++n) out.bP[n] = bE[n];
+            } else {
+#pragma unroll
+                for (int n = 0; n <= NPP; ++n) out.bP[n] = scale * bB[n] - bF[n];
+            }
         }
         if (NI > 0) {
 #pragma unroll

@@ -1,12 +1,23 @@
 """Seeded synthetic MPID systems with the shapes of the benchmark configurations.
 
+Water boxes:
+
 Rigid 3-site waters (O-H 0.9572 A, H-O-H 104.52 deg) at random orientations on a
 jittered cubic lattice; Z-then-X frames (O: z -> H1, x -> H2; H: z -> O, x -> the other
 H); charges O -0.834, H +0.417; dipoles, quadrupoles and octopoles drawn per atom from
 N(0, 0.1 / 0.05 / 0.02 e A^n) and projected traceless; isotropic polarisability 1.0 A^3
 (O) and 0.3 A^3 (H); Thole width 1.3 (default width 1.3, per-atom 0.65 so that excluded
-pairs also use 1.3); intramolecular 1-2 and 1-3 pairs excluded.  Units are converted to
-nm / e nm^k / nm^3.  Nothing here runs on the evaluation path.
+pairs also use 1.3); intramolecular 1-2 and 1-3 pairs excluded.
+
+Solution (waters plus ethane-like solutes): staggered C2H6 (C-C 1.53 A, C-H 1.09 A,
+tetrahedral angles) at random orientations on lattice sites whose 18 face and edge
+neighbours are left empty; charges C -0.18, H +0.06; dipoles, quadrupoles and octopoles from
+N(0, 0.15 / 0.08 / 0.03 e A^n); anisotropic polarisabilities with local-frame diagonal
+U[0.5, 2.0] A^3 (the API takes the diagonal in the local frame); per-atom Thole widths
+U[0.5, 1], so that the pair widths a_i + a_j of excluded pairs lie in U[1, 2];
+1-2 and 1-3 pairs excluded, 1-4 pairs scaled by 0.5.
+
+Units are converted to nm / e nm^k / nm^3.  Nothing here runs on the evaluation path.
 """
 import numpy as np
 
@@ -96,6 +107,91 @@ def water_box(n_waters, box_angstrom, seed=2024, lattice=None, mult_sigma=(0.1, 
     return f, pos, box
 
 
+def _ethane(rng):
+    """Atom positions (A, 8 x 3: C1, C2, H11..H13, H21..H23) of a staggered ethane at the
+    origin, randomly oriented."""
+    cc, ch = 1.53, 1.09
+    tet = np.deg2rad(109.47)
+    c1 = np.array([0.0, 0.0, -cc / 2])
+    c2 = np.array([0.0, 0.0, cc / 2])
+    h = []
+    for k in range(3):
+        phi = 2 * np.pi * k / 3
+        h.append(c1 + ch * np.array([np.sin(tet) * np.cos(phi), np.sin(tet) * np.sin(phi), np.cos(tet)]))
+    for k in range(3):
+        phi = 2 * np.pi * k / 3 + np.pi / 3  # staggered
+        h.append(c2 + ch * np.array([np.sin(tet) * np.cos(phi), np.sin(tet) * np.sin(phi), -np.cos(tet)]))
+    xyz = np.array([c1, c2] + h)
+    R = _random_rotations(rng, 1)[0]
+    return xyz @ R.T
+
+
+def solution_box(n_waters, n_solutes, box_angstrom, seed=2024):
+    """Return (force, positions_nm, box_nm) for n_waters waters and n_solutes ethanes."""
+    rng = np.random.default_rng(seed)
+    L = box_angstrom
+    side = int(np.ceil((n_waters + 19 * n_solutes) ** (1.0 / 3.0)))
+    spacing = L / side
+    idx = np.arange(side ** 3)
+    sites = np.stack(np.unravel_index(idx, (side, side, side)), axis=1)
+    # solute sites with their 18 face and edge neighbours left empty
+    taken = np.zeros(side ** 3, dtype=bool)
+    solutes = []
+    for cand in rng.permutation(side ** 3):
+        if len(solutes) == n_solutes:
+            break
+        i, j, k = sites[cand]
+        nb = [((i + di) % side, (j + dj) % side, (k + dk) % side)
+              for di in (-1, 0, 1) for dj in (-1, 0, 1) for dk in (-1, 0, 1) if abs(di) + abs(dj) + abs(dk) <= 2]
+        nbi = [np.ravel_multi_index(t, (side, side, side)) for t in nb]
+        if taken[nbi].any():
+            continue
+        taken[nbi] = True
+        solutes.append(cand)
+    free = np.flatnonzero(~taken)
+    water_sites = np.sort(rng.choice(free, n_waters, replace=False))
+    jitter = 0.12
+    fw, pw, _ = water_box(n_waters, L, seed=seed + 1)
+    # move the waters of water_box onto the free sites (keep their internal geometry)
+    O_old = pw[0::3] / ANG
+    O_new = (sites[water_sites] + 0.5) * spacing + rng.uniform(-jitter, jitter, size=(n_waters, 3))
+    shift = np.repeat(O_new - O_old, 3, axis=0)
+    pos_w = pw / ANG + shift
+    f = fw
+    pos = [pos_w]
+    nw = 3 * n_waters
+    sig = (0.15, 0.08, 0.03)
+    for m, site in enumerate(solutes):
+        centre = (sites[site] + 0.5) * spacing
+        xyz = centre + _ethane(rng)
+        pos.append(xyz)
+        base = nw + 8 * m
+        c1, c2 = base, base + 1
+        hs1, hs2 = [base + 2, base + 3, base + 4], [base + 5, base + 6, base + 7]
+        dip = rng.normal(0.0, sig[0] * ANG, size=(8, 3))
+        quad = traceless_quadrupole(rng, sig[1] * ANG ** 2, 8)
+        octo = traceless_octopole(rng, sig[2] * ANG ** 3, 8)
+        pol = rng.uniform(0.5, 2.0, size=(8, 3)) * ANG ** 3
+        thole = rng.uniform(0.5, 1.0, size=8)  # per atom: pair widths a_i + a_j in U[1, 2]
+        frames = [(c2, hs1[0]), (c1, hs2[0])] + [(c1, c2)] * 3 + [(c2, c1)] * 3
+        charges = [-0.18, -0.18] + [0.06] * 6
+        for a in range(8):
+            z, x = frames[a]
+            f.addMultipole(charges[a], dip[a], quad[a], octo[a], MPIDForce.ZThenX, z, x, -1, thole[a], pol[a])
+        f.setCovalentMap(c1, MPIDForce.Covalent12, [c2] + hs1)
+        f.setCovalentMap(c1, MPIDForce.Covalent13, hs2)
+        f.setCovalentMap(c2, MPIDForce.Covalent12, [c1] + hs2)
+        f.setCovalentMap(c2, MPIDForce.Covalent13, hs1)
+        for hs, own, other, other_h in ((hs1, c1, c2, hs2), (hs2, c2, c1, hs1)):
+            for h in hs:
+                f.setCovalentMap(h, MPIDForce.Covalent12, [own])
+                f.setCovalentMap(h, MPIDForce.Covalent13, [other] + [g for g in hs if g != h])
+                f.setCovalentMap(h, MPIDForce.Covalent14, other_h)
+    f.set14ScaleFactor(0.5)
+    box = np.diag([L * ANG] * 3)
+    return f, np.concatenate(pos) * ANG, box
+
+
 # Benchmark workloads (BASELINE configurations), sizes in the units above.
 WORKLOADS = {
     # 216 waters, 18.64 A, cutoff 8 A, alpha 0.35 /A, 24^3 grid, order 5, mutual 1e-7 D
@@ -104,13 +200,19 @@ WORKLOADS = {
     "water24k": dict(n_waters=8000, box=62.14, cutoff=0.9, alpha=3.4, grid=72, order=5, eps=1e-7),
     # 96,000 waters, 142.0 A, cutoff 9 A, alpha 0.34 /A, 144^3 grid, order 5, mutual 1e-6 D
     "water288k": dict(n_waters=96000, box=142.0, cutoff=0.9, alpha=3.4, grid=144, order=5, eps=1e-6),
+    # 20,000 waters + 200 ethanes (61,600 atoms), 85.3 A, 96^3 grid; cutoff and alpha not
+    # stated by the configuration: 9 A and 0.34 /A; order 5, mutual 1e-7 D
+    "solution61k": dict(n_waters=20000, n_solutes=200, box=85.3, cutoff=0.9, alpha=3.4, grid=96, order=5, eps=1e-7),
 }
 
 
 def workload(name, polarization=MPIDForce.Mutual, order=None, seed=2024, max_iter=200):
     """Configured force, positions (nm) and box (nm) of a named workload."""
     w = WORKLOADS[name]
-    f, pos, box = water_box(w["n_waters"], w["box"], seed=seed)
+    if w.get("n_solutes"):
+        f, pos, box = solution_box(w["n_waters"], w["n_solutes"], w["box"], seed=seed)
+    else:
+        f, pos, box = water_box(w["n_waters"], w["box"], seed=seed)
     f.setNonbondedMethod(MPIDForce.PME)
     f.setCutoffDistance(w["cutoff"])
     f.setPMEParameters(w["alpha"], w["grid"], w["grid"], w["grid"])

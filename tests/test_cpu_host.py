@@ -132,3 +132,23 @@ def test_double_float_residual_arithmetic(tmp_path, alpha, cutoff):
     assert set(errs) == {"erfc_table", "erf_table", "exp_neg", "div", "sqrt"}
     for name, e in errs.items():
         assert e < 1e-13, (name, e)
+
+
+def test_solution_workload_geometry():
+    """61,600-atom solution: 20,000 waters + 200 neutral ethanes, solutes away from waters,
+    anisotropic polarisabilities and 1-4 partners on the solutes."""
+    from scipy.spatial import cKDTree
+    f, pos, box = synthetic.workload("solution61k")
+    n = f.getNumMultipoles()
+    assert n == 61600 and pos.shape == (n, 3)
+    assert abs(sum(f.getMultipoleParameters(i)[0] for i in range(n))) < 1e-9
+    L = box[0, 0]
+    w = pos - L * np.floor(pos / L)
+    pairs = cKDTree(w, boxsize=L).query_pairs(0.2, output_type="ndarray")
+    mol = np.concatenate([np.repeat(np.arange(20000), 3), 20000 + np.repeat(np.arange(200), 8)])
+    inter = pairs[mol[pairs[:, 0]] != mol[pairs[:, 1]]]
+    assert not (inter >= 60000).any()  # no solute atom within 2 A of another molecule
+    p = f.getMultipoleParameters(60000)
+    assert len(set(p[-1])) == 3  # anisotropic
+    assert f.getCovalentMap(60002, MPIDForce.Covalent14)
+    f.validate(n, box)

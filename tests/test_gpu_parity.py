@@ -181,3 +181,57 @@ def test_preconditioned_cg_matches_plain_cg(precision):
     assert abs(ea - eb) / abs(eb) < 1e-7
     assert helpers.rel_rms(fa, fb) < 2e-6
     assert helpers.rel_rms(a.getInducedDipoles(), b.getInducedDipoles()) < 2e-6
+
+
+@pytest.mark.parametrize("pol", [MPIDForce.Direct, MPIDForce.Mutual, MPIDForce.Extrapolated])
+def test_solution61k_gates(pol):
+    """61,600-atom solution (20,000 waters + 200 ethanes with anisotropic polarisabilities,
+    Thole widths U[1, 2], 1-4 scaling 0.5), 96^3 grid: mixed path against the FP64 path
+    for each polarisation type within the accuracy gates (force 5e-6, energy 1e-6,
+    induced dipoles 5e-6)."""
+    f, pos, box = synthetic.workload("solution61k", polarization=pol)
+    cd, ed, fd = run(f, pos, box, "double")
+    cm, em, fm = run(f, pos, box, "mixed")
+    ferr = helpers.rel_rms(fm, fd)
+    eerr = abs(em - ed) / abs(ed)
+    merr = helpers.rel_rms(cm.getInducedDipoles(), cd.getInducedDipoles())
+    print("solution61k pol %d: energy %.3e force %.3e dipole %.3e; iterations %d / %d" %
+          (pol, eerr, ferr, merr, cm.stats()["solver_iterations"], cd.stats()["solver_iterations"]))
+    assert ferr < 5e-6
+    assert eerr < 1e-6
+    assert merr < 5e-6
+
+
+@pytest.mark.parametrize("pol", [MPIDForce.Mutual, MPIDForce.Extrapolated])
+def test_water288k_gates(pol):
+    """288,000-atom water box, 144^3 grid, Mutual to 1e-6 D and OPT extrapolation: mixed
+    path against the FP64 path within the accuracy gates."""
+    f, pos, box = synthetic.workload("water288k", polarization=pol)
+    cd, ed, fd = run(f, pos, box, "double")
+    cm, em, fm = run(f, pos, box, "mixed")
+    ferr = helpers.rel_rms(fm, fd)
+    eerr = abs(em - ed) / abs(ed)
+    merr = helpers.rel_rms(cm.getInducedDipoles(), cd.getInducedDipoles())
+    print("water288k pol %d: energy %.3e force %.3e dipole %.3e; mixed %.1f ms, double %.1f ms" %
+          (pol, eerr, ferr, merr, cm.stats()["ms_total"], cd.stats()["ms_total"]))
+    assert ferr < 5e-6
+    assert eerr < 1e-6
+    assert merr < 5e-6
+
+
+def test_solution61k_double_matches_oracle():
+    """FP64 path against the oracle port (pinned to the reference) on the 61,600-atom
+    solution, mutual polarisation: anisotropic polarisabilities, 1-4 scaling and per-atom
+    Thole widths at full size."""
+    from oracle import oracle as O
+    if not O.available("port"):
+        O.build("port")
+    f, pos, box = synthetic.workload("solution61k", polarization=MPIDForce.Mutual)
+    f.setMutualInducedTargetEpsilon(1e-9)
+    ctx, e, forces = run(f, pos, box, "double")
+    ref = O.evaluate(helpers.oracle_system(f, pos, box), "port")
+    eerr = abs(e - ref.energy) / abs(ref.energy)
+    ferr = helpers.rel_rms(forces, ref.forces)
+    print("solution61k double vs oracle: energy %.3e force %.3e" % (eerr, ferr))
+    assert eerr < 1e-8
+    assert ferr < 1e-7
