@@ -152,3 +152,21 @@ def test_solution_workload_geometry():
     assert len(set(p[-1])) == 3  # anisotropic
     assert f.getCovalentMap(60002, MPIDForce.Covalent14)
     f.validate(n, box)
+
+
+def test_radial_functions_against_long_double(tmp_path):
+    """Ewald radial functions of the pair kernels (radial_check.cpp) against long double:
+    FP64 to 1e-14; FP32 to a few ulp with no systematic bias in the erfc recursion."""
+    import shutil
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    csrc = os.path.join(ROOT, "mpidopenmmplugin_gb300", "csrc")
+    exe = str(tmp_path / "radial_check")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I", csrc, os.path.join(csrc, "radial_check.cpp"), "-o", exe], check=True)
+    out = subprocess.run([exe, "3.4", "0.9"], check=True, capture_output=True, text=True).stdout
+    res = {k: (float(a), float(b)) for k, a, b in (line.split() for line in out.strip().splitlines())}
+    assert res["erf_double"][0] < 1e-14 and res["erfc_double"][0] < 1e-14
+    assert res["erf_float"][0] < 2e-6 and res["erfc_float"][0] < 4e-6
+    assert abs(res["erfc_float"][1]) < 2e-8
+    assert abs(res["erf_float"][1]) < 1e-7
