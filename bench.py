@@ -133,11 +133,14 @@ def count_pairs_within(pos, box, cutoff):
 # FP32 operations per interacting pair (add/mul = 1, FMA = 2, div/sqrt/exp/erfc = 1),
 # counted from the kernels' own source by mpidopenmmplugin_gb300/csrc/flop_count.cpp and
 # averaged over the pair-distance distribution of a 0.9 nm cutoff with alpha = 3.4/nm.
-FLOP_PER_PAIR = {"pair_kernel": 2714,          # k_electrostatics<float, MUTUAL>
-                 "dipole_field_pairs": 148,    # k_dipole_field<float>
-                 "fixed_field_pairs": 464}     # k_fixed_field<float>
+FLOP_PER_PAIR = {"pair_kernel": 2728,          # k_electrostatics<float, MUTUAL>
+                 "dipole_field_pairs": 154,    # k_dipole_field_packed (CG matrix-vector product)
+                 "fixed_field_pairs": 472}     # k_fixed_field<float>
+# DRAM bytes per launch (read + write) from one ncu capture of each kernel on this
+# workload (profiles/k_*_water24k_mutual.md); ncu is not run by this script.
+DRAM_BYTES_PER_LAUNCH = {"pair_kernel": 36.30e6 + 0.18e6, "dipole_field_pairs": 32.85e6}
 KERNEL_NAMES = {"pair_kernel": "k_electrostatics<float, mutual> (energy/force/torque pair kernel)",
-                "dipole_field_pairs": "k_dipole_field<float> (T.mu pair kernel of the CG solver)",
+                "dipole_field_pairs": "k_dipole_field_packed (FP32 T.mu pair kernel of the CG solver)",
                 "fixed_field_pairs": "k_fixed_field<float> (permanent-field pair kernel)"}
 
 
@@ -193,7 +196,7 @@ def cpu_baseline_sample():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -304,7 +307,9 @@ def main():
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
         roofline = {"bound": "fp32", "kernel": KERNEL_NAMES[dom],
                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                    "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
+                    "frac": (achieved / fp32_peak) if achieved else None,
+                    "traffic": DRAM_BYTES_PER_LAUNCH.get(dom),
+                    "traffic_unit": "bytes per launch (ncu capture, profiles/)",
                     "peak_source": "152 SMs x 128 FP32 lanes x 2 x max SM clock (no measured FP32 peak in "
                                    "MEASURED_PEAKS.json)",
                     "pairs_within_cutoff": npairs, "flop_per_pair": FLOP_PER_PAIR[dom],
