@@ -143,6 +143,21 @@ int mpid_evaluate_device_noalloc(mpid_context* ctx, const double* d_positions, c
  * electric field at each atom (e/nm^2, before multiplication by the polarisability). */
 int mpid_get_dipoles(mpid_context* ctx, int which, double* out);
 
+/* System multipole moments at `positions` (CalcMPIDForceKernel::getSystemMultipoleMoments,
+ * mpidKernels.h:86; MPIDReferenceForce.cpp:2349-2462): induced dipoles are solved at these
+ * positions, positions are taken relative to the centre of `masses` (n doubles), and out
+ * receives 13 values: charge (e), dipole x y z (Debye), quadrupole xx xy xz yx yy yz zx zy
+ * zz (Debye-A, traceless, including the atoms' own quadrupoles). */
+int mpid_get_system_multipole_moments(mpid_context* ctx, const double* positions, const double* box,
+                                      const double* masses, double* out);
+
+/* Electrostatic potential (kJ/mol/e) at ngrid points (3 doubles each), with the induced
+ * dipoles solved at `positions` (CalcMPIDForceKernel::getElectrostaticPotential,
+ * mpidKernels.h:83-84; MPIDReferenceForce.cpp:2464-2528): bare Coulomb potential of each
+ * atom's charge, permanent + induced dipole and quadrupole, minimum-imaged under PME. */
+int mpid_get_electrostatic_potential(mpid_context* ctx, const double* positions, const double* box,
+                                     const double* grid, int ngrid, double* out);
+
 /* PME parameters in use (CalcMPIDForceKernel::getPMEParameters, mpidKernels.h:103). */
 int mpid_get_pme_parameters(mpid_context* ctx, double* alpha, int* nx, int* ny, int* nz);
 

@@ -21,7 +21,8 @@ MPID_FLAG_NEAR_FIELD_PCG = 2
 # Entry points declared in include/mpid_gb300.h
 C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multipoles", "mpid_set_covalent",
          "mpid_evaluate", "mpid_evaluate_device", "mpid_evaluate_device_noalloc", "mpid_get_dipoles",
-         "mpid_get_pme_parameters", "mpid_get_stats", "mpid_last_error"]
+         "mpid_get_pme_parameters", "mpid_get_stats", "mpid_last_error", "mpid_get_system_multipole_moments",
+         "mpid_get_electrostatic_potential"]
 
 
 class Settings(ctypes.Structure):
@@ -95,6 +96,8 @@ def load_library(build=True):
     lib.mpid_evaluate_device_noalloc.argtypes = [vp, vp, dp, vp, vp, vp]
     lib.mpid_get_dipoles.argtypes = [vp, ctypes.c_int, dp]
     lib.mpid_get_pme_parameters.argtypes = [vp, dp, ip, ip, ip]
+    lib.mpid_get_system_multipole_moments.argtypes = [vp, dp, dp, dp, dp]
+    lib.mpid_get_electrostatic_potential.argtypes = [vp, dp, dp, dp, ctypes.c_int, dp]
     lib.mpid_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.mpid_last_error.argtypes = []
     lib.mpid_last_error.restype = ctypes.c_char_p
@@ -209,6 +212,25 @@ class MPIDContext:
     def getPermanentField(self):
         """Permanent electric field at each atom (e/nm^2) of the last evaluation."""
         return self._dipoles(3)
+
+    def getSystemMultipoleMoments(self, positions, box, masses):
+        """MPIDForce::getSystemMultipoleMoments (MPIDForce.h:423): 13 values at `positions`."""
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(self.n, 3)
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        m = np.ascontiguousarray(masses, dtype=np.float64).reshape(self.n)
+        out = np.zeros(13)
+        self._check(self.lib.mpid_get_system_multipole_moments(self._h, _dp(pos), _dp(b), _dp(m), _dp(out)))
+        return out
+
+    def getElectrostaticPotential(self, grid, positions, box):
+        """MPIDForce::getElectrostaticPotential (MPIDForce.h:404): potential (kJ/mol/e) at
+        the (k, 3) grid points, with the induced dipoles at `positions`."""
+        g = np.ascontiguousarray(grid, dtype=np.float64).reshape(-1, 3)
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(self.n, 3)
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        out = np.zeros(len(g))
+        self._check(self.lib.mpid_get_electrostatic_potential(self._h, _dp(pos), _dp(b), _dp(g), len(g), _dp(out)))
+        return out
 
     def getPMEParametersInContext(self):
         a = ctypes.c_double()

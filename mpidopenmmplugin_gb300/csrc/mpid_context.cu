@@ -346,6 +346,7 @@ struct Context {
     int nScaled = 0;
     DBuf<double> energyPartial, energyOut;
     DBuf<double> forcesOut;
+    DBuf<double> masses, momentPartial, momentRed, gridPts, gridOut;  // system moments, potential
     // solver scratch
     DBuf<double> partial, red, sc;
     DBuf<int> iter, done;
@@ -1253,6 +1254,72 @@ struct Context {
         return evaluate_device(d_pos, hbox, d_forces, d_energy);
     }
 
+    // Mass-weighted centre, then the 13 system moments of the last evaluation
+    // (MPIDReferenceForce.cpp:2349-2462; Debye and Debye-A units as the reference).
+    void system_moments(const double* hostMasses, double* out13) {
+        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+        cudaStream_t st = stream;
+        masses.alloc(n);
+        CUDA_CHECK(cudaMemcpyAsync(masses.p, hostMasses, n * 8, cudaMemcpyHostToDevice, st));
+        const int nb = nblk(n, 256);
+        momentPartial.alloc((size_t) 16 * nb);
+        momentRed.alloc(16);
+        const int* rk = mixed ? ef->rank.p : ed->rank.p;
+        for (int pass = 0; pass < 2; ++pass) {
+            if (mixed)
+                launch(k_moment_partials<float>, nb, 256, 0, st, n, npad, pass, (const double*) pos.p,
+                       (const double*) masses.p, rk, (const double*) mom64.p, (const float*) ef->mu.p,
+                       (const double*) momentRed.p, momentPartial.p);
+            else
+                launch(k_moment_partials<double>, nb, 256, 0, st, n, npad, pass, (const double*) pos.p,
+                       (const double*) masses.p, rk, (const double*) mom64.p, (const double*) ed->mu.p,
+                       (const double*) momentRed.p, momentPartial.p);
+            launch(k_reduce_partials, 1, 1024, 0, st, nb, pass == 0 ? 4 : 16, (const double*) momentPartial.p,
+                   momentRed.p, (const int*) nullptr);
+        }
+        double v[16];
+        CUDA_CHECK(cudaMemcpyAsync(v, momentRed.p, 16 * 8, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        const double debye = 4.80321;
+        const double qave = (v[4] + v[7] + v[9]) / 3.0;
+        double m[13];
+        m[0] = v[0];
+        for (int k = 0; k < 3; ++k) m[1 + k] = v[1 + k] * 10.0 * debye;
+        m[4] = 0.5 * (v[4] - qave) + v[10];
+        m[5] = 0.5 * v[5] + v[11];
+        m[6] = 0.5 * v[6] + v[12];
+        m[8] = 0.5 * (v[7] - qave) + v[13];
+        m[9] = 0.5 * v[8] + v[14];
+        m[12] = 0.5 * (v[9] - qave) + v[15];
+        m[7] = m[5];
+        m[10] = m[6];
+        m[11] = m[9];
+        for (int k = 4; k < 13; ++k) m[k] *= 100.0 * 3.0 * debye;
+        std::memcpy(out13, m, sizeof(m));
+    }
+
+    // Potential (kJ/mol/e) of the last evaluation's multipoles and induced dipoles at
+    // ngrid points (MPIDReferenceForce.cpp:2464-2528).
+    void electrostatic_potential(const double* hostGrid, int ngrid, double* out) {
+        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+        if (ngrid < 0) throw Error(MPID_ERR_INVALID, "negative number of grid points");
+        if (ngrid == 0) return;
+        cudaStream_t st = stream;
+        gridPts.alloc(3 * (size_t) ngrid);
+        gridOut.alloc(ngrid);
+        CUDA_CHECK(cudaMemcpyAsync(gridPts.p, hostGrid, 3 * (size_t) ngrid * 8, cudaMemcpyHostToDevice, st));
+        if (mixed)
+            launch(k_potential_grid<float>, nblk(ngrid, 128), 128, 0, st, n, npad, ngrid, (const double*) gridPts.p,
+                   (const double*) wpos.p, (const int*) ef->rank.p, (const double*) mom64.p, (const float*) ef->mu.p, box,
+                   usePme ? 1 : 0, gridOut.p);
+        else
+            launch(k_potential_grid<double>, nblk(ngrid, 128), 128, 0, st, n, npad, ngrid, (const double*) gridPts.p,
+                   (const double*) wpos.p, (const int*) ed->rank.p, (const double*) mom64.p, (const double*) ed->mu.p,
+                   box, usePme ? 1 : 0, gridOut.p);
+        CUDA_CHECK(cudaMemcpyAsync(out, gridOut.p, (size_t) ngrid * 8, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+    }
+
     void get_dipoles(int which, double* host) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
         if (which < 0 || which > 3) throw Error(MPID_ERR_INVALID, "which must be 0, 1, 2 or 3");
@@ -1401,6 +1468,36 @@ int mpid_evaluate_device_noalloc(mpid_context* ctx, const double* d_positions, c
     void* scratch = noalloc_scratch(ctx->ctx.device);
     ctx->ctx.stream = (cudaStream_t) stream;
     ctx->ctx.evaluate_device_noalloc(d_positions, box, d_forces, d_energy, scratch);
+    return MPID_OK;
+    MPID_API_END
+}
+
+// Evaluation at host positions into an internal force buffer (the properties below are
+// defined at the positions given, as the reference recomputes the induced dipoles).
+static void evaluate_at(Context& c, const double* positions, const double* box) {
+    CUDA_CHECK(cudaSetDevice(c.device));
+    const size_t n3 = 3 * (size_t) c.n;
+    CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions, n3 * 8, cudaMemcpyHostToDevice, c.stream));
+    CUDA_CHECK(cudaMemsetAsync(c.forcesOut.p, 0, n3 * 8, c.stream));
+    c.evaluate_device(c.pos.p, box, c.forcesOut.p, nullptr);
+}
+
+int mpid_get_system_multipole_moments(mpid_context* ctx, const double* positions, const double* box,
+                                      const double* masses, double* out) {
+    MPID_API_BEGIN
+    if (!ctx || !positions || !box || !masses || !out) throw Error(MPID_ERR_INVALID, "null argument");
+    evaluate_at(ctx->ctx, positions, box);
+    ctx->ctx.system_moments(masses, out);
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_get_electrostatic_potential(mpid_context* ctx, const double* positions, const double* box,
+                                     const double* grid, int ngrid, double* out) {
+    MPID_API_BEGIN
+    if (!ctx || !positions || !box || (ngrid > 0 && (!grid || !out))) throw Error(MPID_ERR_INVALID, "null argument");
+    evaluate_at(ctx->ctx, positions, box);
+    ctx->ctx.electrostatic_potential(grid, ngrid, out);
     return MPID_OK;
     MPID_API_END
 }

@@ -979,6 +979,90 @@ __global__ void k_scaled_pair_energy(int npairs, const int2* __restrict__ pr, co
 }
 
 // ---------------------------------------------------------------------------
+// getElectrostaticPotential (MPIDReferenceForce.cpp:2464-2528): at each grid point the
+// bare Coulomb potential of every atom's charge, permanent + induced dipole and
+// quadrupole (octopoles are not included there), minimum-imaged under PME, times the
+// electric constant.  FP64; one thread per grid point, all threads reading the same atom
+// at the same time.
+template <typename real>
+__global__ void k_potential_grid(int n, int npad, int ngrid, const double* __restrict__ grid,
+                                 const double* __restrict__ wpos, const int* __restrict__ rank,
+                                 const double* __restrict__ mom64, const real* __restrict__ mu, BoxDev box, int usePbc,
+                                 double* __restrict__ out) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngrid) return;
+    const double gx = grid[3 * g], gy = grid[3 * g + 1], gz = grid[3 * g + 2];
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const int s = rank[i];
+        double d[3] = {wpos[3 * i] - gx, wpos[3 * i + 1] - gy, wpos[3 * i + 2] - gz};
+        if (usePbc)
+            for (int k = 0; k < 3; ++k) d[k] -= box.L[k] * rint(d[k] * box.invL[k]);
+        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const double rr1 = 1.0 / sqrt(r2), rr2 = rr1 * rr1, rr3 = rr1 * rr2;
+        const double q = mom64[s];
+        double sd = 0.0;
+        for (int k = 0; k < 3; ++k) sd += (mom64[(1 + k) * npad + s] + (double) mu[k * npad + s]) * d[k];
+        // Q6 order XX XY XZ YY YZ ZZ
+        const double* Q = mom64 + 4 * (size_t) npad + s;
+        const double qxx = Q[0], qxy = Q[npad], qxz = Q[2 * npad], qyy = Q[3 * npad], qyz = Q[4 * npad],
+                     qzz = Q[5 * npad];
+        const double sq = d[0] * (qxx * d[0] + qxy * d[1] + qxz * d[2]) + d[1] * (qxy * d[0] + qyy * d[1] + qyz * d[2]) +
+                          d[2] * (qxz * d[0] + qyz * d[1] + qzz * d[2]);
+        acc += q * rr1 - sd * rr3 + sq * 3.0 * rr3 * rr2;
+    }
+    out[g] = acc * kElectric;
+}
+
+// getSystemMultipoleMoments (MPIDReferenceForce.cpp:2349-2462), per-block partials:
+// pass 0 sums (m, m x, m y, m z); pass 1 (after the centre of mass is known from
+// com = red[1..3] / red[0]) sums charge, dipole (3), traced second moment (6: xx xy xz yy
+// yz zz) and the atoms' lab quadrupoles (6).
+template <typename real>
+__global__ void __launch_bounds__(256)
+k_moment_partials(int n, int npad, int pass, const double* __restrict__ pos, const double* __restrict__ masses,
+                  const int* __restrict__ rank, const double* __restrict__ mom64, const real* __restrict__ mu,
+                  const double* __restrict__ red, double* __restrict__ partial) {
+    constexpr int NV = 16;
+    __shared__ double sh[NV][256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[NV];
+    for (int k = 0; k < NV; ++k) v[k] = 0.0;
+    if (i < n) {
+        if (pass == 0) {
+            const double m = masses[i];
+            v[0] = m;
+            for (int k = 0; k < 3; ++k) v[1 + k] = m * pos[3 * i + k];
+        } else {
+            const double tm = red[0];
+            double x[3];
+            for (int k = 0; k < 3; ++k) x[k] = pos[3 * i + k] - (tm > 0.0 ? red[1 + k] / tm : 0.0);
+            const int s = rank[i];
+            const double q = mom64[s];
+            double dn[3];
+            for (int k = 0; k < 3; ++k) dn[k] = mom64[(1 + k) * npad + s] + (double) mu[k * npad + s];
+            v[0] = q;
+            for (int k = 0; k < 3; ++k) v[1 + k] = x[k] * q + dn[k];
+            v[4] = x[0] * x[0] * q + 2.0 * x[0] * dn[0];
+            v[5] = x[0] * x[1] * q + x[0] * dn[1] + x[1] * dn[0];
+            v[6] = x[0] * x[2] * q + x[0] * dn[2] + x[2] * dn[0];
+            v[7] = x[1] * x[1] * q + 2.0 * x[1] * dn[1];
+            v[8] = x[1] * x[2] * q + x[1] * dn[2] + x[2] * dn[1];
+            v[9] = x[2] * x[2] * q + 2.0 * x[2] * dn[2];
+            for (int k = 0; k < 6; ++k) v[10 + k] = mom64[(4 + k) * npad + s];
+        }
+    }
+    for (int k = 0; k < NV; ++k) sh[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int k = 0; k < NV; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x < NV) partial[threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x][0];
+}
+
+// ---------------------------------------------------------------------------
 // PME.  B-spline coefficients and weighted fractional multipoles per sorted atom.
 // theta layout: [3 dims][5 derivs][ORDER][npad]; igrid [3][npad].
 template <typename real, int ORDER>

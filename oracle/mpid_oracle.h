@@ -61,6 +61,8 @@ typedef struct {
 } mpid_oracle_output;
 
 int mpidref_evaluate(const mpid_oracle_input* in, mpid_oracle_output* out);
+int mpidref_properties(const mpid_oracle_input* in, const double* masses, const double* grid, int ngrid,
+                       double* moments, double* potential, char* message);
 int mpidport_evaluate(const mpid_oracle_input* in, mpid_oracle_output* out);
 
 #ifdef __cplusplus

@@ -155,7 +155,8 @@ def _lib(which):
     return _LIBS[which]
 
 
-def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False) -> OracleResult:
+def _input(sys_: OracleSystem):
+    """Flat _In structure for sys_ and the arrays it points into (kept alive together)."""
     n = sys_.n
     pos = np.ascontiguousarray(sys_.pos, dtype=np.float64).reshape(-1)
     arrs = dict(
@@ -208,6 +209,12 @@ def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False) -> OracleRe
     inp.extrap_coeffs = _dp(coeffs)
     inp.default_thole = float(sys_.default_thole)
     inp.scale14 = float(sys_.scale14)
+    return inp, (pos, arrs, iarrs, offs, idx, coeffs, box)
+
+
+def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False) -> OracleResult:
+    n = sys_.n
+    inp, keep = _input(sys_)
     forces = np.zeros(3 * n)
     induced = np.zeros(3 * n)
     lab = np.zeros(3 * n) if want_labdipoles else None
@@ -221,6 +228,28 @@ def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False) -> OracleRe
     return OracleResult(energy=out.energy, forces=forces.reshape(n, 3), induced=induced.reshape(n, 3),
                         labdipoles=None if lab is None else lab.reshape(n, 3), iterations=out.iterations,
                         epsilon=out.epsilon, converged=bool(out.converged))
+
+
+def properties(sys_: OracleSystem, masses, grid):
+    """The reference's getSystemMultipoleMoments (13 values) and getElectrostaticPotential
+    at the (k, 3) grid points (MPIDReferenceKernels.cpp:302-341); reference build only."""
+    inp, keep = _input(sys_)
+    lib = ctypes.CDLL(REF_LIB) if os.path.exists(REF_LIB) else None
+    if lib is None:
+        raise OracleError("oracle library %s is not built (make -C oracle ref)" % REF_LIB)
+    fn = lib.mpidref_properties
+    fn.argtypes = [ctypes.POINTER(_In), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_char_p]
+    fn.restype = ctypes.c_int
+    m = np.ascontiguousarray(masses, dtype=np.float64)
+    g = np.ascontiguousarray(grid, dtype=np.float64).reshape(-1, 3)
+    moments = np.zeros(13)
+    potential = np.zeros(len(g))
+    msg = ctypes.create_string_buffer(512)
+    rc = fn(ctypes.byref(inp), _dp(m), _dp(g), len(g), _dp(moments), _dp(potential), msg)
+    if rc != 0:
+        raise OracleError(msg.value.decode(errors="replace"))
+    return moments, potential
 
 
 def system_from_golden(golden: dict, test: dict) -> OracleSystem:

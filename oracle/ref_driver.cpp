@@ -51,7 +51,88 @@ void configure(MPIDReferenceForce* f, const mpid_oracle_input* in) {
     f->set14ScaleFactor(in->scale14);
 }
 
+// The flat oracle input unpacked into the reference's argument vectors.
+struct Unpacked {
+    int n;
+    std::vector<Vec3> pos;
+    std::vector<double> charges, dipoles, quads, octs, tholes, damp;
+    std::vector<std::vector<double> > polarity;
+    std::vector<int> axis, az, ax, ay;
+    std::vector<std::vector<std::vector<int> > > cov;
+    explicit Unpacked(const mpid_oracle_input* in) : n(in->n) {
+        pos.resize(n);
+        charges.resize(n); dipoles.resize(3 * n); quads.resize(6 * n); octs.resize(10 * n); tholes.resize(n);
+        damp.resize(n); polarity.resize(n); axis.resize(n); az.resize(n); ax.resize(n); ay.resize(n); cov.resize(n);
+        for (int i = 0; i < n; ++i) {
+            pos[i] = Vec3(in->pos[3 * i], in->pos[3 * i + 1], in->pos[3 * i + 2]);
+            charges[i] = in->charge[i];
+            for (int k = 0; k < 3; ++k) dipoles[3 * i + k] = in->dipole[3 * i + k];
+            for (int k = 0; k < 6; ++k) quads[6 * i + k] = in->quadrupole[6 * i + k];
+            for (int k = 0; k < 10; ++k) octs[10 * i + k] = in->octopole[10 * i + k];
+            tholes[i] = in->thole[i];
+            polarity[i] = std::vector<double>(in->polarity + 3 * i, in->polarity + 3 * i + 3);
+            damp[i] = pow((polarity[i][0] + polarity[i][1] + polarity[i][2]) / 3.0, 1.0 / 6.0);
+            axis[i] = in->axis_type[i];
+            az[i] = in->atom_z[i];
+            ax[i] = in->atom_x[i];
+            ay[i] = in->atom_y[i];
+            cov[i].resize(8);
+            for (int t = 0; t < 8; ++t)
+                for (int k = in->cov_offsets[8 * i + t]; k < in->cov_offsets[8 * i + t + 1]; ++k)
+                    cov[i][t].push_back(in->cov_index[k]);
+        }
+    }
+};
+
+// PME or no-cutoff reference force configured as setupMPIDReferenceForce does.
+MPIDReferenceForce* make_force(const mpid_oracle_input* in) {
+    MPIDReferenceForce* base = nullptr;
+    if (in->nonbonded_method == 1) {
+        TappedPme* pme = new TappedPme();
+        pme->setAlphaEwald(in->ewald_alpha);
+        pme->setCutoffDistance(in->cutoff);
+        std::vector<int> grid(in->grid, in->grid + 3);
+        pme->setPmeGridDimensions(grid);
+        Vec3 box[3] = {Vec3(in->box[0], in->box[1], in->box[2]), Vec3(in->box[3], in->box[4], in->box[5]),
+                       Vec3(in->box[6], in->box[7], in->box[8])};
+        pme->setPeriodicBoxSize(box);
+        base = pme;
+    } else {
+        base = new TappedNoCut();
+    }
+    configure(base, in);
+    return base;
+}
+
 }  // namespace
+
+/* getSystemMultipoleMoments and getElectrostaticPotential of the reference kernel
+ * (MPIDReferenceKernels.cpp:302-341): 13 moments for the given masses, and the potential
+ * (kJ/mol/e) at ngrid points (3 doubles each). */
+extern "C" int mpidref_properties(const mpid_oracle_input* in, const double* masses, const double* grid, int ngrid,
+                                  double* moments, double* potential, char* message) {
+    message[0] = 0;
+    try {
+        Unpacked u(in);
+        std::vector<double> m(masses, masses + in->n);
+        std::vector<double> mom;
+        MPIDReferenceForce* f = make_force(in);
+        f->calculateMPIDSystemMultipoleMoments(m, u.pos, u.charges, u.dipoles, u.quads, u.octs, u.tholes, u.damp,
+                                               u.polarity, u.axis, u.az, u.ax, u.ay, u.cov, mom);
+        for (int k = 0; k < 13; ++k) moments[k] = mom[k];
+        std::vector<Vec3> g(ngrid);
+        for (int k = 0; k < ngrid; ++k) g[k] = Vec3(grid[3 * k], grid[3 * k + 1], grid[3 * k + 2]);
+        std::vector<double> pot;
+        f->calculateElectrostaticPotential(u.pos, u.charges, u.dipoles, u.quads, u.octs, u.tholes, u.damp, u.polarity,
+                                           u.axis, u.az, u.ax, u.ay, u.cov, g, pot);
+        for (int k = 0; k < ngrid; ++k) potential[k] = pot[k];
+        delete f;
+        return 0;
+    } catch (const std::exception& e) {
+        snprintf(message, 512, "%s", e.what());
+        return 1;
+    }
+}
 
 extern "C" int mpidref_evaluate(const mpid_oracle_input* in, mpid_oracle_output* out) {
     out->message[0] = 0;

@@ -10,7 +10,11 @@ oracle/Makefile) on seeded synthetic systems and stores inputs and outputs as .n
   cycle through ZBisect, ThreeFold, Bisector, ZOnly and ZThenX frames with a chiral Y
   atom, anisotropic polarisabilities, 1-4 partners with scale 0.5, in a 2.2 nm box.
 
-Usage:  python tests/golden/make_fixtures.py   (needs the reference tree)
+* properties_{water648_pme,frames_pme,frames_nocutoff}.npz -- the reference's
+  getSystemMultipoleMoments and getElectrostaticPotential (64 seeded points) with
+  seeded masses.
+
+Usage:  python tests/golden/make_fixtures.py [properties]   (needs the reference tree)
 """
 import os
 import sys
@@ -75,7 +79,7 @@ def frames_system(seed=7):
     return f, np.array(pos), np.diag([L, L, L])
 
 
-def save(name, s, res):
+def save(name, s, res, **extra):
     n = s.n
     offs = [0]
     idx = []
@@ -93,7 +97,7 @@ def save(name, s, res):
         pme_order=s.pme_order, mutual_eps=s.mutual_eps, max_iter=s.max_iter,
         extrap_coeffs=np.array(s.extrap_coeffs), default_thole=s.default_thole, scale14=s.scale14,
         ref_energy=res.energy, ref_forces=res.forces, ref_induced=res.induced, ref_labdipoles=res.labdipoles,
-        ref_iterations=res.iterations)
+        ref_iterations=res.iterations, **extra)
     print("wrote", name, "E =", res.energy, "iterations", res.iterations)
 
 
@@ -112,5 +116,32 @@ def main():
         save("frames_%s.npz" % POL[pol], s, O.evaluate(s, "ref", want_labdipoles=True))
 
 
+def make_properties():
+    """properties_*.npz: the reference's getSystemMultipoleMoments and
+    getElectrostaticPotential (at 64 seeded points in the box) for the water box (PME)
+    and the frames system (PME and no cutoff), with seeded masses."""
+    O.build("ref")
+    rng = np.random.default_rng(11)
+    cases = []
+    f, pos, box = synthetic.workload("water648", polarization=0, order=6)
+    cases.append(("water648_pme", f, pos, box, np.tile([15.999, 1.008, 1.008], f.getNumMultipoles() // 3)))
+    for method, tag in ((1, "pme"), (0, "nocutoff")):
+        f, pos, box = frames_system()
+        f.setNonbondedMethod(method)
+        f.setPolarizationType(0)
+        f.setMutualInducedMaxIterations(200)
+        cases.append(("frames_" + tag, f, pos, box, rng.uniform(1.0, 16.0, size=f.getNumMultipoles())))
+    for name, f, pos, box, masses in cases:
+        f.setMutualInducedTargetEpsilon(1e-9)
+        s = helpers.oracle_system(f, pos, box, pme_order=6)
+        grid = rng.uniform(0.0, 1.0, size=(64, 3)) * np.diag(box)
+        moments, potential = O.properties(s, masses, grid)
+        save("properties_%s.npz" % name, s, O.evaluate(s, "ref", want_labdipoles=True), masses=masses, grid_points=grid,
+             ref_moments=moments, ref_potential=potential)
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "properties":
+        make_properties()
+    else:
+        main()
