@@ -2,9 +2,11 @@
 
 `MPIDForce` mirrors the reference's force class (parameters, covalent maps, PME and
 solver settings); `MPIDContext` evaluates it on one GPU through the C ABI of
-libmpid_gb300.so (include/mpid_gb300.h).
+libmpid_gb300.so (include/mpid_gb300.h); `serialization` reads and writes the
+reference's XML format.
 """
 from .force import MPIDError, MPIDForce
 from .context import MPIDContext, load_library, library_path
+from . import serialization
 
-__all__ = ["MPIDForce", "MPIDContext", "MPIDError", "load_library", "library_path"]
+__all__ = ["MPIDForce", "MPIDContext", "MPIDError", "load_library", "library_path", "serialization"]

@@ -62,8 +62,17 @@ class MPIDForce:
         self._scale14 = 1.0
         self._extrap = [-0.154, 0.017, 0.658, 0.474]
         self._multipoles: List[_Multipole] = []
+        self.forceGroup = 0
 
     # ---- force-wide settings
+    def getForceGroup(self):
+        return self.forceGroup
+
+    def setForceGroup(self, group):
+        if not 0 <= int(group) <= 31:
+            raise MPIDError("Force group must be between 0 and 31")
+        self.forceGroup = int(group)
+
     def getNumMultipoles(self):
         return len(self._multipoles)
 
