@@ -58,6 +58,8 @@ typedef struct {
     double epsilon;             /* final Debye RMS residual (Mutual) */
     int converged;
     char message[512];
+    double* grad;               /* 20n or NULL (port only): dE/d(molecular-frame charge, dipole X Y Z,
+                                   quadrupole XX XY YY XZ YZ ZZ, octopole XXX ... ZZZ) per atom */
 } mpid_oracle_output;
 
 int mpidref_evaluate(const mpid_oracle_input* in, mpid_oracle_output* out);

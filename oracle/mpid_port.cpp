@@ -766,6 +766,7 @@ struct Port {
     // energy, force and torques in a pair-axis frame) ---
     struct PairOut {
         double e, fJ[3], tI[3], tJ[3];
+        double gI[20], gJ[20];  // dE/dM per unique lab component (weighted), both atoms
     };
     static double full(const double* M, const int* idx, int m) { return M[comp_of_indices(idx, m)]; }
     // torque -sum_m m (M^(m) x_1 X^(m)) from unique-comp tensors M and X
@@ -855,6 +856,11 @@ struct Port {
         }
         o.e = Upp + 0.5 * Upi;
         for (int k = 0; k < 3; ++k) o.fJ[k] = F[k];
+        // at stationary induced dipoles dE/dM = d(Upp + Upi)/dM at fixed dipoles
+        for (int a = 0; a < 20; ++a) {
+            o.gI[a] = COMPS[a].w * XI[a];
+            o.gJ[a] = COMPS[a].w * YJ[a];
+        }
         torque_of(MI, XI, o.tI);
         torque_of(MJ, YJ, o.tJ);
         double ti[3], tj[3];
@@ -983,6 +989,106 @@ struct Port {
         }
     }
 
+    // Gradient of the Ewald self energy (MPIDReferenceForce.cpp:4283-4318) with respect to
+    // the unique lab components of atom i, added to g (fixed induced dipole mu).
+    void self_gradient(int i, const double* mu, double* g) const {
+        const Atom& a = at[i];
+        const double al = in->ewald_alpha, a2 = al * al;
+        const double pre = -al * ELECTRIC / SQRT_PI_REF;
+        const double s3 = std::sqrt(3.0);
+        g[0] += pre * 2 * a.q;
+        // the d.mu term is half the permanent-induced self interaction: at stationary
+        // dipoles the whole interaction enters the derivative
+        for (int k = 0; k < 3; ++k) g[1 + k] += pre * 2.0 / 3.0 * a2 * (2 * a.d[k] + 2 * mu[k]);
+        const double cq = pre * 4.0 / 15.0 * a2 * a2, co = pre * 8.0 / 105.0 * a2 * a2 * a2;
+        const double* S = a.sph;
+        // unique comps 4 xx, 5 xy, 6 xz, 7 yy, 8 yz, 9 zz
+        g[4] += cq * 2 * S[7] * s3;
+        g[7] -= cq * 2 * S[7] * s3;
+        g[9] += cq * 2 * S[4] * 3;
+        g[6] += cq * 2 * S[5] * 2 * s3;
+        g[8] += cq * 2 * S[6] * 2 * s3;
+        g[5] += cq * 2 * S[8] * 2 * s3;
+        // unique comps 10 xxx 11 xxy 12 xxz 13 xyy 14 xyz 15 xzz 16 yyy 17 yyz 18 yzz 19 zzz
+        const double r15 = std::sqrt(1.5), r06 = std::sqrt(0.6), r01 = std::sqrt(0.1);
+        g[19] += co * 2 * S[9] * 15;
+        g[15] += co * 2 * S[10] * 15 * r15;
+        g[18] += co * 2 * S[11] * 15 * r15;
+        g[12] += co * 2 * S[12] * 15 * r06;
+        g[17] -= co * 2 * S[12] * 15 * r06;
+        g[14] += co * 2 * S[13] * 30 * r06;
+        g[10] += co * 2 * S[14] * 15 * r01;
+        g[13] -= co * 2 * S[14] * 45 * r01;
+        g[11] += co * 2 * S[15] * 45 * r01;
+        g[16] -= co * 2 * S[15] * 15 * r01;
+    }
+
+    // Unique-lab-component gradient -> molecular-frame API parameters of atom i
+    // (charge, dipole X Y Z, quadrupole XX XY YY XZ YZ ZZ, octopole XXX XXY XYY YYY XXZ
+    // XYZ YYZ XZZ YZZ ZZZ), through the frame rotation and the chirality flip.
+    void local_gradient(int i, const double* g, double* out) const {
+        double R[3][3];
+        frame(i, R);
+        const bool flip = chiral(i);
+        // full-entry lab derivatives
+        double Gd[3], GQ[3][3], GO[3][3][3];
+        for (int x = 0; x < 3; ++x) Gd[x] = g[1 + x];
+        for (int x = 0; x < 3; ++x)
+            for (int y = 0; y < 3; ++y) {
+                int idx[2] = {x, y};
+                int c = comp_of_indices(idx, 2);
+                GQ[x][y] = g[c] / COMPS[c].w;
+                for (int z = 0; z < 3; ++z) {
+                    int idx3[3] = {x, y, z};
+                    int c3 = comp_of_indices(idx3, 3);
+                    GO[x][y][z] = g[c3] / COMPS[c3].w;
+                }
+            }
+        // rotate to the molecular frame: lab = R^T local R
+        double Ld[3], LQ[3][3], LO[3][3][3];
+        for (int k = 0; k < 3; ++k) {
+            Ld[k] = 0;
+            for (int x = 0; x < 3; ++x) Ld[k] += R[k][x] * Gd[x];
+        }
+        for (int k = 0; k < 3; ++k)
+            for (int m = 0; m < 3; ++m) {
+                double s = 0;
+                for (int x = 0; x < 3; ++x)
+                    for (int y = 0; y < 3; ++y) s += R[k][x] * R[m][y] * GQ[x][y];
+                LQ[k][m] = s;
+            }
+        for (int k = 0; k < 3; ++k)
+            for (int l = 0; l < 3; ++l)
+                for (int m = 0; m < 3; ++m) {
+                    double s = 0;
+                    for (int x = 0; x < 3; ++x)
+                        for (int y = 0; y < 3; ++y)
+                            for (int z = 0; z < 3; ++z) s += R[k][x] * R[l][y] * R[m][z] * GO[x][y][z];
+                    LO[k][l][m] = s;
+                }
+        static const int QAPI[6][2] = {{0, 0}, {0, 1}, {1, 1}, {0, 2}, {1, 2}, {2, 2}};
+        static const int OAPI[10][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {1, 1, 1}, {0, 0, 2},
+                                        {0, 1, 2}, {1, 1, 2}, {0, 2, 2}, {1, 2, 2}, {2, 2, 2}};
+        out[0] = g[0];
+        for (int k = 0; k < 3; ++k) out[1 + k] = Ld[k];
+        for (int c = 0; c < 6; ++c) {
+            const int k = QAPI[c][0], m = QAPI[c][1];
+            out[4 + c] = (k == m) ? LQ[k][m] : LQ[k][m] + LQ[m][k];
+        }
+        for (int c = 0; c < 10; ++c) {
+            int idx[3] = {OAPI[c][0], OAPI[c][1], OAPI[c][2]};
+            std::sort(idx, idx + 3);
+            double s = 0;
+            do { s += LO[idx[0]][idx[1]][idx[2]]; } while (std::next_permutation(idx, idx + 3));
+            out[10 + c] = s;
+        }
+        if (flip) {  // the flipped parameters enter with the opposite sign
+            out[2] = -out[2];
+            out[4 + 1] = -out[4 + 1];
+            out[4 + 4] = -out[4 + 4];
+        }
+    }
+
     int run(mpid_oracle_output* out) {
         n = in->n;
         pme = in->nonbonded_method == 1;
@@ -1081,6 +1187,10 @@ struct Port {
         std::vector<std::vector<std::array<double, 6>>> part(nthreads, std::vector<std::array<double, 6>>(n));
         for (auto& pt : part) for (auto& v : pt) v.fill(0.0);
         std::vector<double> epart(nthreads, 0.0);
+        const bool wantGrad = out->grad != nullptr;
+        std::vector<std::vector<std::array<double, 20>>> gpart(wantGrad ? nthreads : 0,
+                                                               std::vector<std::array<double, 20>>(n));
+        for (auto& pt : gpart) for (auto& v : pt) v.fill(0.0);
 #pragma omp parallel for schedule(dynamic, 128)
         for (long p = 0; p < (long) pairs.size(); ++p) {
             int tid = omp_get_thread_num();
@@ -1097,7 +1207,17 @@ struct Port {
                 part[tid][i][3 + k] += ELECTRIC * o.tI[k];
                 part[tid][j][3 + k] += ELECTRIC * o.tJ[k];
             }
+            if (wantGrad)
+                for (int c = 0; c < 20; ++c) {
+                    gpart[tid][i][c] += ELECTRIC * o.gI[c];
+                    gpart[tid][j][c] += ELECTRIC * o.gJ[c];
+                }
         }
+        std::vector<std::array<double, 20>> G(wantGrad ? n : 0);
+        for (auto& g : G) g.fill(0.0);
+        for (int t = 0; t < (int) gpart.size(); ++t)
+            for (int i = 0; i < n; ++i)
+                for (int c = 0; c < 20; ++c) G[i][c] += gpart[t][i][c];
         for (int t = 0; t < nthreads; ++t) {
             energy += epart[t];
             for (int i = 0; i < n; ++i)
@@ -1161,6 +1281,8 @@ struct Port {
                         }
                         X[c] = acc;
                     }
+                    if (wantGrad)
+                        for (int c = 0; c < 20; ++c) G[i][c] += ELECTRIC * COMPS[c].w * X[c];
                     double M[20];
                     std::memcpy(M, a.M, sizeof(M));
                     bool addInd = which == 0 ? a.aniso : (a.aniso && pol == 0);
@@ -1170,6 +1292,7 @@ struct Port {
                     torque_of(M, X, tau);
                     for (int k = 0; k < 3; ++k) T[i][k] += ELECTRIC * tau[k];
                 }
+                if (wantGrad) self_gradient(i, mu[i].data(), G[i].data());
                 cii += a.q * a.q;
                 for (int k = 0; k < 3; ++k) dii += a.d[k] * (a.d[k] + mu[i][k]);
                 for (int k = 4; k < 9; ++k) qii += a.sph[k] * a.sph[k];
@@ -1199,6 +1322,8 @@ struct Port {
                     }
         }
         for (int i = 0; i < n; ++i) torque_to_force(i, T[i].data(), F);
+        if (wantGrad)
+            for (int i = 0; i < n; ++i) local_gradient(i, G[i].data(), out->grad + 20 * i);
         out->energy = energy;
         for (int i = 0; i < n; ++i)
             for (int k = 0; k < 3; ++k) {

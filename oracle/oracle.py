@@ -64,6 +64,7 @@ class OracleResult:
     iterations: int
     epsilon: float
     converged: bool
+    grad: Optional[np.ndarray] = None  # (n, 20) molecular-frame parameter gradients (port)
 
 
 class _In(ctypes.Structure):
@@ -108,6 +109,7 @@ class _Out(ctypes.Structure):
         ("epsilon", ctypes.c_double),
         ("converged", ctypes.c_int),
         ("message", ctypes.c_char * 512),
+        ("grad", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -212,7 +214,7 @@ def _input(sys_: OracleSystem):
     return inp, (pos, arrs, iarrs, offs, idx, coeffs, box)
 
 
-def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False) -> OracleResult:
+def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False, want_grad=False) -> OracleResult:
     n = sys_.n
     inp, keep = _input(sys_)
     forces = np.zeros(3 * n)
@@ -222,12 +224,21 @@ def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False) -> OracleRe
     out.forces = _dp(forces)
     out.induced = _dp(induced)
     out.labdipoles = _dp(lab) if lab is not None else None
+    grad = None
+    if want_grad:
+        if which != "port":
+            raise OracleError("parameter gradients come from the port")
+        grad = np.zeros(20 * n)
+        out.grad = _dp(grad)
+    else:
+        out.grad = None
     rc = _lib(which)(ctypes.byref(inp), ctypes.byref(out))
     if rc != 0:
         raise OracleError(out.message.decode(errors="replace"))
     return OracleResult(energy=out.energy, forces=forces.reshape(n, 3), induced=induced.reshape(n, 3),
                         labdipoles=None if lab is None else lab.reshape(n, 3), iterations=out.iterations,
-                        epsilon=out.epsilon, converged=bool(out.converged))
+                        epsilon=out.epsilon, converged=bool(out.converged),
+                        grad=None if grad is None else grad.reshape(n, 20))
 
 
 def properties(sys_: OracleSystem, masses, grid):
