@@ -158,6 +158,15 @@ int mpid_get_system_multipole_moments(mpid_context* ctx, const double* positions
 int mpid_get_electrostatic_potential(mpid_context* ctx, const double* positions, const double* box,
                                      const double* grid, int ngrid, double* out);
 
+/* Gradient of the energy at `positions` with respect to every atom's molecular-frame
+ * multipole parameters, 20 doubles per atom in caller order: charge, dipole X Y Z,
+ * quadrupole XX XY YY XZ YZ ZZ, octopole XXX XXY XYY YYY XXZ XYZ YYZ XZZ YZZ ZZZ (the
+ * component orders of MPIDForce::addMultipole), kJ/mol per parameter unit.  Each
+ * component is the partial derivative with the other components held fixed.  No
+ * reference counterpart: the reference has no parameter derivatives.  Uses the
+ * stationarity of the induced dipoles, so no extra linear solve is needed. */
+int mpid_get_parameter_gradients(mpid_context* ctx, const double* positions, const double* box, double* out);
+
 /* PME parameters in use (CalcMPIDForceKernel::getPMEParameters, mpidKernels.h:103). */
 int mpid_get_pme_parameters(mpid_context* ctx, double* alpha, int* nx, int* ny, int* nz);
 

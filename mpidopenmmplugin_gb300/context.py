@@ -22,7 +22,7 @@ MPID_FLAG_NEAR_FIELD_PCG = 2
 C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multipoles", "mpid_set_covalent",
          "mpid_evaluate", "mpid_evaluate_device", "mpid_evaluate_device_noalloc", "mpid_get_dipoles",
          "mpid_get_pme_parameters", "mpid_get_stats", "mpid_last_error", "mpid_get_system_multipole_moments",
-         "mpid_get_electrostatic_potential"]
+         "mpid_get_electrostatic_potential", "mpid_get_parameter_gradients"]
 
 
 class Settings(ctypes.Structure):
@@ -98,6 +98,7 @@ def load_library(build=True):
     lib.mpid_get_pme_parameters.argtypes = [vp, dp, ip, ip, ip]
     lib.mpid_get_system_multipole_moments.argtypes = [vp, dp, dp, dp, dp]
     lib.mpid_get_electrostatic_potential.argtypes = [vp, dp, dp, dp, ctypes.c_int, dp]
+    lib.mpid_get_parameter_gradients.argtypes = [vp, dp, dp, dp]
     lib.mpid_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.mpid_last_error.argtypes = []
     lib.mpid_last_error.restype = ctypes.c_char_p
@@ -230,6 +231,15 @@ class MPIDContext:
         b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
         out = np.zeros(len(g))
         self._check(self.lib.mpid_get_electrostatic_potential(self._h, _dp(pos), _dp(b), _dp(g), len(g), _dp(out)))
+        return out
+
+    def getParameterGradients(self, positions, box):
+        """dE/d(molecular-frame multipole parameters) at `positions`, shape (n, 20): charge,
+        dipole X Y Z, quadrupole XX XY YY XZ YZ ZZ, octopole XXX ... ZZZ."""
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(self.n, 3)
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        out = np.zeros((self.n, 20))
+        self._check(self.lib.mpid_get_parameter_gradients(self._h, _dp(pos), _dp(b), _dp(out)))
         return out
 
     def getPMEParametersInContext(self):

@@ -347,6 +347,8 @@ struct Context {
     DBuf<double> energyPartial, energyOut;
     DBuf<double> forcesOut;
     DBuf<double> masses, momentPartial, momentRed, gridPts, gridOut;  // system moments, potential
+    DBuf<unsigned long long> gradFx;  // [20][npad] real-space parameter gradient
+    DBuf<double> gradOut;             // [n][20]
     // solver scratch
     DBuf<double> partial, red, sc;
     DBuf<int> iter, done;
@@ -1320,6 +1322,30 @@ struct Context {
         CUDA_CHECK(cudaStreamSynchronize(st));
     }
 
+    // dE/d(molecular-frame multipole parameters) of every atom for the last evaluation.
+    template <typename real>
+    void parameter_gradients(Engine<real>& e, double* host) {
+        cudaStream_t st = stream;
+        gradFx.alloc((size_t) 20 * npad);
+        gradOut.alloc((size_t) 20 * n);
+        CUDA_CHECK(cudaMemsetAsync(gradFx.p, 0, (size_t) 20 * npad * 8, st));
+        launch(k_multipole_gradient<real>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(),
+               (const real*) e.mu.p, gradFx.p);
+        launch(k_gradient_finish<real>, nblk(n, 128), 128, 0, st, n, npad, box, usePme ? set.ewald_alpha : 0.0,
+               usePme ? 1 : 0, (const int*) order.p, mol(), (const double*) pos.p, (const unsigned long long*) gradFx.p,
+               (const real*) e.phiP.p, (const real*) e.phiD.p, (const double*) mom64.p, (const real*) e.mu.p, gradOut.p);
+        CUDA_CHECK(cudaGetLastError());
+        CUDA_CHECK(cudaMemcpyAsync(host, gradOut.p, (size_t) 20 * n * 8, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+    }
+    void parameter_gradients(double* host) {
+        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+        if (mixed)
+            parameter_gradients(*ef, host);
+        else
+            parameter_gradients(*ed, host);
+    }
+
     void get_dipoles(int which, double* host) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
         if (which < 0 || which > 3) throw Error(MPID_ERR_INVALID, "which must be 0, 1, 2 or 3");
@@ -1498,6 +1524,15 @@ int mpid_get_electrostatic_potential(mpid_context* ctx, const double* positions,
     if (!ctx || !positions || !box || (ngrid > 0 && (!grid || !out))) throw Error(MPID_ERR_INVALID, "null argument");
     evaluate_at(ctx->ctx, positions, box);
     ctx->ctx.electrostatic_potential(grid, ngrid, out);
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_get_parameter_gradients(mpid_context* ctx, const double* positions, const double* box, double* out) {
+    MPID_API_BEGIN
+    if (!ctx || !positions || !box || !out) throw Error(MPID_ERR_INVALID, "null argument");
+    evaluate_at(ctx->ctx, positions, box);
+    ctx->ctx.parameter_gradients(out);
     return MPID_OK;
     MPID_API_END
 }

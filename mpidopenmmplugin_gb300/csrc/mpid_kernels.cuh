@@ -1063,6 +1063,278 @@ k_moment_partials(int n, int npad, int pass, const double* __restrict__ pos, con
 }
 
 // ---------------------------------------------------------------------------
+// Parameter gradients.  At stationary induced dipoles (Mutual; and, because their
+// response matrices are symmetric, Direct and OPT) the derivative of the energy with
+// respect to atom I's lab multipole M_I is d(U_pp + U_pi)/dM_I at fixed dipoles: the
+// potential derivatives at I of every other atom's permanent multipoles (kernel K_p)
+// and induced dipoles (kernel K_i), plus reciprocal and self terms.  Components are the
+// 20 unique lab components (charge, dipole, quadrupole XX XY XZ YY YZ ZZ, octopole XXX
+// XXY XXZ XYY XYZ XZZ YYY YYZ YZZ ZZZ) weighted by their multiplicities.
+
+// Unique components: (t, u, v) x/y/z counts, and the multinomial weight.
+__device__ __forceinline__ void comp_tuv(int c, int& t, int& u, int& v, int& w) {
+    const int T[20] = {0, 1, 0, 0, 2, 1, 1, 0, 0, 0, 3, 2, 2, 1, 1, 1, 0, 0, 0, 0};
+    const int U[20] = {0, 0, 1, 0, 0, 1, 0, 2, 1, 0, 0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+    const int V[20] = {0, 0, 0, 1, 0, 0, 1, 0, 1, 2, 0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+    const int W[20] = {1, 1, 1, 1, 1, 2, 2, 1, 2, 1, 1, 3, 3, 3, 6, 3, 1, 3, 3, 1};
+    t = T[c]; u = U[c]; v = V[c]; w = W[c];
+}
+
+// Index of (t, u, v) among all tuples of rank <= some L, rank-major.
+__host__ __device__ __forceinline__ constexpr int tuv_index(int t, int u, int v) {
+    return (t + u + v) * (t + u + v + 1) * (t + u + v + 2) / 6 + (u + v) * (u + v + 1) / 2 + v;
+}
+
+// Cartesian derivatives D(t,u,v) = d^t/dx^t d^u/dy^u d^v/dz^v f(|R|), t+u+v <= L, from
+// g_n = ((1/r) d/dr)^n f by the recursion R^(n)_(t+1,u,v) = t R^(n+1)_(t-1,u,v) +
+// X R^(n+1)_(t,u,v) (and y, z), level n from n + 1, down to n = 0.
+template <typename real, int L>
+__device__ __forceinline__ void cart_derivatives(const real* R, const real* g, real* D) {
+    constexpr int NT = (L + 1) * (L + 2) * (L + 3) / 6;
+    real nxt[NT];
+    nxt[0] = g[L];
+#pragma unroll
+    for (int n = L - 1; n >= 0; --n) {
+        const int K = L - n;
+        real cur[NT];
+#pragma unroll
+        for (int k = 0; k <= K; ++k)
+#pragma unroll
+            for (int m = 0; m <= k; ++m)
+#pragma unroll
+                for (int v = 0; v <= m; ++v) {
+                    const int u = m - v, t = k - m;
+                    real val;
+                    if (k == 0) {
+                        val = g[n];
+                    } else if (t > 0) {
+                        val = R[0] * nxt[tuv_index(t - 1, u, v)];
+                        if (t > 1) val += real(t - 1) * nxt[tuv_index(t - 2, u, v)];
+                    } else if (u > 0) {
+                        val = R[1] * nxt[tuv_index(t, u - 1, v)];
+                        if (u > 1) val += real(u - 1) * nxt[tuv_index(t, u - 2, v)];
+                    } else {
+                        val = R[2] * nxt[tuv_index(t, u, v - 1)];
+                        if (v > 1) val += real(v - 1) * nxt[tuv_index(t, u, v - 2)];
+                    }
+                    cur[tuv_index(t, u, v)] = val;
+                }
+#pragma unroll
+        for (int q = 0; q < NT; ++q) nxt[q] = cur[q];
+    }
+#pragma unroll
+    for (int q = 0; q < NT; ++q) D[q] = nxt[q];
+}
+
+// Lab multipole of a sorted atom as 20 unique components.
+template <typename real>
+__device__ __forceinline__ void unique_moments(const real* mom, int npad, int s, real* M) {
+#pragma unroll
+    for (int c = 0; c < 20; ++c) M[c] = mom[c * npad + s];
+}
+
+// Real-space part of the gradient: per lane G_I[a] = w_a sum_j [ sum_b (-1)^rank(a) w_b
+// M_J[b] D_P(a+b) + sum_(b dipole) (-1)^rank(a) mu_J[b] D_I(a+b) ], kE applied.
+template <typename real, bool QUAD>
+__device__ __forceinline__ void gradient_loop(const NbrList& nl, const AtomArrays<real>& at, const real* mu,
+                                              const PairTask& t, int origI, real* G) {
+    const PairConsts<real>& pc = pair_consts<real>(nl);
+    const int npad = at.npad, si = t.si;
+    const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+    const typename Vec4<real>::type pi = at.prm[si];
+    for (int k = t.k0; k < t.k1; ++k) {
+        int sj;
+        unsigned flag;
+        real d[3], r2;
+        if (!list_pair<real, QUAD>(nl, pc, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
+        const real r = sqrt(r2);
+        const real scale = list_scale<real>(nl, flag, origI, at.orig[sj]);
+        const typename Vec4<real>::type pj = at.prm[sj];
+        const real a = scale == real(0) ? pi.x + pj.x : pc.thole;
+        PairRadial<real, 6, 4, 0> pr;
+        pair_radial_branch<real, 6, 4, -1, QUAD>(r, pc.ew, scale, a, pi.y * pj.y, pr);
+        real gP[7], gI[5];
+#pragma unroll
+        for (int n = 0; n <= 6; ++n) gP[n] = (n & 1) ? -pr.bP[n] : pr.bP[n];
+        gI[0] = real(0);
+#pragma unroll
+        for (int n = 1; n <= 4; ++n) gI[n] = (n & 1) ? -pr.bI[n] : pr.bI[n];
+        real DP[84], DI[35];
+        cart_derivatives<real, 6>(d, gP, DP);
+        cart_derivatives<real, 4>(d, gI, DI);
+        real MJ[20];
+        unique_moments(at.mom, npad, sj, MJ);
+        const real uj[3] = {mu[sj], mu[npad + sj], mu[2 * npad + sj]};
+#pragma unroll
+        for (int ca = 0; ca < 20; ++ca) {
+            int ta, ua, va, wa;
+            comp_tuv(ca, ta, ua, va, wa);
+            const int ra = ta + ua + va;
+            real x = real(0);
+#pragma unroll
+            for (int cb = 0; cb < 20; ++cb) {
+                int tb, ub, vb, wb;
+                comp_tuv(cb, tb, ub, vb, wb);
+                x += real(wb) * MJ[cb] * DP[tuv_index(ta + tb, ua + ub, va + vb)];
+            }
+            if (ra <= 3)
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+                    x += uj[q] * DI[tuv_index(ta + (q == 0), ua + (q == 1), va + (q == 2))];
+            G[ca] += real(wa) * ((ra & 1) ? -x : x);
+        }
+    }
+}
+
+template <typename real>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_multipole_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ gfx) {
+    PairTask t;
+    if (!t.init(nl)) return;
+    const int origI = at.orig[t.si];
+    if (origI < 0) return;
+    real G[20];
+#pragma unroll
+    for (int c = 0; c < 20; ++c) G[c] = real(0);
+    if (t.quad)
+        gradient_loop<real, true>(nl, at, mu, t, origI, G);
+    else
+        gradient_loop<real, false>(nl, at, mu, t, origI, G);
+    const real E = real(kElectric);
+    for (int c = 0; c < 20; ++c) fx_add(gfx + (size_t) c * at.npad + t.si, E * G[c]);
+}
+
+// Per atom: real-space part + reciprocal (Cartesian derivatives of both reciprocal
+// potentials) + Ewald self terms, then the molecular-frame parameters of the API
+// (charge, dipole X Y Z, quadrupole XX XY YY XZ YZ ZZ, octopole XXX XXY XYY YYY XXZ XYZ
+// YYZ XZZ YZZ ZZZ) through the frame rotation and the chirality flip.  out[20 n] by
+// original index, FP64.
+template <typename real>
+__global__ void k_gradient_finish(int n, int npad, BoxDev box, double alpha, int usePme, const int* __restrict__ order,
+                                  MolArrays mol, const double* __restrict__ pos, const unsigned long long* __restrict__ gfx,
+                                  const real* __restrict__ phiP, const real* __restrict__ phiD,
+                                  const double* __restrict__ mom64, const real* __restrict__ mu, double* __restrict__ out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = order[s];
+    double g[20];
+    for (int c = 0; c < 20; ++c) g[c] = fx_get(gfx, c * npad + s);
+    if (usePme) {
+        real A[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) A[a][b] = real(box.A[a][b]);
+        for (int which = 0; which < 2; ++which) {
+            const real* phi = which == 0 ? phiP : phiD;
+            real ph[35], P0, P1[3], P2[3][3], P3[3][3][3];
+            for (int k = 0; k < 35; ++k) ph[k] = phi[k * npad + s];
+            cartesian_potential(ph, A, P0, P1, P2, P3);
+            for (int c = 0; c < 20; ++c) {
+                int t, u, v, w;
+                comp_tuv(c, t, u, v, w);
+                int idx[3], m = 0;
+                for (int k = 0; k < t; ++k) idx[m++] = 0;
+                for (int k = 0; k < u; ++k) idx[m++] = 1;
+                for (int k = 0; k < v; ++k) idx[m++] = 2;
+                const real x = m == 0 ? P0 : m == 1 ? P1[idx[0]] : m == 2 ? P2[idx[0]][idx[1]] : P3[idx[0]][idx[1]][idx[2]];
+                g[c] += kElectric * w * (double) x;
+            }
+        }
+        // Ewald self energy (MPIDReferenceForce.cpp:4283-4318); the d.mu term is half the
+        // permanent-induced self interaction, all of which enters at stationary dipoles
+        LabMoments<double> m;
+        load_moments(mom64, npad, s, m);
+        const double pre = -alpha * kElectric / kSqrtPiRef, a2 = alpha * alpha;
+        const double u3[3] = {(double) mu[s], (double) mu[npad + s], (double) mu[2 * npad + s]};
+        g[0] += pre * 2 * m.q;
+        for (int k = 0; k < 3; ++k) g[1 + k] += pre * 2.0 / 3.0 * a2 * (2 * m.d[k] + 2 * u3[k]);
+        const double s3 = sqrt(3.0), r15 = sqrt(1.5), r06 = sqrt(0.6), r01 = sqrt(0.1);
+        // quadrupole (XX XY XZ YY YZ ZZ) and octopole spherical components as the
+        // reference forms them (MPIDReferenceForce.cpp:318-342), then d(sum S^2)
+        const double* Q = m.Q;
+        const double* O = m.O;
+        const double S4 = 3 * Q[5], S5 = 2 * s3 * Q[2], S6 = 2 * s3 * Q[4], S7 = s3 * (Q[0] - Q[3]), S8 = 2 * s3 * Q[1];
+        const double cq = pre * 4.0 / 15.0 * a2 * a2, co = pre * 8.0 / 105.0 * a2 * a2 * a2;
+        g[4] += cq * 2 * S7 * s3;
+        g[7] -= cq * 2 * S7 * s3;
+        g[9] += cq * 2 * S4 * 3;
+        g[6] += cq * 2 * S5 * 2 * s3;
+        g[8] += cq * 2 * S6 * 2 * s3;
+        g[5] += cq * 2 * S8 * 2 * s3;
+        // O10: 0 XXX 1 XXY 2 XXZ 3 XYY 4 XYZ 5 XZZ 6 YYY 7 YYZ 8 YZZ 9 ZZZ
+        const double S9 = 15 * O[9], S10 = 15 * r15 * O[5], S11 = 15 * r15 * O[8], S12 = 15 * r06 * (O[2] - O[7]),
+                     S13 = 30 * r06 * O[4], S14 = 15 * r01 * (O[0] - 3 * O[3]), S15 = 15 * r01 * (3 * O[1] - O[6]);
+        g[19] += co * 2 * S9 * 15;
+        g[15] += co * 2 * S10 * 15 * r15;
+        g[18] += co * 2 * S11 * 15 * r15;
+        g[12] += co * 2 * S12 * 15 * r06;
+        g[17] -= co * 2 * S12 * 15 * r06;
+        g[14] += co * 2 * S13 * 30 * r06;
+        g[10] += co * 2 * S14 * 15 * r01;
+        g[13] -= co * 2 * S14 * 45 * r01;
+        g[11] += co * 2 * S15 * 45 * r01;
+        g[16] -= co * 2 * S15 * 15 * r01;
+    }
+    // frame of the original atom
+    const int ax = mol.axis[i], iz = mol.az[i], ix = mol.ax[i], iy = mol.ay[i];
+    const double* pI = pos + 3 * i;
+    const double* pZ = (iz >= 0 && iz < n) ? pos + 3 * iz : pI;
+    const double* pX = (ix >= 0 && ix < n) ? pos + 3 * ix : pI;
+    const double* pY = (iy >= 0 && iy < n) ? pos + 3 * iy : pI;
+    double R[3][3];
+    local_frame<double>(ax, pI, pZ, pX, pY, R);
+    const bool flip = chiral_flip<double>(ax, iy >= 0, pI, pZ, pX, pY);
+    // full-entry lab derivatives, rotated into the molecular frame (lab = R^T local R)
+    double* o = out + 20 * (size_t) i;
+    o[0] = g[0];
+    for (int k = 0; k < 3; ++k) o[1 + k] = R[k][0] * g[1] + R[k][1] * g[2] + R[k][2] * g[3];
+    double GQ[3][3];
+    for (int x = 0; x < 3; ++x)
+        for (int y = 0; y < 3; ++y) {
+            const int c = q6(x, y);
+            GQ[x][y] = g[4 + c] / (x == y ? 1.0 : 2.0);
+        }
+    const int QAPI[6][2] = {{0, 0}, {0, 1}, {1, 1}, {0, 2}, {1, 2}, {2, 2}};
+    for (int c = 0; c < 6; ++c) {
+        const int k = QAPI[c][0], mm = QAPI[c][1];
+        double LQkm = 0.0, LQmk = 0.0;
+        for (int x = 0; x < 3; ++x)
+            for (int y = 0; y < 3; ++y) {
+                LQkm += R[k][x] * R[mm][y] * GQ[x][y];
+                LQmk += R[mm][x] * R[k][y] * GQ[x][y];
+            }
+        o[4 + c] = k == mm ? LQkm : LQkm + LQmk;
+    }
+    const int OAPI[10][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {1, 1, 1}, {0, 0, 2},
+                             {0, 1, 2}, {1, 1, 2}, {0, 2, 2}, {1, 2, 2}, {2, 2, 2}};
+    for (int c = 0; c < 10; ++c) {
+        // sum over the distinct permutations of the API index triple
+        const int a0 = OAPI[c][0], a1 = OAPI[c][1], a2i = OAPI[c][2];
+        const int perm[6][3] = {{a0, a1, a2i}, {a0, a2i, a1}, {a1, a0, a2i}, {a1, a2i, a0}, {a2i, a0, a1}, {a2i, a1, a0}};
+        double acc = 0.0;
+        for (int p = 0; p < 6; ++p) {
+            bool dup = false;
+            for (int q = 0; q < p; ++q)
+                dup = dup || (perm[q][0] == perm[p][0] && perm[q][1] == perm[p][1] && perm[q][2] == perm[p][2]);
+            if (dup) continue;
+            const int k = perm[p][0], l = perm[p][1], mm = perm[p][2];
+            for (int x = 0; x < 3; ++x)
+                for (int y = 0; y < 3; ++y)
+                    for (int z = 0; z < 3; ++z) {
+                        const int oc = o10(x, y, z);
+                        const int w = (x == y && y == z) ? 1 : ((x == y || y == z || x == z) ? 3 : 6);
+                        acc += R[k][x] * R[l][y] * R[mm][z] * g[10 + oc] / w;
+                    }
+        }
+        o[10 + c] = acc;
+    }
+    if (flip) {  // the flipped parameters enter with the opposite sign
+        o[2] = -o[2];
+        o[4 + 1] = -o[4 + 1];
+        o[4 + 4] = -o[4 + 4];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // PME.  B-spline coefficients and weighted fractional multipoles per sorted atom.
 // theta layout: [3 dims][5 derivs][ORDER][npad]; igrid [3][npad].
 template <typename real, int ORDER>

@@ -254,3 +254,65 @@ def test_system_moments_and_potential_match_reference(case, precision):
     scale_m = np.abs(ref_m).max()
     assert np.abs(mom - ref_m).max() <= tol * scale_m + 1e-12, (mom, ref_m)
     assert helpers.rel_rms(pot, ref_p) <= tol
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+@pytest.mark.parametrize("name", ["frames_direct.npz", "frames_mutual.npz", "frames_extrapolated.npz",
+                                  "water648_mutual.npz"])
+def test_parameter_gradients_match_oracle(name, precision):
+    """dE/d(molecular-frame multipole parameters) against the oracle port's gradients
+    (checked there against central differences): FP64 to 1e-9, mixed to 1e-5 (relative
+    RMS over all atoms and components)."""
+    from oracle import oracle as O
+    if not O.available("port"):
+        O.build("port")
+    fx = helpers.load_npz_fixture(name)
+    s = helpers.system_from_fixture(fx)
+    s.mutual_eps, s.max_iter = 1e-10, 500
+    f = helpers.force_from_oracle_system(s)
+    ctx = MPIDContext(f, precision=precision)
+    g = ctx.getParameterGradients(s.pos, s.box)
+    ref = O.evaluate(s, "port", want_grad=True).grad
+    err = helpers.rel_rms(g, ref)
+    worst = np.unravel_index(np.argmax(np.abs(g - ref)), g.shape)
+    print("%s %s: gradient rel RMS %.3e; largest difference at atom %d component %d (axis %d): %.6e vs %.6e" %
+          (name, precision, err, worst[0], worst[1], int(s.axis_type[worst[0]]), g[worst], ref[worst]))
+    assert err < (1e-8 if precision == "double" else 1e-5)
+
+
+def test_parameter_gradients_finite_differences_on_device():
+    """FP64 path: the gradient along random admissible parameter directions (charges,
+    dipoles, traceless quadrupoles and octopoles of a few atoms) against central
+    differences of the device energy, to 1e-6 relative."""
+    f, pos, box = synthetic.workload("water648", polarization=MPIDForce.Mutual, order=5)
+    f.setMutualInducedTargetEpsilon(1e-10)
+    ctx = MPIDContext(f, precision="double")
+    g = ctx.getParameterGradients(pos, box)
+    rng = np.random.default_rng(5)
+    for trial in range(4):
+        atoms = rng.choice(f.getNumMultipoles(), 3, replace=False)
+        v = np.zeros((f.getNumMultipoles(), 20))
+        for a in atoms:
+            v[a, 0] = rng.normal()
+            v[a, 1:4] = rng.normal(size=3) * 0.01
+            v[a, 4:10] = synthetic.traceless_quadrupole(rng, 0.001, 1)[0]
+            v[a, 10:20] = synthetic.traceless_octopole(rng, 1e-4, 1)[0]
+        h = 1e-4
+
+        def energy(sign):
+            f2 = synthetic.workload("water648", polarization=MPIDForce.Mutual, order=5)[0]
+            f2.setMutualInducedTargetEpsilon(1e-10)
+            for a in atoms:
+                p = list(f2.getMultipoleParameters(int(a)))
+                p[0] += sign * h * v[a, 0]
+                p[1] = list(np.asarray(p[1]) + sign * h * v[a, 1:4])
+                p[2] = list(np.asarray(p[2]) + sign * h * v[a, 4:10])
+                p[3] = list(np.asarray(p[3]) + sign * h * v[a, 10:20])
+                f2.setMultipoleParameters(int(a), *p)
+            c2 = MPIDContext(f2, precision="double")
+            return c2.evaluate(pos, box)[0]
+
+        fd = (energy(1) - energy(-1)) / (2 * h)
+        an = float((g * v).sum())
+        print("direction %d: analytic %.10e fd %.10e" % (trial, an, fd))
+        assert abs(an - fd) <= 1e-6 * max(abs(fd), 1.0)
