@@ -167,6 +167,17 @@ int mpid_get_electrostatic_potential(mpid_context* ctx, const double* positions,
  * stationarity of the induced dipoles, so no extra linear solve is needed. */
 int mpid_get_parameter_gradients(mpid_context* ctx, const double* positions, const double* box, double* out);
 
+/* One evaluation at `positions` returning any of: forces (3n, ADDED to, as
+ * mpid_evaluate), the energy, the multipole-parameter gradients (20n, as
+ * mpid_get_parameter_gradients) and the polarisation-parameter gradients (4n per atom:
+ * dE/d(molecular-frame polarisability X Y Z) in kJ/mol/nm^3 and dE/d(Thole width) in
+ * kJ/mol).  Each pointer may be NULL.  The polarisation gradients need stationary induced
+ * dipoles (Mutual or Direct; Extrapolated is rejected with MPID_ERR_INVALID).  A
+ * polarisability of 0 gets a gradient of 0.  No reference counterpart: the fitting
+ * entry point of this library. */
+int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, const double* box, double* forces,
+                                 double* energy, double* multipole_grad, double* polarization_grad);
+
 /* PME parameters in use (CalcMPIDForceKernel::getPMEParameters, mpidKernels.h:103). */
 int mpid_get_pme_parameters(mpid_context* ctx, double* alpha, int* nx, int* ny, int* nz);
 

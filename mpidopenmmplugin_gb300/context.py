@@ -22,7 +22,7 @@ MPID_FLAG_NEAR_FIELD_PCG = 2
 C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multipoles", "mpid_set_covalent",
          "mpid_evaluate", "mpid_evaluate_device", "mpid_evaluate_device_noalloc", "mpid_get_dipoles",
          "mpid_get_pme_parameters", "mpid_get_stats", "mpid_last_error", "mpid_get_system_multipole_moments",
-         "mpid_get_electrostatic_potential", "mpid_get_parameter_gradients"]
+         "mpid_get_electrostatic_potential", "mpid_get_parameter_gradients", "mpid_evaluate_with_gradients"]
 
 
 class Settings(ctypes.Structure):
@@ -99,6 +99,7 @@ def load_library(build=True):
     lib.mpid_get_system_multipole_moments.argtypes = [vp, dp, dp, dp, dp]
     lib.mpid_get_electrostatic_potential.argtypes = [vp, dp, dp, dp, ctypes.c_int, dp]
     lib.mpid_get_parameter_gradients.argtypes = [vp, dp, dp, dp]
+    lib.mpid_evaluate_with_gradients.argtypes = [vp, dp, dp, dp, dp, dp, dp]
     lib.mpid_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.mpid_last_error.argtypes = []
     lib.mpid_last_error.restype = ctypes.c_char_p
@@ -241,6 +242,23 @@ class MPIDContext:
         out = np.zeros((self.n, 20))
         self._check(self.lib.mpid_get_parameter_gradients(self._h, _dp(pos), _dp(b), _dp(out)))
         return out
+
+    def evaluateWithGradients(self, positions, box, forces=True, multipole=True, polarization=True):
+        """One evaluation returning (energy, forces (n, 3) or None, multipole-parameter
+        gradients (n, 20) or None, polarisation gradients (n, 4) or None).  The
+        polarisation gradients are dE/d(molecular-frame polarisability X Y Z) and
+        dE/d(Thole width); they need Mutual or Direct polarisation."""
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(self.n, 3)
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        f = np.zeros((self.n, 3)) if forces else None
+        gm = np.zeros((self.n, 20)) if multipole else None
+        gp = np.zeros((self.n, 4)) if polarization else None
+        e = ctypes.c_double(0.0)
+        null = ctypes.POINTER(ctypes.c_double)()
+        self._check(self.lib.mpid_evaluate_with_gradients(
+            self._h, _dp(pos), _dp(b), null if f is None else _dp(f), ctypes.byref(e),
+            null if gm is None else _dp(gm), null if gp is None else _dp(gp)))
+        return e.value, f, gm, gp
 
     def getPMEParametersInContext(self):
         a = ctypes.c_double()

@@ -287,6 +287,9 @@ struct Context {
     int n = 0, npad = 0, ntiles = 0;
     bool usePme = false, mixed = true;
     cudaStream_t stream = nullptr;
+    // The context's own stream, used by the host-buffer calls so that contexts driven
+    // from different host threads run concurrently.
+    cudaStream_t hostStream = nullptr;
     // Side stream for the reciprocal-space (PME) chains, which run concurrently with the
     // real-space pair kernel on the main stream: fork_pme makes the side stream wait for
     // the main stream's work so far, join_pme makes the main stream wait for the side.
@@ -337,6 +340,9 @@ struct Context {
     // engines
     std::unique_ptr<Engine<float>> ef;
     std::unique_ptr<Engine<double>> ed;
+    // FP64 engine of the gradient pass on the mixed path without a refinement engine
+    // (Direct, Extrapolated); created on the first gradient request
+    std::unique_ptr<Engine<double>> eg;
     // accumulators (sorted order)
     DBuf<unsigned long long> forceFx, torqueFx;
     DBuf<double> energyBlocks;          // per-block real-space energy
@@ -349,6 +355,8 @@ struct Context {
     DBuf<double> masses, momentPartial, momentRed, gridPts, gridOut;  // system moments, potential
     DBuf<unsigned long long> gradFx;  // [20][npad] real-space parameter gradient
     DBuf<double> gradOut;             // [n][20]
+    DBuf<unsigned long long> polFx;   // [2][npad] screening sums W, Z of the polarisation gradient
+    DBuf<double> polOut;              // [n][4]
     // solver scratch
     DBuf<double> partial, red, sc;
     DBuf<int> iter, done;
@@ -367,6 +375,7 @@ struct Context {
     mpid_stats stats{};
     StageTimer timer;
     bool evaluated = false;
+    bool gradPrepared = false;  // FP64 inputs of the gradient pass hold the last evaluation
     BoxDev box{};
 
     ~Context() {
@@ -381,6 +390,7 @@ struct Context {
         if (evStart) cudaEventDestroy(evStart);
         if (evStop) cudaEventDestroy(evStop);
         if (ownStream && stream) cudaStreamDestroy(stream);
+        if (hostStream) cudaStreamDestroy(hostStream);
     }
 
     // ----- set-up -----
@@ -431,6 +441,7 @@ struct Context {
         counters.alloc(3);
         CUDA_CHECK(cudaMemset(counters.p, 0, 3 * sizeof(unsigned)));
         CUDA_CHECK(cudaStreamCreateWithFlags(&pmeStream, cudaStreamNonBlocking));
+        CUDA_CHECK(cudaStreamCreateWithFlags(&hostStream, cudaStreamNonBlocking));
         CUDA_CHECK(cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming));
         CUDA_CHECK(cudaEventCreateWithFlags(&evJoin, cudaEventDisableTiming));
         CUDA_CHECK(cudaMallocHost(&hostDone, 256 * sizeof(int)));
@@ -1215,6 +1226,7 @@ struct Context {
             stats.stage_launches[s] = timer.launches[s];
         }
         evaluated = true;
+        gradPrepared = false;
         CUDA_CHECK(cudaStreamSynchronize(st));
         return energy;
     }
@@ -1322,6 +1334,75 @@ struct Context {
         CUDA_CHECK(cudaStreamSynchronize(st));
     }
 
+    // The gradient passes run in FP64 on both paths.  On the mixed path their inputs are
+    // prepared once per evaluation in the FP64 engine: the atoms (lab moments, offsets,
+    // B-splines), the mixed solve's induced dipoles (the refined FP64 dipoles for Mutual,
+    // the FP32 ones widened otherwise) and the FP64 reciprocal potentials of the
+    // permanent multipoles and of those dipoles.  The per-type sums of a fitting
+    // workload cancel strongly, which FP32 pair and PME terms would not resolve.
+    Engine<double>& gradient_engine() {
+        if (!mixed) return *ed;
+        if (gradPrepared) return ed ? *ed : *eg;
+        cudaStream_t st = stream;
+        // Mutual: the refinement engine, whose dipoles are the refined FP64 ones
+        Engine<double>* dp = ed.get();
+        if (!dp) {
+            if (!eg) {
+                eg.reset(new Engine<double>());
+                eg->init(n, npad, usePme, set.pme_order, set.grid);
+            }
+            dp = eg.get();
+        }
+        Engine<double>& d = *dp;
+        prepare_engine(d, true);
+        if (dp != ed.get()) {
+            const size_t n3 = 3 * (size_t) npad;
+            CUDA_CHECK(cudaMemsetAsync(d.mu.p, 0, n3 * 8, st));
+            launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3, (const float*) ef->mu.p,
+                   d.mu.p);
+        }
+        if (usePme) {
+            fork_pme();
+            cudaStream_t ps = pmeStream;
+            d.pme.template spread<20>(n, npad, box, d.mf.p, nullptr, ps);
+            d.pme.convolve(influence.p, nullptr, ps);
+            d.pme.template gather<35>(n, npad, box, d.phiP.p, nullptr, ps);
+            launch(k_frac_dipoles<double>, nblk(npad, 128), 128, 0, ps, npad, box, (const double*) d.mu.p, d.mfd.p,
+                   (const int*) nullptr);
+            d.pme.template spread<4>(n, npad, box, d.mfd.p, nullptr, ps);
+            d.pme.convolve(influence.p, nullptr, ps);
+            d.pme.template gather<35>(n, npad, box, d.phiD.p, nullptr, ps);
+            join_pme();
+        }
+        CUDA_CHECK(cudaGetLastError());
+        gradPrepared = true;
+        return d;
+    }
+
+    // dE/d(molecular-frame polarisability X Y Z, Thole width) of every atom for the last
+    // evaluation (Mutual, Direct).
+    template <typename real>
+    void polarization_gradients(Engine<real>& e, double* host) {
+        cudaStream_t st = stream;
+        polFx.alloc((size_t) 2 * npad);
+        polOut.alloc((size_t) 4 * n);
+        CUDA_CHECK(cudaMemsetAsync(polFx.p, 0, (size_t) 2 * npad * 8, st));
+        launch(k_polarization_gradient<real>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(),
+               (const real*) e.mu.p, set.polarization_type == MPID_MUTUAL ? 1 : 0, polFx.p);
+        launch(k_polarization_gradient_finish<real>, nblk(n, 128), 128, 0, st, n, npad, (const int*) order.p, mol(),
+               (const double*) pos.p, (const unsigned long long*) polFx.p, (const real*) e.mu.p, polOut.p);
+        CUDA_CHECK(cudaGetLastError());
+        CUDA_CHECK(cudaMemcpyAsync(host, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+    }
+    void polarization_gradients(double* host) {
+        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+        if (set.polarization_type == MPID_EXTRAPOLATED)
+            throw Error(MPID_ERR_INVALID,
+                        "polarizability and Thole gradients need stationary induced dipoles (Mutual or Direct)");
+        polarization_gradients(gradient_engine(), host);
+    }
+
     // dE/d(molecular-frame multipole parameters) of every atom for the last evaluation.
     template <typename real>
     void parameter_gradients(Engine<real>& e, double* host) {
@@ -1340,10 +1421,7 @@ struct Context {
     }
     void parameter_gradients(double* host) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
-        if (mixed)
-            parameter_gradients(*ef, host);
-        else
-            parameter_gradients(*ed, host);
+        parameter_gradients(gradient_engine(), host);
     }
 
     void get_dipoles(int which, double* host) {
@@ -1447,6 +1525,7 @@ int mpid_evaluate(mpid_context* ctx, const double* positions, const double* box,
     if (!ctx || !positions || !box || !forces) throw Error(MPID_ERR_INVALID, "null argument");
     Context& c = ctx->ctx;
     CUDA_CHECK(cudaSetDevice(c.device));
+    c.stream = c.hostStream;
     const size_t n3 = 3 * (size_t) c.n;
     CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions, n3 * 8, cudaMemcpyHostToDevice, c.stream));
     CUDA_CHECK(cudaMemcpyAsync(c.forcesOut.p, forces, n3 * 8, cudaMemcpyHostToDevice, c.stream));
@@ -1502,6 +1581,7 @@ int mpid_evaluate_device_noalloc(mpid_context* ctx, const double* d_positions, c
 // defined at the positions given, as the reference recomputes the induced dipoles).
 static void evaluate_at(Context& c, const double* positions, const double* box) {
     CUDA_CHECK(cudaSetDevice(c.device));
+    c.stream = c.hostStream;
     const size_t n3 = 3 * (size_t) c.n;
     CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions, n3 * 8, cudaMemcpyHostToDevice, c.stream));
     CUDA_CHECK(cudaMemsetAsync(c.forcesOut.p, 0, n3 * 8, c.stream));
@@ -1533,6 +1613,32 @@ int mpid_get_parameter_gradients(mpid_context* ctx, const double* positions, con
     if (!ctx || !positions || !box || !out) throw Error(MPID_ERR_INVALID, "null argument");
     evaluate_at(ctx->ctx, positions, box);
     ctx->ctx.parameter_gradients(out);
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, const double* box, double* forces,
+                                 double* energy, double* multipole_grad, double* polarization_grad) {
+    MPID_API_BEGIN
+    if (!ctx || !positions || !box) throw Error(MPID_ERR_INVALID, "null argument");
+    Context& c = ctx->ctx;
+    if (polarization_grad && c.set.polarization_type == MPID_EXTRAPOLATED)
+        throw Error(MPID_ERR_INVALID,
+                    "polarizability and Thole gradients need stationary induced dipoles (Mutual or Direct)");
+    CUDA_CHECK(cudaSetDevice(c.device));
+    c.stream = c.hostStream;
+    const size_t n3 = 3 * (size_t) c.n;
+    CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions, n3 * 8, cudaMemcpyHostToDevice, c.stream));
+    if (forces)
+        CUDA_CHECK(cudaMemcpyAsync(c.forcesOut.p, forces, n3 * 8, cudaMemcpyHostToDevice, c.stream));
+    else
+        CUDA_CHECK(cudaMemsetAsync(c.forcesOut.p, 0, n3 * 8, c.stream));
+    const double e = c.evaluate_device(c.pos.p, box, c.forcesOut.p, nullptr);
+    if (forces) CUDA_CHECK(cudaMemcpyAsync(forces, c.forcesOut.p, n3 * 8, cudaMemcpyDeviceToHost, c.stream));
+    if (multipole_grad) c.parameter_gradients(multipole_grad);
+    if (polarization_grad) c.polarization_gradients(polarization_grad);
+    CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    if (energy) *energy = e;
     return MPID_OK;
     MPID_API_END
 }

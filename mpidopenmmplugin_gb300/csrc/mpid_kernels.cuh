@@ -1204,6 +1204,19 @@ k_multipole_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict__ m
     for (int c = 0; c < 20; ++c) fx_add(gfx + (size_t) c * at.npad + t.si, E * G[c]);
 }
 
+// Local frame R of original atom i (FP64 positions; lab = R^T local R) and whether its
+// chirality flips the parameters.
+__device__ __forceinline__ bool api_frame(const MolArrays& mol, const double* __restrict__ pos, int n, int i,
+                                          double R[3][3]) {
+    const int ax = mol.axis[i], iz = mol.az[i], ix = mol.ax[i], iy = mol.ay[i];
+    const double* pI = pos + 3 * i;
+    const double* pZ = (iz >= 0 && iz < n) ? pos + 3 * iz : pI;
+    const double* pX = (ix >= 0 && ix < n) ? pos + 3 * ix : pI;
+    const double* pY = (iy >= 0 && iy < n) ? pos + 3 * iy : pI;
+    local_frame<double>(ax, pI, pZ, pX, pY, R);
+    return chiral_flip<double>(ax, iy >= 0, pI, pZ, pX, pY);
+}
+
 // Per atom: real-space part + reciprocal (Cartesian derivatives of both reciprocal
 // potentials) + Ewald self terms, then the molecular-frame parameters of the API
 // (charge, dipole X Y Z, quadrupole XX XY YY XZ YZ ZZ, octopole XXX XXY XYY YYY XXZ XYZ
@@ -1274,15 +1287,8 @@ __global__ void k_gradient_finish(int n, int npad, BoxDev box, double alpha, int
         g[11] += co * 2 * S15 * 45 * r01;
         g[16] -= co * 2 * S15 * 15 * r01;
     }
-    // frame of the original atom
-    const int ax = mol.axis[i], iz = mol.az[i], ix = mol.ax[i], iy = mol.ay[i];
-    const double* pI = pos + 3 * i;
-    const double* pZ = (iz >= 0 && iz < n) ? pos + 3 * iz : pI;
-    const double* pX = (ix >= 0 && ix < n) ? pos + 3 * ix : pI;
-    const double* pY = (iy >= 0 && iy < n) ? pos + 3 * iy : pI;
     double R[3][3];
-    local_frame<double>(ax, pI, pZ, pX, pY, R);
-    const bool flip = chiral_flip<double>(ax, iy >= 0, pI, pZ, pX, pY);
+    const bool flip = api_frame(mol, pos, n, i, R);
     // full-entry lab derivatives, rotated into the molecular frame (lab = R^T local R)
     double* o = out + 20 * (size_t) i;
     o[0] = g[0];
@@ -1332,6 +1338,123 @@ __global__ void k_gradient_finish(int n, int npad, BoxDev box, double alpha, int
         o[4 + 1] = -o[4 + 1];
         o[4 + 4] = -o[4 + 4];
     }
+}
+
+// ---------------------------------------------------------------------------
+// Polarisability and Thole-width gradients (Mutual, Direct).  At stationary dipoles the
+// energy equals F(mu) = U_pp + U_pi + U_uu + kE/2 mu.alpha^-1.mu with U_pi = -mu.E_perm
+// and U_uu = -1/2 mu.T.mu (absent for Direct), so the derivatives are taken at fixed
+// dipoles.  The parameters enter through alpha^-1 and through the screening argument
+// st = a r / (d_i d_j) of the ind and uu kernels, d_i = mean(p_i)^(1/6):
+//   dst/dp_ik = -st / (18 mean(p_i)),   dst/da_i = st / a  (pairs of covalent scale 0,
+//   whose width is a_i + a_j; other pairs use the default width).
+// The pair loop sums, per atom, W_I = sum_j st dF_ij/dst and Z_I over the scale-0 pairs
+// of st/a dF_ij/dst, where dF_ij/dst is the pair's U_pi + U_uu with the kernels' st
+// derivatives, kE applied.
+template <typename real, bool QUAD>
+__device__ __forceinline__ void polarization_loop(const NbrList& nl, const AtomArrays<real>& at, const real* mu,
+                                                  bool mutual, const PairTask& t, int origI, real& W, real& Z) {
+    const PairConsts<real>& pc = pair_consts<real>(nl);
+    const int npad = at.npad, si = t.si;
+    const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
+    const typename Vec4<real>::type pi = at.prm[si];
+    real MI[20];
+    unique_moments(at.mom, npad, si, MI);
+    const real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
+    for (int k = t.k0; k < t.k1; ++k) {
+        int sj;
+        unsigned flag;
+        real d[3], r2;
+        if (!list_pair<real, QUAD>(nl, pc, at, t.I, k, t.lane, oi, sj, flag, d, r2)) continue;
+        const typename Vec4<real>::type pj = at.prm[sj];
+        const real dmp = pi.y * pj.y;
+        if (!(dmp > real(0))) continue;
+        const real r = sqrt(r2);
+        const real scale = list_scale<real>(nl, flag, origI, at.orig[sj]);
+        const real a = scale == real(0) ? pi.x + pj.x : pc.thole;
+        const real st = a * r / dmp;
+        if (st >= real(50)) continue;
+        real dl[5];
+        thole_lambda_derivs<real, 4>(st, dl);
+        const real rinv2 = real(1) / r2;
+        real bB[5];
+        bare_part<real, 4>(real(1) / r, rinv2, bB);
+        // st derivatives of the ind kernel (scale lambda' b_n[1/r]) as signed g_n
+        real g[5];
+        g[0] = real(0);
+#pragma unroll
+        for (int n = 1; n <= 4; ++n) g[n] = ((n & 1) ? -scale : scale) * dl[n] * bB[n];
+        real D[35];
+        cart_derivatives<real, 4>(d, g, D);
+        real MJ[20];
+        unique_moments(at.mom, npad, sj, MJ);
+        const real uj[3] = {mu[sj], mu[npad + sj], mu[2 * npad + sj]};
+        real x = real(0);
+#pragma unroll
+        for (int ca = 0; ca < 20; ++ca) {
+            int ta, ua, va, wa;
+            comp_tuv(ca, ta, ua, va, wa);
+            real s1 = real(0), s2 = real(0);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const real dq = D[tuv_index(ta + (q == 0), ua + (q == 1), va + (q == 2))];
+                s1 += uj[q] * dq;
+                s2 += ui[q] * dq;
+            }
+            const int ra = ta + ua + va;
+            x += real(wa) * (((ra & 1) ? -MI[ca] : MI[ca]) * s1 - MJ[ca] * s2);
+        }
+        if (mutual) {  // -(g1' mu_i.mu_j + g2' (mu_i.d)(mu_j.d)), g1' = -lambda_1' b_1, g2' = lambda_2' b_2
+            const real mm = ui[0] * uj[0] + ui[1] * uj[1] + ui[2] * uj[2];
+            const real mi = ui[0] * d[0] + ui[1] * d[1] + ui[2] * d[2];
+            const real mj = uj[0] * d[0] + uj[1] * d[1] + uj[2] * d[2];
+            x += dl[1] * bB[1] * mm - dl[2] * bB[2] * mi * mj;
+        }
+        W += st * x;
+        if (scale == real(0)) Z += st / a * x;
+    }
+}
+
+template <typename real>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_polarization_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, int mutual,
+                        unsigned long long* __restrict__ gfx) {
+    PairTask t;
+    if (!t.init(nl)) return;
+    const int origI = at.orig[t.si];
+    if (origI < 0) return;
+    real W = real(0), Z = real(0);
+    if (t.quad)
+        polarization_loop<real, true>(nl, at, mu, mutual != 0, t, origI, W, Z);
+    else
+        polarization_loop<real, false>(nl, at, mu, mutual != 0, t, origI, W, Z);
+    const real E = real(kElectric);
+    fx_add(gfx + t.si, E * W);
+    fx_add(gfx + at.npad + t.si, E * Z);
+}
+
+// out[4 n] by original index: dE/d(molecular-frame polarisability X Y Z, Thole width).
+template <typename real>
+__global__ void k_polarization_gradient_finish(int n, int npad, const int* __restrict__ order, MolArrays mol,
+                                               const double* __restrict__ pos, const unsigned long long* __restrict__ gfx,
+                                               const real* __restrict__ mu, double* __restrict__ out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = order[s];
+    const double W = fx_get(gfx, s), Z = fx_get(gfx, npad + s);
+    double R[3][3];
+    api_frame(mol, pos, n, i, R);
+    const double* p = mol.pol + 3 * i;
+    const double pbar = (p[0] + p[1] + p[2]) / 3.0;
+    const double u[3] = {(double) mu[s], (double) mu[npad + s], (double) mu[2 * npad + s]};
+    double* o = out + 4 * (size_t) i;
+    for (int k = 0; k < 3; ++k) {
+        const double nu = R[k][0] * u[0] + R[k][1] * u[1] + R[k][2] * u[2];
+        double g = p[k] > 0.0 ? -0.5 * kElectric * nu * nu / (p[k] * p[k]) : 0.0;
+        if (pbar > 0.0) g -= W / (18.0 * pbar);
+        o[k] = g;
+    }
+    o[3] = Z;
 }
 
 // ---------------------------------------------------------------------------

@@ -263,6 +263,30 @@ MPID_HD void thole_lambdas(real s, real* lam, real* oneMinus) {
     }
 }
 
+// d lambda_(2n+1) / ds = e^-s (P_n(s) - P_n'(s)) for n = 1..NMAX (dl[0] unused), the
+// screening derivative of the polarisability and Thole-width gradients.  Every
+// coefficient of P_n - P_n' is >= 0, so the sum has no cancellation.
+template <typename real, int NMAX>
+MPID_HD void thole_lambda_derivs(real s, real* dl) {
+    const double P[7][8] = {
+        {1, 0.5, 0, 0, 0, 0, 0, 0},
+        {1, 1, 0.5, 0, 0, 0, 0, 0},
+        {1, 1, 0.5, 1.0 / 6, 0, 0, 0, 0},
+        {1, 1, 0.5, 1.0 / 6, 1.0 / 30, 0, 0, 0},
+        {1, 1, 0.5, 1.0 / 6, 4.0 / 105, 1.0 / 210, 0, 0},
+        {1, 1, 0.5, 1.0 / 6, 5.0 / 126, 2.0 / 315, 1.0 / 1890, 0},
+        {1, 1, 0.5, 1.0 / 6, 4.0 / 99, 7.0 / 990, 17.0 / 20790, 1.0 / 20790},
+    };
+    const real es = m_exp(-s);
+#pragma unroll
+    for (int n = 1; n <= NMAX; ++n) {
+        real p = real(P[n][7]);
+#pragma unroll
+        for (int k = 6; k >= 0; --k) p = p * s + real(P[n][k] - (k + 1) * P[n][k + 1]);
+        dl[n] = es * p;
+    }
+}
+
 // Radial functions of one pair for the three kernels of the model:
 //   perm     K_p = (s - erf(alpha r)) / r                 permanent-permanent
 //   ind      K_i = s phi_T - erf(alpha r)/r               permanent-induced, fields

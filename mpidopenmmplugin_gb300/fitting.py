@@ -1,0 +1,193 @@
+"""Energies, forces and per-type parameter gradients over many independent boxes.
+
+Parameter fitting evaluates one force field on many small systems (snapshots of uneven
+size) and needs dE/d(per-type parameters).  `BoxBatch` keeps one device context per
+box.  The boxes are small next to the GPU (a few hundred to a few thousand atoms), so
+the batch drives them concurrently: every context has its own CUDA streams, and a pool
+of host threads issues the evaluations (the C ABI runs without the GIL), which overlaps
+the boxes' kernels on the device.
+
+Per-type parameters (24 per type) are the molecular-frame multipole components of
+MPIDForce::addMultipole (charge, dipole X Y Z, quadrupole XX XY YY XZ YZ ZZ, octopole XXX
+XXY XYY YYY XXZ XYZ YYZ XZZ YZZ ZZZ), the molecular-frame polarisabilities X Y Z and the
+Thole width; every atom of a type takes them in its own local frame.  The gradients
+come from mpid_evaluate_with_gradients (stationary induced dipoles, so Mutual or Direct
+polarisation for the last four), summed over the atoms of each type and over the boxes.
+Quadrupoles and octopoles must stay traceless: `project_traceless` removes the trace
+directions from a gradient before a step.
+"""
+import concurrent.futures as _cf
+
+import numpy as np
+
+from .context import MPIDContext
+from .force import MPIDForce
+
+NPARAM = 24
+COLUMNS = (["charge", "dipoleX", "dipoleY", "dipoleZ", "quadXX", "quadXY", "quadYY", "quadXZ", "quadYZ", "quadZZ"] +
+           ["oct" + c for c in ("XXX", "XXY", "XYY", "YYY", "XXZ", "XYZ", "YYZ", "XZZ", "YZZ", "ZZZ")] +
+           ["polarizabilityX", "polarizabilityY", "polarizabilityZ", "thole"])
+
+
+def per_type(grad, types, ntypes):
+    """(n, k) per-atom gradients -> (ntypes, k) sums over the atoms of each type."""
+    out = np.zeros((ntypes, grad.shape[1]))
+    np.add.at(out, np.asarray(types, dtype=np.int64), grad)
+    return out
+
+
+def project_traceless(g):
+    """Remove the trace directions from the quadrupole (XX, YY, ZZ) and octopole gradient
+    components so that a step along the result keeps the moments traceless."""
+    g = np.array(g, dtype=np.float64, copy=True)
+    q = g[..., 4:10]  # XX XY YY XZ YZ ZZ
+    tr = (q[..., 0] + q[..., 2] + q[..., 5]) / 3.0
+    for c in (0, 2, 5):
+        q[..., c] -= tr
+    o = g[..., 10:20]  # XXX XXY XYY YYY XXZ XYZ YYZ XZZ YZZ ZZZ
+    # the three traces of an octopole: (XXX, XYY, XZZ), (XXY, YYY, YZZ), (XXZ, YYZ, ZZZ)
+    for a, b, c in ((0, 2, 7), (1, 3, 8), (4, 6, 9)):
+        t = (o[..., a] + o[..., b] + o[..., c]) / 3.0
+        o[..., a] -= t
+        o[..., b] -= t
+        o[..., c] -= t
+    return g
+
+
+def atom_parameters(force, i):
+    """The 24 per-type parameters of atom i."""
+    q, d, Q, O, _, _, _, _, thole, pol = force.getMultipoleParameters(i)
+    return np.concatenate([[q], d, Q, O, pol, [thole]])
+
+
+def type_parameters(force, types, ntypes):
+    """(ntypes, 24) parameters read from the first atom of each type."""
+    out = np.zeros((ntypes, NPARAM))
+    seen = np.zeros(ntypes, dtype=bool)
+    for i, t in enumerate(types):
+        if not seen[t]:
+            out[t] = atom_parameters(force, i)
+            seen[t] = True
+    return out
+
+
+def apply_type_parameters(force, types, params):
+    """Give every atom its type's row of params (frames and covalent maps unchanged)."""
+    for i, t in enumerate(types):
+        p = list(force.getMultipoleParameters(i))
+        row = params[t]
+        p[0], p[1], p[2], p[3] = float(row[0]), list(row[1:4]), list(row[4:10]), list(row[10:20])
+        p[8], p[9] = float(row[23]), list(row[20:23])
+        force.setMultipoleParameters(i, *p)
+
+
+class BoxBatch:
+    """Independent boxes sharing per-type parameters.
+
+    systems: list of (force, positions (n, 3) nm, box (3, 3) nm, types (n,) ints).
+    precision: "mixed" or "double", as MPIDContext.  threads: host threads driving the
+    contexts concurrently.
+    """
+
+    def __init__(self, systems, ntypes, precision="mixed", threads=8, device=0):
+        self.ntypes = int(ntypes)
+        self.systems = [(f, np.asarray(p, dtype=np.float64), np.asarray(b, dtype=np.float64), np.asarray(t))
+                        for f, p, b, t in systems]
+        self.contexts = [MPIDContext(f, precision=precision, device=device, box=b) for f, p, b, t in self.systems]
+        self.polarization = self.systems[0][0].getPolarizationType()
+        self.threads = max(1, int(threads))
+        self._pool = _cf.ThreadPoolExecutor(max_workers=self.threads)
+
+    def set_parameters(self, params):
+        """Apply (ntypes, 24) parameters to every box (host update + upload)."""
+        params = np.asarray(params, dtype=np.float64).reshape(self.ntypes, NPARAM)
+        for (f, p, b, t), ctx in zip(self.systems, self.contexts):
+            apply_type_parameters(f, t, params)
+            ctx.update_parameters(f)
+
+    def _one(self, k, forces):
+        f, p, b, t = self.systems[k]
+        pol = self.polarization != MPIDForce.Extrapolated
+        e, fo, gm, gp = self.contexts[k].evaluateWithGradients(p, b, forces=forces, multipole=True, polarization=pol)
+        g = np.zeros((self.ntypes, NPARAM))
+        g[:, :20] = per_type(gm, t, self.ntypes)
+        if pol:
+            g[:, 20:] = per_type(gp, t, self.ntypes)
+        return e, fo, g
+
+    def evaluate(self, forces=True):
+        """Energies (nbox,) kJ/mol, per-box forces (list of (n, 3) or None) and the gradient
+        of the summed energy with respect to the per-type parameters (ntypes, 24).  The
+        polarisation columns are zero for Extrapolated polarisation."""
+        results = list(self._pool.map(lambda k: self._one(k, forces), range(len(self.systems))))
+        energies = np.array([r[0] for r in results])
+        grad = np.zeros((self.ntypes, NPARAM))
+        for r in results:
+            grad += r[2]
+        return energies, [r[1] for r in results], grad
+
+    def close(self):
+        self._pool.shutdown(wait=True)
+        for c in self.contexts:
+            c.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def torch_energy(batch: BoxBatch):
+    """A torch.autograd.Function for the batch: params (ntypes, 24) -> summed energy of the
+    boxes, whose backward is the per-type gradient of the same evaluation."""
+    import torch
+
+    class _BatchEnergy(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, params):
+            batch.set_parameters(params.detach().cpu().double().numpy())
+            energies, _, grad = batch.evaluate(forces=False)
+            ctx.save_for_backward(torch.as_tensor(grad, dtype=params.dtype, device=params.device))
+            return torch.as_tensor(energies.sum(), dtype=params.dtype, device=params.device)
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            (grad,) = ctx.saved_tensors
+            return grad_out * grad
+
+    return _BatchEnergy.apply
+
+
+FFT_FRIENDLY = (16, 18, 20, 24, 25, 27, 30, 32, 36)
+
+
+def water_batch(nboxes=64, seed=2024, min_waters=128, max_waters=512, cutoff=0.7, alpha=4.0, order=5,
+                polarization=MPIDForce.Mutual, eps=1e-7):
+    """Batched-fitting workload: nboxes water boxes with a uniformly random (seeded) number
+    of waters in [min_waters, max_waters], edge (n x 29.915 A^3)^(1/3) (1.0 g/cm^3), PME
+    grid of at least 1 point per A rounded up to an FFT-friendly size, cutoff 0.7 nm and
+    Ewald alpha 4.0 /nm.  Two types (0 = O, 1 = H) whose parameters are those of the first
+    O and H of the first box.  Returns (systems, type parameters (2, 24))."""
+    from . import synthetic
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(min_waters, max_waters + 1, size=nboxes)
+    systems = []
+    params = None
+    for k, nw in enumerate(sizes):
+        edge = (int(nw) * 29.915) ** (1.0 / 3.0)
+        f, pos, box = synthetic.water_box(int(nw), edge, seed=seed + 1 + k, placement="random")
+        grid = next(g for g in FFT_FRIENDLY if g >= int(np.ceil(edge)))
+        f.setNonbondedMethod(MPIDForce.PME)
+        f.setCutoffDistance(cutoff)
+        f.setPMEParameters(alpha, grid, grid, grid)
+        f.setPmeBSplineOrder(order)
+        f.setPolarizationType(polarization)
+        f.setMutualInducedTargetEpsilon(eps)
+        f.setMutualInducedMaxIterations(200)
+        types = np.tile([0, 1, 1], int(nw))
+        if params is None:
+            params = type_parameters(f, types, 2)
+        apply_type_parameters(f, types, params)
+        systems.append((f, pos, box, types))
+    return systems, params

@@ -66,24 +66,76 @@ def traceless_octopole(rng, sigma, n):
     return np.stack([full[:, i, j, k] for (i, j, k) in _OCT], axis=1)
 
 
-def water_box(n_waters, box_angstrom, seed=2024, lattice=None, mult_sigma=(0.1, 0.05, 0.02)):
-    """Return (force, positions_nm (n,3), box_nm (3,3)) for n_waters waters."""
+_THETA = np.deg2rad(104.52)
+_ROH = 0.9572
+_H1 = np.array([_ROH * np.sin(_THETA / 2), 0.0, _ROH * np.cos(_THETA / 2)])
+_H2 = np.array([-_ROH * np.sin(_THETA / 2), 0.0, _ROH * np.cos(_THETA / 2)])
+
+
+def _random_waters(rng, n, L, min_oo=2.6, min_atom=1.6, batch=64, rounds=2000):
+    """Random sequential placement of n rigid waters in a periodic cube of edge L (A):
+    each new water (uniform O position, random orientation) is kept when its O is at least
+    min_oo from every other O and all its atoms at least min_atom from every atom of the
+    other waters.  Candidates are drawn `batch` at a time; the first admissible one is
+    kept.  Returns O positions (n, 3) and rotations (n, 3, 3)."""
+    O = np.zeros((n, 3))
+    R = np.zeros((n, 3, 3))
+    atoms = np.zeros((3 * n, 3))
+    for w in range(n):
+        for _ in range(rounds):
+            o = rng.uniform(0.0, L, size=(batch, 3))
+            rot = _random_rotations(rng, batch)
+            if w:
+                d = O[None, :w, :] - o[:, None, :]
+                d -= L * np.round(d / L)
+                ok = np.min(np.einsum("kij,kij->ki", d, d), axis=1) >= min_oo ** 2
+                if not ok.any():
+                    continue
+                o, rot = o[ok], rot[ok]
+                k = -1
+                for c in range(len(o)):  # atom check against the waters within reach
+                    d = O[:w] - o[c]
+                    d -= L * np.round(d / L)
+                    near = np.flatnonzero(np.einsum("ij,ij->i", d, d) < (min_atom + 2.0 * _ROH + 0.01) ** 2)
+                    mine = np.stack([o[c], o[c] + rot[c] @ _H1, o[c] + rot[c] @ _H2])
+                    other = atoms[(3 * near[:, None] + np.arange(3)).reshape(-1)]
+                    d = other[None, :, :] - mine[:, None, :]
+                    d -= L * np.round(d / L)
+                    if len(other) == 0 or np.min(np.einsum("aij,aij->ai", d, d)) >= min_atom ** 2:
+                        k = c
+                        break
+                if k < 0:
+                    continue
+            else:
+                k = 0
+            O[w], R[w] = o[k], rot[k]
+            atoms[3 * w:3 * w + 3] = [o[k], o[k] + rot[k] @ _H1, o[k] + rot[k] @ _H2]
+            break
+        else:
+            raise RuntimeError("could not place water %d of %d in a %.2f A box" % (w, n, L))
+    return O, R
+
+
+def water_box(n_waters, box_angstrom, seed=2024, lattice=None, mult_sigma=(0.1, 0.05, 0.02), placement="lattice"):
+    """Return (force, positions_nm (n,3), box_nm (3,3)) for n_waters waters.  placement
+    "lattice" puts the oxygens on a jittered cubic lattice (sites drawn at random when
+    n_waters is not a cube); "random" places the waters one by one at random with minimum
+    O-O (2.6 A) and atom-atom (1.6 A) distances between molecules."""
     rng = np.random.default_rng(seed)
     L = box_angstrom
-    side = lattice or int(np.ceil(round(n_waters ** (1.0 / 3.0), 6)))
-    sites = np.array([(i, j, k) for i in range(side) for j in range(side) for k in range(side)], dtype=np.float64)
-    if len(sites) > n_waters:
-        sites = sites[np.sort(rng.choice(len(sites), n_waters, replace=False))]
-    spacing = L / side
-    jitter = 0.12  # A; with >= 3.08 A spacing every O-O distance stays >= 2.6 A
-    O = (sites + 0.5) * spacing + rng.uniform(-jitter, jitter, size=sites.shape)
-    theta = np.deg2rad(104.52)
-    roh = 0.9572
-    h1 = np.array([roh * np.sin(theta / 2), 0.0, roh * np.cos(theta / 2)])
-    h2 = np.array([-roh * np.sin(theta / 2), 0.0, roh * np.cos(theta / 2)])
-    R = _random_rotations(rng, n_waters)
-    H1 = O + R @ h1
-    H2 = O + R @ h2
+    if placement == "random":
+        O, R = _random_waters(rng, n_waters, L)
+    else:
+        side = lattice or int(np.ceil(round(n_waters ** (1.0 / 3.0), 6)))
+        sites = np.array([(i, j, k) for i in range(side) for j in range(side) for k in range(side)], dtype=np.float64)
+        if len(sites) > n_waters:
+            sites = sites[np.sort(rng.choice(len(sites), n_waters, replace=False))]
+        spacing = L / side
+        jitter = 0.12  # A; with >= 3.08 A spacing every O-O distance stays >= 2.6 A
+        O = (sites + 0.5) * spacing + rng.uniform(-jitter, jitter, size=sites.shape)
+        R = _random_rotations(rng, n_waters)
+    H1 = O + R @ _H1
+    H2 = O + R @ _H2
     pos = np.empty((3 * n_waters, 3))
     pos[0::3], pos[1::3], pos[2::3] = O, H1, H2
     pos *= ANG

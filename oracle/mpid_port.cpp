@@ -82,20 +82,33 @@ void erfc_g(double r, double alpha, int nmax, double* g) {
 // Thole screening lambda_(2n+1) for the damped MPID potential (1-(1+s/2)e^-s)/r,
 // s = a r/(d_i d_j); lambda_3..lambda_11 as MPIDReferenceForce.cpp:818-833 and the
 // pair-kernel factors of :4509-4523 imply.
+const double THOLE_P[6][7] = {
+    {1, 0.5, 0, 0, 0, 0, 0},
+    {1, 1, 0.5, 0, 0, 0, 0},
+    {1, 1, 0.5, 1.0 / 6, 0, 0, 0},
+    {1, 1, 0.5, 1.0 / 6, 1.0 / 30, 0, 0},
+    {1, 1, 0.5, 1.0 / 6, 4.0 / 105, 1.0 / 210, 0},
+    {1, 1, 0.5, 1.0 / 6, 5.0 / 126, 2.0 / 315, 1.0 / 1890},
+};
 void thole_lambda(double s, int nmax, double* lam) {
-    static const double P[6][7] = {
-        {1, 0.5, 0, 0, 0, 0, 0},
-        {1, 1, 0.5, 0, 0, 0, 0},
-        {1, 1, 0.5, 1.0 / 6, 0, 0, 0},
-        {1, 1, 0.5, 1.0 / 6, 1.0 / 30, 0, 0},
-        {1, 1, 0.5, 1.0 / 6, 4.0 / 105, 1.0 / 210, 0},
-        {1, 1, 0.5, 1.0 / 6, 5.0 / 126, 2.0 / 315, 1.0 / 1890},
-    };
     double e = std::exp(-s);
     for (int n = 0; n <= nmax; ++n) {
         double p = 0, sk = 1;
-        for (int k = 0; k < 7; ++k) { p += P[n][k] * sk; sk *= s; }
+        for (int k = 0; k < 7; ++k) { p += THOLE_P[n][k] * sk; sk *= s; }
         lam[n] = 1.0 - e * p;
+    }
+}
+// d lambda / ds = e^-s (P_n(s) - P_n'(s)), for the polarisability and Thole gradients.
+void thole_lambda_ds(double s, int nmax, double* dl) {
+    double e = std::exp(-s);
+    for (int n = 0; n <= nmax; ++n) {
+        double p = 0, sk = 1;
+        for (int k = 0; k < 7; ++k) {
+            const double next = k + 1 < 7 ? (k + 1) * THOLE_P[n][k + 1] : 0.0;
+            p += (THOLE_P[n][k] - next) * sk;
+            sk *= s;
+        }
+        dl[n] = e * p;
     }
 }
 
@@ -396,6 +409,22 @@ struct Port {
             double sc = kind == 0 ? s : (kind == 1 ? s * lam[k] : lam[k]);
             g[k] = ge[k] - (1.0 - sc) * gb[k];
         }
+    }
+
+    // Derivative of kernel kind 1 or 2 (as kernel_g) with respect to the screening
+    // argument st = a r / (d_i d_j), for n = 0..nmax.  Returns false where the pair is
+    // not screened (zero polarisability, or st beyond the cut of kernel_g).
+    bool kernel_g_ds(int kind, int i, int j, double r, double s, int nmax, double* gd, double& st, double& a) const {
+        const double dmp = at[i].damp * at[j].damp;
+        a = s == 0.0 ? at[i].thole + at[j].thole : in->default_thole;
+        if (!(dmp > 0)) return false;
+        st = a * r / dmp;
+        if (st >= 50.0) return false;
+        double gb[9], dl[9];
+        bare_g(r, nmax, gb);
+        thole_lambda_ds(st, std::min(nmax, 5), dl);
+        for (int k = 0; k <= nmax; ++k) gd[k] = (kind == 1 ? s : 1.0) * dl[k] * gb[k];
+        return true;
     }
 
     // Field at a point displaced by D from a source multipole (unique comps M, ranks <= maxRank):
@@ -1023,6 +1052,73 @@ struct Port {
         g[16] -= co * 2 * S[15] * 15 * r01;
     }
 
+    // dE/d(molecular-frame polarisability X Y Z, Thole width) per atom, out[4n].  At
+    // stationary dipoles (Mutual, Direct) E = F(mu) with F = U_pp + U_pi + U_uu +
+    // 1/2 mu.alpha^-1.mu, U_pi = -mu.E_perm and U_uu = -1/2 mu.T.mu (U_uu absent for
+    // Direct), so every derivative is taken at fixed dipoles:
+    //  - alpha^-1 term: -1/2 nu_k^2 / p_k^2 with nu = R mu the molecular-frame dipole
+    //    (alpha_lab = R^T diag(p) R);
+    //  - the screening st = a r / (d_i d_j), d_i = mean(p_i)^(1/6): dst/dp_ik =
+    //    -st / (18 mean(p_i)) and, for pairs of covalent scale 0 (whose width is
+    //    a_i + a_j), dst/da_i = st / a.
+    void polarization_gradient(const std::vector<std::array<double, 3>>& mu, double* out) const {
+        const int pol = in->polarization_type;
+        if (pol == 2) throw std::runtime_error("polarisability and Thole gradients need Mutual or Direct polarization");
+        std::vector<double> W(n, 0.0), Z(n, 0.0);
+        for (const auto& pr : pairs) {
+            const int i = pr.first, j = pr.second;
+            double d[3];
+            for (int k = 0; k < 3; ++k) d[k] = in->pos[3 * j + k] - in->pos[3 * i + k];
+            minimg(d);
+            const double r = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            const double s = getscale(i, j);
+            double g[9], st, a;
+            if (!kernel_g_ds(1, i, j, r, s, 4, g, st, a)) continue;
+            // dU_pi/dst: the permanent field's screening derivative at each dipole
+            DTensor T;
+            derivative_tensor(d, g, 4, T);
+            DTensor Tm = T;
+            for (int t = 0; t <= 4; ++t)
+                for (int u = 0; t + u <= 4; ++u)
+                    for (int v = 0; t + u + v <= 4; ++v)
+                        if ((t + u + v) & 1) Tm.d[t][u][v] = -T.d[t][u][v];
+            double Ej[3], Ei[3];
+            field_from(at[i].M, 3, T, Ej);
+            field_from(at[j].M, 3, Tm, Ei);
+            double D = 0;
+            for (int k = 0; k < 3; ++k) D -= mu[j][k] * Ej[k] + mu[i][k] * Ei[k];
+            if (pol == 0) {  // dU_uu/dst = -(g1' mu_i.mu_j + g2' (mu_i.d)(mu_j.d))
+                kernel_g_ds(2, i, j, r, s, 2, g, st, a);
+                double mm = 0, mi = 0, mj = 0;
+                for (int k = 0; k < 3; ++k) {
+                    mm += mu[i][k] * mu[j][k];
+                    mi += mu[i][k] * d[k];
+                    mj += mu[j][k] * d[k];
+                }
+                D -= g[1] * mm + g[2] * mi * mj;
+            }
+            W[i] += st * D;
+            W[j] += st * D;
+            if (s == 0.0) {
+                Z[i] += st * D / a;
+                Z[j] += st * D / a;
+            }
+        }
+        for (int i = 0; i < n; ++i) {
+            double R[3][3];
+            frame(i, R);
+            const double* p = in->polarity + 3 * i;
+            const double pbar = (p[0] + p[1] + p[2]) / 3.0;
+            for (int k = 0; k < 3; ++k) {
+                const double nu = R[k][0] * mu[i][0] + R[k][1] * mu[i][1] + R[k][2] * mu[i][2];
+                double g = p[k] > 0 ? -0.5 * nu * nu / (p[k] * p[k]) : 0.0;
+                if (pbar > 0) g -= W[i] / (18.0 * pbar);
+                out[4 * i + k] = ELECTRIC * g;
+            }
+            out[4 * i + 3] = ELECTRIC * Z[i];
+        }
+    }
+
     // Unique-lab-component gradient -> molecular-frame API parameters of atom i
     // (charge, dipole X Y Z, quadrupole XX XY YY XZ YZ ZZ, octopole XXX XXY XYY YYY XXZ
     // XYZ YYZ XZZ YZZ ZZZ), through the frame rotation and the chirality flip.
@@ -1301,6 +1397,7 @@ struct Port {
             const double a2 = al * al;  // self energy, :4283-4318
             energy += -al * ELECTRIC / SQRT_PI_REF * (cii + 2.0 / 3.0 * a2 * dii + 4.0 / 15.0 * a2 * a2 * qii + 8.0 / 105.0 * a2 * a2 * a2 * oii);
         }
+        if (out->polgrad) polarization_gradient(mu, out->polgrad);
         if (pol == 2) {  // OPT response, :4956-4984
             int nPT = in->n_extrap;
             for (int i = 0; i < n; ++i)

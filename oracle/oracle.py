@@ -65,6 +65,7 @@ class OracleResult:
     epsilon: float
     converged: bool
     grad: Optional[np.ndarray] = None  # (n, 20) molecular-frame parameter gradients (port)
+    polgrad: Optional[np.ndarray] = None  # (n, 4) polarisability X Y Z and Thole gradients (port)
 
 
 class _In(ctypes.Structure):
@@ -110,6 +111,7 @@ class _Out(ctypes.Structure):
         ("converged", ctypes.c_int),
         ("message", ctypes.c_char * 512),
         ("grad", ctypes.POINTER(ctypes.c_double)),
+        ("polgrad", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -232,13 +234,20 @@ def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False, want_grad=F
         out.grad = _dp(grad)
     else:
         out.grad = None
+    polgrad = None
+    if want_grad:
+        polgrad = np.zeros(4 * n)
+        out.polgrad = _dp(polgrad) if sys_.polarization_type != 2 else None
+    else:
+        out.polgrad = None
     rc = _lib(which)(ctypes.byref(inp), ctypes.byref(out))
     if rc != 0:
         raise OracleError(out.message.decode(errors="replace"))
     return OracleResult(energy=out.energy, forces=forces.reshape(n, 3), induced=induced.reshape(n, 3),
                         labdipoles=None if lab is None else lab.reshape(n, 3), iterations=out.iterations,
                         epsilon=out.epsilon, converged=bool(out.converged),
-                        grad=None if grad is None else grad.reshape(n, 20))
+                        grad=None if grad is None else grad.reshape(n, 20),
+                        polgrad=None if polgrad is None or sys_.polarization_type == 2 else polgrad.reshape(n, 4))
 
 
 def properties(sys_: OracleSystem, masses, grid):

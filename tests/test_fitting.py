@@ -1,0 +1,261 @@
+"""Polarisation-parameter gradients and the batched per-type fitting interface.
+
+CPU tests cover the host logic of mpidopenmmplugin_gb300.fitting (per-type sums,
+traceless projection, parameter round trips, the batched-boxes workload's geometry).
+GPU tests check, through the C ABI:
+* dE/d(polarisability X Y Z, Thole width) of the device against the oracle port (itself
+  checked against central differences of its own energy): FP64 to 1e-8, mixed to 1e-5
+  relative RMS (the gradient pass runs in FP64 on both paths; on the mixed path the
+  induced dipoles of the mixed solve carry its ~1e-6 error);
+* the batch's per-type gradient (24 parameters per type, summed over boxes) along
+  admissible parameter directions against the oracle port's (FP64 to 1e-6, mixed to
+  1e-5) and against differences of the device's FP64 energy; the port's own per-type
+  gradient is checked on the CPU against central differences with h = 1e-4;
+* that boxes evaluated concurrently on several host threads give bit-identical results
+  to one-by-one evaluation, and the torch.autograd.Function's backward.
+"""
+import numpy as np
+import pytest
+
+from mpidopenmmplugin_gb300 import MPIDContext, MPIDForce, fitting, synthetic
+from mpidopenmmplugin_gb300.context import MPIDError
+
+import helpers
+
+
+def small_batch(nboxes=4, polarization=MPIDForce.Mutual, seed=11):
+    """A few boxes of 128-160 waters, the batched-fitting workload at a test size."""
+    return fitting.water_batch(nboxes=nboxes, seed=seed, min_waters=128, max_waters=160, polarization=polarization,
+                               eps=1e-9)
+
+
+# --------------------------------------------------------------------------- CPU
+
+
+def test_per_type_sums_and_traceless_projection():
+    rng = np.random.default_rng(0)
+    g = rng.normal(size=(9, 24))
+    types = np.array([0, 1, 1, 0, 2, 2, 2, 1, 0])
+    s = fitting.per_type(g, types, 3)
+    for t in range(3):
+        assert np.allclose(s[t], g[types == t].sum(axis=0))
+    p = fitting.project_traceless(g)
+    assert np.allclose(p[:, 4] + p[:, 6] + p[:, 9], 0.0)
+    o = p[:, 10:20]
+    for a, b, c in ((0, 2, 7), (1, 3, 8), (4, 6, 9)):
+        assert np.allclose(o[:, a] + o[:, b] + o[:, c], 0.0)
+    # components off the trace directions are untouched
+    for c in (0, 1, 2, 3, 5, 7, 8, 20, 21, 22, 23):
+        assert np.array_equal(p[:, c], g[:, c])
+
+
+def test_type_parameters_round_trip():
+    f, pos, box = synthetic.water_box(8, 6.2, seed=3)
+    types = np.tile([0, 1, 1], 8)
+    params = np.arange(48, dtype=np.float64).reshape(2, 24) * 0.01 + 0.1
+    fitting.apply_type_parameters(f, types, params)
+    for i, t in enumerate(types):
+        assert np.allclose(fitting.atom_parameters(f, i), params[t])
+        assert f.getMultipoleParameters(i)[4] == MPIDForce.ZThenX  # frames kept
+    assert np.allclose(fitting.type_parameters(f, types, 2), params)
+
+
+def test_batch_workload_geometry():
+    systems, params = fitting.water_batch(nboxes=4, seed=5)
+    assert params.shape == (2, 24)
+    for f, pos, box, types in systems:
+        nw = len(pos) // 3
+        assert 128 <= nw <= 512
+        edge = box[0, 0] * 10.0
+        assert abs(edge - (nw * 29.915) ** (1.0 / 3.0)) < 1e-9
+        alpha, nx, ny, nz = f.getPMEParameters()
+        assert nx == ny == nz and nx in fitting.FFT_FRIENDLY and nx >= edge and alpha == 4.0
+        assert f.getCutoffDistance() < box[0, 0] / 2
+        # every atom of a type has the type's parameters
+        for i in (0, 1, 2, len(pos) - 3, len(pos) - 1):
+            assert np.allclose(fitting.atom_parameters(f, i), params[types[i]])
+        # molecules do not overlap: intermolecular atom distances >= 1.6 A
+        d = pos[None] - pos[:, None]
+        d -= box[0, 0] * np.round(d / box[0, 0])
+        r = np.sqrt((d ** 2).sum(-1))
+        mol = np.arange(len(pos)) // 3
+        r[mol[:, None] == mol[None]] = 1.0
+        assert r.min() >= 0.16 - 1e-12
+
+
+# --------------------------------------------------------------------------- GPU
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+@pytest.mark.parametrize("name", ["frames_mutual.npz", "frames_direct.npz"])
+def test_polarization_gradients_match_oracle(name, precision):
+    from oracle import oracle as O
+    if not O.available("port"):
+        O.build("port")
+    fx = helpers.load_npz_fixture(name)
+    s = helpers.system_from_fixture(fx)
+    s.mutual_eps, s.max_iter = 1e-10, 500
+    f = helpers.force_from_oracle_system(s)
+    ctx = MPIDContext(f, precision=precision)
+    e, forces, gm, gp = ctx.evaluateWithGradients(s.pos, s.box)
+    ref = O.evaluate(s, "port", want_grad=True)
+    err_p = helpers.rel_rms(gp[:, :3], ref.polgrad[:, :3])
+    err_t = helpers.rel_rms(gp[:, 3], ref.polgrad[:, 3]) if np.any(ref.polgrad[:, 3]) else 0.0
+    err_m = helpers.rel_rms(gm, ref.grad)
+    print("%s %s: polarisability %.3e thole %.3e multipole %.3e" % (name, precision, err_p, err_t, err_m))
+    tol = 1e-8 if precision == "double" else 1e-5
+    assert err_p < tol and err_t < tol and err_m < tol
+    # the combined call agrees with the separate entry points: energies and forces bit for
+    # bit on the mixed path (fixed-point accumulation); the FP64 passes (all gradients,
+    # and the FP64 path's evaluation) spread their PME grids with floating-point atomics
+    e2, f2 = ctx.evaluate(s.pos, s.box)
+    gm2 = ctx.getParameterGradients(s.pos, s.box)
+    if precision == "mixed":
+        assert e2 == e and np.array_equal(f2, forces)
+    else:
+        assert abs(e2 - e) <= 1e-12 * abs(e) and helpers.rel_rms(f2, forces) < 1e-12
+    assert helpers.rel_rms(gm2, gm) < 1e-12
+
+
+@pytest.mark.gpu
+def test_polarization_gradients_rejected_for_extrapolated():
+    f, pos, box = synthetic.workload("water648", polarization=MPIDForce.Extrapolated, order=5)
+    ctx = MPIDContext(f, precision="mixed")
+    with pytest.raises(MPIDError, match="Mutual or Direct"):
+        ctx.evaluateWithGradients(pos, box)
+    e, forces, gm, gp = ctx.evaluateWithGradients(pos, box, polarization=False)
+    assert gp is None and np.all(np.isfinite(gm))
+
+
+def _directions(rng):
+    """Admissible per-type directions: (ntypes, 24) with traceless quadrupole and
+    octopole parts, scaled to each parameter's size."""
+    v = np.zeros((2, 24))
+    v[:, 0] = rng.normal(size=2) * 0.1
+    v[:, 1:4] = rng.normal(size=(2, 3)) * 0.01
+    v[:, 4:10] = synthetic.traceless_quadrupole(rng, 0.002, 2)
+    v[:, 10:20] = synthetic.traceless_octopole(rng, 0.0005, 2)
+    v[:, 20:23] = rng.normal(size=(2, 3)) * 1e-4
+    v[:, 23] = rng.normal(size=2) * 0.1
+    return v
+
+
+def _block_directions(rng):
+    """One direction per parameter block (charge, dipole, quadrupole, octopole,
+    polarisability, Thole width), then one along all of them."""
+    blocks = [slice(0, 1), slice(1, 4), slice(4, 10), slice(10, 20), slice(20, 23), slice(23, 24)]
+    vs = []
+    for b in blocks:
+        v = np.zeros((2, 24))
+        v[:, b] = _directions(rng)[:, b]
+        vs.append(v)
+    vs.append(_directions(rng))
+    return vs
+
+
+def _port_per_type(systems):
+    """Per-type gradient of the summed energy from the oracle port (FP64)."""
+    from oracle import oracle as O
+    if not O.available("port"):
+        O.build("port")
+    g = np.zeros((2, 24))
+    for f, pos, box, types in systems:
+        r = O.evaluate(helpers.oracle_system(f, pos, box), "port", want_grad=True)
+        g[:, :20] += fitting.per_type(r.grad, types, 2)
+        g[:, 20:] += fitting.per_type(r.polgrad, types, 2)
+    return g
+
+
+def test_port_per_type_gradient_matches_finite_differences():
+    """The oracle port's per-type gradient (24 parameters per type) on a 128-water box of
+    the batched-fitting workload against central differences, h = 1e-4, of its own FP64
+    energy: to 1e-5 relative along each parameter block."""
+    systems, params = small_batch(nboxes=1, seed=11)
+    f, pos, box, types = systems[0]
+    f.setMutualInducedTargetEpsilon(1e-11)
+    g = _port_per_type(systems)
+    from oracle import oracle as O
+
+    def energy(p):
+        fitting.apply_type_parameters(f, types, p)
+        return O.evaluate(helpers.oracle_system(f, pos, box), "port").energy
+
+    h = 1e-4
+    for v in _block_directions(np.random.default_rng(7))[:6]:
+        fd = (energy(params + h * v) - energy(params - h * v)) / (2 * h)
+        an = float((g * v).sum())
+        assert abs(an - fd) <= 1e-5 * max(abs(fd), 1.0), (fd, an)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("polarization", [MPIDForce.Mutual, MPIDForce.Direct])
+def test_batch_per_type_gradients(polarization):
+    """Per-type gradients of 4 boxes (128-160 waters) evaluated concurrently, along each
+    parameter block: FP64 within 1e-6 and mixed within 1e-5 of the oracle port's FP64
+    gradient; FP64 within 1e-6 of five-point differences (h = 1e-2) of the device's FP64
+    summed energy.  (Central differences with h = 1e-4 are run on the port's energy on
+    the CPU: the device's FP64 energy carries ~1e-8 kJ/mol of rounding noise from the
+    floating-point atomics of its PME spread, 5e-5 in an h = 1e-4 quotient.)"""
+    systems, params = small_batch(polarization=polarization)
+    rng = np.random.default_rng(7)
+    for f, _, _, _ in systems:
+        f.setMutualInducedTargetEpsilon(1e-11)
+    ref = _port_per_type(systems)
+    dbl = fitting.BoxBatch(systems, 2, precision="double", threads=4)
+    for f, _, _, _ in systems:
+        f.setMutualInducedTargetEpsilon(1e-9)
+    with dbl, fitting.BoxBatch(systems, 2, precision="mixed", threads=4) as mix:
+        _, _, gd = dbl.evaluate(forces=False)
+        _, _, gmx = mix.evaluate(forces=False)
+        h = 1e-2
+
+        def energy(p):
+            dbl.set_parameters(p)
+            return dbl.evaluate(forces=False)[0].sum()
+
+        for v in _block_directions(rng):
+            r, an_d, an_m = float((ref * v).sum()), float((gd * v).sum()), float((gmx * v).sum())
+            fd = (energy(params - 2 * h * v) - 8 * energy(params - h * v) + 8 * energy(params + h * v) -
+                  energy(params + 2 * h * v)) / (12 * h)
+            dbl.set_parameters(params)
+            print("pol %d: port %.10e double %.10e mixed %.10e fd %.10e" % (polarization, r, an_d, an_m, fd))
+            scale = max(abs(r), 1.0)
+            assert abs(an_d - r) <= 1e-6 * scale
+            assert abs(an_m - r) <= 1e-5 * scale
+            assert abs(an_d - fd) <= 1e-6 * scale
+
+
+@pytest.mark.gpu
+def test_concurrent_boxes_match_one_by_one():
+    systems, params = small_batch(nboxes=6, seed=13)
+    with fitting.BoxBatch(systems, 2, precision="mixed", threads=6) as par:
+        e_par, f_par, g_par = par.evaluate()
+        e_par2, f_par2, g_par2 = par.evaluate()
+    with fitting.BoxBatch(systems, 2, precision="mixed", threads=1) as seq:
+        e_seq, f_seq, g_seq = seq.evaluate()
+    assert np.array_equal(e_par, e_seq) and np.array_equal(e_par, e_par2)
+    for a, b in zip(f_par, f_seq):
+        assert np.array_equal(a, b)
+    # the FP64 gradient pass spreads its PME grids with floating-point atomics: equal to
+    # rounding
+    assert np.abs(g_par - g_seq).max() <= 1e-11 * np.abs(g_seq).max()
+    assert np.abs(g_par - g_par2).max() <= 1e-11 * np.abs(g_seq).max()
+    # and each box against its own plain context
+    for (f, pos, box, types), e in zip(systems, e_seq):
+        ctx = MPIDContext(f, precision="mixed", box=box)
+        assert ctx.evaluate(pos, box)[0] == e
+
+
+@pytest.mark.gpu
+def test_torch_autograd_function():
+    torch = pytest.importorskip("torch")
+    systems, params = small_batch(nboxes=2, seed=17)
+    with fitting.BoxBatch(systems, 2, precision="mixed", threads=2) as batch:
+        energies, _, grad = batch.evaluate(forces=False)
+        p = torch.tensor(params, dtype=torch.float64, requires_grad=True)
+        e = fitting.torch_energy(batch)(p)
+        (3.0 * e).backward()
+        assert float(e.detach()) == energies.sum()
+        # a second evaluation: the FP64 gradient pass agrees to rounding
+        assert np.abs(p.grad.numpy() - 3.0 * grad).max() <= 1e-11 * np.abs(3.0 * grad).max()

@@ -75,3 +75,40 @@ def test_port_parameter_gradients_match_finite_differences():
 
             fd = (energy(h) - energy(-h)) / (2 * h)
             assert abs(fd - g[i][c]) <= 1e-6 * max(abs(fd), 1.0), (name, i, c, fd, g[i][c])
+
+
+def test_port_polarization_gradients_match_finite_differences():
+    """dE/d(molecular-frame polarisability X Y Z, Thole width) of the oracle port against
+    central differences (h = 1e-3 relative; the energy is ~1e4 kJ/mol, so
+    smaller steps are dominated by rounding) of its own energy on the 160-atom frames
+    system, for the stationary polarisation types (Mutual, Direct)."""
+    import copy
+    from oracle import oracle as O
+    if not O.available("port"):
+        O.build("port")
+    rng = np.random.default_rng(4)
+    for name in ("frames_direct.npz", "frames_mutual.npz"):
+        fx = helpers.load_npz_fixture(name)
+        s = helpers.system_from_fixture(fx)
+        s.mutual_eps, s.max_iter = 1e-11, 500
+        pg = O.evaluate(s, "port", want_grad=True).polgrad
+        picks = [(int(rng.integers(s.n)), c) for c in range(4) for _ in range(2)]
+        for i, c in picks:
+            pol = np.array(s.polarity, dtype=np.float64).reshape(s.n, 3)
+            base = pol[i][c] if c < 3 else float(np.asarray(s.thole)[i])
+            h = 1e-3 * max(abs(base), 1e-6)
+
+            def energy(delta):
+                t = copy.deepcopy(s)
+                if c < 3:
+                    a = pol.copy()
+                    a[i][c] += delta
+                    t.polarity = a
+                else:
+                    a = np.array(t.thole, dtype=np.float64)
+                    a[i] += delta
+                    t.thole = a
+                return O.evaluate(t, "port").energy
+
+            fd = (energy(h) - energy(-h)) / (2 * h)
+            assert abs(fd - pg[i][c]) <= 1e-5 * max(abs(fd), 1.0), (name, i, c, fd, pg[i][c])
