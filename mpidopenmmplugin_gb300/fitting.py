@@ -138,6 +138,39 @@ class BoxBatch:
         self.close()
 
 
+def shard_indices(sizes, rank, world):
+    """Boxes of one rank when independent boxes are spread over `world` GPUs: greedy
+    longest-processing-time assignment by atom count (largest box first, to the least
+    loaded rank; ties to the lower rank), so every rank gets a near-equal share of
+    atoms.  Deterministic, so every rank computes the same partition without talking."""
+    order = sorted(range(len(sizes)), key=lambda k: (-int(sizes[k]), k))
+    load = [0] * world
+    owner = [0] * len(sizes)
+    for k in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[k] = r
+        load[r] += int(sizes[k])
+    return [k for k in range(len(sizes)) if owner[k] == rank]
+
+
+def allreduce_results(energies, indices, nboxes, grad, group=None):
+    """Combine per-rank results of a sharded batch: each rank holds the energies of its
+    boxes (`indices`) and its partial per-type gradient.  Returns (energies of all
+    boxes, summed gradient), identical on every rank.  One all-reduce of
+    nboxes + ntypes x 24 doubles (torch.distributed; on the GPU under NCCL)."""
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
+    g = np.asarray(grad, dtype=np.float64)
+    buf = np.zeros(nboxes + g.size)
+    buf[np.asarray(list(indices), dtype=np.int64)] = np.asarray(energies, dtype=np.float64)
+    buf[nboxes:] = g.reshape(-1)
+    t = torch.as_tensor(buf, device=dev)
+    dist.all_reduce(t, group=group)
+    out = t.cpu().numpy()
+    return out[:nboxes], out[nboxes:].reshape(g.shape)
+
+
 def torch_energy(batch: BoxBatch):
     """A torch.autograd.Function for the batch: params (ntypes, 24) -> summed energy of the
     boxes, whose backward is the per-type gradient of the same evaluation."""

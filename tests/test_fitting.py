@@ -259,3 +259,54 @@ def test_torch_autograd_function():
         assert float(e.detach()) == energies.sum()
         # a second evaluation: the FP64 gradient pass agrees to rounding
         assert np.abs(p.grad.numpy() - 3.0 * grad).max() <= 1e-11 * np.abs(3.0 * grad).max()
+
+
+def test_shard_indices_partition_and_balance():
+    rng = np.random.default_rng(1)
+    sizes = rng.integers(384, 1537, size=64)
+    for world in (1, 2, 3, 4, 8):
+        parts = [fitting.shard_indices(sizes, r, world) for r in range(world)]
+        flat = sorted(k for p in parts for k in p)
+        assert flat == list(range(64))
+        loads = [int(sizes[p].sum()) for p in parts]
+        assert max(loads) - min(loads) <= sizes.max()
+
+
+def _sharded_worker(rank, world, port, out):
+    import os
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sizes = np.arange(10) * 7 + 3
+        mine = fitting.shard_indices(sizes, rank, world)
+        # stand-ins for each box's energy and per-type gradient
+        energies = [float(sizes[k]) * 0.5 for k in mine]
+        grad = sum((np.full((2, 24), float(k)) for k in mine), np.zeros((2, 24)))
+        e, g = fitting.allreduce_results(energies, mine, len(sizes), grad)
+        out.put((rank, e.tolist(), g.tolist()))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_batch_allreduce_gloo():
+    """Two ranks (gloo, CPU) split 10 boxes and combine energies and gradients."""
+    import multiprocessing as mp
+    import socket
+    ctx = mp.get_context("spawn")
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_sharded_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    sizes = np.arange(10) * 7 + 3
+    for rank, e, g in res:
+        assert np.allclose(e, sizes * 0.5)
+        assert np.allclose(g, np.full((2, 24), float(sum(range(10)))))
