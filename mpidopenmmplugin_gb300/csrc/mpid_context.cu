@@ -1379,49 +1379,74 @@ struct Context {
         return d;
     }
 
+    // Sub-ranges per work item for a gradient launch whose busy items number `items`:
+    // enough warps to cover every SM several times (a power of two dividing the chunk).
+    int gradient_split(long long items) const {
+        int split = 1;
+        while (split < chunk && items * split < 16LL * 152) split *= 2;
+        return split;
+    }
+    int gradient_blocks(int split) const { return std::max(1, nblk((long long) pair_tasks() * split, kWarpsPerBlock)); }
+
     // dE/d(molecular-frame polarisability X Y Z, Thole width) of every atom for the last
     // evaluation (Mutual, Direct).
-    template <typename real>
-    void polarization_gradients(Engine<real>& e, double* host) {
-        cudaStream_t st = stream;
-        polFx.alloc((size_t) 2 * npad);
-        polOut.alloc((size_t) 4 * n);
-        CUDA_CHECK(cudaMemsetAsync(polFx.p, 0, (size_t) 2 * npad * 8, st));
-        launch(k_polarization_gradient<real>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(),
-               (const real*) e.mu.p, set.polarization_type == MPID_MUTUAL ? 1 : 0, polFx.p);
-        launch(k_polarization_gradient_finish<real>, nblk(n, 128), 128, 0, st, n, npad, (const int*) order.p, mol(),
-               (const double*) pos.p, (const unsigned long long*) polFx.p, (const real*) e.mu.p, polOut.p);
-        CUDA_CHECK(cudaGetLastError());
-        CUDA_CHECK(cudaMemcpyAsync(host, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaStreamSynchronize(st));
-    }
     void polarization_gradients(double* host) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
         if (set.polarization_type == MPID_EXTRAPOLATED)
             throw Error(MPID_ERR_INVALID,
                         "polarizability and Thole gradients need stationary induced dipoles (Mutual or Direct)");
-        polarization_gradients(gradient_engine(), host);
+        Engine<double>& d = gradient_engine();
+        cudaStream_t st = stream;
+        polFx.alloc((size_t) 2 * npad);
+        polOut.alloc((size_t) 4 * n);
+        CUDA_CHECK(cudaMemsetAsync(polFx.p, 0, (size_t) 2 * npad * 8, st));
+        const int mutual = set.polarization_type == MPID_MUTUAL ? 1 : 0;
+        const int sL = gradient_split((long long) ntiles * nchunksL), sS = gradient_split((long long) ntiles * nchunksS);
+        const int sA = gradient_split(pair_tasks());
+        if (mixed) {
+            launch(k_polarization_gradient<float>, gradient_blocks(sL), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+                   ef->arrays(), (const float*) ef->mu.p, mutual, polFx.p, kSegErfc, sL);
+            launch(k_polarization_gradient<double>, gradient_blocks(sS), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+                   d.arrays(), (const double*) d.mu.p, mutual, polFx.p, kSegQuad, sS);
+        } else {
+            launch(k_polarization_gradient<double>, gradient_blocks(sA), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+                   d.arrays(), (const double*) d.mu.p, mutual, polFx.p, kSegAll, sA);
+        }
+        launch(k_polarization_gradient_finish<double>, nblk(n, 32), 32, 0, st, n, npad, (const int*) order.p, mol(),
+               (const double*) pos.p, (const unsigned long long*) polFx.p, (const double*) d.mu.p, polOut.p);
+        CUDA_CHECK(cudaGetLastError());
+        CUDA_CHECK(cudaMemcpyAsync(host, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
     }
 
     // dE/d(molecular-frame multipole parameters) of every atom for the last evaluation.
-    template <typename real>
-    void parameter_gradients(Engine<real>& e, double* host) {
+    // The real-space sum runs in FP64 except, on the mixed path, over the erfc segment of
+    // the lists (alpha r >= 1.5, no excluded pairs), which runs in FP32.
+    void parameter_gradients(double* host) {
+        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+        Engine<double>& d = gradient_engine();
         cudaStream_t st = stream;
         gradFx.alloc((size_t) 20 * npad);
         gradOut.alloc((size_t) 20 * n);
         CUDA_CHECK(cudaMemsetAsync(gradFx.p, 0, (size_t) 20 * npad * 8, st));
-        launch(k_multipole_gradient<real>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(),
-               (const real*) e.mu.p, gradFx.p);
-        launch(k_gradient_finish<real>, nblk(n, 128), 128, 0, st, n, npad, box, usePme ? set.ewald_alpha : 0.0,
+        const int sL = gradient_split((long long) ntiles * nchunksL), sS = gradient_split((long long) ntiles * nchunksS);
+        const int sA = gradient_split(pair_tasks());
+        if (mixed) {
+            launch(k_multipole_gradient<float>, gradient_blocks(sL), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+                   ef->arrays(), (const float*) ef->mu.p, gradFx.p, kSegErfc, sL);
+            launch(k_multipole_gradient<double>, gradient_blocks(sS), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+                   d.arrays(), (const double*) d.mu.p, gradFx.p, kSegQuad, sS);
+        } else {
+            launch(k_multipole_gradient<double>, gradient_blocks(sA), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+                   d.arrays(), (const double*) d.mu.p, gradFx.p, kSegAll, sA);
+        }
+        launch(k_gradient_finish<double>, nblk(n, 32), 32, 0, st, n, npad, box, usePme ? set.ewald_alpha : 0.0,
                usePme ? 1 : 0, (const int*) order.p, mol(), (const double*) pos.p, (const unsigned long long*) gradFx.p,
-               (const real*) e.phiP.p, (const real*) e.phiD.p, (const double*) mom64.p, (const real*) e.mu.p, gradOut.p);
+               (const double*) d.phiP.p, (const double*) d.phiD.p, (const double*) mom64.p, (const double*) d.mu.p,
+               gradOut.p);
         CUDA_CHECK(cudaGetLastError());
         CUDA_CHECK(cudaMemcpyAsync(host, gradOut.p, (size_t) 20 * n * 8, cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
-    }
-    void parameter_gradients(double* host) {
-        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
-        parameter_gradients(gradient_engine(), host);
     }
 
     void get_dipoles(int which, double* host) {

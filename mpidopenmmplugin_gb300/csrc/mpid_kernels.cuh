@@ -480,6 +480,24 @@ struct PairTask {
         k1 = min(k0 + nl.chunk, quad ? nl.countS[si] : nl.countL[si]);
         return true;
     }
+    // The same items, each cut into `split` consecutive sub-ranges of chunk / split
+    // entries (split divides the chunk), one warp per sub-range: more warps for kernels
+    // whose per-pair work is long (the FP64 gradient passes of small systems).
+    __device__ __forceinline__ bool init_split(const NbrList& nl, int split) {
+        const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        const int item = w / split, part = w - item * split;
+        const int nLong = nl.ntiles * nl.nchunksL;
+        lane = threadIdx.x & 31;
+        quad = item >= nLong;
+        const int wq = quad ? item - nLong : item, nch = quad ? nl.nchunksS : nl.nchunksL;
+        I = nch > 0 ? wq / nch : nl.ntiles;
+        const int span = nl.chunk / split;
+        k0 = (wq - I * nch) * nl.chunk + part * span;
+        si = I * 32 + lane;
+        if (I >= nl.ntiles || k0 >= (quad ? nl.tmaxS[I] : nl.tmaxL[I])) return false;
+        k1 = min(k0 + span, quad ? nl.countS[si] : nl.countL[si]);
+        return true;
+    }
 };
 
 template <typename real>
@@ -1186,11 +1204,19 @@ __device__ __forceinline__ void gradient_loop(const NbrList& nl, const AtomArray
     }
 }
 
+// Segments of the neighbour lists a gradient launch covers (bit 0: erfc segment, bit 1:
+// quadrature segment).  The mixed path runs the erfc segment in FP32 and the quadrature
+// segment, which holds the excluded and short pairs whose terms cancel against the
+// reciprocal potentials, in FP64.
+constexpr int kSegErfc = 1, kSegQuad = 2, kSegAll = 3;
+
 template <typename real>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_multipole_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ gfx) {
+k_multipole_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ gfx,
+                     int segments, int split) {
     PairTask t;
-    if (!t.init(nl)) return;
+    if (!t.init_split(nl, split)) return;
+    if (!(segments & (t.quad ? kSegQuad : kSegErfc))) return;
     const int origI = at.orig[t.si];
     if (origI < 0) return;
     real G[20];
@@ -1310,28 +1336,29 @@ __global__ void k_gradient_finish(int n, int npad, BoxDev box, double alpha, int
             }
         o[4 + c] = k == mm ? LQkm : LQkm + LQmk;
     }
+    // full-entry lab octopole derivative (symmetric), rotated one index at a time; the
+    // molecular-frame tensor is symmetric too, so an API component is its entry times
+    // the number of distinct orderings of its index triple
+    double GO[3][3][3], W1[3][3][3];
+    for (int x = 0; x < 3; ++x)
+        for (int y = 0; y < 3; ++y)
+            for (int z = 0; z < 3; ++z) {
+                const int w = (x == y && y == z) ? 1 : ((x == y || y == z || x == z) ? 3 : 6);
+                GO[x][y][z] = g[10 + o10(x, y, z)] / w;
+            }
+    for (int k = 0; k < 3; ++k)
+        for (int y = 0; y < 3; ++y)
+            for (int z = 0; z < 3; ++z) W1[k][y][z] = R[k][0] * GO[0][y][z] + R[k][1] * GO[1][y][z] + R[k][2] * GO[2][y][z];
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l)
+            for (int z = 0; z < 3; ++z) GO[k][l][z] = R[l][0] * W1[k][0][z] + R[l][1] * W1[k][1][z] + R[l][2] * W1[k][2][z];
     const int OAPI[10][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {1, 1, 1}, {0, 0, 2},
                              {0, 1, 2}, {1, 1, 2}, {0, 2, 2}, {1, 2, 2}, {2, 2, 2}};
     for (int c = 0; c < 10; ++c) {
-        // sum over the distinct permutations of the API index triple
         const int a0 = OAPI[c][0], a1 = OAPI[c][1], a2i = OAPI[c][2];
-        const int perm[6][3] = {{a0, a1, a2i}, {a0, a2i, a1}, {a1, a0, a2i}, {a1, a2i, a0}, {a2i, a0, a1}, {a2i, a1, a0}};
-        double acc = 0.0;
-        for (int p = 0; p < 6; ++p) {
-            bool dup = false;
-            for (int q = 0; q < p; ++q)
-                dup = dup || (perm[q][0] == perm[p][0] && perm[q][1] == perm[p][1] && perm[q][2] == perm[p][2]);
-            if (dup) continue;
-            const int k = perm[p][0], l = perm[p][1], mm = perm[p][2];
-            for (int x = 0; x < 3; ++x)
-                for (int y = 0; y < 3; ++y)
-                    for (int z = 0; z < 3; ++z) {
-                        const int oc = o10(x, y, z);
-                        const int w = (x == y && y == z) ? 1 : ((x == y || y == z || x == z) ? 3 : 6);
-                        acc += R[k][x] * R[l][y] * R[mm][z] * g[10 + oc] / w;
-                    }
-        }
-        o[10 + c] = acc;
+        const int nperm = (a0 == a1 && a1 == a2i) ? 1 : ((a0 == a1 || a1 == a2i || a0 == a2i) ? 3 : 6);
+        const double LO = R[a2i][0] * GO[a0][a1][0] + R[a2i][1] * GO[a0][a1][1] + R[a2i][2] * GO[a0][a1][2];
+        o[10 + c] = nperm * LO;
     }
     if (flip) {  // the flipped parameters enter with the opposite sign
         o[2] = -o[2];
@@ -1418,9 +1445,10 @@ __device__ __forceinline__ void polarization_loop(const NbrList& nl, const AtomA
 template <typename real>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 k_polarization_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, int mutual,
-                        unsigned long long* __restrict__ gfx) {
+                        unsigned long long* __restrict__ gfx, int segments, int split) {
     PairTask t;
-    if (!t.init(nl)) return;
+    if (!t.init_split(nl, split)) return;
+    if (!(segments & (t.quad ? kSegQuad : kSegErfc))) return;
     const int origI = at.orig[t.si];
     if (origI < 0) return;
     real W = real(0), Z = real(0);

@@ -1038,7 +1038,8 @@ MPID_HD void cartesian_potential(const real* phi, const real A[3][3], real& Phi0
                                  real Phi3[3][3][3]) {
     Phi0 = phi[0];
     for (int i = 0; i < 3; ++i) Phi1[i] = A[0][i] * phi[1] + A[1][i] * phi[2] + A[2][i] * phi[3];
-    real H[3][3];
+    // Phi2 = A^T H A and Phi3 = (A^T)^3 G, one index at a time (separable contraction)
+    real H[3][3], T[3][3];
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) {
             int c[3] = {0, 0, 0};
@@ -1046,13 +1047,10 @@ MPID_HD void cartesian_potential(const real* phi, const real A[3][3], real& Phi0
             H[a][b] = phi[hermite_index(c[0], c[1], c[2])];
         }
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            real acc = real(0);
-            for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) acc += A[a][i] * A[b][j] * H[a][b];
-            Phi2[i][j] = acc;
-        }
-    real G[3][3][3];
+        for (int b = 0; b < 3; ++b) T[i][b] = A[0][i] * H[0][b] + A[1][i] * H[1][b] + A[2][i] * H[2][b];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Phi2[i][j] = A[0][j] * T[i][0] + A[1][j] * T[i][1] + A[2][j] * T[i][2];
+    real G[3][3][3], U[3][3][3];
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b)
             for (int c = 0; c < 3; ++c) {
@@ -1061,14 +1059,15 @@ MPID_HD void cartesian_potential(const real* phi, const real A[3][3], real& Phi0
                 G[a][b][c] = phi[hermite_index(n[0], n[1], n[2])];
             }
     for (int i = 0; i < 3; ++i)
+        for (int b = 0; b < 3; ++b)
+            for (int c = 0; c < 3; ++c) U[i][b][c] = A[0][i] * G[0][b][c] + A[1][i] * G[1][b][c] + A[2][i] * G[2][b][c];
+    for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
-            for (int k = 0; k < 3; ++k) {
-                real acc = real(0);
-                for (int a = 0; a < 3; ++a)
-                    for (int b = 0; b < 3; ++b)
-                        for (int c = 0; c < 3; ++c) acc += A[a][i] * A[b][j] * A[c][k] * G[a][b][c];
-                Phi3[i][j][k] = acc;
-            }
+            for (int c = 0; c < 3; ++c) G[i][j][c] = A[0][j] * U[i][0][c] + A[1][j] * U[i][1][c] + A[2][j] * U[i][2][c];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k)
+                Phi3[i][j][k] = A[0][k] * G[i][j][0] + A[1][k] * G[i][j][1] + A[2][k] * G[i][j][2];
 }
 
 // Torque on a multipole (q, dipole d, Q6, O10) in an external potential with
