@@ -434,13 +434,18 @@ struct Context {
         forceFx.alloc(3 * (size_t) npad); torqueFx.alloc(3 * (size_t) npad);
         mom64.alloc(20 * (size_t) npad); prm64.alloc(2 * (size_t) n);
         scaledPairs.alloc(1); scaledScale.alloc(1); scaledPartial.alloc(1);
-        energyPartial.alloc(nblk(npad, 256)); energyOut.alloc(4);
+        energyPartial.alloc(nblk(npad, 32)); energyOut.alloc(4);
         forcesOut.alloc(3 * (size_t) n);
         partial.alloc(2 * (size_t) nblk(npad, 256)); red.alloc(4); sc.alloc(8);
         iter.alloc(1); done.alloc(1);
         counters.alloc(3);
         CUDA_CHECK(cudaMemset(counters.p, 0, 3 * sizeof(unsigned)));
-        CUDA_CHECK(cudaStreamCreateWithFlags(&pmeStream, cudaStreamNonBlocking));
+        // The reciprocal-space chain (spread, FFTs, convolution, gather) is the longer of
+        // the two branches of every field evaluation, so its kernels get the highest
+        // stream priority and take SMs ahead of the wide real-space pair kernels.
+        int prLeast = 0, prGreatest = 0;
+        CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&prLeast, &prGreatest));
+        CUDA_CHECK(cudaStreamCreateWithPriority(&pmeStream, cudaStreamNonBlocking, prGreatest));
         CUDA_CHECK(cudaStreamCreateWithFlags(&hostStream, cudaStreamNonBlocking));
         CUDA_CHECK(cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming));
         CUDA_CHECK(cudaEventCreateWithFlags(&evJoin, cudaEventDisableTiming));
@@ -661,7 +666,8 @@ struct Context {
         if (entries > ((size_t) 1 << 34)) throw Error(MPID_ERR_INVALID, "neighbour list would exceed 64 GB");
         list.alloc(entries);
         listEntries = (long long) entries;
-        energyBlocks.alloc((size_t) ntiles * (cap / chunk + 2));
+        // one entry per warp task; split tasks stay below twice the split target
+        energyBlocks.alloc(std::max((size_t) ntiles * (cap / chunk + 2), (size_t) 4 * 152 * 64));
     }
 
     static void upload(DBuf<float>& d, const std::vector<float>& h) {
@@ -730,6 +736,7 @@ struct Context {
         c.tmaxS = tmaxS.p;
         c.list = list.p;
         c.usePbc = usePme ? 1 : 0;
+        c.split = 1;
         c.cf = pair_consts_host<float>();
         c.cd = pair_consts_host<double>();
         c.covOff = covOff.p;
@@ -741,6 +748,23 @@ struct Context {
     // warp tasks (tile, chunk) of the pair kernels
     int pair_tasks() const { return ntiles * (nchunksL + nchunksS); }
     int pair_blocks() const { return std::max(1, nblk(pair_tasks(), kWarpsPerBlock)); }
+    // The field and energy pair kernels cut each work item into sub-ranges until the
+    // launch holds two full waves of warps (152 SMs x 64 resident warps): their per-pair
+    // gathers are latency-bound, and one work item per warp leaves SMs idle (most of
+    // them below a few thousand atoms).  The lists and results are the same.  Measured
+    // on the 24,000-atom box: the CG pair kernel goes from 87 to 75 us per launch
+    // (split 4); on a 660-atom box the FP32 CG field from 41 to 10 us.
+    int field_split() const {
+        int split = 1;
+        while (split < chunk && (long long) pair_tasks() * split < 2LL * 152 * 64) split *= 2;
+        return split;
+    }
+    NbrList field_list() const {
+        NbrList c = nbr_list();
+        c.split = field_split();
+        return c;
+    }
+    int field_blocks() const { return gradient_blocks(field_split()); }
 
     // Spatial sort (PME) or caller order (no cutoff), then tile centres and extents.
     void sort_and_tiles() {
@@ -848,7 +872,7 @@ struct Context {
             timer.end(ps);
         }
         timer.begin(ST_FIXED_REAL, st);
-        launch(k_fixed_field<real>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), e.fieldFx.p);
+        launch(k_fixed_field<real>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), e.fieldFx.p);
         timer.end(st);
         if (usePme) join_pme();
         launch(k_record_fixed<real>, nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
@@ -882,14 +906,14 @@ struct Context {
         if (mixed && sizeof(real) == 8) {
             // residual refinement: real-space part in double-float on the FP32 pipes
             launch(k_to_df, nblk(3LL * npad, 256), 256, 0, st, 3 * npad, (const double*) mu, muDF.p);
-            launch(k_dipole_field_df, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), df_radial(), df_atoms(),
+            launch(k_dipole_field_df, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), df_radial(), df_atoms(),
                    (const int*) e.orig.p, e.fieldFx.p);
         } else if (G) {
             CUDA_CHECK(cudaMemsetAsync(e.gradFx.p, 0, 6 * (size_t) npad * 8, st));
-            launch(k_dipole_field<real, true, sizeof(real) == 8>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), mu, e.fieldFx.p,
+            launch(k_dipole_field<real, true, sizeof(real) == 8>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), mu, e.fieldFx.p,
                                                                                      e.gradFx.p, skip);
         } else {
-            launch(k_dipole_field<real, false, sizeof(real) == 8>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), e.arrays(), mu,
+            launch(k_dipole_field<real, false, sizeof(real) == 8>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), mu,
                                                                                       e.fieldFx.p, nullptr, skip);
         }
         timer.end(st);
@@ -920,10 +944,10 @@ struct Context {
         }
         timer.begin(ST_DIPOLE_REAL, st);
         if (packed)
-            launch(k_dipole_field_packed, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(), (const float4*) pack0.p,
+            launch(k_dipole_field_packed, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), (const float4*) pack0.p,
                    (const float4*) pack1.p, npad, (const int*) e.orig.p, e.fieldFx.p, (const int*) done.p);
         else
-            launch(k_dipole_field<real, false, sizeof(real) == 8>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+            launch(k_dipole_field<real, false, sizeof(real) == 8>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(),
                    e.arrays(), (const real*) e.sp.p, e.fieldFx.p, (unsigned long long*) nullptr, (const int*) done.p);
         timer.end(st);
         if (usePme) join_pme();
@@ -1098,20 +1122,21 @@ struct Context {
         }
         CUDA_CHECK(cudaMemsetAsync(forceFx.p, 0, 3 * (size_t) npad * 8, st));
         CUDA_CHECK(cudaMemsetAsync(torqueFx.p, 0, 3 * (size_t) npad * 8, st));
-        const int eb = pair_tasks();
+        const NbrList tc = field_list();
+        const int eb = pair_tasks() * tc.split;
+        if ((size_t) eb > energyBlocks.n) throw Error(MPID_ERR_CUDA, "energy partials too small");
         CUDA_CHECK(cudaMemsetAsync(energyBlocks.p, 0, eb * sizeof(double), st));
         timer.begin(ST_PAIR, st);
         const bool exact = (set.flags & MPID_FLAG_EXACT_ANISO_TORQUE) != 0;
-        const NbrList tc = nbr_list();
         const AtomArrays<real> aa = e.arrays();
         if (set.polarization_type == MPID_MUTUAL && !exact)
-            launch(k_electrostatics<real, true, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+            launch(k_electrostatics<real, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                              torqueFx.p, energyBlocks.p);
         else if (set.polarization_type == MPID_MUTUAL)
-            launch(k_electrostatics<real, true, false>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+            launch(k_electrostatics<real, true, false>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
         else
-            launch(k_electrostatics<real, false, true>, pair_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+            launch(k_electrostatics<real, false, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
         timer.end(st);
         if (usePme) join_pme();
@@ -1127,8 +1152,10 @@ struct Context {
             opt.E = ptE;
             opt.G = ptG;
         }
-        const int nb = nblk(npad, 256);
-        launch(k_recip_self<real>, nb, 256, 0, st, n, npad, box, set.ewald_alpha, set.polarization_type,
+        // per-atom work is long: blocks small enough that a small system spans the SMs
+        const int rb = npad >= 256 * 2 * 152 ? 256 : (npad >= 128 * 152 ? 128 : (npad >= 64 * 152 ? 64 : 32));
+        const int nb = nblk(npad, rb);
+        launch(k_recip_self<real>, nb, rb, 0, st, n, npad, box, set.ewald_alpha, set.polarization_type,
                                                 usePme ? e.phiP.p : nullptr, e.phiD.p, e.mu.p, e.arrays(), mom64.p, opt,
                                                 forceFx.p, torqueFx.p, energyPartial.p);
         launch(k_reduce_partials, 1, 1024, 0, st, nb, 1, energyPartial.p, energyOut.p, nullptr);

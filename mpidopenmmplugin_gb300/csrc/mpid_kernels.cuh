@@ -448,6 +448,7 @@ struct NbrList {
     const int* tmaxS;
     const unsigned* list;
     int usePbc;
+    int split;                // sub-ranges per work item (PairTask::init), a power of two dividing chunk
     PairConsts<float> cf;
     PairConsts<double> cd;
     const int* covOff;
@@ -464,22 +465,12 @@ template <> __device__ __forceinline__ const PairConsts<double>& pair_consts<dou
 struct PairTask {
     int I, k0, k1, lane, si;
     bool quad;
-    __device__ __forceinline__ int tasks(const NbrList& nl) const { return nl.ntiles * (nl.nchunksL + nl.nchunksS); }
+    __device__ __forceinline__ int tasks(const NbrList& nl) const {
+        return nl.ntiles * (nl.nchunksL + nl.nchunksS) * nl.split;
+    }
     // Work items: all erfc-segment items (tile-major), then all quadrature-segment items,
     // so that resident warps mostly run the same branch of the code.
-    __device__ __forceinline__ bool init(const NbrList& nl) {
-        const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-        const int nLong = nl.ntiles * nl.nchunksL;
-        lane = threadIdx.x & 31;
-        quad = w >= nLong;
-        const int wq = quad ? w - nLong : w, nch = quad ? nl.nchunksS : nl.nchunksL;
-        I = nch > 0 ? wq / nch : nl.ntiles;
-        k0 = (wq - I * nch) * nl.chunk;
-        si = I * 32 + lane;
-        if (I >= nl.ntiles || k0 >= (quad ? nl.tmaxS[I] : nl.tmaxL[I])) return false;
-        k1 = min(k0 + nl.chunk, quad ? nl.countS[si] : nl.countL[si]);
-        return true;
-    }
+    __device__ __forceinline__ bool init(const NbrList& nl) { return init_split(nl, nl.split); }
     // The same items, each cut into `split` consecutive sub-ranges of chunk / split
     // entries (split divides the chunk), one warp per sub-range: more warps for kernels
     // whose per-pair work is long (the FP64 gradient passes of small systems).
@@ -917,7 +908,7 @@ __device__ __forceinline__ void electrostatics_loop(const NbrList& nl, const Ato
     }
 }
 
-// out: force[3][npad], torque[3][npad] fixed point; energy[task] (already x kElectric).
+// out: force[3][npad], torque[3][npad] fixed point; energy[warp task] (already x kElectric).
 template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, sizeof(real) == 4 ? 4 : 1)
 k_electrostatics(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ force,
