@@ -1,0 +1,98 @@
+"""The OpenMM CUDA-platform adapter (mpidopenmmplugin_gb300/openmm) run outside OpenMM.
+
+tests/openmm_stub/fake_openmm.cu defines the OpenMM members the adapter calls on a fake
+CUDA context: posq in a shuffled atom order (as OpenMM's reordering leaves it), OpenMM's
+fixed-point force buffer and its atom index.  The adapter gathers positions, evaluates
+through the C ABI and scatters forces; the results must equal a direct MPIDContext
+evaluation at the same positions (double posq: the FP64 path; float posq: the mixed path
+at the float-rounded positions), up to the 2^-32 quantum of the force buffer.
+"""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from mpidopenmmplugin_gb300 import MPIDContext, MPIDForce, synthetic
+from mpidopenmmplugin_gb300.context import load_library
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    lib = load_library()  # builds libmpid_gb300.so if needed
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    libdir = os.path.join(ROOT, "mpidopenmmplugin_gb300", "_lib")
+    out = str(tmp_path_factory.mktemp("adapter") / "libadapter_harness.so")
+    cmd = [nvcc, "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-fPIC", "-shared",
+           "-I", os.path.join(ROOT, "tests", "openmm_stub", "include"), "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(ROOT, "mpidopenmmplugin_gb300", "openmm"),
+           os.path.join(ROOT, "tests", "openmm_stub", "fake_openmm.cu"),
+           os.path.join(ROOT, "mpidopenmmplugin_gb300", "openmm", "GB300MPIDKernels.cu"),
+           "-o", out, "-L", libdir, "-lmpid_gb300", "-Xlinker", "-rpath", "-Xlinker", libdir]
+    subprocess.run(cmd, check=True, capture_output=True)
+    h = ctypes.CDLL(out)
+    h.harness_run.restype = ctypes.c_int
+    return h
+
+
+def _p(a, t=ctypes.c_double):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def run_adapter(h, f, pos, box, perm, dbl):
+    a = f.arrays()
+    n = f.getNumMultipoles()
+    alpha, nx, ny, nz = f.getPMEParameters()
+    coeffs = list(f.getExtrapolationCoefficients())
+    si = np.array([f.getNonbondedMethod(), f.getPolarizationType(), f.getPmeBSplineOrder(),
+                   f.getMutualInducedMaxIterations(), nx, ny, nz, len(coeffs)], dtype=np.int32)
+    sd = np.array([f.getCutoffDistance(), alpha, f.getMutualInducedTargetEpsilon(), f.getDefaultTholeWidth(),
+                   f.get14ScaleFactor()] + coeffs)
+    energy = np.zeros(1)
+    forces = np.zeros((n, 3))
+    induced = np.zeros((n, 3))
+    msg = ctypes.create_string_buffer(512)
+    i32 = ctypes.c_int
+    arrs = [np.ascontiguousarray(a[k], dtype=np.float64) for k in ("charge", "dipole", "quadrupole", "octopole")]
+    iarr = [np.ascontiguousarray(a[k], dtype=np.int32) for k in ("axis_type", "atom_z", "atom_x", "atom_y")]
+    th = np.ascontiguousarray(a["thole"], dtype=np.float64)
+    pol = np.ascontiguousarray(a["polarity"], dtype=np.float64)
+    off = np.ascontiguousarray(a["cov_offsets"], dtype=np.int32)
+    idx = np.ascontiguousarray(a["cov_index"], dtype=np.int32) if len(a["cov_index"]) else np.zeros(1, np.int32)
+    posc = np.ascontiguousarray(pos, dtype=np.float64)
+    boxc = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+    permc = np.ascontiguousarray(perm, dtype=np.int32)
+    rc = h.harness_run(n, int(dbl), _p(permc, i32), _p(posc), _p(boxc), _p(si, i32), _p(sd), *[_p(x) for x in arrs],
+                       *[_p(x, i32) for x in iarr], _p(th), _p(pol), _p(off, i32), _p(idx, i32), _p(energy),
+                       _p(forces), _p(induced), msg)
+    assert rc == 0, msg.value.decode()
+    return energy[0], forces, induced
+
+
+@pytest.mark.parametrize("pol", [MPIDForce.Mutual, MPIDForce.Extrapolated])
+def test_adapter_matches_direct_evaluation(harness, pol):
+    f, pos, box = synthetic.workload("water648", polarization=pol, order=5)
+    n = f.getNumMultipoles()
+    perm = np.random.default_rng(3).permutation(n)
+    # double posq: the FP64 path at the same positions
+    e, forces, mu = run_adapter(harness, f, pos, box, perm, dbl=True)
+    ctx = MPIDContext(f, precision="double")
+    e_ref, f_ref = ctx.evaluate(pos, box)
+    mu_ref = ctx.getInducedDipoles()
+    assert abs(e - e_ref) <= 1e-10 * abs(e_ref)
+    assert np.abs(forces - f_ref).max() <= 1e-9 * max(1.0, np.abs(f_ref).max())
+    assert np.abs(mu - mu_ref).max() <= 1e-10 * np.abs(mu_ref).max()
+    # float posq: the mixed path at the float-rounded positions
+    e, forces, mu = run_adapter(harness, f, pos, box, perm, dbl=False)
+    pos32 = pos.astype(np.float32).astype(np.float64)
+    ctx = MPIDContext(f, precision="mixed")
+    e_ref, f_ref = ctx.evaluate(pos32, box)
+    assert e == e_ref
+    assert np.abs(forces - f_ref).max() <= 2.0 ** -31
+    assert np.array_equal(mu, ctx.getInducedDipoles())
