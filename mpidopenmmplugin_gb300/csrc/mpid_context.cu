@@ -1257,11 +1257,20 @@ struct Context {
             prepare_engine(e, true);
             launch(k_pack_atoms, nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
                    pack0.p);
-            launch_lists(e);
             if (ed) {
+                // the FP64 engine of the residual check is prepared on the check's stream,
+                // beside the list build (it is first read by the check)
+                CUDA_CHECK(cudaEventRecord(evRefStart, st));
+                CUDA_CHECK(cudaStreamWaitEvent(refStream, evRefStart, 0));
+                std::swap(stream, refStream);
+                std::swap(pmeStream, refPmeStream);
                 prepare_engine(*ed, false);
-                launch(k_df_atoms, nblk(npad, 128), 128, 0, st, npad, ed->off.p, ed->prm.p, offDF.p, tholeDF.p, dampDF.p);
+                launch(k_df_atoms, nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p, tholeDF.p,
+                       dampDF.p);
+                std::swap(stream, refStream);
+                std::swap(pmeStream, refPmeStream);
             }
+            launch_lists(e);
             finish_lists(e);
             stats.max_neighbours = lastMaxList;
             timer.end(st);

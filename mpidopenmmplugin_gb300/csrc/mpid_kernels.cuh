@@ -318,7 +318,9 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
             int* __restrict__ countS, int* __restrict__ loL, int* __restrict__ loS, int* __restrict__ tmaxL,
             int* __restrict__ tmaxS, unsigned* __restrict__ list, int* __restrict__ maxCounts) {
     constexpr int kCache = 8;
+    constexpr int kMasks = 16;  // tile pairs per warp whose hits the first pass keeps for the second
     __shared__ int cnt[kListWarps][4][32];  // nL, nS, lowL, lowS per warp and lane
+    __shared__ unsigned hits[kListWarps][kMasks][32], near[kListWarps][kMasks][32];
     const int I = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (I >= ntiles) return;
     const int si = I * 32 + lane;
@@ -345,6 +347,34 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
     for (int pass = 0; pass < 2; ++pass) {
         int nL = 0, nS = 0, lowL = 0, lowS = 0;
         for (int s = s0; s < s1; ++s) {
+            if (pass == 1 && s - s0 < kMasks) {
+                // second pass over a kept tile pair: only its hits, in the same order
+                if (!fits) continue;
+                const int J = tileJ[(size_t) I * tcap + s] & 0x7fffffff;
+                unsigned m = hits[w][s - s0][lane];
+                const unsigned q = near[w][s - s0][lane];
+                while (m) {
+                    const int jl = __ffs(m) - 1;
+                    m &= m - 1;
+                    const int oj = orig[J * 32 + jl];
+                    unsigned flag = 0;
+#pragma unroll
+                    for (int k = 0; k < kCache; ++k)
+                        if (pJ[k] == oj) flag = pF[k];
+                    if (ce - cb > kCache)
+                        for (int k = cb + kCache; k < ce; ++k)
+                            if (covJ[k] == oj) {
+                                flag = scale_flag(covS[k]);
+                                break;
+                            }
+                    const bool quad = usePme && (((q >> jl) & 1u) || flag == 1u);
+                    const unsigned code = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
+                    out[(size_t) (quad ? cap - 1 - (baseS + nS) : baseL + nL) * 32] = code;
+                    if (quad) ++nS; else ++nL;
+                }
+                continue;
+            }
+            unsigned hitMask = 0, nearMask = 0;
             const int Jw = tileJ[(size_t) I * tcap + s];
             const int J = Jw & 0x7fffffff;
             const bool wrap = Jw < 0;
@@ -376,8 +406,14 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
                     const unsigned code = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
                     out[(size_t) (quad ? cap - 1 - (baseS + nS) : baseL + nL) * 32] = code;
                 }
+                hitMask |= 1u << jl;
+                if (r2 < quadR2) nearMask |= 1u << jl;
                 const int low = J * 32 + jl < si;
                 if (quad) { ++nS; lowS += low; } else { ++nL; lowL += low; }
+            }
+            if (pass == 0 && s - s0 < kMasks) {
+                hits[w][s - s0][lane] = hitMask;
+                near[w][s - s0][lane] = nearMask;
             }
         }
         if (pass == 0) {
