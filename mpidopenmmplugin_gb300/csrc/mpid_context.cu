@@ -1185,13 +1185,13 @@ struct Context {
         const bool exact = (set.flags & MPID_FLAG_EXACT_ANISO_TORQUE) != 0;
         const AtomArrays<real> aa = e.arrays();
         if (set.polarization_type == MPID_MUTUAL && !exact)
-            launch(k_electrostatics<real, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+            launch(k_electrostatics<real, true, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                              torqueFx.p, energyBlocks.p);
         else if (set.polarization_type == MPID_MUTUAL)
-            launch(k_electrostatics<real, true, false>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+            launch(k_electrostatics<real, true, false, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
         else
-            launch(k_electrostatics<real, false, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+            launch(k_electrostatics<real, false, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
         timer.end(st);
         if (usePme) join_pme();

@@ -904,13 +904,17 @@ struct KahanSum {
 };
 
 // Real-space energy, forces and torques (MPIDReferenceForce.cpp:4335-4920).  Each lane
-// evaluates its atom's pairs (both atoms of a pair evaluate it), adds force and torque
-// on its own atom, and counts the energy of pairs with i < j; pairs of covalent scale
-// other than 1 leave their energy to k_scaled_pair_energy.
-template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE, bool QUAD>
+// evaluates its atom's pairs and adds force and torque on its own atom; with HALF only
+// the pairs with j > i (sorted order), adding the pair's force and torque on j with
+// fixed-point atomics (measured on the 24,000-atom box: FP32 0.52 -> 0.50 ms, FP64 path
+// 8 % faster overall; the same for the CG field kernel, whose pairs are cheap, was
+// slower: 87 -> 103 us).  The energy of pairs with i < j is counted; pairs of covalent
+// scale other than 1 leave their energy to k_scaled_pair_energy.
+template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE, bool QUAD, bool HALF>
 __device__ __forceinline__ void electrostatics_loop(const NbrList& nl, const AtomArrays<real>& at, const real* mu,
                                                     const PairTask& t, int origI, real* accF, real* accT,
-                                                    KahanSum<real>& eSum) {
+                                                    KahanSum<real>& eSum, unsigned long long* __restrict__ force,
+                                                    unsigned long long* __restrict__ torque) {
     const PairConsts<real>& pc = pair_consts<real>(nl);
     const int npad = at.npad, si = t.si;
     const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
@@ -918,7 +922,8 @@ __device__ __forceinline__ void electrostatics_loop(const NbrList& nl, const Ato
     LabMoments<real> mi;
     load_moments(at.mom, npad, si, mi);
     const typename Vec4<real>::type pi = at.prm[si];
-    for (int k = t.k0; k < t.k1; ++k) {
+    const int kb = HALF ? max(t.k0, QUAD ? nl.loS[si] : nl.loL[si]) : t.k0;
+    for (int k = kb; k < t.k1; ++k) {
         int sj;
         unsigned flag;
         real d[3], r2;
@@ -941,11 +946,18 @@ __device__ __forceinline__ void electrostatics_loop(const NbrList& nl, const Ato
             accF[q] -= po.fJ[q];
             accT[q] += po.tI[q];
         }
+        if (HALF) {  // j > i only: the pair's force and torque on j as well
+            const real E = real(kElectric);
+            for (int q = 0; q < 3; ++q) {
+                fx_add(force + q * npad + sj, E * po.fJ[q]);
+                fx_add(torque + q * npad + sj, E * po.tJ[q]);
+            }
+        }
     }
 }
 
 // out: force[3][npad], torque[3][npad] fixed point; energy[warp task] (already x kElectric).
-template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE>
+template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE, bool HALF>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, sizeof(real) == 4 ? 4 : 1)
 k_electrostatics(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ force,
                  unsigned long long* __restrict__ torque, double* __restrict__ energy) {
@@ -957,9 +969,11 @@ k_electrostatics(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, u
     if (origI >= 0) {
         real accF[3] = {real(0), real(0), real(0)}, accT[3] = {real(0), real(0), real(0)};
         if (t.quad)
-            electrostatics_loop<real, MUTUAL, REF_ANISO_TORQUE, true>(nl, at, mu, t, origI, accF, accT, eSum);
+            electrostatics_loop<real, MUTUAL, REF_ANISO_TORQUE, true, HALF>(nl, at, mu, t, origI, accF, accT, eSum,
+                                                                             force, torque);
         else
-            electrostatics_loop<real, MUTUAL, REF_ANISO_TORQUE, false>(nl, at, mu, t, origI, accF, accT, eSum);
+            electrostatics_loop<real, MUTUAL, REF_ANISO_TORQUE, false, HALF>(nl, at, mu, t, origI, accF, accT, eSum,
+                                                                              force, torque);
         const real E = real(kElectric);
         for (int q = 0; q < 3; ++q) {
             fx_add(force + q * npad + si, E * accF[q]);
