@@ -422,6 +422,9 @@ struct Context {
                 throw Error(MPID_ERR_INVALID, "PME needs explicit ewald_alpha > 0 and grid dimensions > 0");
             if (s.pme_order != 5 && s.pme_order != 6)
                 throw Error(MPID_ERR_INVALID, "pme_order must be 5 or 6");
+            // a stencil wraps around the grid at most once
+            if (s.grid[0] < s.pme_order || s.grid[1] < s.pme_order || s.grid[2] < s.pme_order)
+                throw Error(MPID_ERR_INVALID, "each PME grid dimension must be at least the B-spline order");
             if (!(s.cutoff > 0)) throw Error(MPID_ERR_INVALID, "cutoff must be positive");
         }
         if (s.polarization_type == MPID_EXTRAPOLATED && (s.n_extrap < 1 || s.n_extrap > 8))
