@@ -163,6 +163,11 @@ def test_validation_errors_on_device():
     ctx = MPIDContext(f, precision="double")
     with pytest.raises(Exception, match="did not converge"):
         ctx.evaluate(pos, box)
+    # a B-spline stencil may wrap around the grid only once
+    alpha = f.getPMEParameters()[0]
+    f.setPMEParameters(alpha, 24, 4, 24)
+    with pytest.raises(Exception, match="at least the B-spline order"):
+        MPIDContext(f, precision="mixed")
 
 
 @pytest.mark.parametrize("precision", ["mixed", "double"])
