@@ -171,10 +171,10 @@ int mpid_get_parameter_gradients(mpid_context* ctx, const double* positions, con
  * mpid_evaluate), the energy, the multipole-parameter gradients (20n, as
  * mpid_get_parameter_gradients) and the polarisation-parameter gradients (4n per atom:
  * dE/d(molecular-frame polarisability X Y Z) in kJ/mol/nm^3 and dE/d(Thole width) in
- * kJ/mol).  Each pointer may be NULL.  The polarisation gradients need stationary induced
- * dipoles (Mutual or Direct; Extrapolated is rejected with MPID_ERR_INVALID).  A
- * polarisability of 0 gets a gradient of 0.  No reference counterpart: the fitting
- * entry point of this library. */
+ * kJ/mol).  Each pointer may be NULL.  Mutual and Direct use the stationarity of the
+ * induced dipoles; Extrapolated adds the explicit adjoint sums over its perturbation
+ * orders.  A polarisability of 0 gets a gradient of 0 (Mutual, Direct).  No reference
+ * counterpart: the fitting entry point of this library. */
 int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, const double* box, double* forces,
                                  double* energy, double* multipole_grad, double* polarization_grad);
 

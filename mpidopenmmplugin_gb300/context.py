@@ -247,7 +247,7 @@ class MPIDContext:
         """One evaluation returning (energy, forces (n, 3) or None, multipole-parameter
         gradients (n, 20) or None, polarisation gradients (n, 4) or None).  The
         polarisation gradients are dE/d(molecular-frame polarisability X Y Z) and
-        dE/d(Thole width); they need Mutual or Direct polarisation."""
+        dE/d(Thole width)."""
         pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(self.n, 3)
         b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
         f = np.zeros((self.n, 3)) if forces else None

@@ -362,6 +362,7 @@ struct Context {
     DBuf<unsigned long long> gradFx;  // [20][npad] real-space parameter gradient
     DBuf<double> gradOut;             // [n][20]
     DBuf<unsigned long long> polFx;   // [2][npad] screening sums W, Z of the polarisation gradient
+    DBuf<double> gradPtMu, gradPtE, gradEfix;  // FP64 copies of the mixed path's OPT orders and fields
     DBuf<double> polOut;              // [n][4]
     // solver scratch
     DBuf<double> partial, red, sc;
@@ -1489,28 +1490,63 @@ struct Context {
     // evaluation (Mutual, Direct).
     void polarization_gradients(double* host) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
-        if (set.polarization_type == MPID_EXTRAPOLATED)
-            throw Error(MPID_ERR_INVALID,
-                        "polarizability and Thole gradients need stationary induced dipoles (Mutual or Direct)");
         Engine<double>& d = gradient_engine();
         cudaStream_t st = stream;
         polFx.alloc((size_t) 2 * npad);
         polOut.alloc((size_t) 4 * n);
         CUDA_CHECK(cudaMemsetAsync(polFx.p, 0, (size_t) 2 * npad * 8, st));
         const int mutual = set.polarization_type == MPID_MUTUAL ? 1 : 0;
+        // Extrapolated: the perturbation orders, their fields and the permanent field
+        // (FP64 copies of the mixed path's FP32 ones for the FP64 parts)
+        OptOrders<float> optF{};
+        OptOrders<double> optD{};
+        const double* efixD = d.Efix.p;
+        const double* ptED = this->ptED.p;
+        if (set.polarization_type == MPID_EXTRAPOLATED) {
+            const int nPT = set.n_extrap;
+            optF.nPT = optD.nPT = nPT;
+            for (int i = 0; i < nPT; ++i) {
+                double c = 0.0;
+                for (int j = i; j < nPT; ++j) c += set.extrap_coeffs[j];
+                optF.cbar[i] = optD.cbar[i] = c;
+            }
+            if (mixed) {
+                const size_t n3 = 3 * (size_t) npad;
+                gradPtMu.alloc((size_t) nPT * n3);
+                gradPtE.alloc((size_t) std::max(nPT - 1, 1) * n3);
+                gradEfix.alloc(n3);
+                CUDA_CHECK(cudaMemsetAsync(gradPtMu.p, 0, (size_t) nPT * n3 * 8, st));
+                CUDA_CHECK(cudaMemsetAsync(gradPtE.p, 0, (size_t) std::max(nPT - 1, 1) * n3 * 8, st));
+                CUDA_CHECK(cudaMemsetAsync(gradEfix.p, 0, n3 * 8, st));
+                launch(k_axpy_to_double<float>, nblk((long long) nPT * n3, 256), 256, 0, st, (int) (nPT * n3),
+                       (const float*) ptMuF.p, gradPtMu.p);
+                if (nPT > 1)
+                    launch(k_axpy_to_double<float>, nblk((long long) (nPT - 1) * n3, 256), 256, 0, st,
+                           (int) ((nPT - 1) * n3), (const float*) ptEF.p, gradPtE.p);
+                launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3,
+                       (const float*) ef->Efix.p, gradEfix.p);
+                optF.mu = ptMuF.p;
+                optD.mu = gradPtMu.p;
+                efixD = gradEfix.p;
+                ptED = gradPtE.p;
+            } else {
+                optD.mu = ptMuD.p;
+            }
+        }
         const int sL = gradient_split((long long) ntiles * nchunksL), sS = gradient_split((long long) ntiles * nchunksS);
         const int sA = gradient_split(pair_tasks());
         if (mixed) {
             launch(k_polarization_gradient<float>, gradient_blocks(sL), 32 * kWarpsPerBlock, 0, st, nbr_list(),
-                   ef->arrays(), (const float*) ef->mu.p, mutual, polFx.p, kSegErfc, sL);
+                   ef->arrays(), (const float*) ef->mu.p, mutual, optF, polFx.p, kSegErfc, sL);
             launch(k_polarization_gradient<double>, gradient_blocks(sS), 32 * kWarpsPerBlock, 0, st, nbr_list(),
-                   d.arrays(), (const double*) d.mu.p, mutual, polFx.p, kSegQuad, sS);
+                   d.arrays(), (const double*) d.mu.p, mutual, optD, polFx.p, kSegQuad, sS);
         } else {
             launch(k_polarization_gradient<double>, gradient_blocks(sA), 32 * kWarpsPerBlock, 0, st, nbr_list(),
-                   d.arrays(), (const double*) d.mu.p, mutual, polFx.p, kSegAll, sA);
+                   d.arrays(), (const double*) d.mu.p, mutual, optD, polFx.p, kSegAll, sA);
         }
         launch(k_polarization_gradient_finish<double>, nblk(n, 32), 32, 0, st, n, npad, (const int*) order.p, mol(),
-               (const double*) pos.p, (const unsigned long long*) polFx.p, (const double*) d.mu.p, polOut.p);
+               (const double*) pos.p, (const unsigned long long*) polFx.p, (const double*) d.mu.p, optD, efixD, ptED,
+               polOut.p);
         CUDA_CHECK(cudaGetLastError());
         CUDA_CHECK(cudaMemcpyAsync(host, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
@@ -1744,9 +1780,6 @@ int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, con
     MPID_API_BEGIN
     if (!ctx || !positions || !box) throw Error(MPID_ERR_INVALID, "null argument");
     Context& c = ctx->ctx;
-    if (polarization_grad && c.set.polarization_type == MPID_EXTRAPOLATED)
-        throw Error(MPID_ERR_INVALID,
-                    "polarizability and Thole gradients need stationary induced dipoles (Mutual or Direct)");
     CUDA_CHECK(cudaSetDevice(c.device));
     c.stream = c.hostStream;
     const size_t n3 = 3 * (size_t) c.n;

@@ -1419,9 +1419,19 @@ __global__ void k_gradient_finish(int n, int npad, BoxDev box, double alpha, int
 // The pair loop sums, per atom, W_I = sum_j st dF_ij/dst and Z_I over the scale-0 pairs
 // of st/a dF_ij/dst, where dF_ij/dst is the pair's U_pi + U_uu with the kernels' st
 // derivatives, kE applied.
+// Perturbation orders of the Extrapolated (OPT) solver for the polarisation gradient:
+// nPT dipole sets [3][npad] each, and cbar_k = sum_(j >= k) c_j.
+template <typename real>
+struct OptOrders {
+    int nPT;  // 0: not Extrapolated
+    double cbar[8];
+    const real* mu;
+};
+
 template <typename real, bool QUAD>
 __device__ __forceinline__ void polarization_loop(const NbrList& nl, const AtomArrays<real>& at, const real* mu,
-                                                  bool mutual, const PairTask& t, int origI, real& W, real& Z) {
+                                                  bool mutual, const OptOrders<real>& opt, const PairTask& t, int origI,
+                                                  real& W, real& Z) {
     const PairConsts<real>& pc = pair_consts<real>(nl);
     const int npad = at.npad, si = t.si;
     const real oi[3] = {at.off[si], at.off[npad + si], at.off[2 * npad + si]};
@@ -1429,6 +1439,16 @@ __device__ __forceinline__ void polarization_loop(const NbrList& nl, const AtomA
     real MI[20];
     unique_moments(at.mom, npad, si, MI);
     const real ui[3] = {mu[si], mu[npad + si], mu[2 * npad + si]};
+    // OPT: A_m = sum_(j <= nPT-2-m) cbar_(j+m+1) mu_(j,i), so that the pair's sums are
+    // S1 = sum_m A_m.mu_(m,l) and S2 = sum_m (A_m.d)(mu_(m,l).d)
+    real A[7][3];
+    const int nm = opt.nPT > 1 ? opt.nPT - 1 : 0;
+    for (int m = 0; m < 7; ++m)
+        for (int q = 0; q < 3; ++q) A[m][q] = real(0);
+    for (int m = 0; m < nm; ++m)
+        for (int j = 0; j + m + 1 < opt.nPT; ++j)
+            for (int q = 0; q < 3; ++q)
+                A[m][q] += real(opt.cbar[j + m + 1]) * opt.mu[((size_t) j * 3 + q) * npad + si];
     for (int k = t.k0; k < t.k1; ++k) {
         int sj;
         unsigned flag;
@@ -1477,6 +1497,15 @@ __device__ __forceinline__ void polarization_loop(const NbrList& nl, const AtomA
             const real mi = ui[0] * d[0] + ui[1] * d[1] + ui[2] * d[2];
             const real mj = uj[0] * d[0] + uj[1] * d[1] + uj[2] * d[2];
             x += dl[1] * bB[1] * mm - dl[2] * bB[2] * mi * mj;
+        } else if (nm > 0) {  // OPT: -(g1' S1 + g2' S2)
+            real S1 = real(0), S2 = real(0);
+            for (int m = 0; m < nm; ++m) {
+                const real* um = opt.mu + (size_t) m * 3 * npad;
+                const real ul[3] = {um[sj], um[npad + sj], um[2 * npad + sj]};
+                S1 += A[m][0] * ul[0] + A[m][1] * ul[1] + A[m][2] * ul[2];
+                S2 += (A[m][0] * d[0] + A[m][1] * d[1] + A[m][2] * d[2]) * (ul[0] * d[0] + ul[1] * d[1] + ul[2] * d[2]);
+            }
+            x += dl[1] * bB[1] * S1 - dl[2] * bB[2] * S2;
         }
         W += st * x;
         if (scale == real(0)) Z += st / a * x;
@@ -1486,7 +1515,7 @@ __device__ __forceinline__ void polarization_loop(const NbrList& nl, const AtomA
 template <typename real>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 k_polarization_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, int mutual,
-                        unsigned long long* __restrict__ gfx, int segments, int split) {
+                        OptOrders<real> opt, unsigned long long* __restrict__ gfx, int segments, int split) {
     PairTask t;
     if (!t.init_split(nl, split)) return;
     if (!(segments & (t.quad ? kSegQuad : kSegErfc))) return;
@@ -1494,19 +1523,24 @@ k_polarization_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict_
     if (origI < 0) return;
     real W = real(0), Z = real(0);
     if (t.quad)
-        polarization_loop<real, true>(nl, at, mu, mutual != 0, t, origI, W, Z);
+        polarization_loop<real, true>(nl, at, mu, mutual != 0, opt, t, origI, W, Z);
     else
-        polarization_loop<real, false>(nl, at, mu, mutual != 0, t, origI, W, Z);
+        polarization_loop<real, false>(nl, at, mu, mutual != 0, opt, t, origI, W, Z);
     const real E = real(kElectric);
     fx_add(gfx + t.si, E * W);
     fx_add(gfx + at.npad + t.si, E * Z);
 }
 
 // out[4 n] by original index: dE/d(molecular-frame polarisability X Y Z, Thole width).
+// Extrapolated: the alpha^-1 term is replaced by -1/2 sum_k cbar_k sum_(j <= k) F_j F_(k-j)
+// (molecular frame, per axis) with F_0 = the permanent field (Efix) and F_j = the field
+// of order j - 1 (ptE).
 template <typename real>
 __global__ void k_polarization_gradient_finish(int n, int npad, const int* __restrict__ order, MolArrays mol,
                                                const double* __restrict__ pos, const unsigned long long* __restrict__ gfx,
-                                               const real* __restrict__ mu, double* __restrict__ out) {
+                                               const real* __restrict__ mu, OptOrders<real> opt,
+                                               const real* __restrict__ Efix, const real* __restrict__ ptE,
+                                               double* __restrict__ out) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int i = order[s];
@@ -1517,9 +1551,21 @@ __global__ void k_polarization_gradient_finish(int n, int npad, const int* __res
     const double pbar = (p[0] + p[1] + p[2]) / 3.0;
     const double u[3] = {(double) mu[s], (double) mu[npad + s], (double) mu[2 * npad + s]};
     double* o = out + 4 * (size_t) i;
+    double F[8][3];
+    for (int j = 0; j < opt.nPT; ++j) {
+        const real* v = j == 0 ? Efix : ptE + (size_t) (j - 1) * 3 * npad;
+        const double lab[3] = {(double) v[s], (double) v[npad + s], (double) v[2 * npad + s]};
+        for (int k = 0; k < 3; ++k) F[j][k] = R[k][0] * lab[0] + R[k][1] * lab[1] + R[k][2] * lab[2];
+    }
     for (int k = 0; k < 3; ++k) {
-        const double nu = R[k][0] * u[0] + R[k][1] * u[1] + R[k][2] * u[2];
-        double g = p[k] > 0.0 ? -0.5 * kElectric * nu * nu / (p[k] * p[k]) : 0.0;
+        double g = 0.0;
+        if (opt.nPT > 0) {
+            for (int ko = 0; ko < opt.nPT; ++ko)
+                for (int j = 0; j <= ko; ++j) g -= 0.5 * kElectric * opt.cbar[ko] * F[j][k] * F[ko - j][k];
+        } else {
+            const double nu = R[k][0] * u[0] + R[k][1] * u[1] + R[k][2] * u[2];
+            g = p[k] > 0.0 ? -0.5 * kElectric * nu * nu / (p[k] * p[k]) : 0.0;
+        }
         if (pbar > 0.0) g -= W / (18.0 * pbar);
         o[k] = g;
     }

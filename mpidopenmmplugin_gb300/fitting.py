@@ -11,8 +11,8 @@ Per-type parameters (24 per type) are the molecular-frame multipole components o
 MPIDForce::addMultipole (charge, dipole X Y Z, quadrupole XX XY YY XZ YZ ZZ, octopole XXX
 XXY XYY YYY XXZ XYZ YYZ XZZ YZZ ZZZ), the molecular-frame polarisabilities X Y Z and the
 Thole width; every atom of a type takes them in its own local frame.  The gradients
-come from mpid_evaluate_with_gradients (stationary induced dipoles, so Mutual or Direct
-polarisation for the last four), summed over the atoms of each type and over the boxes.
+come from mpid_evaluate_with_gradients, summed over the atoms of each type and over the
+boxes.
 Quadrupoles and octopoles must stay traceless: `project_traceless` removes the trace
 directions from a gradient before a step.
 """
@@ -94,7 +94,6 @@ class BoxBatch:
         self.systems = [(f, np.asarray(p, dtype=np.float64), np.asarray(b, dtype=np.float64), np.asarray(t))
                         for f, p, b, t in systems]
         self.contexts = [MPIDContext(f, precision=precision, device=device, box=b) for f, p, b, t in self.systems]
-        self.polarization = self.systems[0][0].getPolarizationType()
         self.threads = max(1, int(threads))
         self._pool = _cf.ThreadPoolExecutor(max_workers=self.threads)
 
@@ -107,18 +106,15 @@ class BoxBatch:
 
     def _one(self, k, forces):
         f, p, b, t = self.systems[k]
-        pol = self.polarization != MPIDForce.Extrapolated
-        e, fo, gm, gp = self.contexts[k].evaluateWithGradients(p, b, forces=forces, multipole=True, polarization=pol)
+        e, fo, gm, gp = self.contexts[k].evaluateWithGradients(p, b, forces=forces)
         g = np.zeros((self.ntypes, NPARAM))
         g[:, :20] = per_type(gm, t, self.ntypes)
-        if pol:
-            g[:, 20:] = per_type(gp, t, self.ntypes)
+        g[:, 20:] = per_type(gp, t, self.ntypes)
         return e, fo, g
 
     def evaluate(self, forces=True):
         """Energies (nbox,) kJ/mol, per-box forces (list of (n, 3) or None) and the gradient
-        of the summed energy with respect to the per-type parameters (ntypes, 24).  The
-        polarisation columns are zero for Extrapolated polarisation."""
+        of the summed energy with respect to the per-type parameters (ntypes, 24)."""
         results = list(self._pool.map(lambda k: self._one(k, forces), range(len(self.systems))))
         energies = np.array([r[0] for r in results])
         grad = np.zeros((self.ntypes, NPARAM))

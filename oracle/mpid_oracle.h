@@ -60,7 +60,7 @@ typedef struct {
     char message[512];
     double* grad;               /* 20n or NULL (port only): dE/d(molecular-frame charge, dipole X Y Z,
                                    quadrupole XX XY YY XZ YZ ZZ, octopole XXX ... ZZZ) per atom */
-    double* polgrad;            /* 4n or NULL (port only, Mutual and Direct): dE/d(molecular-frame
+    double* polgrad;            /* 4n or NULL (port only): dE/d(molecular-frame
                                    polarisability X Y Z, Thole width) per atom */
 } mpid_oracle_output;
 

@@ -1061,9 +1061,24 @@ struct Port {
     //  - the screening st = a r / (d_i d_j), d_i = mean(p_i)^(1/6): dst/dp_ik =
     //    -st / (18 mean(p_i)) and, for pairs of covalent scale 0 (whose width is
     //    a_i + a_j), dst/da_i = st / a.
-    void polarization_gradient(const std::vector<std::array<double, 3>>& mu, double* out) const {
+    //
+    // Extrapolated (OPT, mu = sum_k cbar_k mu_k, mu_0 = alpha E, mu_(k+1) = alpha T mu_k) is
+    // not stationary; its energy -1/2 E.P.E with P = sum_k cbar_k (alpha T)^k alpha
+    // (symmetric) gives the explicit adjoint sums
+    //   d/dalpha: -1/2 sum_k cbar_k sum_(j=0..k) F_j dalpha F_(k-j), F_0 = E_perm and
+    //             F_j = T mu_(j-1) (the field of the previous order);
+    //   d/dst (uu kernel): -(g1' S1 + g2' S2) per pair, S1 = sum_(j+m<=n-2)
+    //             cbar_(j+m+1) mu_(j,i).mu_(m,l), S2 the same with (mu.d)(mu.d);
+    // while the permanent field's screening enters as -mu.dE_perm as for the others.
+    void polarization_gradient(const std::vector<std::array<double, 3>>& mu, double* out,
+                               const std::vector<std::array<double, 3>>* Efix = nullptr,
+                               const std::vector<std::vector<std::array<double, 3>>>* ptMu = nullptr,
+                               const std::vector<std::vector<std::array<double, 3>>>* ptE = nullptr,
+                               const std::vector<double>* cbar = nullptr) const {
         const int pol = in->polarization_type;
-        if (pol == 2) throw std::runtime_error("polarisability and Thole gradients need Mutual or Direct polarization");
+        if (pol == 2 && !(Efix && ptMu && ptE && cbar))
+            throw std::runtime_error("the extrapolated polarisation gradient needs the perturbation orders");
+        const int nPT = pol == 2 ? (int) cbar->size() : 0;
         std::vector<double> W(n, 0.0), Z(n, 0.0);
         for (const auto& pr : pairs) {
             const int i = pr.first, j = pr.second;
@@ -1096,6 +1111,23 @@ struct Port {
                     mj += mu[j][k] * d[k];
                 }
                 D -= g[1] * mm + g[2] * mi * mj;
+            } else if (pol == 2 && nPT > 1) {
+                kernel_g_ds(2, i, j, r, s, 2, g, st, a);
+                double S1 = 0, S2 = 0;
+                for (int jo = 0; jo + 1 < nPT; ++jo)
+                    for (int mo = 0; jo + mo + 1 < nPT; ++mo) {
+                        const auto& ui = (*ptMu)[jo][i];
+                        const auto& ul = (*ptMu)[mo][j];
+                        double mm = 0, mi = 0, ml = 0;
+                        for (int k = 0; k < 3; ++k) {
+                            mm += ui[k] * ul[k];
+                            mi += ui[k] * d[k];
+                            ml += ul[k] * d[k];
+                        }
+                        S1 += (*cbar)[jo + mo + 1] * mm;
+                        S2 += (*cbar)[jo + mo + 1] * mi * ml;
+                    }
+                D -= g[1] * S1 + g[2] * S2;
             }
             W[i] += st * D;
             W[j] += st * D;
@@ -1109,9 +1141,21 @@ struct Port {
             frame(i, R);
             const double* p = in->polarity + 3 * i;
             const double pbar = (p[0] + p[1] + p[2]) / 3.0;
+            // molecular-frame fields of the OPT orders: F_0 = E_perm, F_j = T mu_(j-1)
+            std::vector<std::array<double, 3>> F(nPT);
+            for (int jo = 0; jo < nPT; ++jo) {
+                const auto& v = jo == 0 ? (*Efix)[i] : (*ptE)[jo - 1][i];
+                for (int k = 0; k < 3; ++k) F[jo][k] = R[k][0] * v[0] + R[k][1] * v[1] + R[k][2] * v[2];
+            }
             for (int k = 0; k < 3; ++k) {
-                const double nu = R[k][0] * mu[i][0] + R[k][1] * mu[i][1] + R[k][2] * mu[i][2];
-                double g = p[k] > 0 ? -0.5 * nu * nu / (p[k] * p[k]) : 0.0;
+                double g = 0.0;
+                if (pol == 2) {
+                    for (int ko = 0; ko < nPT; ++ko)
+                        for (int jo = 0; jo <= ko; ++jo) g -= 0.5 * (*cbar)[ko] * F[jo][k] * F[ko - jo][k];
+                } else {
+                    const double nu = R[k][0] * mu[i][0] + R[k][1] * mu[i][1] + R[k][2] * mu[i][2];
+                    g = p[k] > 0 ? -0.5 * nu * nu / (p[k] * p[k]) : 0.0;
+                }
                 if (pbar > 0) g -= W[i] / (18.0 * pbar);
                 out[4 * i + k] = ELECTRIC * g;
             }
@@ -1397,7 +1441,7 @@ struct Port {
             const double a2 = al * al;  // self energy, :4283-4318
             energy += -al * ELECTRIC / SQRT_PI_REF * (cii + 2.0 / 3.0 * a2 * dii + 4.0 / 15.0 * a2 * a2 * qii + 8.0 / 105.0 * a2 * a2 * a2 * oii);
         }
-        if (out->polgrad) polarization_gradient(mu, out->polgrad);
+        if (out->polgrad) polarization_gradient(mu, out->polgrad, &E, &ptMu, &ptE, &cbar);
         if (pol == 2) {  // OPT response, :4956-4984
             int nPT = in->n_extrap;
             for (int i = 0; i < n; ++i)

@@ -237,7 +237,7 @@ def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False, want_grad=F
     polgrad = None
     if want_grad:
         polgrad = np.zeros(4 * n)
-        out.polgrad = _dp(polgrad) if sys_.polarization_type != 2 else None
+        out.polgrad = _dp(polgrad)
     else:
         out.polgrad = None
     rc = _lib(which)(ctypes.byref(inp), ctypes.byref(out))
@@ -247,7 +247,7 @@ def evaluate(sys_: OracleSystem, which="ref", want_labdipoles=False, want_grad=F
                         labdipoles=None if lab is None else lab.reshape(n, 3), iterations=out.iterations,
                         epsilon=out.epsilon, converged=bool(out.converged),
                         grad=None if grad is None else grad.reshape(n, 20),
-                        polgrad=None if polgrad is None or sys_.polarization_type == 2 else polgrad.reshape(n, 4))
+                        polgrad=None if polgrad is None else polgrad.reshape(n, 4))
 
 
 def properties(sys_: OracleSystem, masses, grid):

@@ -18,7 +18,6 @@ import numpy as np
 import pytest
 
 from mpidopenmmplugin_gb300 import MPIDContext, MPIDForce, fitting, synthetic
-from mpidopenmmplugin_gb300.context import MPIDError
 
 import helpers
 
@@ -88,7 +87,7 @@ def test_batch_workload_geometry():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["double", "mixed"])
-@pytest.mark.parametrize("name", ["frames_mutual.npz", "frames_direct.npz"])
+@pytest.mark.parametrize("name", ["frames_mutual.npz", "frames_direct.npz", "frames_extrapolated.npz"])
 def test_polarization_gradients_match_oracle(name, precision):
     from oracle import oracle as O
     if not O.available("port"):
@@ -116,16 +115,6 @@ def test_polarization_gradients_match_oracle(name, precision):
     else:
         assert abs(e2 - e) <= 1e-12 * abs(e) and helpers.rel_rms(f2, forces) < 1e-12
     assert helpers.rel_rms(gm2, gm) < 1e-12
-
-
-@pytest.mark.gpu
-def test_polarization_gradients_rejected_for_extrapolated():
-    f, pos, box = synthetic.workload("water648", polarization=MPIDForce.Extrapolated, order=5)
-    ctx = MPIDContext(f, precision="mixed")
-    with pytest.raises(MPIDError, match="Mutual or Direct"):
-        ctx.evaluateWithGradients(pos, box)
-    e, forces, gm, gp = ctx.evaluateWithGradients(pos, box, polarization=False)
-    assert gp is None and np.all(np.isfinite(gm))
 
 
 def _directions(rng):
@@ -189,7 +178,7 @@ def test_port_per_type_gradient_matches_finite_differences():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("polarization", [MPIDForce.Mutual, MPIDForce.Direct])
+@pytest.mark.parametrize("polarization", [MPIDForce.Mutual, MPIDForce.Direct, MPIDForce.Extrapolated])
 def test_batch_per_type_gradients(polarization):
     """Per-type gradients of 4 boxes (128-160 waters) evaluated concurrently, along each
     parameter block: FP64 within 1e-6 and mixed within 1e-5 of the oracle port's FP64

@@ -81,13 +81,13 @@ def test_port_polarization_gradients_match_finite_differences():
     """dE/d(molecular-frame polarisability X Y Z, Thole width) of the oracle port against
     central differences (h = 1e-3 relative; the energy is ~1e4 kJ/mol, so
     smaller steps are dominated by rounding) of its own energy on the 160-atom frames
-    system, for the stationary polarisation types (Mutual, Direct)."""
+    system, for every polarisation type (Extrapolated through its explicit adjoint sums)."""
     import copy
     from oracle import oracle as O
     if not O.available("port"):
         O.build("port")
     rng = np.random.default_rng(4)
-    for name in ("frames_direct.npz", "frames_mutual.npz"):
+    for name in ("frames_direct.npz", "frames_mutual.npz", "frames_extrapolated.npz"):
         fx = helpers.load_npz_fixture(name)
         s = helpers.system_from_fixture(fx)
         s.mutual_eps, s.max_iter = 1e-11, 500
