@@ -1535,7 +1535,7 @@ struct Context {
         }
         const int sL = gradient_split((long long) ntiles * nchunksL), sS = gradient_split((long long) ntiles * nchunksS);
         const int sA = gradient_split(pair_tasks());
-        if (mixed) {
+        if (mixed && usePme) {
             launch(k_polarization_gradient<float>, gradient_blocks(sL), 32 * kWarpsPerBlock, 0, st, nbr_list(),
                    ef->arrays(), (const float*) ef->mu.p, mutual, optF, polFx.p, kSegErfc, sL);
             launch(k_polarization_gradient<double>, gradient_blocks(sS), 32 * kWarpsPerBlock, 0, st, nbr_list(),
@@ -1553,8 +1553,10 @@ struct Context {
     }
 
     // dE/d(molecular-frame multipole parameters) of every atom for the last evaluation.
-    // The real-space sum runs in FP64 except, on the mixed path, over the erfc segment of
-    // the lists (alpha r >= 1.5, no excluded pairs), which runs in FP32.
+    // The real-space sum runs in FP64 except, on the mixed path under PME, over the erfc
+    // segment of the lists (alpha r >= 1.5, no excluded pairs), which runs in FP32.  Without
+    // a cutoff every pair is bare 1/r, near ones included, and FP32 rank-6 derivative
+    // tensors of those cost 1.6e-4 relative (160-atom test system), so all run in FP64.
     void parameter_gradients(double* host) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
         Engine<double>& d = gradient_engine();
@@ -1564,7 +1566,7 @@ struct Context {
         CUDA_CHECK(cudaMemsetAsync(gradFx.p, 0, (size_t) 20 * npad * 8, st));
         const int sL = gradient_split((long long) ntiles * nchunksL), sS = gradient_split((long long) ntiles * nchunksS);
         const int sA = gradient_split(pair_tasks());
-        if (mixed) {
+        if (mixed && usePme) {
             launch(k_multipole_gradient<float>, gradient_blocks(sL), 32 * kWarpsPerBlock, 0, st, nbr_list(),
                    ef->arrays(), (const float*) ef->mu.p, gradFx.p, kSegErfc, sL);
             launch(k_multipole_gradient<double>, gradient_blocks(sS), 32 * kWarpsPerBlock, 0, st, nbr_list(),

@@ -299,3 +299,28 @@ def test_sharded_batch_allreduce_gloo():
     for rank, e, g in res:
         assert np.allclose(e, sizes * 0.5)
         assert np.allclose(g, np.full((2, 24), float(sum(range(10)))))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pol", [MPIDForce.Mutual, MPIDForce.Extrapolated])
+def test_gradients_without_cutoff_match_oracle(pol):
+    """Multipole and polarisation gradients of the 160-atom frames system under NoCutoff
+    (no reciprocal or self terms; every pair in the lists), FP64 and mixed, against the
+    oracle port."""
+    from oracle import oracle as O
+    if not O.available("port"):
+        O.build("port")
+    fx = helpers.load_npz_fixture("properties_frames_nocutoff.npz")
+    s = helpers.system_from_fixture(fx)
+    s.polarization_type = pol
+    s.mutual_eps, s.max_iter = 1e-10, 500
+    f = helpers.force_from_oracle_system(s)
+    ref = O.evaluate(s, "port", want_grad=True)
+    box = np.eye(3) * 10.0
+    for precision, tol in (("double", 1e-8), ("mixed", 1e-5)):
+        ctx = MPIDContext(f, precision=precision)
+        e, forces, gm, gp = ctx.evaluateWithGradients(s.pos, box)
+        errs = (helpers.rel_rms(gm, ref.grad), helpers.rel_rms(gp[:, :3], ref.polgrad[:, :3]),
+                helpers.rel_rms(gp[:, 3], ref.polgrad[:, 3]))
+        print("nocutoff pol %d %s: multipole %.2e polarisability %.2e thole %.2e" % ((pol, precision) + errs))
+        assert max(errs) < tol, (precision, errs)
