@@ -105,7 +105,9 @@ int mpid_set_multipoles(mpid_context* ctx, const double* charge, const double* d
 int mpid_set_covalent(mpid_context* ctx, const int* offsets, const int* index);
 
 /* Evaluate with host buffers (CalcMPIDForceKernel::execute, mpidKernels.h:77).
- * positions: 3n; box: 9 (row vectors, rectangular); forces: 3n, ADDED to;
+ * positions: 3n; box: 9, the rows a, b, c of the periodic box in OpenMM's reduced form
+ * (a = (ax, 0, 0), b = (bx, by, 0), c = (cx, cy, cz), |bx|, |cx| <= ax/2, |cy| <= by/2;
+ * rectangular or triclinic; MPIDReferenceForce.cpp:2620-2675); forces: 3n, ADDED to;
  * energy: returns the energy (may be NULL). */
 int mpid_evaluate(mpid_context* ctx, const double* positions, const double* box, double* forces, double* energy);
 

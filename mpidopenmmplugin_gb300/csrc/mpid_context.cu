@@ -647,13 +647,17 @@ struct Context {
     }
 
     void set_box(const double* b) {
-        for (int k = 0; k < 9; ++k)
-            if ((k % 4) != 0 && b[k] != 0.0)
-                throw Error(MPID_ERR_INVALID, "only rectangular periodic boxes are supported");
+        // OpenMM's reduced form: a = (ax, 0, 0), b = (bx, by, 0), c = (cx, cy, cz)
+        if (b[1] != 0.0 || b[2] != 0.0 || b[5] != 0.0)
+            throw Error(MPID_ERR_INVALID, "the periodic box must be in reduced form: a = (ax, 0, 0), b = (bx, by, 0)");
         const double L[3] = {b[0], b[4], b[8]};
+        const bool tri = b[3] != 0.0 || b[6] != 0.0 || b[7] != 0.0;
         if (usePme) {
             for (int k = 0; k < 3; ++k)
                 if (!(L[k] > 0)) throw Error(MPID_ERR_INVALID, "Box size of zero is invalid.");
+            if (tri && (std::fabs(b[3]) > 0.5 * L[0] * (1 + 1e-12) || std::fabs(b[6]) > 0.5 * L[0] * (1 + 1e-12) ||
+                        std::fabs(b[7]) > 0.5 * L[1] * (1 + 1e-12)))
+                throw Error(MPID_ERR_INVALID, "the periodic box must be in reduced form: |bx|, |cx| <= ax/2, |cy| <= by/2");
             const double minAllowed = 1.999999 * set.cutoff;  // MPIDReferenceKernels.cpp:193-197
             if (L[0] < minAllowed || L[1] < minAllowed || L[2] < minAllowed)
                 throw Error(MPID_ERR_INVALID, "The periodic box size has decreased to less than twice the nonbonded cutoff.");
@@ -663,13 +667,23 @@ struct Context {
             box.invL[k] = usePme ? 1.0 / L[k] : 1.0;
             box.grid[k] = usePme ? set.grid[k] : 1;
         }
+        for (int k = 0; k < 9; ++k) box.V[k] = usePme ? b[k] : ((k % 4) == 0 ? 1.0 : 0.0);
+        box.tri = usePme && tri ? 1 : 0;
+        // reciprocal vectors as MPIDReferenceForce.cpp:2627-2632 stores them
+        const double* v = box.V;
+        const double scale = 1.0 / (v[0] * v[4] * v[8]);
+        const double R[3][3] = {{v[4] * v[8] * scale, 0.0, 0.0},
+                                {-v[3] * v[8] * scale, v[0] * v[8] * scale, 0.0},
+                                {(v[3] * v[7] - v[4] * v[6]) * scale, -v[0] * v[7] * scale, v[0] * v[4] * scale}};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) box.R[i][j] = R[i][j];
+        // fractional grid coordinates: frac_j = grid_j sum_i x_i R[i][j]
         for (int j = 0; j < 3; ++j)
-            for (int i = 0; i < 3; ++i) box.A[j][i] = (usePme && i == j) ? set.grid[j] / L[j] : 0.0;
+            for (int i = 0; i < 3; ++i) box.A[j][i] = usePme ? set.grid[j] * R[i][j] : 0.0;
         if (usePme && std::memcmp(lastBox, b, sizeof(lastBox)) != 0) {
             const size_t Gh = (size_t) set.grid[0] * set.grid[1] * (set.grid[2] / 2 + 1);
-            launch(k_influence, std::min<long long>(nblk(Gh, 256), 152 * 8), 256, 0, stream, 
-                box, set.ewald_alpha, modx.p, mody.p, modz.p, 1.0 / L[0], 1.0 / L[1], 1.0 / L[2], L[0] * L[1] * L[2],
-                influence.p);
+            launch(k_influence, std::min<long long>(nblk(Gh, 256), 152 * 8), 256, 0, stream, box, set.ewald_alpha,
+                   modx.p, mody.p, modz.p, L[0] * L[1] * L[2], influence.p);
             CUDA_CHECK(cudaGetLastError());
             std::memcpy(lastBox, b, sizeof(lastBox));
         }
@@ -707,8 +721,10 @@ struct Context {
         for (int k = 0; k < 3; ++k) {
             R.L[k] = (float) box.L[k];
             R.iL[k] = (float) box.invL[k];
-            const dfloat v = df_from_double(box.L[k]);
-            R.Ldf[k] = make_float2(v.hi, v.lo);
+        }
+        for (int k = 0; k < 9; ++k) {
+            const dfloat v = df_from_double(box.V[k]);
+            R.Vdf[k] = make_float2(v.hi, v.lo);
         }
         const dfloat th = df_from_double(set.default_thole);
         R.tholeDefault = make_float2(th.hi, th.lo);
@@ -732,6 +748,7 @@ struct Context {
             c.L[k] = (real) box.L[k];
             c.iL[k] = (real) box.invL[k];
         }
+        for (int k = 0; k < 9; ++k) c.V[k] = (real) box.V[k];
         c.rc2 = usePme ? (real) (set.cutoff * set.cutoff) : (real) 3.0e38f;
         c.thole = (real) set.default_thole;
         c.ew = EwaldAlpha<real>(usePme ? set.ewald_alpha : 0.0);

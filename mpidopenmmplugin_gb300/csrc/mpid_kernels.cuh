@@ -40,11 +40,34 @@ template <> struct Vec4<double> {
     static __host__ __device__ __forceinline__ double4 make(double a, double b, double c, double d) { return make_double4(a, b, c, d); }
 };
 
+// Periodic box in OpenMM's reduced form: rows a = (ax, 0, 0), b = (bx, by, 0),
+// c = (cx, cy, cz) with |bx|, |cx| <= ax / 2 and |cy| <= by / 2 (rectangular when the
+// off-diagonal entries are 0).
 struct BoxDev {
-    double L[3], invL[3];    // rectangular box edge lengths
-    double A[3][3];          // Cartesian -> fractional grid, frac_j = sum_i A[j][i] x_i
+    double L[3], invL[3];    // ax, by, cz and their inverses
+    double V[9];             // a, b, c as rows
+    double R[3][3];          // reciprocal vectors as the reference stores them (fractional w_j = sum_i x_i R[i][j])
+    double A[3][3];          // Cartesian -> fractional grid, frac_j = sum_i A[j][i] x_i = grid_j w_j
     int grid[3];
+    int tri;                 // off-diagonal entries present
 };
+
+// Minimum image of a displacement in a reduced-form box (c, then b, then a; the order of
+// MPIDReferenceForce.cpp:2673-2675).  V: box rows, iL: 1/ax, 1/by, 1/cz.  With a
+// rectangular box the off-diagonal products are exact zeros, so the result equals the
+// per-axis image.
+template <typename real>
+__host__ __device__ __forceinline__ void min_image(real* d, const real* V, const real* iL) {
+    real s = rint(d[2] * iL[2]);
+    d[0] -= s * V[6];
+    d[1] -= s * V[7];
+    d[2] -= s * V[8];
+    s = rint(d[1] * iL[1]);
+    d[0] -= s * V[3];
+    d[1] -= s * V[4];
+    s = rint(d[0] * iL[0]);
+    d[0] -= s * V[0];
+}
 
 // ---------------------------------------------------------------------------
 // Spatial sort into near-cubic 32-atom tiles: the box is cut into x-y columns about
@@ -56,13 +79,16 @@ __global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, i
                             unsigned long long* __restrict__ keys, int* __restrict__ vals, double* __restrict__ wpos) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double w[3];
+    double w[3], x[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    // into [0, ax) x [0, by) x [0, cz): c, then b, then a (a lattice translation)
+    for (int k = 2; k >= 0; --k) {
+        double f = floor(x[k] * box.invL[k]);
+        if (x[k] - f * box.L[k] >= box.L[k]) f += 1.0;  // rounding at the upper edge
+        for (int q = 0; q <= k; ++q) x[q] -= f * box.V[3 * k + q];
+    }
     for (int k = 0; k < 3; ++k) {
-        double x = pos[3 * i + k];
-        x -= box.L[k] * floor(x * box.invL[k]);
-        if (x >= box.L[k]) x -= box.L[k];
-        wpos[3 * i + k] = x;
-        w[k] = x * box.invL[k];
+        wpos[3 * i + k] = x[k];
+        w[k] = x[k] * box.invL[k];
     }
     int cx = min(ncx - 1, (int) (w[0] * ncx));
     int cy = min(ncy - 1, (int) (w[1] * ncy));
@@ -134,7 +160,39 @@ __global__ void k_tile_list(int ntiles, const double* __restrict__ center, const
         const int J = J0 + lane;
         bool hit = false, wrap = false;
         double sh[3] = {0.0, 0.0, 0.0};
-        if (J < ntiles) {
+        if (J < ntiles && usePbc && box.tri) {
+            // triclinic: the bounding boxes are tested at every lattice image next to the
+            // minimum image of the centres, and every hit is imaged pair by pair
+            const float cut = (float) cutoff * 1.0001f + 1e-4f;
+            float Vf[9], iLf[3];
+            for (int q = 0; q < 9; ++q) Vf[q] = (float) box.V[q];
+            for (int q = 0; q < 3; ++q) iLf[q] = (float) box.invL[q];
+            float dc[3], ext[3];
+            for (int k = 0; k < 3; ++k) {
+                dc[k] = (float) center[3 * J + k] - cI[k];
+                ext[k] = hI[k] + (float) half[3 * J + k];
+            }
+            min_image(dc, Vf, iLf);
+            float best = 3.0e38f;
+            for (int ia = -1; ia <= 1; ++ia)
+                for (int ib = -1; ib <= 1; ++ib)
+                    for (int ic = -1; ic <= 1; ++ic) {
+                        const float v[3] = {dc[0] + ia * Vf[0] + ib * Vf[3] + ic * Vf[6], dc[1] + ib * Vf[4] + ic * Vf[7],
+                                            dc[2] + ic * Vf[8]};
+                        float d2 = 0.f;
+                        for (int k = 0; k < 3; ++k) {
+                            const float g = fabsf(v[k]) - ext[k];
+                            if (g > 0.f) d2 += g * g;
+                        }
+                        best = fminf(best, d2);
+                    }
+            hit = best < cut * cut;
+            wrap = true;
+            if (hit) {
+                for (int k = 0; k < 3; ++k) sh[k] = center[3 * J + k] - center[3 * I + k];
+                min_image(sh, box.V, box.invL);
+            }
+        } else if (J < ntiles) {
             // bounding-box test in float with a margin far above its rounding
             const float cut = (float) cutoff * 1.0001f + 1e-4f;
             float d2 = 0.f;
@@ -326,8 +384,9 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
     const int si = I * 32 + lane;
     const float oi[3] = {(float) off[si], (float) off[npad + si], (float) off[2 * npad + si]};
     const int origI = orig[si];
-    const float L[3] = {(float) box.L[0], (float) box.L[1], (float) box.L[2]};
     const float iL[3] = {(float) box.invL[0], (float) box.invL[1], (float) box.invL[2]};
+    float Vb[9];
+    for (int q = 0; q < 9; ++q) Vb[q] = (float) box.V[q];
     // covalent partners of this atom: the first kCache in registers
     int cb = 0, ce = 0;
     if (origI >= 0) { cb = covOff[origI]; ce = covOff[origI + 1]; }
@@ -387,8 +446,7 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
                               sh.y + (__shfl_sync(0xffffffffu, oj1, jl) - oi[1]),
                               sh.z + (__shfl_sync(0xffffffffu, oj2, jl) - oi[2])};
                 const int oj = __shfl_sync(0xffffffffu, origJl, jl);
-                if (wrap)
-                    for (int k = 0; k < 3; ++k) d[k] -= L[k] * rintf(d[k] * iL[k]);
+                if (wrap) min_image(d, Vb, iL);
                 const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
                 if (origI < 0 || oj < 0 || r2 >= cutoff2 || (J == I && jl == lane)) continue;
                 unsigned flag = 0;
@@ -463,6 +521,7 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
 template <typename real>
 struct PairConsts {
     real L[3], iL[3];
+    real V[9];      // box rows (reduced form)
     real rc2;       // exact cutoff squared
     real thole;     // default Thole width
     EwaldAlpha<real> ew;
@@ -556,9 +615,7 @@ __device__ __forceinline__ bool list_pair(const NbrList& nl, const PairConsts<re
     const int npad = at.npad;
 #pragma unroll
     for (int q = 0; q < 3; ++q) d[q] = sh[q] + (at.off[q * npad + sj] - oi[q]);
-    if (Jw < 0)
-#pragma unroll
-        for (int q = 0; q < 3; ++q) d[q] -= pc.L[q] * rint(d[q] * pc.iL[q]);
+    if (Jw < 0) min_image(d, pc.V, pc.iL);
     r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
     return !(nl.usePbc && r2 > pc.rc2);
 }
@@ -696,9 +753,7 @@ __device__ __forceinline__ void dipole_field_packed_loop(const NbrList& nl, cons
         const int sj = (Jw & 0x7fffffff) * 32 + (int) (code & 31u);
         const float4 aj = A0[sj], bj = A1[sj];
         float d[3] = {sh.x + (aj.x - ai.x), sh.y + (aj.y - ai.y), sh.z + (aj.z - ai.z)};
-        if (Jw < 0)
-#pragma unroll
-            for (int q = 0; q < 3; ++q) d[q] -= pc.L[q] * rintf(d[q] * pc.iL[q]);
+        if (Jw < 0) min_image(d, pc.V, pc.iL);
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (nl.usePbc && r2 > pc.rc2) continue;
         const float r = sqrtf(r2);
@@ -767,7 +822,7 @@ struct DfRadial {
     int usePme;
     float rc2;
     float L[3], iL[3];
-    float2 Ldf[3];
+    float2 Vdf[9];  // box rows as double-float
     float2 tholeDefault;
 };
 
@@ -824,11 +879,12 @@ __device__ __forceinline__ void df_field_loop(const NbrList& nl, const DfRadial&
         dfloat d[3];
 #pragma unroll
         for (int q = 0; q < 3; ++q) d[q] = df_add(df_sub(df_load(A.off, q * npad + sj), oi[q]), df_load(nl.shDF, 3 * s + q));
-        if (Jw < 0)
+        if (Jw < 0)  // minimum image in double-float: c, then b, then a
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const float m = rintf(d[q].hi * R.iL[q]);
-                d[q] = df_sub(d[q], df_mul(df_make(R.Ldf[q].x, R.Ldf[q].y), m));
+            for (int k = 2; k >= 0; --k) {
+                const float m = rintf(d[k].hi * R.iL[k]);
+#pragma unroll
+                for (int q = 0; q <= k; ++q) d[q] = df_sub(d[q], df_mul(df_make(R.Vdf[3 * k + q].x, R.Vdf[3 * k + q].y), m));
             }
         const dfloat r2 = df_add(df_add(df_mul(d[0], d[0]), df_mul(d[1], d[1])), df_mul(d[2], d[2]));
         if (R.usePme && r2.hi > R.rc2) continue;
@@ -1004,11 +1060,8 @@ __global__ void k_scaled_pair_energy(int npairs, const int2* __restrict__ pr, co
         const int i = pr[p].x, j = pr[p].y;
         const int si = rank[i], sj = rank[j];
         double d[3];
-        for (int k = 0; k < 3; ++k) {
-            double x = pos[3 * j + k] - pos[3 * i + k];
-            if (usePbc) x -= box.L[k] * rint(x * box.invL[k]);
-            d[k] = x;
-        }
+        for (int k = 0; k < 3; ++k) d[k] = pos[3 * j + k] - pos[3 * i + k];
+        if (usePbc) min_image(d, box.V, box.invL);
         const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (!usePbc || r2 <= cutoff * cutoff) {
             const double r = sqrt(r2), s = prs[p];
@@ -1055,8 +1108,7 @@ __global__ void k_potential_grid(int n, int npad, int ngrid, const double* __res
     for (int i = 0; i < n; ++i) {
         const int s = rank[i];
         double d[3] = {wpos[3 * i] - gx, wpos[3 * i + 1] - gy, wpos[3 * i + 2] - gz};
-        if (usePbc)
-            for (int k = 0; k < 3; ++k) d[k] -= box.L[k] * rint(d[k] * box.invL[k]);
+        if (usePbc) min_image(d, box.V, box.invL);
         const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         const double rr1 = 1.0 / sqrt(r2), rr2 = rr1 * rr1, rr3 = rr1 * rr2;
         const double q = mom64[s];
@@ -1591,7 +1643,8 @@ __global__ void k_bsplines(int npad, int n, const int* __restrict__ order, const
     for (int d = 0; d < 3; ++d) {
         // Fractional coordinate with the grid origin of MPIDReferenceForce.cpp:3058-3060:
         // the minimum-image coordinate w in [-1/2, 1/2) maps to n (w + 1/2).
-        double w = wpos[3 * i + d] * box.invL[d] + 0.5;
+        // fractional coordinate w_d = sum_k x_k R[k][d] (MPIDReferenceForce.cpp:3058)
+        double w = wpos[3 * i] * box.R[0][d] + wpos[3 * i + 1] * box.R[1][d] + wpos[3 * i + 2] * box.R[2][d] + 0.5;
         w -= floor(w);
         double fr = box.grid[d] * w;
         int ifr = (int) floor(fr);
@@ -1687,8 +1740,7 @@ __global__ void k_grid_finish(size_t total, typename GridAcc<real>::type* __rest
 // Reciprocal influence function on the half-complex grid (kx, ky, kz <= nz/2),
 // MPIDReferenceForce.cpp:3329-3366: exp(-pi^2 m^2/alpha^2)/(pi V m^2 B(m)), 0 at m = 0.
 __global__ void k_influence(BoxDev box, double alpha, const double* __restrict__ modx, const double* __restrict__ mody,
-                            const double* __restrict__ modz, double recip00, double recip11, double recip22,
-                            double volume, double* __restrict__ out) {
+                            const double* __restrict__ modz, double volume, double* __restrict__ out) {
     const int nx = box.grid[0], ny = box.grid[1], nz = box.grid[2], nzh = nz / 2 + 1;
     const size_t total = (size_t) nx * ny * nzh;
     for (size_t idx = (size_t) blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t) gridDim.x * blockDim.x) {
@@ -1699,7 +1751,10 @@ __global__ void k_influence(BoxDev box, double alpha, const double* __restrict__
         const int mx = kx < (nx + 1) / 2 ? kx : kx - nx;
         const int my = ky < (ny + 1) / 2 ? ky : ky - ny;
         const int mz = kz < (nz + 1) / 2 ? kz : kz - nz;
-        const double hx = mx * recip00, hy = my * recip11, hz = mz * recip22;
+        // reciprocal lattice vector m_x a* + m_y b* + m_z c* (MPIDReferenceForce.cpp:3351-3353)
+        const double hx = mx * box.R[0][0];
+        const double hy = mx * box.R[1][0] + my * box.R[1][1];
+        const double hz = mx * box.R[2][0] + my * box.R[2][1] + mz * box.R[2][2];
         const double m2 = hx * hx + hy * hy + hz * hz;
         const double expF = M_PI * M_PI / (alpha * alpha);
         out[idx] = exp(-expF * m2) / (M_PI * volume * m2 * modx[kx] * mody[ky] * modz[kz]);

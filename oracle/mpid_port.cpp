@@ -169,6 +169,9 @@ struct Port {
     bool pme;
     int order;
     double box[3], recip[3];
+    double V[9];        // box rows a, b, c (reduced form; rectangular: diagonal)
+    double R[3][3];     // reciprocal vectors as MPIDReferenceForce.cpp:2627-2632 stores them
+    bool tri = false;
     double A[3][3];  // frac_j = sum_i A[j][i] x_i
     std::vector<Atom> at;
     std::vector<std::map<int, double>> scale;  // per lower-index atom
@@ -186,9 +189,13 @@ struct Port {
         auto it = scale[a].find(b);
         return it == scale[a].end() ? 1.0 : it->second;
     }
+    // minimum image: c, then b, then a (MPIDReferenceForce.cpp:2673-2675)
     void minimg(double* d) const {
         if (!pme) return;
-        for (int k = 0; k < 3; ++k) d[k] -= box[k] * std::floor(d[k] / box[k] + 0.5);
+        for (int k = 2; k >= 0; --k) {
+            const double s = std::floor(d[k] / box[k] + 0.5);
+            for (int q = 0; q <= k; ++q) d[q] -= s * V[3 * k + q];
+        }
     }
 
     // --- frames (MPIDReferenceForce.cpp:357-563) ---
@@ -348,7 +355,7 @@ struct Port {
         int nc[3] = {1, 1, 1};
         if (pme)
             for (int k = 0; k < 3; ++k) nc[k] = std::max(1, (int) std::floor(box[k] / rc));
-        if (!pme || nc[0] < 3 || nc[1] < 3 || nc[2] < 3) {
+        if (!pme || tri || nc[0] < 3 || nc[1] < 3 || nc[2] < 3) {  // all pairs (cells assume a rectangular box)
             for (int i = 0; i < n; ++i)
                 for (int j = i + 1; j < n; ++j) {
                     double d[3];
@@ -449,8 +456,8 @@ struct Port {
         const int gdim[3] = {nx, ny, nz};
         for (int i = 0; i < n; ++i)
             for (int d = 0; d < 3; ++d) {
-                double x = in->pos[3 * i + d];
-                double w = x / box[d];
+                const double* x = in->pos + 3 * i;
+                double w = x[0] * R[0][d] + x[1] * R[1][d] + x[2] * R[2][d];  // fractional (:3058)
                 w -= std::floor(w + 0.5);  // minimum image in [-1/2, 1/2)
                 double fr = gdim[d] * (w - (int) (w + 0.5) + 0.5);
                 int ifr = (int) std::floor(fr);
@@ -563,7 +570,7 @@ struct Port {
         fftpack_t plan;
         fftpack_init_3d(&plan, nx, ny, nz);
         fftpack_exec_3d(plan, FFTPACK_FORWARD, g.data(), g.data());
-        const double V = box[0] * box[1] * box[2], al = in->ewald_alpha;
+        const double vol = box[0] * box[1] * box[2], al = in->ewald_alpha;
 #pragma omp parallel for
         for (int kx = 0; kx < nx; ++kx)
             for (int ky = 0; ky < ny; ++ky)
@@ -571,8 +578,10 @@ struct Port {
                     t_complex& c = g[((size_t) kx * ny + ky) * nz + kz];
                     if (!kx && !ky && !kz) { c.re = c.im = 0; continue; }
                     int mx = kx < (nx + 1) / 2 ? kx : kx - nx, my = ky < (ny + 1) / 2 ? ky : ky - ny, mz = kz < (nz + 1) / 2 ? kz : kz - nz;
-                    double hx = mx / box[0], hy = my / box[1], hz = mz / box[2], m2 = hx * hx + hy * hy + hz * hz;
-                    double e = std::exp(-M_PI * M_PI * m2 / (al * al)) / (M_PI * V * m2 * modx[kx] * mody[ky] * modz[kz]);
+                    // m_x a* + m_y b* + m_z c* (:3351-3353)
+                    double hx = mx * R[0][0], hy = mx * R[1][0] + my * R[1][1],
+                           hz = mx * R[2][0] + my * R[2][1] + mz * R[2][2], m2 = hx * hx + hy * hy + hz * hz;
+                    double e = std::exp(-M_PI * M_PI * m2 / (al * al)) / (M_PI * vol * m2 * modx[kx] * mody[ky] * modz[kz]);
                     c.re *= e;
                     c.im *= e;
                 }
@@ -1236,14 +1245,23 @@ struct Port {
         nthreads = omp_get_max_threads();
         if (pme) {
             for (int k = 0; k < 3; ++k) box[k] = in->box[4 * k];
-            if (in->box[1] != 0 || in->box[2] != 0 || in->box[3] != 0 || in->box[5] != 0 || in->box[6] != 0 || in->box[7] != 0)
-                throw std::runtime_error("port: only rectangular boxes");
+            if (in->box[1] != 0 || in->box[2] != 0 || in->box[5] != 0)
+                throw std::runtime_error("port: the box must be in reduced form");
+            for (int k = 0; k < 9; ++k) V[k] = in->box[k];
+            tri = V[3] != 0 || V[6] != 0 || V[7] != 0;
+            const double sc = 1.0 / (V[0] * V[4] * V[8]);
+            const double Rr[3][3] = {{V[4] * V[8] * sc, 0, 0},
+                                     {-V[3] * V[8] * sc, V[0] * V[8] * sc, 0},
+                                     {(V[3] * V[7] - V[4] * V[6]) * sc, -V[0] * V[7] * sc, V[0] * V[4] * sc}};
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) R[i][j] = Rr[i][j];
             double minAllowed = 1.999999 * in->cutoff;
             if (box[0] < minAllowed || box[1] < minAllowed || box[2] < minAllowed)
                 throw std::runtime_error("The periodic box size has decreased to less than twice the nonbonded cutoff.");
             nx = in->grid[0]; ny = in->grid[1]; nz = in->grid[2];
+            // fractional grid transform a[j][i] = n_j R[i][j] (MPIDReferenceForce.cpp:3081-3084)
             for (int j = 0; j < 3; ++j)
-                for (int i = 0; i < 3; ++i) A[j][i] = (i == j) ? in->grid[j] / box[j] : 0.0;
+                for (int i = 0; i < 3; ++i) A[j][i] = in->grid[j] * R[i][j];
             modx = moduli(order, nx); mody = moduli(order, ny); modz = moduli(order, nz);
         }
         load_atoms();

@@ -14,7 +14,10 @@ oracle/Makefile) on seeded synthetic systems and stores inputs and outputs as .n
   getSystemMultipoleMoments and getElectrostaticPotential (64 seeded points) with
   seeded masses.
 
-Usage:  python tests/golden/make_fixtures.py [properties]   (needs the reference tree)
+* triclinic_{direct,mutual,extrapolated}.npz -- the water box in a reduced triclinic
+  cell (all three off-diagonal box entries non-zero).
+
+Usage:  python tests/golden/make_fixtures.py [properties | triclinic]   (needs the reference tree)
 """
 import os
 import sys
@@ -140,8 +143,35 @@ def make_properties():
              ref_moments=moments, ref_potential=potential)
 
 
+def triclinic_water(pol):
+    """The water648 system in a reduced triclinic cell: a = (L, 0, 0), b = (0.25 L,
+    0.97 L, 0), c = (-0.2 L, 0.3 L, 0.95 L), L = 1.864 nm; each oxygen keeps its
+    fractional coordinates, the hydrogens their offsets from it."""
+    f, pos, box = synthetic.workload("water648", polarization=pol, order=6)
+    L = box[0, 0]
+    cell = np.array([[L, 0, 0], [0.25 * L, 0.97 * L, 0], [-0.2 * L, 0.3 * L, 0.95 * L]])
+    o = pos[0::3]
+    newo = (o / L) @ cell
+    out = pos.copy()
+    for k in range(3):
+        out[k::3] = pos[k::3] - o + newo
+    return f, out, cell
+
+
+def make_triclinic():
+    """triclinic_{direct,mutual,extrapolated}.npz: the reference on triclinic_water."""
+    O.build("ref")
+    for pol in (1, 0, 2):
+        f, pos, box = triclinic_water(pol)
+        f.setMutualInducedTargetEpsilon(1e-9)
+        s = helpers.oracle_system(f, pos, box, pme_order=6)
+        save("triclinic_%s.npz" % POL[pol], s, O.evaluate(s, "ref", want_labdipoles=True))
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "properties":
         make_properties()
+    elif len(sys.argv) > 1 and sys.argv[1] == "triclinic":
+        make_triclinic()
     else:
         main()

@@ -29,7 +29,8 @@ def test_port_matches_golden(port, case):
 
 
 @pytest.mark.parametrize("name", ["water648_direct", "water648_mutual", "water648_extrapolated", "frames_direct",
-                                  "frames_mutual", "frames_extrapolated"])
+                                  "frames_mutual", "frames_extrapolated", "triclinic_direct", "triclinic_mutual",
+                                  "triclinic_extrapolated"])
 def test_port_matches_reference_fixtures(port, name):
     fx = helpers.load_npz_fixture(name + ".npz")
     s = helpers.system_from_fixture(fx)

@@ -62,7 +62,7 @@ def _torque_mapped_zonly(s):
 
 
 @pytest.mark.parametrize("pol", ["direct", "mutual", "extrapolated"])
-@pytest.mark.parametrize("system", ["water648", "frames"])
+@pytest.mark.parametrize("system", ["water648", "frames", "triclinic"])
 def test_fixture_double(system, pol):
     fx, s, f = _fixture_case("%s_%s.npz" % (system, pol))
     ctx, e, forces = run(f, s.pos, s.box, "double")
@@ -77,7 +77,7 @@ def test_fixture_double(system, pol):
 
 
 @pytest.mark.parametrize("pol", ["direct", "mutual", "extrapolated"])
-@pytest.mark.parametrize("system", ["water648", "frames"])
+@pytest.mark.parametrize("system", ["water648", "frames", "triclinic"])
 def test_fixture_mixed(system, pol):
     fx, s, f = _fixture_case("%s_%s.npz" % (system, pol))
     ctx, e, forces = run(f, s.pos, s.box, "mixed")
