@@ -126,7 +126,11 @@ class MPIDContext:
     """
 
     def __init__(self, force: MPIDForce, num_particles=None, device=0, precision="mixed",
-                 exact_aniso_torque=False, box=None, preconditioner=False):
+                 exact_aniso_torque=False, box=None, preconditioner=False, masses=None):
+        """masses: per-atom masses for getSystemMultipoleMoments through the force's
+        context methods (the System's masses in the reference).  box: the periodic box,
+        needed when the force's PME parameters are 0 (chosen from its Ewald error
+        tolerance, as the reference kernel does through OpenMM)."""
         self.lib = load_library()
         n = force.getNumMultipoles() if num_particles is None else int(num_particles)
         force.validate(n, box)
@@ -136,6 +140,18 @@ class MPIDContext:
         s.polarization_type = force.getPolarizationType()
         s.cutoff = force.getCutoffDistance()
         alpha, nx, ny, nz = force.getPMEParameters()
+        if force.getNonbondedMethod() == MPIDForce.PME and (alpha == 0.0 or 0 in (nx, ny, nz)):
+            # the automatic choice of MPIDCudaKernels.cpp:440-449 (OpenMM's rule)
+            if box is None:
+                raise MPIDError("MPIDForce: PME parameters are 0; give the periodic box to choose them from the "
+                                "Ewald error tolerance")
+            from .forcefield import pme_parameters
+            b = np.asarray(box, dtype=np.float64).reshape(3, 3)
+            alpha, (nx, ny, nz) = pme_parameters(force.getCutoffDistance(), [b[0, 0], b[1, 1], b[2, 2]],
+                                                 force.getEwaldErrorTolerance(), minimum=force.getPmeBSplineOrder())
+        self.masses = None if masses is None else np.asarray(masses, dtype=np.float64).reshape(n)
+        self.last_positions = None
+        self.last_box = None
         s.ewald_alpha = alpha
         s.grid[0], s.grid[1], s.grid[2] = nx, ny, nz
         s.pme_order = force.getPmeBSplineOrder()
@@ -178,6 +194,7 @@ class MPIDContext:
         """Energy (kJ/mol) and forces (n, 3) (kJ/mol/nm); forces are ADDED to `forces` if given."""
         pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(self.n, 3)
         b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+        self.last_positions, self.last_box = pos.copy(), b.copy()
         f = np.zeros((self.n, 3)) if forces is None else np.ascontiguousarray(forces, dtype=np.float64)
         e = ctypes.c_double(0.0)
         self._check(self.lib.mpid_evaluate(self._h, _dp(pos), _dp(b), _dp(f), ctypes.byref(e)))

@@ -226,6 +226,35 @@ class MPIDForce:
         )
 
     # ---- validation of MPIDForceImpl::initialize (MPIDForceImpl.cpp:56-150)
+    # Context-side queries of the reference's MPIDForce (MPIDForce.h:228, 379-435), taking
+    # an MPIDContext in place of an OpenMM Context.
+    def getPMEParametersInContext(self, context):
+        return context.getPMEParametersInContext()
+
+    def getLabFramePermanentDipoles(self, context):
+        return context.getLabFramePermanentDipoles()
+
+    def getInducedDipoles(self, context):
+        return context.getInducedDipoles()
+
+    def getTotalDipoles(self, context):
+        return context.getTotalDipoles()
+
+    def getElectrostaticPotential(self, inputGrid, context):
+        """At the context's last positions (those of its last evaluate call)."""
+        if context.last_positions is None:
+            raise MPIDError("getElectrostaticPotential: the context has no positions yet")
+        return context.getElectrostaticPotential(inputGrid, context.last_positions, context.last_box)
+
+    def getSystemMultipoleMoments(self, context):
+        """At the context's last positions, with the masses the context was created with."""
+        if context.last_positions is None or context.masses is None:
+            raise MPIDError("getSystemMultipoleMoments: the context needs masses and positions")
+        return context.getSystemMultipoleMoments(context.last_positions, context.last_box, context.masses)
+
+    def updateParametersInContext(self, context):
+        context.update_parameters(self)
+
     def validate(self, num_particles, box=None):
         if self.getNumMultipoles() != num_particles:
             raise MPIDError("MPIDForce must have exactly as many particles as the System it belongs to.")

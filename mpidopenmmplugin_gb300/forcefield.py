@@ -339,10 +339,11 @@ class ForceField:
         return force
 
 
-def pme_parameters(cutoff, box, tolerance=5e-4):
+def pme_parameters(cutoff, box, tolerance=5e-4, minimum=5):
     """Ewald alpha (1/nm) and grid for a cutoff (nm), box edges (nm) and error tolerance,
     by the published rule OpenMM documents for its PME: alpha = sqrt(-ln(2 tol)) / cutoff,
-    n_k = ceil(2 alpha L_k / (3 tol^(1/5))) rounded up to a product of 2, 3, 5 and 7."""
+    n_k = ceil(2 alpha L_k / (3 tol^(1/5))) rounded up to a product of 2, 3, 5 and 7 (at
+    least `minimum`, the B-spline order)."""
     alpha = math.sqrt(-math.log(2.0 * tolerance)) / cutoff
 
     def smooth(n):
@@ -355,5 +356,5 @@ def pme_parameters(cutoff, box, tolerance=5e-4):
                 return n
             n += 1
 
-    grid = [smooth(max(5, int(math.ceil(2.0 * alpha * L / (3.0 * tolerance ** 0.2))))) for L in box]
+    grid = [smooth(max(minimum, int(math.ceil(2.0 * alpha * L / (3.0 * tolerance ** 0.2))))) for L in box]
     return alpha, grid

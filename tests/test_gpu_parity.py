@@ -321,3 +321,39 @@ def test_parameter_gradients_finite_differences_on_device():
         an = float((g * v).sum())
         print("direction %d: analytic %.10e fd %.10e" % (trial, an, fd))
         assert abs(an - fd) <= 1e-6 * max(abs(fd), 1.0)
+
+
+def test_automatic_pme_parameters_and_force_side_queries():
+    """PME parameters left at 0 are chosen from the Ewald error tolerance (OpenMM's rule,
+    as the reference kernel does); the force's context queries of the reference API
+    (getInducedDipoles(context), getPMEParametersInContext(context), ...) answer through
+    an MPIDContext."""
+    from mpidopenmmplugin_gb300.forcefield import pme_parameters
+    f, pos, box = synthetic.workload("water648", polarization=MPIDForce.Mutual, order=5)
+    f.setPMEParameters(0.0, 0, 0, 0)
+    f.setEwaldErrorTolerance(5e-4)
+    with pytest.raises(Exception, match="PME parameters are 0"):
+        MPIDContext(f, precision="double")
+    masses = np.tile([15.999, 1.008, 1.008], f.getNumMultipoles() // 3)
+    ctx = MPIDContext(f, precision="double", box=box, masses=masses)
+    alpha, grid = pme_parameters(f.getCutoffDistance(), np.diag(box), 5e-4, minimum=5)
+    assert f.getPMEParametersInContext(ctx) == (alpha, grid[0], grid[1], grid[2])
+    e, forces = ctx.evaluate(pos, box)
+    f2 = synthetic.workload("water648", polarization=MPIDForce.Mutual, order=5)[0]
+    f2.setPMEParameters(alpha, *grid)
+    e2, forces2 = MPIDContext(f2, precision="double").evaluate(pos, box)
+    assert abs(e - e2) <= 1e-12 * abs(e2) and helpers.rel_rms(forces, forces2) < 1e-12
+    assert np.array_equal(f.getInducedDipoles(ctx), ctx.getInducedDipoles())
+    assert np.array_equal(f.getTotalDipoles(ctx), ctx.getTotalDipoles())
+    assert np.array_equal(f.getLabFramePermanentDipoles(ctx), ctx.getLabFramePermanentDipoles())
+    m = f.getSystemMultipoleMoments(ctx)
+    assert np.allclose(m, ctx.getSystemMultipoleMoments(pos, box, masses), rtol=1e-12, atol=1e-12)
+    grid_pts = np.random.default_rng(2).uniform(0, box[0, 0], size=(5, 3))
+    assert np.allclose(f.getElectrostaticPotential(grid_pts, ctx), ctx.getElectrostaticPotential(grid_pts, pos, box),
+                       rtol=1e-12, atol=1e-12)
+    # updateParametersInContext: a changed charge reaches the context
+    p = list(f.getMultipoleParameters(0))
+    p[0] += 0.01
+    f.setMultipoleParameters(0, *p)
+    f.updateParametersInContext(ctx)
+    assert ctx.evaluate(pos, box)[0] != e
