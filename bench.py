@@ -256,6 +256,8 @@ def run_fitting(args, world, rank, local):
             "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded water boxes)",
             "config": {"workload": FITTING_WORKLOAD, "atoms": natoms, "host_threads": args.threads,
+                       "solver_graphs": True,
+                       "device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                        "l2": "inputs copied from host each step"},
             "arms": out,
             "mixed_vs_fp64_gradient_rel": None if gd is None else float(np.linalg.norm(gm - gd) / np.linalg.norm(gd)),
@@ -276,6 +278,10 @@ def main():
     ap.add_argument("--threads", type=int, default=8, help="host threads driving the boxes of fitting64")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.workload == "fitting64":
+        # 64 contexts on 4 streams each: more hardware work queues than the default 8, so
+        # that independent boxes do not queue behind one another (read at CUDA start-up)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     world, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -17,6 +17,7 @@ MPID_PRECISION_MIXED = 0
 MPID_PRECISION_DOUBLE = 1
 MPID_FLAG_EXACT_ANISO_TORQUE = 1
 MPID_FLAG_NEAR_FIELD_PCG = 2
+MPID_FLAG_GRAPH_SOLVER = 4
 
 # Entry points declared in include/mpid_gb300.h
 C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multipoles", "mpid_set_covalent",
@@ -126,11 +127,13 @@ class MPIDContext:
     """
 
     def __init__(self, force: MPIDForce, num_particles=None, device=0, precision="mixed",
-                 exact_aniso_torque=False, box=None, preconditioner=False, masses=None):
+                 exact_aniso_torque=False, box=None, preconditioner=False, masses=None, solver_graphs=False):
         """masses: per-atom masses for getSystemMultipoleMoments through the force's
         context methods (the System's masses in the reference).  box: the periodic box,
         needed when the force's PME parameters are 0 (chosen from its Ewald error
-        tolerance, as the reference kernel does through OpenMM)."""
+        tolerance, as the reference kernel does through OpenMM).  solver_graphs: replay the
+        mutual solver's iterations from captured CUDA graphs (small systems, many
+        contexts driven at once)."""
         self.lib = load_library()
         n = force.getNumMultipoles() if num_particles is None else int(num_particles)
         force.validate(n, box)
@@ -167,7 +170,8 @@ class MPIDContext:
         s.scale14 = force.get14ScaleFactor()
         s.precision = {"mixed": MPID_PRECISION_MIXED, "double": MPID_PRECISION_DOUBLE}[precision]
         s.flags = ((MPID_FLAG_EXACT_ANISO_TORQUE if exact_aniso_torque else 0) |
-                   (MPID_FLAG_NEAR_FIELD_PCG if preconditioner else 0))
+                   (MPID_FLAG_NEAR_FIELD_PCG if preconditioner else 0) |
+                   (MPID_FLAG_GRAPH_SOLVER if solver_graphs else 0))
         self.n = n
         self.precision = precision
         self._h = ctypes.c_void_p()

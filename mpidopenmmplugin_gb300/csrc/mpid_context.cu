@@ -7,6 +7,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -78,6 +79,10 @@ static inline void launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_
 // cuFFT executions and cub sorts (library code launching its own kernels).
 static thread_local long long t_library_calls = 0;
 
+// Device allocations made by any buffer so far: captured graphs key on it, so that no
+// graph outlives a pointer it holds.
+static std::atomic<unsigned long long> g_device_allocs{0};
+
 // Simple owning device buffer.
 template <typename T>
 struct DBuf {
@@ -88,6 +93,7 @@ struct DBuf {
         free();
         CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
         n = count;
+        ++g_device_allocs;
     }
     void free() {
         if (p) cudaFree(p);
@@ -240,6 +246,7 @@ struct StageTimer {
     std::vector<cudaEvent_t> ev;
     std::vector<int> stage;
     int count = 0, open = -1;
+    bool paused = false;  // while a stream capture is open: captured events cannot be timed
     double ms[ST_COUNT] = {0};
     int launches[ST_COUNT] = {0};
     void init() {
@@ -257,7 +264,7 @@ struct StageTimer {
         for (int s = 0; s < ST_COUNT; ++s) { ms[s] = 0; launches[s] = 0; }
     }
     void begin(int s, cudaStream_t st) {
-        if (count >= kMax || ev.empty()) return;
+        if (count >= kMax || ev.empty() || paused) return;
         stage[count] = s;
         CUDA_CHECK(cudaEventRecord(ev[2 * count], st));
         open = count;
@@ -374,7 +381,8 @@ struct Context {
     // extrapolated
     DBuf<float> ptMuF, ptEF, ptGF;
     DBuf<double> ptMuD, ptED, ptGD;
-    int* hostDone = nullptr;
+    int* hostDone = nullptr;       // pinned: 256 iteration flags, then the solve's iteration count
+    double* hostSc = nullptr;      // pinned: the solver scalars after a solve
     int* hostMax = nullptr;        // list maxima (pinned)
     cudaEvent_t evLists = nullptr;
     std::vector<cudaEvent_t> iterEvents;
@@ -385,9 +393,26 @@ struct Context {
     bool gradPrepared = false;  // FP64 inputs of the gradient pass hold the last evaluation
     BoxDev box{};
 
+    // Captured segments of the evaluation (MPID_FLAG_GRAPH_SOLVER); `key` holds every
+    // value the launches bake in (graph_key), so a changed list shape, buffer or box
+    // captures a new graph.
+    struct SolverGraph {
+        std::vector<long long> key;
+        long long nodes = 0;  // kernel launches one replay stands for
+        long long library = 0;
+        unsigned long long used = 0;
+        cudaGraphExec_t exec = nullptr;
+    };
+    std::vector<SolverGraph> graphs;
+    unsigned long long graphClock = 0;
+    int predictedIters = 0;  // iterations of the last solve: the first replayed chunk's length
+
     ~Context() {
+        for (auto& g : graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
         timer.destroy();
         if (hostDone) cudaFreeHost(hostDone);
+        if (hostSc) cudaFreeHost(hostSc);
         if (evFork) cudaEventDestroy(evFork);
         if (evJoin) cudaEventDestroy(evJoin);
         if (pmeStream) cudaStreamDestroy(pmeStream);
@@ -471,7 +496,8 @@ struct Context {
         }
         CUDA_CHECK(cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming));
         CUDA_CHECK(cudaEventCreateWithFlags(&evJoin, cudaEventDisableTiming));
-        CUDA_CHECK(cudaMallocHost(&hostDone, 256 * sizeof(int)));
+        CUDA_CHECK(cudaMallocHost(&hostDone, 260 * sizeof(int)));
+        CUDA_CHECK(cudaMallocHost(&hostSc, 8 * sizeof(double)));
         CUDA_CHECK(cudaMallocHost(&hostMax, 4 * sizeof(int)));
         CUDA_CHECK(cudaEventCreateWithFlags(&evLists, cudaEventDisableTiming));
         CUDA_CHECK(cudaEventCreate(&evStart));
@@ -830,7 +856,7 @@ struct Context {
     // Tile lists and per-atom lists from the sorted offsets of engine e; the list maxima
     // go to pinned host memory, read by finish_lists.
     template <typename real>
-    void launch_lists(Engine<real>& e) {
+    void launch_lists(Engine<real>& e, bool record = true) {
         cudaStream_t st = stream;
         const double listCut = list_cutoff();
         const float cut2 = usePme ? (float) (listCut * listCut) : 3.0e38f;
@@ -843,7 +869,7 @@ struct Context {
                (const int*) e.orig.p, box, cut2, quadR2, usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, covOff.p,
                covJ.p, covS.p, cap, countL.p, countS.p, loL.p, loS.p, tmaxL.p, tmaxS.p, list.p, listMax.p + 1);
         CUDA_CHECK(cudaMemcpyAsync(hostMax, listMax.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaEventRecord(evLists, st));
+        if (record) CUDA_CHECK(cudaEventRecord(evLists, st));
     }
 
     // Waits for the list maxima (work queued after launch_lists keeps the GPU busy), grows
@@ -1006,48 +1032,192 @@ struct Context {
                p, first ? 1 : 0, partial.p, counters.p + 2, sc.p, (const int*) done.p);
     }
 
-    // Preconditioned CG on B y = b, B = I - S T S, in precision `real`; x accumulates in xreal.
-    // Convergence: 48.033324 sqrt(|S r|^2/n) < target.  Returns iterations used.
+    // Graph replay is used under PME (the configuration it is tested on).
+    bool graph_mode() const { return (set.flags & MPID_FLAG_GRAPH_SOLVER) != 0 && usePme; }
+
+    // One CG iteration: q = B p = p - S T S p, p.q, then the update and the scalars
+    // (PCG: p from z = P r).  Launches only.
     template <typename real, typename xreal>
-    int cg_solve(Engine<real>& e, const real* b, xreal* x, real* r, real* p, real* q, double target, int maxIter,
-                 double* finalMetric) {
+    void cg_iteration(Engine<real>& e, xreal* x, real* r, real* p, real* q, double target, int maxIter, bool first) {
+        const bool pcg = (set.flags & MPID_FLAG_NEAR_FIELD_PCG) != 0;
+        cg_matvec(e, pcg ? (const real*) e.zc.p : (const real*) r, p, q, first);
+        launch(k_cg_update_scalars<real, xreal>, nblk(npad, 256), 256, 0, stream, n, npad, e.sroot.p, sc.p, p, q, x, r,
+               partial.p, counters.p + 1, target, iter.p, maxIter, done.p, pcg ? 1 : 0);
+        if (pcg) precondition(e, r, p, false);
+        CUDA_CHECK(cudaGetLastError());
+    }
+
+    // Preconditioned CG on B y = b, B = I - S T S, in precision `real`; x accumulates in xreal.
+    // Convergence: 48.033324 sqrt(|S r|^2/n) < target.  cg_begin queues the start (and,
+    // with solver graphs, iteration 0) without waiting; cg_finish runs the iterations to
+    // convergence and returns the number used.
+    template <typename real, typename xreal>
+    void cg_begin(Engine<real>& e, const real* b, xreal* x, real* r, real* p, real* q, double target, int maxIter) {
         cudaStream_t st = stream;
         const int nb = nblk(npad, 256);
         launch(k_cg_start<real, xreal>, nb, 256, 0, st, npad, e.sroot.p, b, x, r, p, partial.p, nb);
         launch(k_reduce_partials, 1, 1024, 0, st, nb, 2, partial.p, red.p, nullptr);
         launch(k_cg_init_scalars, 1, 1, 0, st, sc.p, red.p, n, target, iter.p, done.p);
         CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));  // cleared again by each matvec
-        const bool pcg = (set.flags & MPID_FLAG_NEAR_FIELD_PCG) != 0;
-        if (pcg) {
+        if (set.flags & MPID_FLAG_NEAR_FIELD_PCG) {
             CUDA_CHECK(cudaMemsetAsync(e.precFx.p, 0, 3 * (size_t) npad * 8, st));  // cleared by each application
             precondition(e, r, p, true);
         }
         CUDA_CHECK(cudaGetLastError());
-        int it = 0;
-        for (it = 0; it < maxIter; ++it) {
-            // q = B p = p - S T S p, p.q, then the update and the scalars (PCG: p from z = P r)
-            cg_matvec(e, pcg ? (const real*) e.zc.p : (const real*) r, p, q, it == 0);
-            launch(k_cg_update_scalars<real, xreal>, nb, 256, 0, st, n, npad, e.sroot.p, sc.p, p, q, x, r, partial.p,
-                   counters.p + 1, target, iter.p, maxIter, done.p, pcg ? 1 : 0);
-            if (pcg) precondition(e, r, p, false);
-            CUDA_CHECK(cudaGetLastError());
-            const int slot = it % (int) iterEvents.size();
-            CUDA_CHECK(cudaMemcpyAsync(hostDone + (slot % 256), done.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-            CUDA_CHECK(cudaEventRecord(iterEvents[slot], st));
-            // Check the previous iteration's flag while this one runs (one-iteration lag).
-            if (it >= 1) {
-                const int prev = (it - 1) % (int) iterEvents.size();
-                CUDA_CHECK(cudaEventSynchronize(iterEvents[prev]));
-                if (hostDone[prev % 256]) break;
+        if (graph_mode() && maxIter > 1) cg_iteration(e, x, r, p, q, target, maxIter, true);
+    }
+
+    template <typename real, typename xreal>
+    int cg_finish(Engine<real>& e, const real* b, xreal* x, real* r, real* p, real* q, double target, int maxIter,
+                  double* finalMetric) {
+        cudaStream_t st = stream;
+        if (graph_mode() && maxIter > 1) {
+            // Chunks replayed from graphs: first the length the last solve needed, then two
+            // at a time.  Every iteration kernel returns at once when `done` is set, so a
+            // chunk that overshoots costs only its launches.
+            const bool pcg = (set.flags & MPID_FLAG_NEAR_FIELD_PCG) != 0;
+            int it = 1, len = predictedIters > 1 ? predictedIters - 1 : 4;
+            std::vector<long long> key = graph_key(kSegChunk);
+            const void* ptrs[] = {&e, b, x, r, p, q};
+            const long long more[] = {maxIter, pcg ? 1 : 0};
+            key_put(key, ptrs, sizeof ptrs);
+            key_put(key, more, sizeof more);
+            key_put(key, &target, sizeof target);
+            while (it < maxIter) {
+                len = std::min(len, maxIter - it);
+                std::vector<long long> k = key;
+                k.push_back(len);
+                replay(k, [&] {
+                    for (int i = 0; i < len; ++i) cg_iteration(e, x, r, p, q, target, maxIter, false);
+                });
+                it += len;
+                CUDA_CHECK(cudaMemcpyAsync(hostDone, done.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CUDA_CHECK(cudaEventRecord(iterEvents[0], st));
+                CUDA_CHECK(cudaEventSynchronize(iterEvents[0]));
+                if (hostDone[0]) break;
+                len = 2;
+            }
+        } else {
+            for (int it = 0; it < maxIter; ++it) {
+                cg_iteration(e, x, r, p, q, target, maxIter, it == 0);
+                const int slot = it % (int) iterEvents.size();
+                CUDA_CHECK(cudaMemcpyAsync(hostDone + (slot % 256), done.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CUDA_CHECK(cudaEventRecord(iterEvents[slot], st));
+                // Check the previous iteration's flag while this one runs (one-iteration lag).
+                if (it >= 1) {
+                    const int prev = (it - 1) % (int) iterEvents.size();
+                    CUDA_CHECK(cudaEventSynchronize(iterEvents[prev]));
+                    if (hostDone[prev % 256]) break;
+                }
             }
         }
+        CUDA_CHECK(cudaMemcpyAsync(hostDone + 256, iter.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaMemcpyAsync(hostSc, sc.p, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
-        int used = 0;
-        double h_sc[8];
-        CUDA_CHECK(cudaMemcpy(&used, iter.p, sizeof(int), cudaMemcpyDeviceToHost));
-        CUDA_CHECK(cudaMemcpy(h_sc, sc.p, 8 * sizeof(double), cudaMemcpyDeviceToHost));
-        if (finalMetric) *finalMetric = h_sc[6];
+        const int used = hostDone[256];
+        if (finalMetric) *finalMetric = hostSc[6];
+        predictedIters = used;
         return used;
+    }
+
+    template <typename real, typename xreal>
+    int cg_solve(Engine<real>& e, const real* b, xreal* x, real* r, real* p, real* q, double target, int maxIter,
+                 double* finalMetric) {
+        cg_begin(e, b, x, r, p, q, target, maxIter);
+        return cg_finish(e, b, x, r, p, q, target, maxIter, finalMetric);
+    }
+
+    // ----- CUDA graphs (MPID_FLAG_GRAPH_SOLVER) -----
+    // Segments of an evaluation between host synchronisations are captured once and
+    // replayed.  A graph is found by a key of 64-bit words holding every value its
+    // launches bake in: the segment, the device-buffer generation (any reallocation
+    // anywhere changes it), the list buffers (the no-alloc call points them at its
+    // scratch), the list shape and launch sizes, the box and the constants.
+    enum { kSegChunk = 1, kSegSetup, kSegSolveStart, kSegFinish, kSegGradients };
+
+    static void key_put(std::vector<long long>& k, const void* v, size_t bytes) {
+        const size_t o = k.size();
+        k.resize(o + (bytes + 7) / 8, 0);
+        std::memcpy(k.data() + o, v, bytes);
+    }
+
+    std::vector<long long> graph_key(int segment) const {
+        std::vector<long long> k;
+        const long long ints[] = {segment, (long long) g_device_allocs.load(), n, npad, ntiles, tcap, cap, chunk,
+                                  nchunksL, nchunksS, field_split(), field_blocks(), nScaled, mixed ? 1 : 0,
+                                  usePme ? 1 : 0, (long long) energyBlocks.n, (long long) list.n};
+        key_put(k, ints, sizeof ints);
+        const void* ptrs[] = {list.p, energyBlocks.p};
+        key_put(k, ptrs, sizeof ptrs);
+        const double dbl[] = {self_coef(), set.ewald_alpha, set.cutoff, set.default_thole, set.mutual_eps};
+        key_put(k, dbl, sizeof dbl);
+        static_assert(sizeof(BoxDev) == 33 * sizeof(double) + 4 * sizeof(int), "BoxDev has padding");
+        key_put(k, &box, sizeof box);
+        return k;
+    }
+
+    // Runs `body` (launches only: no host synchronisation, allocation or host-side state
+    // that a replay would skip) directly, or with graphs from the graph of `key`,
+    // capturing it on first use.
+    template <typename Body>
+    void replay(const std::vector<long long>& key, Body&& body) {
+        if (!graph_mode()) {
+            body();
+            return;
+        }
+        const SolverGraph& g = solver_graph(key, body);
+        CUDA_CHECK(cudaGraphLaunch(g.exec, stream));
+        t_launches += g.nodes;
+        t_library_calls += g.library;
+    }
+
+    // The graph of `key`, captured by running `body` on the main stream under stream
+    // capture (side streams join the capture through the fork/join events and must be
+    // joined back by the end of `body`).  At most eight graphs are kept; the least
+    // recently used goes.
+    template <typename Body>
+    const SolverGraph& solver_graph(const std::vector<long long>& key, Body&& body) {
+        for (auto& g : graphs)
+            if (g.key == key) {
+                g.used = ++graphClock;
+                return g;
+            }
+        cudaStream_t st = stream;
+        const long long l0 = t_launches, c0 = t_library_calls;
+        cudaGraph_t graph = nullptr;
+        timer.paused = true;
+        CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            body();
+        } catch (...) {
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            timer.paused = false;
+            t_launches = l0;
+            t_library_calls = c0;
+            throw;
+        }
+        timer.paused = false;
+        CUDA_CHECK(cudaStreamEndCapture(st, &graph));
+        SolverGraph g;
+        g.key = key;
+        g.nodes = t_launches - l0;
+        g.library = t_library_calls - c0;
+        t_launches = l0;  // counted when replayed
+        t_library_calls = c0;
+        const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CUDA_CHECK(ie);
+        g.used = ++graphClock;
+        if (graphs.size() < 8) {
+            graphs.push_back(std::move(g));
+            return graphs.back();
+        }
+        auto lru = std::min_element(graphs.begin(), graphs.end(),
+                                    [](const SolverGraph& a, const SolverGraph& c) { return a.used < c.used; });
+        CUDA_CHECK(cudaGraphExecDestroy(lru->exec));
+        *lru = std::move(g);
+        return *lru;
     }
 
     template <typename real>
@@ -1107,31 +1277,42 @@ struct Context {
     // the check and, if the residual misses the target, continues the outer iterations
     // (returning false: the force/energy phase must run again).
     void solve_mutual_mixed(Engine<float>& e, Engine<double>& d) {
-        cudaStream_t st = stream;
-        const size_t n3 = 3 * (size_t) npad;
-        // Efix in FP64 for the residual
-        CUDA_CHECK(cudaMemsetAsync(Efix64.p, 0, n3 * 8, st));
-        launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3, e.Efix.p, Efix64.p);
-        CUDA_CHECK(cudaMemsetAsync(y64.p, 0, n3 * 8, st));
-        CUDA_CHECK(cudaMemcpyAsync(b32.p, e.SE.p, n3 * 4, cudaMemcpyDeviceToDevice, st));
+        mutual_mixed_start(e);
         refOuter = 0;
         refTotal = 0;
         inner_solve_and_check(e, d);
     }
 
+    // FP64 permanent field for the residual, y = 0, b = S E (launches only).
+    void mutual_mixed_start(Engine<float>& e) {
+        cudaStream_t st = stream;
+        const size_t n3 = 3 * (size_t) npad;
+        CUDA_CHECK(cudaMemsetAsync(Efix64.p, 0, n3 * 8, st));
+        launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3, e.Efix.p, Efix64.p);
+        CUDA_CHECK(cudaMemsetAsync(y64.p, 0, n3 * 8, st));
+        CUDA_CHECK(cudaMemcpyAsync(b32.p, e.SE.p, n3 * 4, cudaMemcpyDeviceToDevice, st));
+    }
+
+    // inner FP32 solves stop at half the target: the FP64 residual then meets the target
+    // with a 2x margin for the FP32 operator's rounding (water24k: 9 iterations, final
+    // FP64 residual 4.3e-8 D for a 1e-7 D target)
+    double inner_target() const { return 0.5 * set.mutual_eps; }
+
     // One outer step: inner FP32 solve from b32, y += x, dipoles from y on the main
     // stream, and the FP64 residual S (E + T S y) - y launched on the refinement streams.
     void inner_solve_and_check(Engine<float>& e, Engine<double>& d) {
+        const int maxIter = std::max(1, set.max_iter - refTotal);
+        refTotal += cg_solve<float, float>(e, b32.p, x32.p, r32.p, p32.p, q32.p, inner_target(), maxIter, nullptr);
+        launch_check(e, d);
+        ++refOuter;
+    }
+
+    // y += x, the dipoles from y, and the FP64 residual check on the refinement streams,
+    // which ends with evRefDone recorded there (launches only).
+    void launch_check(Engine<float>& e, Engine<double>& d) {
         cudaStream_t st = stream;
         const int nb = nblk(npad, 256);
         const size_t n3 = 3 * (size_t) npad;
-        // inner FP32 solves stop at half the target: the FP64 residual then meets the target
-        // with a 2x margin for the FP32 operator's rounding (water24k: 9 iterations, final
-        // FP64 residual 4.3e-8 D for a 1e-7 D target)
-        const double innerTarget = 0.5 * set.mutual_eps;
-        double innerMetric = 0.0;
-        refTotal += cg_solve<float, float>(e, b32.p, x32.p, r32.p, p32.p, q32.p, innerTarget,
-                                           std::max(1, set.max_iter - refTotal), &innerMetric);
         launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3, x32.p, y64.p);
         launch(k_mu_from_y<double, float>, nblk(npad, 128), 128, 0, st, npad, d.sroot.p, y64.p, e.mu.p);
         CUDA_CHECK(cudaEventRecord(evRefStart, st));
@@ -1153,7 +1334,29 @@ struct Context {
         std::swap(pmeStream, refPmeStream);
         std::swap(evFork, evRefFork);
         std::swap(evJoin, evRefJoin);
+    }
+
+    // The mixed Mutual evaluation from the permanent field on, as three captured segments
+    // and two host waits: (permanent field, solver start, iteration 0) | iterations | (check
+    // on the refinement streams beside the force/energy phase, joined at the end).  The
+    // rare second outer step runs as in the direct flow.
+    void mutual_mixed_graphs(Engine<float>& e, Engine<double>& d) {
+        const int maxIter = std::max(1, set.max_iter);
+        replay(graph_key(kSegSolveStart), [&] {
+            fixed_field(e);
+            mutual_mixed_start(e);
+            cg_begin<float, float>(e, b32.p, x32.p, r32.p, p32.p, q32.p, inner_target(), maxIter);
+        });
+        refOuter = 0;
+        refTotal = cg_finish<float, float>(e, b32.p, x32.p, r32.p, p32.p, q32.p, inner_target(), maxIter, nullptr);
+        replay(graph_key(kSegFinish), [&] {
+            launch_check(e, d);
+            finish(e, ptMuF.p, ptEF.p, ptGF.p);
+            CUDA_CHECK(cudaStreamWaitEvent(stream, evRefDone, 0));
+        });
         ++refOuter;
+        CUDA_CHECK(cudaEventRecord(evRefDone, stream));  // the check's result is in refHost once this passes
+        if (!finish_mutual_mixed(e, d)) finish(e, ptMuF.p, ptEF.p, ptGF.p);
     }
 
     // Wait for the pending check; true if the dipoles the force/energy phase used stand.
@@ -1272,41 +1475,52 @@ struct Context {
         timer.reset();
         timer.begin(ST_SETUP, st);
         set_box(hbox);
-        sort_and_tiles();
         if (mixed) {
             Engine<float>& e = *ef;
-            prepare_engine(e, true);
-            launch(k_pack_atoms, nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
-                   pack0.p);
-            if (ed) {
-                // the FP64 engine of the residual check is prepared on the check's stream,
-                // beside the list build (it is first read by the check)
-                CUDA_CHECK(cudaEventRecord(evRefStart, st));
-                CUDA_CHECK(cudaStreamWaitEvent(refStream, evRefStart, 0));
-                std::swap(stream, refStream);
-                std::swap(pmeStream, refPmeStream);
-                prepare_engine(*ed, false);
-                launch(k_df_atoms, nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p, tholeDF.p,
-                       dampDF.p);
-                std::swap(stream, refStream);
-                std::swap(pmeStream, refPmeStream);
-            }
-            launch_lists(e);
+            replay(graph_key(kSegSetup), [&] {
+                sort_and_tiles();
+                prepare_engine(e, true);
+                launch(k_pack_atoms, nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
+                       pack0.p);
+                if (ed) {
+                    // the FP64 engine of the residual check is prepared on the check's stream,
+                    // beside the list build (it is first read by the check)
+                    CUDA_CHECK(cudaEventRecord(evRefStart, st));
+                    CUDA_CHECK(cudaStreamWaitEvent(refStream, evRefStart, 0));
+                    std::swap(stream, refStream);
+                    std::swap(pmeStream, refPmeStream);
+                    prepare_engine(*ed, false);
+                    launch(k_df_atoms, nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p,
+                           tholeDF.p, dampDF.p);
+                    std::swap(stream, refStream);
+                    std::swap(pmeStream, refPmeStream);
+                    if (graph_mode()) {  // a captured side stream joins back before the capture ends
+                        CUDA_CHECK(cudaEventRecord(evRefStart, refStream));
+                        CUDA_CHECK(cudaStreamWaitEvent(st, evRefStart, 0));
+                    }
+                }
+                launch_lists(e, false);
+            });
+            CUDA_CHECK(cudaEventRecord(evLists, st));
             finish_lists(e);
             stats.max_neighbours = lastMaxList;
             timer.end(st);
-            fixed_field(e);
-            if (set.polarization_type == MPID_MUTUAL) {
+            if (set.polarization_type == MPID_MUTUAL && graph_mode()) {
+                mutual_mixed_graphs(e, *ed);
+            } else if (set.polarization_type == MPID_MUTUAL) {
+                fixed_field(e);
                 solve_mutual_mixed(e, *ed);
                 finish(e, ptMuF.p, ptEF.p, ptGF.p);  // concurrent with the residual check
                 if (!finish_mutual_mixed(e, *ed)) finish(e, ptMuF.p, ptEF.p, ptGF.p);
             } else {
+                fixed_field(e);
                 solve_dipoles(e, ptMuF.p, ptEF.p, ptGF.p);
                 finish(e, ptMuF.p, ptEF.p, ptGF.p);
             }
             launch(k_forces_out, nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, d_forces);
         } else {
             Engine<double>& e = *ed;
+            sort_and_tiles();
             prepare_engine(e, true);
             launch_lists(e);
             finish_lists(e);
@@ -1504,13 +1718,43 @@ struct Context {
     int gradient_blocks(int split) const { return std::max(1, nblk((long long) pair_tasks() * split, kWarpsPerBlock)); }
 
     // dE/d(molecular-frame polarisability X Y Z, Thole width) of every atom for the last
-    // evaluation (Mutual, Direct).
-    void polarization_gradients(double* host) {
+    // evaluation (Mutual, Direct, Extrapolated).
+    void polarization_gradients(double* host, bool wait = true) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+        gradient_buffers(false, true);
+        polarization_gradient_launches();
+        CUDA_CHECK(cudaMemcpyAsync(host, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, stream));
+        if (wait) CUDA_CHECK(cudaStreamSynchronize(stream));
+    }
+
+    // Device buffers of the gradient passes (allocated before any launch is queued, so
+    // that the launches can be captured).
+    void gradient_buffers(bool multipole, bool polarization) {
+        if (mixed && !ed && !eg) {
+            eg.reset(new Engine<double>());
+            eg->init(n, npad, usePme, set.pme_order, set.grid);
+        }
+        if (multipole) {
+            gradFx.alloc((size_t) 20 * npad);
+            gradOut.alloc((size_t) 20 * n);
+        }
+        if (polarization) {
+            polFx.alloc((size_t) 2 * npad);
+            polOut.alloc((size_t) 4 * n);
+            if (set.polarization_type == MPID_EXTRAPOLATED && mixed) {
+                const size_t n3 = 3 * (size_t) npad;
+                const int nPT = set.n_extrap;
+                gradPtMu.alloc((size_t) nPT * n3);
+                gradPtE.alloc((size_t) std::max(nPT - 1, 1) * n3);
+                gradEfix.alloc(n3);
+            }
+        }
+    }
+
+    // The polarisation-gradient pass into polOut (launches only).
+    void polarization_gradient_launches() {
         Engine<double>& d = gradient_engine();
         cudaStream_t st = stream;
-        polFx.alloc((size_t) 2 * npad);
-        polOut.alloc((size_t) 4 * n);
         CUDA_CHECK(cudaMemsetAsync(polFx.p, 0, (size_t) 2 * npad * 8, st));
         const int mutual = set.polarization_type == MPID_MUTUAL ? 1 : 0;
         // Extrapolated: the perturbation orders, their fields and the permanent field
@@ -1529,9 +1773,6 @@ struct Context {
             }
             if (mixed) {
                 const size_t n3 = 3 * (size_t) npad;
-                gradPtMu.alloc((size_t) nPT * n3);
-                gradPtE.alloc((size_t) std::max(nPT - 1, 1) * n3);
-                gradEfix.alloc(n3);
                 CUDA_CHECK(cudaMemsetAsync(gradPtMu.p, 0, (size_t) nPT * n3 * 8, st));
                 CUDA_CHECK(cudaMemsetAsync(gradPtE.p, 0, (size_t) std::max(nPT - 1, 1) * n3 * 8, st));
                 CUDA_CHECK(cudaMemsetAsync(gradEfix.p, 0, n3 * 8, st));
@@ -1565,8 +1806,6 @@ struct Context {
                (const double*) pos.p, (const unsigned long long*) polFx.p, (const double*) d.mu.p, optD, efixD, ptED,
                polOut.p);
         CUDA_CHECK(cudaGetLastError());
-        CUDA_CHECK(cudaMemcpyAsync(host, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaStreamSynchronize(st));
     }
 
     // dE/d(molecular-frame multipole parameters) of every atom for the last evaluation.
@@ -1574,12 +1813,18 @@ struct Context {
     // segment of the lists (alpha r >= 1.5, no excluded pairs), which runs in FP32.  Without
     // a cutoff every pair is bare 1/r, near ones included, and FP32 rank-6 derivative
     // tensors of those cost 1.6e-4 relative (160-atom test system), so all run in FP64.
-    void parameter_gradients(double* host) {
+    void parameter_gradients(double* host, bool wait = true) {
         if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+        gradient_buffers(true, false);
+        multipole_gradient_launches();
+        CUDA_CHECK(cudaMemcpyAsync(host, gradOut.p, (size_t) 20 * n * 8, cudaMemcpyDeviceToHost, stream));
+        if (wait) CUDA_CHECK(cudaStreamSynchronize(stream));
+    }
+
+    // The multipole-gradient pass into gradOut (launches only).
+    void multipole_gradient_launches() {
         Engine<double>& d = gradient_engine();
         cudaStream_t st = stream;
-        gradFx.alloc((size_t) 20 * npad);
-        gradOut.alloc((size_t) 20 * n);
         CUDA_CHECK(cudaMemsetAsync(gradFx.p, 0, (size_t) 20 * npad * 8, st));
         const int sL = gradient_split((long long) ntiles * nchunksL), sS = gradient_split((long long) ntiles * nchunksS);
         const int sA = gradient_split(pair_tasks());
@@ -1597,8 +1842,25 @@ struct Context {
                (const double*) d.phiP.p, (const double*) d.phiD.p, (const double*) mom64.p, (const double*) d.mu.p,
                gradOut.p);
         CUDA_CHECK(cudaGetLastError());
-        CUDA_CHECK(cudaMemcpyAsync(host, gradOut.p, (size_t) 20 * n * 8, cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaStreamSynchronize(st));
+    }
+
+    // Both gradient passes after an evaluation: with graphs, one captured segment (the
+    // FP64 inputs of the pass, then each pass), then the copies to the host.
+    void gradients(double* multipoleHost, double* polarizationHost) {
+        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+        const bool mg = multipoleHost != nullptr, pg = polarizationHost != nullptr;
+        if (!mg && !pg) return;
+        gradient_buffers(mg, pg);
+        const bool prepared = gradPrepared;
+        std::vector<long long> key = graph_key(kSegGradients);
+        key.push_back((mg ? 1 : 0) | (pg ? 2 : 0) | (prepared ? 4 : 0));
+        replay(key, [&] {
+            if (mg) multipole_gradient_launches();
+            if (pg) polarization_gradient_launches();
+        });
+        gradPrepared = true;  // a replay does not run gradient_engine's host side
+        if (mg) CUDA_CHECK(cudaMemcpyAsync(multipoleHost, gradOut.p, (size_t) 20 * n * 8, cudaMemcpyDeviceToHost, stream));
+        if (pg) CUDA_CHECK(cudaMemcpyAsync(polarizationHost, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, stream));
     }
 
     void get_dipoles(int which, double* host) {
@@ -1809,8 +2071,7 @@ int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, con
         CUDA_CHECK(cudaMemsetAsync(c.forcesOut.p, 0, n3 * 8, c.stream));
     const double e = c.evaluate_device(c.pos.p, box, c.forcesOut.p, nullptr);
     if (forces) CUDA_CHECK(cudaMemcpyAsync(forces, c.forcesOut.p, n3 * 8, cudaMemcpyDeviceToHost, c.stream));
-    if (multipole_grad) c.parameter_gradients(multipole_grad);
-    if (polarization_grad) c.polarization_gradients(polarization_grad);
+    c.gradients(multipole_grad, polarization_grad);
     CUDA_CHECK(cudaStreamSynchronize(c.stream));
     if (energy) *energy = e;
     return MPID_OK;

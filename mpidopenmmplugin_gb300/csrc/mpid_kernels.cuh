@@ -36,8 +36,8 @@ template <> struct Vec4<float> {
     static __host__ __device__ __forceinline__ float4 make(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
 };
 template <> struct Vec4<double> {
-    typedef double4 type;
-    static __host__ __device__ __forceinline__ double4 make(double a, double b, double c, double d) { return make_double4(a, b, c, d); }
+    typedef double4_16a type;
+    static __host__ __device__ __forceinline__ double4_16a make(double a, double b, double c, double d) { return make_double4_16a(a, b, c, d); }
 };
 
 // Periodic box in OpenMM's reduced form: rows a = (ax, 0, 0), b = (bx, by, 0),
@@ -845,7 +845,7 @@ __global__ void k_to_df(int count, const double* __restrict__ src, float2* __res
 }
 
 // df offsets, Thole widths and damping factors of the FP64 engine's atoms
-__global__ void k_df_atoms(int npad, const double* __restrict__ off, const double4* __restrict__ prm,
+__global__ void k_df_atoms(int npad, const double* __restrict__ off, const double4_16a* __restrict__ prm,
                            float2* __restrict__ offDF, float2* __restrict__ tholeDF, float2* __restrict__ dampDF) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npad) return;
@@ -853,7 +853,7 @@ __global__ void k_df_atoms(int npad, const double* __restrict__ off, const doubl
         const dfloat v = df_from_double(off[k * npad + i]);
         offDF[k * npad + i] = make_float2(v.hi, v.lo);
     }
-    const double4 p = prm[i];
+    const double4_16a p = prm[i];
     const dfloat t = df_from_double(p.x), d = df_from_double(p.y);
     tholeDF[i] = make_float2(t.hi, t.lo);
     dampDF[i] = make_float2(d.hi, d.lo);

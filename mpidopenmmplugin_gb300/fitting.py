@@ -86,14 +86,16 @@ class BoxBatch:
 
     systems: list of (force, positions (n, 3) nm, box (3, 3) nm, types (n,) ints).
     precision: "mixed" or "double", as MPIDContext.  threads: host threads driving the
-    contexts concurrently.
+    contexts concurrently.  solver_graphs: each context replays its mutual solver's
+    iterations from captured CUDA graphs (MPIDContext).
     """
 
-    def __init__(self, systems, ntypes, precision="mixed", threads=8, device=0):
+    def __init__(self, systems, ntypes, precision="mixed", threads=8, device=0, solver_graphs=True):
         self.ntypes = int(ntypes)
         self.systems = [(f, np.asarray(p, dtype=np.float64), np.asarray(b, dtype=np.float64), np.asarray(t))
                         for f, p, b, t in systems]
-        self.contexts = [MPIDContext(f, precision=precision, device=device, box=b) for f, p, b, t in self.systems]
+        self.contexts = [MPIDContext(f, precision=precision, device=device, box=b, solver_graphs=solver_graphs)
+                         for f, p, b, t in self.systems]
         self.threads = max(1, int(threads))
         self._pool = _cf.ThreadPoolExecutor(max_workers=self.threads)
 
