@@ -43,9 +43,10 @@ extern "C" {
 #define MPID_FLAG_NEAR_FIELD_PCG 2u      /* mutual solver preconditioned with the near-field dipole
                                             coupling (fewer iterations for strongly coupled systems;
                                             on water it saves one iteration and costs more) */
-#define MPID_FLAG_GRAPH_SOLVER 4u        /* mutual solver iterations replayed from CUDA graphs captured
-                                            once per neighbour-list shape and box (small systems, where
-                                            the ~11 launches of an iteration cost more than its work) */
+#define MPID_FLAG_GRAPH_SOLVER 4u        /* PME: evaluation segments and mutual-solver iterations
+                                            replayed from CUDA graphs captured once per neighbour-list
+                                            shape and box (small systems, where launches cost more than
+                                            the work); on the legacy default stream they run directly */
 
 typedef struct mpid_context mpid_context;
 

@@ -127,13 +127,14 @@ class MPIDContext:
     """
 
     def __init__(self, force: MPIDForce, num_particles=None, device=0, precision="mixed",
-                 exact_aniso_torque=False, box=None, preconditioner=False, masses=None, solver_graphs=False):
+                 exact_aniso_torque=False, box=None, preconditioner=False, masses=None, solver_graphs=True):
         """masses: per-atom masses for getSystemMultipoleMoments through the force's
         context methods (the System's masses in the reference).  box: the periodic box,
         needed when the force's PME parameters are 0 (chosen from its Ewald error
-        tolerance, as the reference kernel does through OpenMM).  solver_graphs: replay the
-        mutual solver's iterations from captured CUDA graphs (small systems, many
-        contexts driven at once)."""
+        tolerance, as the reference kernel does through OpenMM).  solver_graphs: under PME,
+        replay the evaluation's launches (set-up, solver start, solver iterations,
+        force/energy phase, gradient passes) from CUDA graphs captured on first use; calls
+        on the legacy default stream (device pointers with stream 0) launch directly."""
         self.lib = load_library()
         n = force.getNumMultipoles() if num_particles is None else int(num_particles)
         force.validate(n, box)

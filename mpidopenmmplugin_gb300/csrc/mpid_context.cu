@@ -241,14 +241,28 @@ struct Engine {
 // Device time of the evaluation stages, from CUDA events on the launching stream.
 enum Stage { ST_SETUP = 0, ST_FIXED_REAL, ST_PME, ST_DIPOLE_REAL, ST_SOLVER, ST_PAIR, ST_FINISH, ST_REFINE_REAL, ST_COUNT };
 
+// Start/stop events of one timed stage.
+struct TimedPair {
+    int stage;
+    cudaEvent_t a, b;
+};
+
 struct StageTimer {
     static constexpr int kMax = 4096;
     std::vector<cudaEvent_t> ev;
     std::vector<int> stage;
     int count = 0, open = -1;
-    bool paused = false;  // while a stream capture is open: captured events cannot be timed
     double ms[ST_COUNT] = {0};
     int launches[ST_COUNT] = {0};
+    // Inside a stream capture the events are recorded as graph nodes
+    // (cudaEventRecordExternal), drawn from the capturing graph's own pool, and the graph
+    // keeps the pairs; each replay hands them back through `replayed`.  A graph replayed
+    // more than once in an evaluation is timed by its last replay, once per replay.
+    std::vector<cudaEvent_t>* capPool = nullptr;
+    std::vector<TimedPair>* capPairs = nullptr;
+    size_t capNext = 0;
+    TimedPair capOpen{-1, nullptr, nullptr};
+    std::vector<TimedPair> replayed;
     void init() {
         ev.resize(2 * kMax);
         stage.resize(kMax);
@@ -261,29 +275,47 @@ struct StageTimer {
     void reset() {
         count = 0;
         open = -1;
+        replayed.clear();
         for (int s = 0; s < ST_COUNT; ++s) { ms[s] = 0; launches[s] = 0; }
     }
     void begin(int s, cudaStream_t st) {
-        if (count >= kMax || ev.empty() || paused) return;
+        if (capPool) {
+            if (capNext + 2 > capPool->size()) return;
+            capOpen = {s, (*capPool)[capNext], (*capPool)[capNext + 1]};
+            capNext += 2;
+            CUDA_CHECK(cudaEventRecordWithFlags(capOpen.a, st, cudaEventRecordExternal));
+            return;
+        }
+        if (count >= kMax || ev.empty()) return;
         stage[count] = s;
         CUDA_CHECK(cudaEventRecord(ev[2 * count], st));
         open = count;
     }
     void end(cudaStream_t st) {
+        if (capPool) {
+            if (capOpen.stage < 0) return;
+            CUDA_CHECK(cudaEventRecordWithFlags(capOpen.b, st, cudaEventRecordExternal));
+            capPairs->push_back(capOpen);
+            capOpen.stage = -1;
+            return;
+        }
         if (open < 0) return;
         CUDA_CHECK(cudaEventRecord(ev[2 * open + 1], st));
         ++count;
         open = -1;
     }
+    void add(int s, cudaEvent_t a, cudaEvent_t b) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, a, b) == cudaSuccess) {
+            ms[s] += t;
+            launches[s] += 1;
+        }
+    }
     // after the stream has been synchronised
     void collect() {
-        for (int i = 0; i < count; ++i) {
-            float t = 0.f;
-            if (cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]) == cudaSuccess) {
-                ms[stage[i]] += t;
-                launches[stage[i]] += 1;
-            }
-        }
+        for (int i = 0; i < count; ++i) add(stage[i], ev[2 * i], ev[2 * i + 1]);
+        for (const TimedPair& p : replayed) add(p.stage, p.a, p.b);
+        (void) cudaGetLastError();  // a pair that could not be timed leaves no error behind
     }
 };
 
@@ -402,14 +434,22 @@ struct Context {
         long long library = 0;
         unsigned long long used = 0;
         cudaGraphExec_t exec = nullptr;
+        std::vector<cudaEvent_t> events;  // the stage timer's events inside the graph
+        std::vector<TimedPair> pairs;
+        void destroy() {
+            if (exec) cudaGraphExecDestroy(exec);
+            exec = nullptr;
+            for (cudaEvent_t e : events) cudaEventDestroy(e);
+            events.clear();
+            pairs.clear();
+        }
     };
     std::vector<SolverGraph> graphs;
     unsigned long long graphClock = 0;
     int predictedIters = 0;  // iterations of the last solve: the first replayed chunk's length
 
     ~Context() {
-        for (auto& g : graphs)
-            if (g.exec) cudaGraphExecDestroy(g.exec);
+        for (auto& g : graphs) g.destroy();
         timer.destroy();
         if (hostDone) cudaFreeHost(hostDone);
         if (hostSc) cudaFreeHost(hostSc);
@@ -1032,8 +1072,22 @@ struct Context {
                p, first ? 1 : 0, partial.p, counters.p + 2, sc.p, (const int*) done.p);
     }
 
-    // Graph replay is used under PME (the configuration it is tested on).
-    bool graph_mode() const { return (set.flags & MPID_FLAG_GRAPH_SOLVER) != 0 && usePme; }
+    // Graph replay is used under PME (the configuration it is tested on), on a created
+    // stream that is not itself being captured by the caller (the legacy default stream
+    // cannot be captured; a capture cannot nest): otherwise the launches run directly.
+    // Decided once per evaluation.
+    bool graphsActive = false;
+    bool graph_mode() const { return graphsActive; }
+    void choose_graph_mode() {
+        graphsActive = false;
+        // the no-allocation call creates no graphs (instantiating one allocates)
+        if (!(set.flags & MPID_FLAG_GRAPH_SOLVER) || !usePme || growForbidden || stream == nullptr ||
+            stream == cudaStreamLegacy || stream == cudaStreamPerThread)
+            return;
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CUDA_CHECK(cudaStreamIsCapturing(stream, &cs));
+        graphsActive = cs == cudaStreamCaptureStatusNone;
+    }
 
     // One CG iteration: q = B p = p - S T S p, p.q, then the update and the scalars
     // (PCG: p from z = P r).  Launches only.
@@ -1089,7 +1143,7 @@ struct Context {
                 k.push_back(len);
                 replay(k, [&] {
                     for (int i = 0; i < len; ++i) cg_iteration(e, x, r, p, q, target, maxIter, false);
-                });
+                }, 2 * len + 2);
                 it += len;
                 CUDA_CHECK(cudaMemcpyAsync(hostDone, done.p, sizeof(int), cudaMemcpyDeviceToHost, st));
                 CUDA_CHECK(cudaEventRecord(iterEvents[0], st));
@@ -1160,15 +1214,16 @@ struct Context {
     // that a replay would skip) directly, or with graphs from the graph of `key`,
     // capturing it on first use.
     template <typename Body>
-    void replay(const std::vector<long long>& key, Body&& body) {
+    void replay(const std::vector<long long>& key, Body&& body, int timedPairs = 8) {
         if (!graph_mode()) {
             body();
             return;
         }
-        const SolverGraph& g = solver_graph(key, body);
+        const SolverGraph& g = solver_graph(key, body, timedPairs);
         CUDA_CHECK(cudaGraphLaunch(g.exec, stream));
         t_launches += g.nodes;
         t_library_calls += g.library;
+        timer.replayed.insert(timer.replayed.end(), g.pairs.begin(), g.pairs.end());
     }
 
     // The graph of `key`, captured by running `body` on the main stream under stream
@@ -1176,46 +1231,64 @@ struct Context {
     // joined back by the end of `body`).  At most eight graphs are kept; the least
     // recently used goes.
     template <typename Body>
-    const SolverGraph& solver_graph(const std::vector<long long>& key, Body&& body) {
+    const SolverGraph& solver_graph(const std::vector<long long>& key, Body&& body, int timedPairs) {
         for (auto& g : graphs)
             if (g.key == key) {
                 g.used = ++graphClock;
                 return g;
             }
         cudaStream_t st = stream;
+        SolverGraph g;
+        g.key = key;
+        g.events.resize(2 * (size_t) timedPairs);
+        for (auto& ev : g.events) CUDA_CHECK(cudaEventCreate(&ev));
         const long long l0 = t_launches, c0 = t_library_calls;
         cudaGraph_t graph = nullptr;
-        timer.paused = true;
-        CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        auto stop_timing = [&] {
+            timer.capPool = nullptr;
+            timer.capPairs = nullptr;
+            timer.capOpen.stage = -1;
+        };
+        cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (ce != cudaSuccess) {
+            g.destroy();
+            CUDA_CHECK(ce);
+        }
+        timer.capPool = &g.events;
+        timer.capPairs = &g.pairs;
+        timer.capNext = 0;
         try {
             body();
         } catch (...) {
+            stop_timing();
             cudaStreamEndCapture(st, &graph);
             if (graph) cudaGraphDestroy(graph);
-            timer.paused = false;
+            (void) cudaGetLastError();
+            g.destroy();
             t_launches = l0;
             t_library_calls = c0;
             throw;
         }
-        timer.paused = false;
-        CUDA_CHECK(cudaStreamEndCapture(st, &graph));
-        SolverGraph g;
-        g.key = key;
+        stop_timing();
+        ce = cudaStreamEndCapture(st, &graph);
         g.nodes = t_launches - l0;
         g.library = t_library_calls - c0;
         t_launches = l0;  // counted when replayed
         t_library_calls = c0;
-        const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
-        cudaGraphDestroy(graph);
-        CUDA_CHECK(ie);
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) {
+            g.destroy();
+            CUDA_CHECK(ce);
+        }
         g.used = ++graphClock;
         if (graphs.size() < 8) {
             graphs.push_back(std::move(g));
             return graphs.back();
         }
         auto lru = std::min_element(graphs.begin(), graphs.end(),
-                                    [](const SolverGraph& a, const SolverGraph& c) { return a.used < c.used; });
-        CUDA_CHECK(cudaGraphExecDestroy(lru->exec));
+                                    [](const SolverGraph& x, const SolverGraph& y) { return x.used < y.used; });
+        lru->destroy();
         *lru = std::move(g);
         return *lru;
     }
@@ -1469,6 +1542,7 @@ struct Context {
         if (!haveParams) throw Error(MPID_ERR_STATE, "mpid_set_multipoles must be called before evaluating");
         CUDA_CHECK(cudaSetDevice(device));
         cudaStream_t st = stream;
+        choose_graph_mode();
         const long long launches0 = t_launches, library0 = t_library_calls;
         CUDA_CHECK(cudaEventRecord(evStart, st));
         if (d_pos != pos.p) CUDA_CHECK(cudaMemcpyAsync(pos.p, d_pos, 3 * (size_t) n * 8, cudaMemcpyDeviceToDevice, st));

@@ -114,6 +114,9 @@ void GB300CalcMPIDForceKernel::initialize(const System& system, const MPIDForce&
     settings.default_thole = force.getDefaultTholeWidth();
     settings.scale14 = force.get14ScaleFactor();
     settings.precision = cu.getUseDoublePrecision() ? MPID_PRECISION_DOUBLE : MPID_PRECISION_MIXED;
+    // replay evaluation segments from CUDA graphs on OpenMM's stream (launches run directly
+    // while OpenMM itself captures that stream)
+    settings.flags |= MPID_FLAG_GRAPH_SOLVER;
     int device = 0;
     cudaGetDevice(&device);
     check(mpid_create(&settings, device, &handle));

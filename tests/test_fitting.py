@@ -246,7 +246,7 @@ def test_graph_solver_matches_direct_launches(precision, polarization):
     bit on the mixed path; to rounding on the FP64 path, whose PME spread uses
     floating-point atomics."""
     (f, pos, box, types), = small_batch(nboxes=1, seed=21, polarization=polarization)[0]
-    plain = MPIDContext(f, precision=precision, box=box)
+    plain = MPIDContext(f, precision=precision, box=box, solver_graphs=False)
     graph = MPIDContext(f, precision=precision, box=box, solver_graphs=True)
     tol = 0.0 if precision == "mixed" else 1e-12
 
@@ -269,6 +269,19 @@ def test_graph_solver_matches_direct_launches(precision, polarization):
     assert same(g0[0], g1[0])
     for a, b in zip(g0[2:], g1[2:]):
         assert np.abs(a - b).max() <= 1e-11 * np.abs(a).max()
+    # device buffers on the legacy default stream (not capturable: launched directly) and
+    # on a created stream (replayed)
+    import torch
+    e_ref, f_ref = plain.evaluate(pos, box)
+    d_pos = torch.tensor(pos, dtype=torch.float64, device="cuda")
+    side = torch.cuda.Stream()
+    for stream in (0, side.cuda_stream):
+        d_f = torch.zeros((len(pos), 3), dtype=torch.float64, device="cuda")
+        d_e = torch.zeros(1, dtype=torch.float64, device="cuda")
+        graph.evaluate_device(d_pos.data_ptr(), box, d_f.data_ptr(), d_e.data_ptr(), stream)
+        torch.cuda.synchronize()
+        assert same(float(d_e.cpu()[0]), e_ref)
+        assert same(d_f.cpu().numpy(), f_ref)
 
 
 @pytest.mark.gpu
