@@ -211,6 +211,7 @@ def run_fitting(args, world, rank, local):
     from mpidopenmmplugin_gb300 import fitting
     torch.cuda.set_device(local)
     all_systems, params = fitting.water_batch()
+    all_systems = all_systems[:args.boxes]  # a prefix of the 64 boxes for profiling runs
     natoms = sum(len(sy[1]) for sy in all_systems)
     # N > 1: each rank takes a share of the boxes (balanced by atoms); the energies and
     # the per-type gradient are all-reduced once per step
@@ -218,8 +219,9 @@ def run_fitting(args, world, rank, local):
     systems = [all_systems[k] for k in mine]
     out = {}
     grads = {}
-    arms = (("mixed", 1), ("mixed", args.threads), ("double", args.threads)) if world == 1 else (
-        ("mixed", args.threads),)
+    arms = [("mixed", args.threads)]
+    if world == 1:
+        arms = ([("mixed", 1)] if args.threads != 1 else []) + arms + ([] if args.no_fp64 else [("double", args.threads)])
     for precision, threads in arms:
         with fitting.BoxBatch(systems, 2, precision=precision, threads=threads, device=local) as b:
 
@@ -258,7 +260,9 @@ def run_fitting(args, world, rank, local):
             "steps": out["mixed_t%d" % args.threads]["steps"], "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded water boxes)",
-            "config": {"workload": FITTING_WORKLOAD, "atoms": natoms, "host_threads": args.threads,
+            "config": {"workload": FITTING_WORKLOAD if args.boxes >= 64 else
+                       "first %d boxes of %s" % (len(all_systems), FITTING_WORKLOAD),
+                       "atoms": natoms, "host_threads": args.threads,
                        "solver_graphs": True,
                        "device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                        "l2": "inputs copied from host each step"},
@@ -279,6 +283,7 @@ def main():
     ap.add_argument("--workload", default="water24k", choices=["water24k", "fitting64"],
                     help="water24k: the headline evaluation; fitting64: the batched per-type gradient workload")
     ap.add_argument("--threads", type=int, default=8, help="host threads driving the boxes of fitting64")
+    ap.add_argument("--boxes", type=int, default=64, help="fitting64: evaluate only the first N boxes (profiling)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.workload == "fitting64":
