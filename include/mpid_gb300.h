@@ -79,9 +79,9 @@ typedef struct {
     double ms_total;           /* device time of the last evaluation */
     /* device time (ms) and timed launch groups per stage: 0 sort/tiles/atom set-up,
      * 1 permanent-field pair kernel, 2 PME spread/FFT/convolution/gather, 3 dipole-field
-     * pair kernels, 4 solver vector work, 5 energy/force/torque pair kernel,
-     * 6 reciprocal/self terms and torque mapping, 7 FP64 dipole-field pair kernel of the
-     * mixed path's residual refinement */
+     * pair kernels, 4 reserved (not timed: the solver's vector kernels run inside the
+     * iterations), 5 energy/force/torque pair kernel, 6 reciprocal/self terms and torque
+     * mapping, 7 FP64 dipole-field pair kernel of the mixed path's residual refinement */
     double ms_stage[8];
     int stage_launches[8];
     double energy_parts[3];    /* reciprocal + self, real-space pairs, covalently scaled pairs */

@@ -61,7 +61,7 @@ class Stats(ctypes.Structure):
     ]
 
 
-STAGES = ["setup", "fixed_field_pairs", "pme", "dipole_field_pairs", "solver_vectors", "pair_kernel", "recip_self_torque",
+STAGES = ["setup", "fixed_field_pairs", "pme", "dipole_field_pairs", "reserved", "pair_kernel", "recip_self_torque",
           "refinement_field_pairs"]
 
 
