@@ -177,10 +177,15 @@ struct PmeStage {
     }
     template <int NTERM>
     void gather(int n, int npad, const BoxDev& box, real* phi, const int* skip, cudaStream_t st) {
-        if (order == 5)
-            launch(k_gather<real, 5, NTERM>, nblk(npad, 128), 128, 0, st, n, npad, box, theta.p, igrid.p, rgrid.p, phi, skip);
-        else
-            launch(k_gather<real, 6, NTERM>, nblk(npad, 128), 128, 0, st, n, npad, box, theta.p, igrid.p, rgrid.p, phi, skip);
+        if (order == 5) {
+            using G = GatherShape<real, 5, NTERM>;
+            launch(k_gather<real, 5, NTERM>, nblk(npad, G::atoms), G::threads, 0, st, n, npad, box, theta.p, igrid.p,
+                   rgrid.p, phi, skip);
+        } else {
+            using G = GatherShape<real, 6, NTERM>;
+            launch(k_gather<real, 6, NTERM>, nblk(npad, G::atoms), G::threads, 0, st, n, npad, box, theta.p, igrid.p,
+                   rgrid.p, phi, skip);
+        }
     }
 };
 
