@@ -87,6 +87,8 @@ typedef struct {
     double energy_parts[3];    /* reciprocal + self, real-space pairs, covalently scaled pairs */
     int kernel_launches;       /* launches of this library's kernels in the last evaluation */
     int library_calls;         /* cuFFT executions and cub sorts in the last evaluation */
+    int graph_captures;        /* CUDA graphs captured by the last evaluation and its gradients */
+    int graph_replays;         /* graph launches of the last evaluation and its gradients */
 } mpid_stats;
 
 /* Fill `s` with the MPIDForce defaults for n atoms (PME not configured). */

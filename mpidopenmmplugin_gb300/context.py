@@ -58,6 +58,8 @@ class Stats(ctypes.Structure):
         ("energy_parts", ctypes.c_double * 3),
         ("kernel_launches", ctypes.c_int),
         ("library_calls", ctypes.c_int),
+        ("graph_captures", ctypes.c_int),
+        ("graph_replays", ctypes.c_int),
     ]
 
 
@@ -298,7 +300,8 @@ class MPIDContext:
                     stage_launches={STAGES[k]: s.stage_launches[k] for k in range(len(STAGES))},
                     energy_parts=dict(recip_self=s.energy_parts[0], real_space=s.energy_parts[1],
                                       scaled_pairs=s.energy_parts[2]),
-                    kernel_launches=s.kernel_launches, library_calls=s.library_calls)
+                    kernel_launches=s.kernel_launches, library_calls=s.library_calls,
+                    graph_captures=s.graph_captures, graph_replays=s.graph_replays)
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -1082,9 +1082,29 @@ struct Context {
     // cannot be captured; a capture cannot nest): otherwise the launches run directly.
     // Decided once per evaluation.
     bool graphsActive = false;
+    // Evaluations whose shape keeps changing (a box rescaled every step, lists that change
+    // length) would capture new graphs every time, which costs more than launching
+    // directly: after captures in 4 of the last 5 evaluations, the next 32 launch directly.
+    unsigned captureHistory = 0;
+    int graphPause = 0;
     bool graph_mode() const { return graphsActive; }
+    void note_captures() {
+        if (!graphsActive) return;
+        captureHistory = (captureHistory << 1) | (stats.graph_captures > 0 ? 1u : 0u);
+        if (__builtin_popcount(captureHistory & 0x1fu) >= 4) {
+            graphPause = 32;
+            captureHistory = 0;
+        }
+    }
     void choose_graph_mode() {
+        note_captures();  // the previous evaluation and its gradient passes
         graphsActive = false;
+        stats.graph_captures = 0;
+        stats.graph_replays = 0;
+        if (graphPause > 0) {
+            --graphPause;
+            return;
+        }
         // the no-allocation call creates no graphs (instantiating one allocates)
         if (!(set.flags & MPID_FLAG_GRAPH_SOLVER) || !usePme || growForbidden || stream == nullptr ||
             stream == cudaStreamLegacy || stream == cudaStreamPerThread)
@@ -1226,6 +1246,7 @@ struct Context {
         }
         const SolverGraph& g = solver_graph(key, body, timedPairs);
         CUDA_CHECK(cudaGraphLaunch(g.exec, stream));
+        ++stats.graph_replays;
         t_launches += g.nodes;
         t_library_calls += g.library;
         timer.replayed.insert(timer.replayed.end(), g.pairs.begin(), g.pairs.end());
@@ -1243,6 +1264,7 @@ struct Context {
                 return g;
             }
         cudaStream_t st = stream;
+        ++stats.graph_captures;
         SolverGraph g;
         g.key = key;
         g.events.resize(2 * (size_t) timedPairs);

@@ -285,6 +285,36 @@ def test_graph_solver_matches_direct_launches(precision, polarization):
 
 
 @pytest.mark.gpu
+def test_graph_replay_reuse_and_recapture_guard():
+    """Graphs are captured once and replayed afterwards; a box that changes at every
+    evaluation captures new graphs each time until the context pauses replay (captures
+    in 4 of 5 evaluations), after which it launches directly, with the same results."""
+    (f, pos, box, types), = small_batch(nboxes=1, seed=23)[0]
+    plain = MPIDContext(f, box=box, solver_graphs=False)
+    graph = MPIDContext(f, box=box)
+    for _ in range(3):
+        graph.evaluate(pos, box)
+    s = graph.stats()
+    assert s["graph_captures"] == 0 and s["graph_replays"] >= 4
+    paused = None
+    for k in range(1, 9):
+        b, p = box * (1.0 + 0.002 * k), pos * (1.0 + 0.002 * k)
+        e1, f1 = graph.evaluate(p, b)
+        e0, f0 = plain.evaluate(p, b)
+        assert e0 == e1 and np.array_equal(f0, f1)
+        s = graph.stats()
+        if s["graph_replays"] == 0 and paused is None:
+            paused = k
+        if paused is None:
+            assert s["graph_captures"] > 0
+        else:  # paused for the following evaluations too
+            assert s["graph_replays"] == 0 and s["graph_captures"] == 0
+    # the two warm-up evaluations that captured count in the window of five
+    assert paused is not None and paused <= 5
+    assert plain.stats()["graph_replays"] == 0
+
+
+@pytest.mark.gpu
 def test_torch_autograd_function():
     torch = pytest.importorskip("torch")
     systems, params = small_batch(nboxes=2, seed=17)
