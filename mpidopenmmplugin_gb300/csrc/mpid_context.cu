@@ -1084,14 +1084,15 @@ struct Context {
     bool graphsActive = false;
     // Evaluations whose shape keeps changing (a box rescaled every step, lists that change
     // length) would capture new graphs every time, which costs more than launching
-    // directly: after captures in 4 of the last 5 evaluations, the next 32 launch directly.
+    // directly: after captures in each of the last 5 evaluations, the next 32 launch
+    // directly.  (Warm-up evaluations capture too, also when other contexts allocate.)
     unsigned captureHistory = 0;
     int graphPause = 0;
     bool graph_mode() const { return graphsActive; }
     void note_captures() {
         if (!graphsActive) return;
         captureHistory = (captureHistory << 1) | (stats.graph_captures > 0 ? 1u : 0u);
-        if (__builtin_popcount(captureHistory & 0x1fu) >= 4) {
+        if ((captureHistory & 0x1fu) == 0x1fu) {
             graphPause = 32;
             captureHistory = 0;
         }
@@ -1417,10 +1418,7 @@ struct Context {
         launch(k_mu_from_y<double, float>, nblk(npad, 128), 128, 0, st, npad, d.sroot.p, y64.p, e.mu.p);
         CUDA_CHECK(cudaEventRecord(evRefStart, st));
         // the check, on the refinement streams (members swapped for the launches)
-        std::swap(stream, refStream);
-        std::swap(pmeStream, refPmeStream);
-        std::swap(evFork, evRefFork);
-        std::swap(evJoin, evRefJoin);
+        RefStreams scope(*this);
         cudaStream_t rs = stream;
         CUDA_CHECK(cudaStreamWaitEvent(rs, evRefStart, 0));
         if (usePme) d.pme.set_stream(pmeStream);
@@ -1430,11 +1428,24 @@ struct Context {
         launch(k_reduce_partials, 1, 1024, 0, rs, nb, 1, partial.p, red.p, nullptr);
         CUDA_CHECK(cudaMemcpyAsync(refHost, red.p, 8, cudaMemcpyDeviceToHost, rs));
         CUDA_CHECK(cudaEventRecord(evRefDone, rs));
+    }
+
+    // The refinement streams and their fork/join events take the place of the main ones
+    // for the scope (also when a launch throws), so that the FP64 check's launches go
+    // through the same helpers as the main path's.
+    void swap_ref() {
         std::swap(stream, refStream);
         std::swap(pmeStream, refPmeStream);
         std::swap(evFork, evRefFork);
         std::swap(evJoin, evRefJoin);
     }
+    struct RefStreams {
+        Context& c;
+        explicit RefStreams(Context& x) : c(x) { c.swap_ref(); }
+        ~RefStreams() { c.swap_ref(); }
+        RefStreams(const RefStreams&) = delete;
+        RefStreams& operator=(const RefStreams&) = delete;
+    };
 
     // The mixed Mutual evaluation from the permanent field on, as three captured segments
     // and two host waits: (permanent field, solver start, iteration 0) | iterations | (check
@@ -1588,13 +1599,12 @@ struct Context {
                     // beside the list build (it is first read by the check)
                     CUDA_CHECK(cudaEventRecord(evRefStart, st));
                     CUDA_CHECK(cudaStreamWaitEvent(refStream, evRefStart, 0));
-                    std::swap(stream, refStream);
-                    std::swap(pmeStream, refPmeStream);
-                    prepare_engine(*ed, false);
-                    launch(k_df_atoms, nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p,
-                           tholeDF.p, dampDF.p);
-                    std::swap(stream, refStream);
-                    std::swap(pmeStream, refPmeStream);
+                    {
+                        RefStreams scope(*this);
+                        prepare_engine(*ed, false);
+                        launch(k_df_atoms, nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p,
+                               tholeDF.p, dampDF.p);
+                    }
                     if (graph_mode()) {  // a captured side stream joins back before the capture ends
                         CUDA_CHECK(cudaEventRecord(evRefStart, refStream));
                         CUDA_CHECK(cudaStreamWaitEvent(st, evRefStart, 0));
