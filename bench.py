@@ -12,7 +12,7 @@ Arms
   (positions and forces copied in, forces and energy copied out each step).  The FP64
   path is timed on the same box for the mixed-vs-FP64 speed-up and accuracy.
 * --impl reference: the reference's CPU algorithm on the host cores.  The reference's
-  own build needs its source tree, absent on the GPU machine, so the oracle port
+  own build needs its source tree, absent where the benchmark runs, so the oracle port
   (oracle/mpid_port.cpp, pinned to the reference in tests) is timed with all host
   threads, one full evaluation per step.
 
@@ -25,6 +25,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -72,8 +73,9 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/mpid_bench_clocks.csv"
+        # the raw samples (the summary goes into the JSON line)
+        self.path = os.environ.get("MPID_BENCH_CLOCKS_CSV",
+                                   os.path.join(tempfile.gettempdir(), "mpid_bench_clocks_%d.csv" % os.getpid()))
 
     def __enter__(self):
         q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -140,7 +142,7 @@ FLOP_PER_PAIR = {"pair_kernel": 2728,          # k_electrostatics<float, MUTUAL>
                  "dipole_field_pairs": 154,    # k_dipole_field_packed (CG matrix-vector product)
                  "fixed_field_pairs": 472}     # k_fixed_field<float>
 # DRAM bytes per launch (read + write) from one ncu capture of each kernel on this
-# workload (profiles/k_*_water24k_mutual.md); ncu is not run by this script.
+# workload (the captures summarised under profiles/); ncu is not run by this script.
 DRAM_BYTES_PER_LAUNCH = {"pair_kernel": 29.42e6 + 0.39e6, "dipole_field_pairs": 32.86e6}
 KERNEL_NAMES = {"pair_kernel": "k_electrostatics<float, mutual> (energy/force/torque pair kernel)",
                 "dipole_field_pairs": "k_dipole_field_packed (FP32 T.mu pair kernel of the CG solver)",

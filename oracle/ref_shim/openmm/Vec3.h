@@ -2,7 +2,7 @@
  * Minimal 3-vector with the member functions that the reference's FP64 CPU force
  * (platforms/reference/src/SimTKReference/MPIDReferenceForce.cpp) uses from OpenMM's
  * Vec3: construction, indexing, +, -, unary -, scalar * and /, compound assignment,
- * dot and cross.  OpenMM itself is not available in this build environment. */
+ * dot and cross.  OpenMM itself is not installed, so the force is built against this. */
 #ifndef MPID_ORACLE_SHIM_VEC3_H
 #define MPID_ORACLE_SHIM_VEC3_H
 #include <cassert>

@@ -171,7 +171,8 @@ def test_pme_parameters_rule():
         assert m == 1 and n >= r and n - r < 8
 
 
-REF_PARAMS = "/root/reference/examples/parameters"
+# the reference tree, where it is present (read only by these CPU tests)
+REF_PARAMS = os.path.join(os.environ.get("MPID_REFERENCE_ROOT", "/root/reference"), "examples", "parameters")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_PARAMS), reason="reference tree absent")
