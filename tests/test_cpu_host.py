@@ -194,3 +194,21 @@ def test_openmm_adapter_compiles_against_interface_stubs():
                                 "-I", inc, os.path.join(src, f), "-o", os.path.join(tmp, f + ".o")],
                                capture_output=True, text=True)
             assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_bench_reference_arm_json_line():
+    """`bench.py --impl reference` (the CPU arm the GPU line is compared with) prints one
+    JSON line with the GPU arm's metric and unit, the cpu_baseline and e2e objects, and a
+    time bound: here one warm-up and one timed evaluation of the 24,000-atom box."""
+    import json
+    import sys
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "3"], capture_output=True, text=True, check=True, cwd=ROOT).stdout
+    lines = [l for l in out.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "evals/s" and d["higher_is_better"] is True
+    assert d["metric"].startswith("force+energy evals/s")
+    assert d["steps"] == 1 and d["warmup"] == 1 and d["steps_requested"] == 1 and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
