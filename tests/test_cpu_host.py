@@ -1,5 +1,6 @@
 """CPU tests: host-side API, C ABI exports, synthetic inputs, and the oracle port pinned
 to the reference's known answers and to reference runs (no GPU needed)."""
+import ctypes
 import os
 import re
 import subprocess
@@ -212,3 +213,29 @@ def test_bench_reference_arm_json_line():
     assert d["steps"] == 1 and d["warmup"] == 1 and d["steps_requested"] == 1 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of mpid_settings and mpid_stats have the header's size and field
+    offsets (checked against a C program compiled from include/mpid_gb300.h)."""
+    import shutil
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("gcc not available")
+    structs = {"mpid_settings": context.Settings, "mpid_stats": context.Stats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "mpid_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for field, _ in py._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, field, cname, field))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = str(tmp_path / "layout")
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", exe], check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
