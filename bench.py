@@ -260,7 +260,10 @@ def run_fitting(args, world, rank, local):
                 torch.cuda.synchronize()
                 dt = (time.perf_counter() - t0) / steps
                 clocks.mark("stop")
-            out["%s_t%d" % (precision, threads)] = {"ms_per_step": dt * 1e3, "steps": steps}
+            # kernel launches of one step: each box's last evaluation and gradient passes
+            per_step = sum(c.stats()["kernel_launches"] for c in b.contexts)
+            out["%s_t%d" % (precision, threads)] = {"ms_per_step": dt * 1e3, "steps": steps,
+                                                    "launches_per_step": per_step}
             if threads == args.threads:
                 grads[precision] = g
                 if precision == "mixed":
@@ -270,6 +273,7 @@ def run_fitting(args, world, rank, local):
         return
     gm = grads["mixed"]
     gd = grads.get("double")
+    main_arm = out["mixed_t%d" % args.threads]
     line = {"metric": FITTING_METRIC, "value": 1000.0 / ms, "unit": "steps/s", "n_gpus": world,
             "steps": out["mixed_t%d" % args.threads]["steps"], "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32+f64",
@@ -280,6 +284,7 @@ def run_fitting(args, world, rank, local):
                        "solver_graphs": True,
                        "device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                        "l2": "inputs copied from host each step"},
+            "gpu_launches": main_arm["launches_per_step"] * main_arm["steps"],
             "arms": out,
             "mixed_vs_fp64_gradient_rel": None if gd is None else float(np.linalg.norm(gm - gd) / np.linalg.norm(gd)),
             "clocks": clock_summary}

@@ -85,8 +85,9 @@ typedef struct {
     double ms_stage[8];
     int stage_launches[8];
     double energy_parts[3];    /* reciprocal + self, real-space pairs, covalently scaled pairs */
-    int kernel_launches;       /* launches of this library's kernels in the last evaluation */
-    int library_calls;         /* cuFFT executions and cub sorts in the last evaluation */
+    int kernel_launches;       /* launches of this library's kernels in the last evaluation
+                                  (with its gradient passes, mpid_evaluate_with_gradients) */
+    int library_calls;         /* cuFFT executions and cub sorts, counted the same way */
     int graph_captures;        /* CUDA graphs captured by the last evaluation and its gradients */
     int graph_replays;         /* graph launches of the last evaluation and its gradients */
 } mpid_stats;

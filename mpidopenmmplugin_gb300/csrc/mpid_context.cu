@@ -1965,10 +1965,14 @@ struct Context {
         const bool prepared = gradPrepared;
         std::vector<long long> key = graph_key(kSegGradients);
         key.push_back((mg ? 1 : 0) | (pg ? 2 : 0) | (prepared ? 4 : 0));
+        const long long launches0 = t_launches, library0 = t_library_calls;
         replay(key, [&] {
             if (mg) multipole_gradient_launches();
             if (pg) polarization_gradient_launches();
         });
+        // the gradient passes count with the evaluation they belong to
+        stats.kernel_launches += (int) (t_launches - launches0);
+        stats.library_calls += (int) (t_library_calls - library0);
         gradPrepared = true;  // a replay does not run gradient_engine's host side
         if (mg) CUDA_CHECK(cudaMemcpyAsync(multipoleHost, gradOut.p, (size_t) 20 * n * 8, cudaMemcpyDeviceToHost, stream));
         if (pg) CUDA_CHECK(cudaMemcpyAsync(polarizationHost, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, stream));
