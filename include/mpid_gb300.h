@@ -90,6 +90,8 @@ typedef struct {
     int library_calls;         /* cuFFT executions and cub sorts, counted the same way */
     int graph_captures;        /* CUDA graphs captured by the last evaluation and its gradients */
     int graph_replays;         /* graph launches of the last evaluation and its gradients */
+    long long device_allocations; /* cudaMalloc calls made by this library in this process so far
+                                     (all contexts; read when mpid_get_stats is called) */
 } mpid_stats;
 
 /* Fill `s` with the MPIDForce defaults for n atoms (PME not configured). */
@@ -126,11 +128,14 @@ int mpid_evaluate_device(mpid_context* ctx, const double* d_positions, const dou
 
 /* mpid_evaluate_device without any allocation.  No reference counterpart: the reference
  * kernel runs inside OpenMM, which owns all memory.  For callers that may not allocate
- * device memory while they evaluate: code under CUDA stream capture, integrators with a
- * fixed memory budget, hosts whose own allocator holds the device memory.  The ordinary
- * call allocates only when its neighbour lists must grow; this one keeps the neighbour
- * lists and the pair kernel's per-task energies in one static 8 MiB device array per
- * device and never grows anything.
+ * device memory while they evaluate: integrators that reserve a fixed device-memory
+ * budget up front and must not exceed it mid-run, and hosts whose own allocator holds
+ * the device memory (a framework's caching allocator or a plugin host that forbids
+ * foreign cudaMalloc calls, which would otherwise fail or fragment its pool).  The
+ * ordinary call allocates only when its neighbour lists must grow; this one keeps the
+ * neighbour lists and the pair kernel's per-task energies in one static 8 MiB device
+ * array per device and never grows anything (mpid_stats.device_allocations does not
+ * change across it).
  *  - PME only.  Size limit: npad x (longest neighbour list rounded up to 32) <= 1,835,008
  *    entries (npad = atoms rounded up to 32), e.g. about 5,000 water atoms at a 0.9 nm
  *    cutoff.  Larger systems, and systems whose tile lists have not been sized by one
@@ -142,7 +147,10 @@ int mpid_evaluate_device(mpid_context* ctx, const double* d_positions, const dou
  *    first call before any stream capture.
  *  - The array is shared by every context of the process on that device: calls must not
  *    overlap in time on a device, from any thread or stream, or they race on it.
- * Arguments and results as mpid_evaluate_device. */
+ *  - The caller's current device is left as it was.
+ * Arguments and results as mpid_evaluate_device; the getters and gradient calls that
+ * follow work as after mpid_evaluate_device (the gradient calls rebuild the context's own
+ * neighbour lists before they read them). */
 int mpid_evaluate_device_noalloc(mpid_context* ctx, const double* d_positions, const double* box, double* d_forces,
                                  double* d_energy, void* stream);
 

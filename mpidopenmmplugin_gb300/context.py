@@ -60,6 +60,7 @@ class Stats(ctypes.Structure):
         ("library_calls", ctypes.c_int),
         ("graph_captures", ctypes.c_int),
         ("graph_replays", ctypes.c_int),
+        ("device_allocations", ctypes.c_longlong),
     ]
 
 
@@ -301,7 +302,8 @@ class MPIDContext:
                     energy_parts=dict(recip_self=s.energy_parts[0], real_space=s.energy_parts[1],
                                       scaled_pairs=s.energy_parts[2]),
                     kernel_launches=s.kernel_launches, library_calls=s.library_calls,
-                    graph_captures=s.graph_captures, graph_replays=s.graph_replays)
+                    graph_captures=s.graph_captures, graph_replays=s.graph_replays,
+                    device_allocations=s.device_allocations)
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

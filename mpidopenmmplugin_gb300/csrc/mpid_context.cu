@@ -27,13 +27,13 @@
 
 // ---------------------------------------------------------------------------
 // Static scratch of the allocation-free evaluation (mpid_evaluate_device_noalloc).
-// Some callers may not allocate device memory at the moment they evaluate: code being
-// captured into a CUDA graph (cudaMalloc is not a capturable operation), integrators
-// that run under a fixed memory budget, or hosts whose allocator owns the device
-// memory.  The ordinary evaluation allocates only when its neighbour lists outgrow
-// their capacity; the allocation-free variant keeps the per-atom neighbour lists and
-// the pair kernel's per-task energy partials in this fixed array instead and fails
-// with MPID_ERR_INVALID rather than grow.  8 MiB: 1,835,008 list entries (npad x
+// Some callers may not allocate device memory at the moment they evaluate: integrators
+// that reserve a fixed device-memory budget up front and must stay inside it, or hosts
+// whose own allocator owns the device memory (a caching allocator, a plugin host that
+// forbids foreign cudaMalloc calls).  The ordinary evaluation allocates only when its
+// neighbour lists outgrow their capacity; the allocation-free variant keeps the
+// per-atom neighbour lists and the pair kernel's per-task energy partials in this fixed
+// array instead and fails with MPID_ERR_INVALID rather than grow.  8 MiB: 1,835,008 list entries (npad x
 // neighbours per atom, e.g. about 5,000 water atoms at a 0.9 nm cutoff) and 131,072
 // FP64 task energies.  The array is one per device and per process, so calls must not
 // overlap in time on a device (from any context, thread or stream): overlapping calls
@@ -66,6 +66,21 @@ struct Error : std::runtime_error {
     } while (0)
 
 static inline int nblk(long long n, int b) { return (int) ((n + b - 1) / b); }
+
+// Makes `device` current for one C-ABI call and gives the caller's current device back
+// at its end, so that a host thread driving several GPUs keeps its own choice.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        CUDA_CHECK(cudaSetDevice(device));
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+};
 
 // Kernel launches made by this thread (every launch of the library goes through
 // launch(); evaluations report their own count).
@@ -384,6 +399,10 @@ struct Context {
     int lastTiles = 0, lastMaxList = 0;
     long long listEntries = 0;
     bool growForbidden = false;  // set by the allocation-free entry point
+    // The counts and segment sizes of the last list build describe lists that lived in
+    // the allocation-free call's scratch, not in `list`: passes that read the lists
+    // outside an evaluation must rebuild them first (every evaluation does).
+    bool listsInScratch = false;
     // PME tables
     DBuf<double> modx, mody, modz, influence;
     double lastBox[9] = {0};
@@ -1614,6 +1633,7 @@ struct Context {
             });
             CUDA_CHECK(cudaEventRecord(evLists, st));
             finish_lists(e);
+            listsInScratch = growForbidden;
             stats.max_neighbours = lastMaxList;
             timer.end(st);
             if (set.polarization_type == MPID_MUTUAL && graph_mode()) {
@@ -1635,6 +1655,7 @@ struct Context {
             prepare_engine(e, true);
             launch_lists(e);
             finish_lists(e);
+            listsInScratch = growForbidden;
             stats.max_neighbours = lastMaxList;
             timer.end(st);
             fixed_field(e);
@@ -1841,6 +1862,9 @@ struct Context {
     // Device buffers of the gradient passes (allocated before any launch is queued, so
     // that the launches can be captured).
     void gradient_buffers(bool multipole, bool polarization) {
+        if (listsInScratch)
+            throw Error(MPID_ERR_STATE, "the last evaluation kept its neighbour lists in the allocation-free call's "
+                                        "scratch; evaluate with mpid_evaluate_device or a host-buffer call first");
         if (mixed && !ed && !eg) {
             eg.reset(new Engine<double>());
             eg->init(n, npad, usePme, set.pme_order, set.grid);
@@ -2045,6 +2069,7 @@ void mpid_default_settings(mpid_settings* s, int num_atoms) {
 int mpid_create(const mpid_settings* settings, int device, mpid_context** out) {
     MPID_API_BEGIN
     if (!settings || !out) throw Error(MPID_ERR_INVALID, "null argument");
+    mpid::DeviceScope scope(device);
     std::unique_ptr<mpid_context> c(new mpid_context());
     c->ctx.create(*settings, device);
     *out = c.release();
@@ -2052,7 +2077,14 @@ int mpid_create(const mpid_settings* settings, int device, mpid_context** out) {
     MPID_API_END
 }
 
-void mpid_destroy(mpid_context* ctx) { delete ctx; }
+void mpid_destroy(mpid_context* ctx) {
+    if (!ctx) return;
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    cudaSetDevice(ctx->ctx.device);
+    delete ctx;
+    if (prev >= 0) cudaSetDevice(prev);
+}
 
 int mpid_set_multipoles(mpid_context* ctx, const double* charge, const double* dipole, const double* quadrupole,
                         const double* octopole, const int* axis_type, const int* atom_z, const int* atom_x,
@@ -2061,6 +2093,7 @@ int mpid_set_multipoles(mpid_context* ctx, const double* charge, const double* d
     if (!ctx || !charge || !dipole || !quadrupole || !octopole || !axis_type || !atom_z || !atom_x || !atom_y || !thole ||
         !polarity)
         throw Error(MPID_ERR_INVALID, "null argument");
+    mpid::DeviceScope scope(ctx->ctx.device);
     ctx->ctx.set_multipoles(charge, dipole, quadrupole, octopole, axis_type, atom_z, atom_x, atom_y, thole, polarity);
     return MPID_OK;
     MPID_API_END
@@ -2069,6 +2102,7 @@ int mpid_set_multipoles(mpid_context* ctx, const double* charge, const double* d
 int mpid_set_covalent(mpid_context* ctx, const int* offsets, const int* index) {
     MPID_API_BEGIN
     if (!ctx || !offsets) throw Error(MPID_ERR_INVALID, "null argument");
+    mpid::DeviceScope scope(ctx->ctx.device);
     ctx->ctx.set_covalent(offsets, index);
     return MPID_OK;
     MPID_API_END
@@ -2078,7 +2112,7 @@ int mpid_evaluate(mpid_context* ctx, const double* positions, const double* box,
     MPID_API_BEGIN
     if (!ctx || !positions || !box || !forces) throw Error(MPID_ERR_INVALID, "null argument");
     Context& c = ctx->ctx;
-    CUDA_CHECK(cudaSetDevice(c.device));
+    mpid::DeviceScope scope(c.device);
     c.stream = c.hostStream;
     const size_t n3 = 3 * (size_t) c.n;
     CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions, n3 * 8, cudaMemcpyHostToDevice, c.stream));
@@ -2095,14 +2129,16 @@ int mpid_evaluate_device(mpid_context* ctx, const double* d_positions, const dou
                          double* d_energy, void* stream) {
     MPID_API_BEGIN
     if (!ctx || !d_positions || !box || !d_forces) throw Error(MPID_ERR_INVALID, "null argument");
+    mpid::DeviceScope scope(ctx->ctx.device);
     ctx->ctx.stream = (cudaStream_t) stream;
     ctx->ctx.evaluate_device(d_positions, box, d_forces, d_energy);
     return MPID_OK;
     MPID_API_END
 }
 
-// Device address of the static scratch on the current device, looked up once per device
-// (the first call on a device must not run under stream capture).
+// Device address of the static scratch on `device`, looked up once per device with that
+// device current (the caller's DeviceScope restores the caller's device afterwards); the
+// first call on a device must not run under stream capture.
 static std::mutex g_noallocMutex;
 static void* g_noallocPtr[mpid::kNoAllocMaxDevices] = {};
 
@@ -2124,6 +2160,7 @@ int mpid_evaluate_device_noalloc(mpid_context* ctx, const double* d_positions, c
                                  double* d_energy, void* stream) {
     MPID_API_BEGIN
     if (!ctx || !d_positions || !box || !d_forces) throw Error(MPID_ERR_INVALID, "null argument");
+    mpid::DeviceScope scope(ctx->ctx.device);
     void* scratch = noalloc_scratch(ctx->ctx.device);
     ctx->ctx.stream = (cudaStream_t) stream;
     ctx->ctx.evaluate_device_noalloc(d_positions, box, d_forces, d_energy, scratch);
@@ -2134,7 +2171,6 @@ int mpid_evaluate_device_noalloc(mpid_context* ctx, const double* d_positions, c
 // Evaluation at host positions into an internal force buffer (the properties below are
 // defined at the positions given, as the reference recomputes the induced dipoles).
 static void evaluate_at(Context& c, const double* positions, const double* box) {
-    CUDA_CHECK(cudaSetDevice(c.device));
     c.stream = c.hostStream;
     const size_t n3 = 3 * (size_t) c.n;
     CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions, n3 * 8, cudaMemcpyHostToDevice, c.stream));
@@ -2146,6 +2182,7 @@ int mpid_get_system_multipole_moments(mpid_context* ctx, const double* positions
                                       const double* masses, double* out) {
     MPID_API_BEGIN
     if (!ctx || !positions || !box || !masses || !out) throw Error(MPID_ERR_INVALID, "null argument");
+    mpid::DeviceScope scope(ctx->ctx.device);
     evaluate_at(ctx->ctx, positions, box);
     ctx->ctx.system_moments(masses, out);
     return MPID_OK;
@@ -2156,6 +2193,7 @@ int mpid_get_electrostatic_potential(mpid_context* ctx, const double* positions,
                                      const double* grid, int ngrid, double* out) {
     MPID_API_BEGIN
     if (!ctx || !positions || !box || (ngrid > 0 && (!grid || !out))) throw Error(MPID_ERR_INVALID, "null argument");
+    mpid::DeviceScope scope(ctx->ctx.device);
     evaluate_at(ctx->ctx, positions, box);
     ctx->ctx.electrostatic_potential(grid, ngrid, out);
     return MPID_OK;
@@ -2165,6 +2203,7 @@ int mpid_get_electrostatic_potential(mpid_context* ctx, const double* positions,
 int mpid_get_parameter_gradients(mpid_context* ctx, const double* positions, const double* box, double* out) {
     MPID_API_BEGIN
     if (!ctx || !positions || !box || !out) throw Error(MPID_ERR_INVALID, "null argument");
+    mpid::DeviceScope scope(ctx->ctx.device);
     evaluate_at(ctx->ctx, positions, box);
     ctx->ctx.parameter_gradients(out);
     return MPID_OK;
@@ -2176,7 +2215,7 @@ int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, con
     MPID_API_BEGIN
     if (!ctx || !positions || !box) throw Error(MPID_ERR_INVALID, "null argument");
     Context& c = ctx->ctx;
-    CUDA_CHECK(cudaSetDevice(c.device));
+    mpid::DeviceScope scope(c.device);
     c.stream = c.hostStream;
     const size_t n3 = 3 * (size_t) c.n;
     CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions, n3 * 8, cudaMemcpyHostToDevice, c.stream));
@@ -2196,6 +2235,7 @@ int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, con
 int mpid_get_dipoles(mpid_context* ctx, int which, double* out) {
     MPID_API_BEGIN
     if (!ctx || !out) throw Error(MPID_ERR_INVALID, "null argument");
+    mpid::DeviceScope scope(ctx->ctx.device);
     ctx->ctx.get_dipoles(which, out);
     return MPID_OK;
     MPID_API_END
@@ -2218,6 +2258,7 @@ int mpid_get_stats(mpid_context* ctx, mpid_stats* out) {
     MPID_API_BEGIN
     if (!ctx || !out) throw Error(MPID_ERR_INVALID, "null argument");
     *out = ctx->ctx.stats;
+    out->device_allocations = (long long) mpid::g_device_allocs.load();
     return MPID_OK;
     MPID_API_END
 }
