@@ -47,6 +47,11 @@ extern "C" {
                                             replayed from CUDA graphs captured once per neighbour-list
                                             shape and box (small systems, where launches cost more than
                                             the work); on the legacy default stream they run directly */
+#define MPID_FLAG_SERIAL_STAGES 8u       /* profiling: the context's side streams (PME chains, the FP64
+                                            residual check) fold onto the caller's stream, so that the
+                                            stage times of mpid_stats add up to the evaluation's device
+                                            time, and cuFFT executions are timed as their own stage (4);
+                                            slower than the default overlapped schedule, same results */
 
 typedef struct mpid_context mpid_context;
 
@@ -78,10 +83,14 @@ typedef struct {
     int max_neighbours;        /* longest per-atom neighbour list of the last evaluation */
     double ms_total;           /* device time of the last evaluation */
     /* device time (ms) and timed launch groups per stage: 0 sort/tiles/atom set-up,
-     * 1 permanent-field pair kernel, 2 PME spread/FFT/convolution/gather, 3 dipole-field
-     * pair kernels, 4 reserved (not timed: the solver's vector kernels run inside the
-     * iterations), 5 energy/force/torque pair kernel, 6 reciprocal/self terms and torque
-     * mapping, 7 FP64 dipole-field pair kernel of the mixed path's residual refinement */
+     * 1 permanent-field pair kernel, 2 PME spread/FFT/convolution/gather (without the FFTs
+     * under MPID_FLAG_SERIAL_STAGES), 3 dipole-field pair kernels, 4 cuFFT executions (timed
+     * only under MPID_FLAG_SERIAL_STAGES; otherwise inside stage 2), 5 energy/force/torque
+     * pair kernel, 6 reciprocal/self terms and torque mapping, 7 FP64 dipole-field pair
+     * kernel of the mixed path's residual refinement.  The solver's vector kernels are not
+     * timed as a stage.  Stages on different streams overlap unless MPID_FLAG_SERIAL_STAGES
+     * is set, and inside replayed graphs a stage's time includes its waits for other
+     * streams, so only the serial stage times add up to ms_total. */
     double ms_stage[8];
     int stage_launches[8];
     double energy_parts[3];    /* reciprocal + self, real-space pairs, covalently scaled pairs */

@@ -18,6 +18,7 @@ MPID_PRECISION_DOUBLE = 1
 MPID_FLAG_EXACT_ANISO_TORQUE = 1
 MPID_FLAG_NEAR_FIELD_PCG = 2
 MPID_FLAG_GRAPH_SOLVER = 4
+MPID_FLAG_SERIAL_STAGES = 8
 
 # Entry points declared in include/mpid_gb300.h
 C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multipoles", "mpid_set_covalent",
@@ -64,7 +65,7 @@ class Stats(ctypes.Structure):
     ]
 
 
-STAGES = ["setup", "fixed_field_pairs", "pme", "dipole_field_pairs", "reserved", "pair_kernel", "recip_self_torque",
+STAGES = ["setup", "fixed_field_pairs", "pme", "dipole_field_pairs", "cufft", "pair_kernel", "recip_self_torque",
           "refinement_field_pairs"]
 
 
@@ -130,14 +131,18 @@ class MPIDContext:
     """
 
     def __init__(self, force: MPIDForce, num_particles=None, device=0, precision="mixed",
-                 exact_aniso_torque=False, box=None, preconditioner=False, masses=None, solver_graphs=True):
+                 exact_aniso_torque=False, box=None, preconditioner=False, masses=None, solver_graphs=True,
+                 serial_stages=False):
         """masses: per-atom masses for getSystemMultipoleMoments through the force's
         context methods (the System's masses in the reference).  box: the periodic box,
         needed when the force's PME parameters are 0 (chosen from its Ewald error
         tolerance, as the reference kernel does through OpenMM).  solver_graphs: under PME,
         replay the evaluation's launches (set-up, solver start, solver iterations,
         force/energy phase, gradient passes) from CUDA graphs captured on first use; calls
-        on the legacy default stream (device pointers with stream 0) launch directly."""
+        on the legacy default stream (device pointers with stream 0) launch directly.
+        serial_stages: profiling; the side streams fold onto the calling stream so that the
+        stage times of stats() add up to the evaluation's device time, with the cuFFT
+        executions as their own stage ("cufft")."""
         self.lib = load_library()
         n = force.getNumMultipoles() if num_particles is None else int(num_particles)
         force.validate(n, box)
@@ -175,7 +180,8 @@ class MPIDContext:
         s.precision = {"mixed": MPID_PRECISION_MIXED, "double": MPID_PRECISION_DOUBLE}[precision]
         s.flags = ((MPID_FLAG_EXACT_ANISO_TORQUE if exact_aniso_torque else 0) |
                    (MPID_FLAG_NEAR_FIELD_PCG if preconditioner else 0) |
-                   (MPID_FLAG_GRAPH_SOLVER if solver_graphs else 0))
+                   (MPID_FLAG_GRAPH_SOLVER if solver_graphs else 0) |
+                   (MPID_FLAG_SERIAL_STAGES if serial_stages else 0))
         self.n = n
         self.precision = precision
         self._h = ctypes.c_void_p()

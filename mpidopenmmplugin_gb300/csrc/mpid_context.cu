@@ -136,6 +136,7 @@ template <> struct FftTypes<double> {
 template <typename real>
 struct PmeStage {
     int order = 6, nx = 0, ny = 0, nz = 0;
+    int sms = 1;  // multiprocessors of the device (grid-stride launch sizes)
     size_t G = 0, Gh = 0;
     DBuf<typename GridAcc<real>::type> acc;
     DBuf<real> rgrid;
@@ -145,8 +146,9 @@ struct PmeStage {
     cufftHandle fwd = 0, inv = 0;
     bool planned = false;
 
-    void init(int ord, int gx, int gy, int gz, int npad) {
+    void init(int ord, int gx, int gy, int gz, int npad, int numSMs) {
         order = ord;
+        sms = numSMs;
         nx = gx; ny = gy; nz = gz;
         G = (size_t) nx * ny * nz;
         Gh = (size_t) nx * ny * (nz / 2 + 1);
@@ -183,11 +185,13 @@ struct PmeStage {
             launch(k_spread<real, 5, NCOMP>, nblk(threads, 256), 256, 0, st, n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
         else
             launch(k_spread<real, 6, NCOMP>, nblk(threads, 256), 256, 0, st, n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
-        launch(k_grid_finish<real>, std::min<long long>(nblk(G, 256), 152 * 16), 256, 0, st, G, acc.p, rgrid.p, skip);
+        launch(k_grid_finish<real>, std::min<long long>(nblk(G, 256), (long long) sms * 16), 256, 0, st, G, acc.p, rgrid.p,
+               skip);
     }
     void convolve(const double* influence, const int* skip, cudaStream_t st) {
         FftTypes<real>::exec_fwd(fwd, rgrid.p, cgrid.p);
-        launch(k_convolve<real>, std::min<long long>(nblk(Gh, 256), 152 * 16), 256, 0, st, Gh, influence, cgrid.p, skip);
+        launch(k_convolve<real>, std::min<long long>(nblk(Gh, 256), (long long) sms * 16), 256, 0, st, Gh, influence,
+               cgrid.p, skip);
         FftTypes<real>::exec_inv(inv, cgrid.p, rgrid.p);
     }
     template <int NTERM>
@@ -227,7 +231,7 @@ struct Engine {
         a.prm = prm.p; a.orig = orig.p; a.rank = rank.p;
         return a;
     }
-    void init(int natoms, int pad, bool pme_, int order, const int* grid) {
+    void init(int natoms, int pad, bool pme_, int order, const int* grid, int numSMs) {
         n = natoms;
         npad = pad;
         usePme = pme_;
@@ -254,12 +258,12 @@ struct Engine {
         sp.alloc(3 * (size_t) npad);
         zc.alloc(3 * (size_t) npad);
         precFx.alloc(3 * (size_t) npad);
-        if (usePme) pme.init(order, grid[0], grid[1], grid[2], npad);
+        if (usePme) pme.init(order, grid[0], grid[1], grid[2], npad, numSMs);
     }
 };
 
 // Device time of the evaluation stages, from CUDA events on the launching stream.
-enum Stage { ST_SETUP = 0, ST_FIXED_REAL, ST_PME, ST_DIPOLE_REAL, ST_SOLVER, ST_PAIR, ST_FINISH, ST_REFINE_REAL, ST_COUNT };
+enum Stage { ST_SETUP = 0, ST_FIXED_REAL, ST_PME, ST_DIPOLE_REAL, ST_FFT, ST_PAIR, ST_FINISH, ST_REFINE_REAL, ST_COUNT };
 
 // Start/stop events of one timed stage.
 struct TimedPair {
@@ -343,6 +347,7 @@ struct StageTimer {
 struct Context {
     mpid_settings set;
     int device = 0;
+    int numSMs = 1;  // multiprocessors of the device, read at creation (launch sizes)
     int n = 0, npad = 0, ntiles = 0;
     bool usePme = false, mixed = true;
     cudaStream_t stream = nullptr;
@@ -354,6 +359,15 @@ struct Context {
     // the main stream's work so far, join_pme makes the main stream wait for the side.
     cudaStream_t pmeStream = nullptr;
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
+    // The side streams the context owns; bind_streams points the working members at them,
+    // or at the caller's stream under MPID_FLAG_SERIAL_STAGES.
+    cudaStream_t pmeOwn = nullptr, refOwn = nullptr, refPmeOwn = nullptr;
+    bool serialStages = false;
+    void bind_streams() {
+        pmeStream = serialStages ? stream : pmeOwn;
+        refStream = serialStages ? stream : refOwn;
+        refPmeStream = serialStages ? stream : refPmeOwn;
+    }
     // The mixed Mutual solver's FP64 residual check runs on its own pair of streams,
     // concurrently with the force/energy phase that assumes it passes.
     cudaStream_t refStream = nullptr, refPmeStream = nullptr;
@@ -479,7 +493,7 @@ struct Context {
         if (hostSc) cudaFreeHost(hostSc);
         if (evFork) cudaEventDestroy(evFork);
         if (evJoin) cudaEventDestroy(evJoin);
-        if (pmeStream) cudaStreamDestroy(pmeStream);
+        if (pmeOwn) cudaStreamDestroy(pmeOwn);
         if (hostMax) cudaFreeHost(hostMax);
         if (evLists) cudaEventDestroy(evLists);
         for (auto e : iterEvents) cudaEventDestroy(e);
@@ -487,8 +501,8 @@ struct Context {
         if (evStop) cudaEventDestroy(evStop);
         if (ownStream && stream) cudaStreamDestroy(stream);
         if (hostStream) cudaStreamDestroy(hostStream);
-        if (refStream) cudaStreamDestroy(refStream);
-        if (refPmeStream) cudaStreamDestroy(refPmeStream);
+        if (refOwn) cudaStreamDestroy(refOwn);
+        if (refPmeOwn) cudaStreamDestroy(refPmeOwn);
         for (cudaEvent_t e : {evRefFork, evRefJoin, evRefStart, evRefDone})
             if (e) cudaEventDestroy(e);
         if (refHost) cudaFreeHost(refHost);
@@ -521,6 +535,8 @@ struct Context {
             throw Error(MPID_ERR_INVALID, "extrapolation needs 1..8 coefficients");
         mixed = s.precision == MPID_PRECISION_MIXED;
         CUDA_CHECK(cudaSetDevice(device));
+        CUDA_CHECK(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device));
+        numSMs = std::max(numSMs, 1);
         npad = ((n + 31) / 32) * 32;
         ntiles = npad / 32;
         charge.alloc(n); dipole.alloc(3 * n); quad.alloc(6 * n); oct.alloc(10 * n); thole.alloc(n); pol.alloc(3 * n);
@@ -549,17 +565,19 @@ struct Context {
         // stream priority and take SMs ahead of the wide real-space pair kernels.
         int prLeast = 0, prGreatest = 0;
         CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&prLeast, &prGreatest));
-        CUDA_CHECK(cudaStreamCreateWithPriority(&pmeStream, cudaStreamNonBlocking, prGreatest));
+        CUDA_CHECK(cudaStreamCreateWithPriority(&pmeOwn, cudaStreamNonBlocking, prGreatest));
         CUDA_CHECK(cudaStreamCreateWithFlags(&hostStream, cudaStreamNonBlocking));
         if (s.precision == MPID_PRECISION_MIXED && s.polarization_type == MPID_MUTUAL) {
-            CUDA_CHECK(cudaStreamCreateWithFlags(&refStream, cudaStreamNonBlocking));
-            CUDA_CHECK(cudaStreamCreateWithPriority(&refPmeStream, cudaStreamNonBlocking, prGreatest));
+            CUDA_CHECK(cudaStreamCreateWithFlags(&refOwn, cudaStreamNonBlocking));
+            CUDA_CHECK(cudaStreamCreateWithPriority(&refPmeOwn, cudaStreamNonBlocking, prGreatest));
             for (cudaEvent_t* e : {&evRefFork, &evRefJoin, &evRefStart, &evRefDone})
                 CUDA_CHECK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
             CUDA_CHECK(cudaMallocHost(&refHost, sizeof(double)));
         }
         CUDA_CHECK(cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming));
         CUDA_CHECK(cudaEventCreateWithFlags(&evJoin, cudaEventDisableTiming));
+        serialStages = (s.flags & MPID_FLAG_SERIAL_STAGES) != 0;
+        bind_streams();
         CUDA_CHECK(cudaMallocHost(&hostDone, 260 * sizeof(int)));
         CUDA_CHECK(cudaMallocHost(&hostSc, 8 * sizeof(double)));
         CUDA_CHECK(cudaMallocHost(&hostMax, 4 * sizeof(int)));
@@ -572,14 +590,14 @@ struct Context {
         const int nPT = s.polarization_type == MPID_EXTRAPOLATED ? s.n_extrap : 0;
         if (mixed) {
             ef.reset(new Engine<float>());
-            ef->init(n, npad, usePme, s.pme_order, s.grid);
+            ef->init(n, npad, usePme, s.pme_order, s.grid, numSMs);
             pack0.alloc(npad); pack1.alloc(npad);
             r32.alloc(3 * (size_t) npad); p32.alloc(3 * (size_t) npad); q32.alloc(3 * (size_t) npad);
             x32.alloc(3 * (size_t) npad); b32.alloc(3 * (size_t) npad); res32.alloc(3 * (size_t) npad);
             if (nPT) { ptMuF.alloc((size_t) nPT * 3 * npad); ptEF.alloc((size_t) nPT * 3 * npad); ptGF.alloc((size_t) nPT * 6 * npad); }
             if (s.polarization_type == MPID_MUTUAL) {
                 ed.reset(new Engine<double>());  // FP64 residual of the refinement loop
-                ed->init(n, npad, usePme, s.pme_order, s.grid);
+                ed->init(n, npad, usePme, s.pme_order, s.grid, numSMs);
                 offDF.alloc(3 * (size_t) npad); muDF.alloc(3 * (size_t) npad);
                 tholeDF.alloc(npad); dampDF.alloc(npad);
                 if (usePme) {
@@ -592,7 +610,7 @@ struct Context {
             }
         } else {
             ed.reset(new Engine<double>());
-            ed->init(n, npad, usePme, s.pme_order, s.grid);
+            ed->init(n, npad, usePme, s.pme_order, s.grid, numSMs);
             if (nPT) { ptMuD.alloc((size_t) nPT * 3 * npad); ptED.alloc((size_t) nPT * 3 * npad); ptGD.alloc((size_t) nPT * 6 * npad); }
         }
         if (s.polarization_type == MPID_MUTUAL) {
@@ -772,7 +790,7 @@ struct Context {
             for (int i = 0; i < 3; ++i) box.A[j][i] = usePme ? set.grid[j] * R[i][j] : 0.0;
         if (usePme && std::memcmp(lastBox, b, sizeof(lastBox)) != 0) {
             const size_t Gh = (size_t) set.grid[0] * set.grid[1] * (set.grid[2] / 2 + 1);
-            launch(k_influence, std::min<long long>(nblk(Gh, 256), 152 * 8), 256, 0, stream, box, set.ewald_alpha,
+            launch(k_influence, std::min<long long>(nblk(Gh, 256), (long long) numSMs * 8), 256, 0, stream, box, set.ewald_alpha,
                    modx.p, mody.p, modz.p, L[0] * L[1] * L[2], influence.p);
             CUDA_CHECK(cudaGetLastError());
             std::memcpy(lastBox, b, sizeof(lastBox));
@@ -793,7 +811,7 @@ struct Context {
         list.alloc(entries);
         listEntries = (long long) entries;
         // one entry per warp task; split tasks stay below twice the split target
-        energyBlocks.alloc(std::max((size_t) ntiles * (cap / chunk + 2), (size_t) 4 * 152 * 64));
+        energyBlocks.alloc(std::max((size_t) ntiles * (cap / chunk + 2), (size_t) 4 * numSMs * 64));
     }
 
     static void upload(DBuf<float>& d, const std::vector<float>& h) {
@@ -878,14 +896,14 @@ struct Context {
     int pair_tasks() const { return ntiles * (nchunksL + nchunksS); }
     int pair_blocks() const { return std::max(1, nblk(pair_tasks(), kWarpsPerBlock)); }
     // The field and energy pair kernels cut each work item into sub-ranges until the
-    // launch holds two full waves of warps (152 SMs x 64 resident warps): their per-pair
+    // launch holds two full waves of warps (the device's SMs x 64 resident warps): their per-pair
     // gathers are latency-bound, and one work item per warp leaves SMs idle (most of
     // them below a few thousand atoms).  The lists and results are the same.  Measured
     // on the 24,000-atom box: the CG pair kernel goes from 87 to 75 us per launch
     // (split 4); on a 660-atom box the FP32 CG field from 41 to 10 us.
     int field_split() const {
         int split = 1;
-        while (split < chunk && (long long) pair_tasks() * split < 2LL * 152 * 64) split *= 2;
+        while (split < chunk && (long long) pair_tasks() * split < 2LL * numSMs * 64) split *= 2;
         return split;
     }
     NbrList field_list() const {
@@ -982,6 +1000,30 @@ struct Context {
         CUDA_CHECK(cudaGetLastError());
     }
 
+    // Forward FFT, convolution, inverse FFT of engine e's grid on the PME stream `ps`,
+    // inside an open ST_PME interval.  Under MPID_FLAG_SERIAL_STAGES the two cuFFT
+    // executions are timed as their own stage.
+    template <typename real>
+    void convolve(Engine<real>& e, const int* skip, cudaStream_t ps) {
+        if (!serialStages) {
+            e.pme.convolve(influence.p, skip, ps);
+            return;
+        }
+        PmeStage<real>& p = e.pme;
+        timer.end(ps);
+        timer.begin(ST_FFT, ps);
+        FftTypes<real>::exec_fwd(p.fwd, p.rgrid.p, p.cgrid.p);
+        timer.end(ps);
+        timer.begin(ST_PME, ps);
+        launch(k_convolve<real>, std::min<long long>(nblk(p.Gh, 256), (long long) p.sms * 16), 256, 0, ps, p.Gh,
+               (const double*) influence.p, p.cgrid.p, skip);
+        timer.end(ps);
+        timer.begin(ST_FFT, ps);
+        FftTypes<real>::exec_inv(p.inv, p.cgrid.p, p.rgrid.p);
+        timer.end(ps);
+        timer.begin(ST_PME, ps);
+    }
+
     double self_coef() const {
         return usePme ? 4.0 / 3.0 * set.ewald_alpha * set.ewald_alpha * set.ewald_alpha / kSqrtPiRef : 0.0;
     }
@@ -996,7 +1038,7 @@ struct Context {
             cudaStream_t ps = pmeStream;
             timer.begin(ST_PME, ps);
             e.pme.template spread<20>(n, npad, box, e.mf.p, nullptr, ps);
-            e.pme.convolve(influence.p, nullptr, ps);
+            convolve(e, nullptr, ps);
             e.pme.template gather<35>(n, npad, box, e.phiP.p, nullptr, ps);
             timer.end(ps);
         }
@@ -1021,7 +1063,7 @@ struct Context {
             timer.begin(ST_PME, ps);
             launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, ps, npad, box, mu, e.mfd.p, skip);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, skip, ps);
-            e.pme.convolve(influence.p, skip, ps);
+            convolve(e, skip, ps);
             if (nterm == 4)
                 e.pme.template gather<4>(n, npad, box, e.phiT.p, skip, ps);
             else if (nterm == 10)
@@ -1067,7 +1109,7 @@ struct Context {
             cudaStream_t ps = pmeStream;
             timer.begin(ST_PME, ps);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, done.p, ps);
-            e.pme.convolve(influence.p, done.p, ps);
+            convolve(e, done.p, ps);
             e.pme.template gather<4>(n, npad, box, e.phiT.p, done.p, ps);
             timer.end(ps);
         }
@@ -1188,7 +1230,7 @@ struct Context {
                 k.push_back(len);
                 replay(k, [&] {
                     for (int i = 0; i < len; ++i) cg_iteration(e, x, r, p, q, target, maxIter, false);
-                }, 2 * len + 2);
+                }, 6 * len + 2);
                 it += len;
                 CUDA_CHECK(cudaMemcpyAsync(hostDone, done.p, sizeof(int), cudaMemcpyDeviceToHost, st));
                 CUDA_CHECK(cudaEventRecord(iterEvents[0], st));
@@ -1259,7 +1301,7 @@ struct Context {
     // that a replay would skip) directly, or with graphs from the graph of `key`,
     // capturing it on first use.
     template <typename Body>
-    void replay(const std::vector<long long>& key, Body&& body, int timedPairs = 8) {
+    void replay(const std::vector<long long>& key, Body&& body, int timedPairs = 24) {
         if (!graph_mode()) {
             body();
             return;
@@ -1525,7 +1567,7 @@ struct Context {
             timer.begin(ST_PME, ps);
             launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, ps, npad, box, e.mu.p, e.mfd.p, nullptr);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, nullptr, ps);
-            e.pme.convolve(influence.p, nullptr, ps);
+            convolve(e, nullptr, ps);
             e.pme.template gather<35>(n, npad, box, e.phiD.p, nullptr, ps);
             timer.end(ps);
         }
@@ -1562,7 +1604,7 @@ struct Context {
             opt.G = ptG;
         }
         // per-atom work is long: blocks small enough that a small system spans the SMs
-        const int rb = npad >= 256 * 2 * 152 ? 256 : (npad >= 128 * 152 ? 128 : (npad >= 64 * 152 ? 64 : 32));
+        const int rb = npad >= 256 * 2 * numSMs ? 256 : (npad >= 128 * numSMs ? 128 : (npad >= 64 * numSMs ? 64 : 32));
         const int nb = nblk(npad, rb);
         launch(k_recip_self<real>, nb, rb, 0, st, n, npad, box, set.ewald_alpha, set.polarization_type,
                                                 usePme ? e.phiP.p : nullptr, e.phiD.p, e.mu.p, e.arrays(), mom64.p, opt,
@@ -1598,6 +1640,7 @@ struct Context {
     double evaluate_device(const double* d_pos, const double* hbox, double* d_forces, double* d_energy) {
         if (!haveParams) throw Error(MPID_ERR_STATE, "mpid_set_multipoles must be called before evaluating");
         CUDA_CHECK(cudaSetDevice(device));
+        bind_streams();
         cudaStream_t st = stream;
         choose_graph_mode();
         const long long launches0 = t_launches, library0 = t_library_calls;
@@ -1810,7 +1853,7 @@ struct Context {
         if (!dp) {
             if (!eg) {
                 eg.reset(new Engine<double>());
-                eg->init(n, npad, usePme, set.pme_order, set.grid);
+                eg->init(n, npad, usePme, set.pme_order, set.grid, numSMs);
             }
             dp = eg.get();
         }
@@ -1844,7 +1887,7 @@ struct Context {
     // enough warps to cover every SM several times (a power of two dividing the chunk).
     int gradient_split(long long items) const {
         int split = 1;
-        while (split < chunk && items * split < 16LL * 152) split *= 2;
+        while (split < chunk && items * split < 16LL * numSMs) split *= 2;
         return split;
     }
     int gradient_blocks(int split) const { return std::max(1, nblk((long long) pair_tasks() * split, kWarpsPerBlock)); }
@@ -1867,7 +1910,7 @@ struct Context {
                                         "scratch; evaluate with mpid_evaluate_device or a host-buffer call first");
         if (mixed && !ed && !eg) {
             eg.reset(new Engine<double>());
-            eg->init(n, npad, usePme, set.pme_order, set.grid);
+            eg->init(n, npad, usePme, set.pme_order, set.grid, numSMs);
         }
         if (multipole) {
             gradFx.alloc((size_t) 20 * npad);

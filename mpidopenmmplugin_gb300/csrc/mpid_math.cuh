@@ -34,12 +34,10 @@ template <> struct Prec<float> {
     // Below this alpha*r the erf part of the kernels comes from the Boys function series
     // (the erfc recursion above it).
     static constexpr float kQuadX = 1.5f;
-    static constexpr int kQuadNodes = 8;
     static constexpr int kBoysTerms = 16;   // series truncation < 3e-11 relative at (alpha r)^2 <= 2.25
 };
 template <> struct Prec<double> {
     static constexpr double kQuadX = 1.5;
-    static constexpr int kQuadNodes = 14;
     static constexpr int kBoysTerms = 26;   // < 1e-16
 };
 
@@ -58,35 +56,6 @@ MPID_HD float m_fma(float a, float b, float c) { return fmaf(a, b, c); }
 MPID_HD double m_fma(double a, double b, double c) { return fma(a, b, c); }
 
 // ---------------------------------------------------------------------------
-// Gauss-Legendre nodes/weights on [0, 1] (8 and 14 points), used to integrate
-//   F_n(x) = int_0^1 v^(2n) exp(-x^2 v^2) dv,
-// which gives the erf(alpha r)/r part of every kernel without cancellation:
-//   b_n[erf(alpha r)/r] = 2^(n+1) alpha^(2n+1) / sqrt(pi) * F_n(alpha r).
-template <typename real, int K>
-struct GaussLegendre01;
-template <typename real>
-struct GaussLegendre01<real, 8> {
-    MPID_HD static real node(int i) {
-        const double t[8] = {0.019855071751231912, 0.10166676129318664, 0.2372337950418355, 0.40828267875217511, 0.59171732124782483, 0.7627662049581645, 0.89833323870681336, 0.98014492824876809};
-        return real(t[i]);
-    }
-    MPID_HD static real weight(int i) {
-        const double w[8] = {0.050614268145188532, 0.11119051722668721, 0.15685332293894344, 0.18134189168918083, 0.18134189168918083, 0.15685332293894344, 0.11119051722668721, 0.050614268145188532};
-        return real(w[i]);
-    }
-};
-template <typename real>
-struct GaussLegendre01<real, 14> {
-    MPID_HD static real node(int i) {
-        const double t[14] = {0.0068580956515937874, 0.035782558168213241, 0.08639934246511749, 0.15635354759415726, 0.24237568182092295, 0.34044381553605513, 0.44597252564632817, 0.55402747435367183, 0.65955618446394482, 0.75762431817907705, 0.84364645240584268, 0.91360065753488251, 0.96421744183178681, 0.99314190434840621};
-        return real(t[i]);
-    }
-    MPID_HD static real weight(int i) {
-        const double w[14] = {0.017559730165875875, 0.040079043579879993, 0.060759285343951655, 0.078601583579096815, 0.092769198738968939, 0.10259923186064786, 0.10763192673157897, 0.10763192673157897, 0.10259923186064786, 0.092769198738968939, 0.078601583579096815, 0.060759285343951655, 0.040079043579879993, 0.017559730165875875};
-        return real(w[i]);
-    }
-};
-
 // Ewald parameter split so that products with alpha are formed without rounding alpha
 // itself: alpha = hi + lo with hi = real(alpha).  Rounding alpha once would bias every
 // erfc(alpha r) the same way (by up to ~13x its relative error near alpha r = 2.5).
@@ -111,35 +80,6 @@ struct EwaldAlpha {
     // v * 2 alpha / sqrt(pi) without the rounding of the constant
     MPID_HD real times_pre(real v) const { return m_fma(pre_hi, v, pre_lo * v); }
 };
-
-// b_n (n = 0..NMAX) of erf(alpha r)/r for alpha r below the quadrature threshold.
-template <typename real, int NMAX>
-MPID_HD void erf_part_quadrature(real r, const EwaldAlpha<real>& al, real* bF) {
-    constexpr int K = Prec<real>::kQuadNodes;
-    real acc[NMAX + 1];
-#pragma unroll
-    for (int n = 0; n <= NMAX; ++n) acc[n] = real(0);
-    const real x = al.times(r);
-    const real x2 = x * x;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const real v = GaussLegendre01<real, K>::node(k);
-        const real v2 = v * v;
-        real term = GaussLegendre01<real, K>::weight(k) * m_exp(-x2 * v2);
-#pragma unroll
-        for (int n = 0; n <= NMAX; ++n) {
-            acc[n] += term;
-            term *= v2;
-        }
-    }
-    // prefactor 2^(n+1) alpha^(2n+1) / sqrt(pi), the leading factor kept as hi + lo
-    real scale = real(1);
-#pragma unroll
-    for (int n = 0; n <= NMAX; ++n) {
-        bF[n] = al.times_pre(acc[n]) * scale;
-        scale = al.times_a2x2(scale);
-    }
-}
 
 // 1/m as an unevaluated sum hi + lo of the arithmetic type (so that products with it
 // carry no systematic rounding of the constant).
@@ -302,9 +242,10 @@ struct PairRadial {
 };
 
 // Compute the requested radial arrays.  NP/NI/NU < 0 disables a kernel.  QUAD selects
-// the branch at compile time: true integrates the erf part by quadrature (needed where
-// erf(alpha r)/r must not be formed as a difference: alpha r below the threshold, or
-// covalent scale 0), false uses the erfc recursion.  pair_radial picks by alpha r.
+// the branch at compile time (the name of the lists' near segment): true takes the erf
+// part from the Boys-function series (needed where erf(alpha r)/r must not be formed as
+// a difference: alpha r below the threshold, or covalent scale 0), false uses the erfc
+// recursion.  pair_radial picks by alpha r.
 template <typename real, int NP, int NI, int NU, bool QUAD>
 MPID_HD void pair_radial_branch(real r, const EwaldAlpha<real>& alpha, real scale, real tholeA, real dampProd,
                                 PairRadial<real, (NP > 0 ? NP : 0), (NI > 0 ? NI : 0), (NU > 0 ? NU : 0)>& out) {

@@ -17,7 +17,12 @@ oracle/Makefile) on seeded synthetic systems and stores inputs and outputs as .n
 * triclinic_{direct,mutual,extrapolated}.npz -- the water box in a reduced triclinic
   cell (all three off-diagonal box entries non-zero).
 
-Usage:  python tests/golden/make_fixtures.py [properties | triclinic]   (needs the reference tree)
+* converged_water648_{full,nooctopoles}.npz -- the water box (Mutual, 1e-11 D) on a
+  128^3 grid at the reference's order 6, where its PME has converged to the Ewald sum
+  to ~1e-7 in forces: the target that order-5 PME must approach as its grid is refined
+  (the second variant with the octopoles set to zero).
+
+Usage:  python tests/golden/make_fixtures.py [properties | triclinic | converged]   (needs the reference tree)
 """
 import os
 import sys
@@ -168,8 +173,31 @@ def make_triclinic():
         save("triclinic_%s.npz" % POL[pol], s, O.evaluate(s, "ref", want_labdipoles=True))
 
 
+def converged_water(variant):
+    """The water648 box (Mutual) with tight solver tolerance; variant "nooctopoles" sets
+    every octopole to zero."""
+    f, pos, box = synthetic.workload("water648", polarization=0, order=6)
+    f.setMutualInducedTargetEpsilon(1e-11)
+    f.setMutualInducedMaxIterations(500)
+    s = helpers.oracle_system(f, pos, box, pme_order=6)
+    if variant == "nooctopoles":
+        s.octopole = np.zeros_like(s.octopole)
+    return s
+
+
+def make_converged():
+    """converged_water648_{full,nooctopoles}.npz: the reference at order 6 on 128^3."""
+    O.build("ref")
+    for variant in ("full", "nooctopoles"):
+        s = converged_water(variant)
+        s.grid = (128, 128, 128)
+        save("converged_water648_%s.npz" % variant, s, O.evaluate(s, "ref", want_labdipoles=True))
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 1 and sys.argv[1] == "properties":
+    if len(sys.argv) > 1 and sys.argv[1] == "converged":
+        make_converged()
+    elif len(sys.argv) > 1 and sys.argv[1] == "properties":
         make_properties()
     elif len(sys.argv) > 1 and sys.argv[1] == "triclinic":
         make_triclinic()

@@ -2,15 +2,17 @@
 // kernel source itself: the per-pair mathematics of mpid_math.cuh is instantiated with
 // a number type that counts every arithmetic operation it performs.
 //
-//   g++ -O0 -std=c++17 -I mpidopenmmplugin_gb300/csrc mpidopenmmplugin_gb300/csrc/flop_count.cpp -o /tmp/flop_count
+//   g++ -O0 -std=c++17 -I mpidopenmmplugin_gb300/csrc tests/native/flop_count.cpp -o /tmp/flop_count
 //   /tmp/flop_count
 //
 // Convention: add, sub, mul = 1; an FMA appears as its mul + add = 2; div, sqrt, exp,
 // erfc, rint = 1 each (they are also reported separately, as special functions).
-// Two representative pairs are counted: alpha r below the quadrature threshold (erf
-// part by 8-point Gauss-Legendre) and above it (erfc recursion); the per-pair average
-// weights them by the fraction of pair volume inside a 0.9 nm cutoff with alpha = 3.4:
-// r < 1.5 / 3.4 nm holds (0.441 / 0.9)^3 = 11.8 % of the pairs.
+// Two representative pairs are counted: alpha r below the near-segment threshold (erf
+// part from the Boys-function series and its downward recursion) and above it (erfc
+// recursion); the per-pair average weights them by the fraction of pair volume inside a
+// 0.9 nm cutoff with alpha = 3.4: r < 1.5 / 3.4 nm holds (0.441 / 0.9)^3 = 11.8 % of the
+// pairs.  tests/test_cpu_host.py checks that the averages are the FLOP/pair figures that
+// bench.py uses for the roofline.
 #include <cmath>
 #include <cstdio>
 
@@ -62,7 +64,6 @@ static inline CF sqrt(CF x) { ++g.special; return mk(std::sqrt(x.v)); }
 namespace mpid {
 template <> struct Prec<CF> {
     static constexpr float kQuadX = 1.5f;
-    static constexpr int kQuadNodes = 8;
     static constexpr int kBoysTerms = 16;
 };
 }  // namespace mpid

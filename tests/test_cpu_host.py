@@ -128,7 +128,7 @@ def test_double_float_residual_arithmetic(tmp_path, alpha, cutoff):
         pytest.skip("g++ not available")
     csrc = os.path.join(ROOT, "mpidopenmmplugin_gb300", "csrc")
     exe = str(tmp_path / "df_check")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-I", csrc, os.path.join(csrc, "df_check.cpp"), "-o", exe], check=True)
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I", csrc, os.path.join(ROOT, "tests", "native", "df_check.cpp"), "-o", exe], check=True)
     out = subprocess.run([exe, str(alpha), str(cutoff)], check=True, capture_output=True, text=True).stdout
     errs = {k: float(v) for k, v in (line.split() for line in out.strip().splitlines())}
     assert set(errs) == {"erfc_table", "erf_table", "exp_neg", "div", "sqrt"}
@@ -157,7 +157,7 @@ def test_solution_workload_geometry():
 
 
 def test_radial_functions_against_long_double(tmp_path):
-    """Ewald radial functions of the pair kernels (radial_check.cpp) against long double:
+    """Ewald radial functions of the pair kernels (tests/native/radial_check.cpp) against long double:
     FP64 to 1e-14; FP32 to a few ulp with no systematic bias in the erfc recursion."""
     import shutil
     cxx = shutil.which("g++")
@@ -165,7 +165,7 @@ def test_radial_functions_against_long_double(tmp_path):
         pytest.skip("g++ not available")
     csrc = os.path.join(ROOT, "mpidopenmmplugin_gb300", "csrc")
     exe = str(tmp_path / "radial_check")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-I", csrc, os.path.join(csrc, "radial_check.cpp"), "-o", exe], check=True)
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I", csrc, os.path.join(ROOT, "tests", "native", "radial_check.cpp"), "-o", exe], check=True)
     out = subprocess.run([exe, "3.4", "0.9"], check=True, capture_output=True, text=True).stdout
     res = {k: (float(a), float(b)) for k, a, b in (line.split() for line in out.strip().splitlines())}
     assert res["erf_double"][0] < 1e-14 and res["erfc_double"][0] < 1e-14
@@ -200,7 +200,8 @@ def test_openmm_adapter_compiles_against_interface_stubs():
 def test_bench_reference_arm_json_line():
     """`bench.py --impl reference` (the CPU arm the GPU line is compared with) prints one
     JSON line with the GPU arm's metric and unit, the cpu_baseline and e2e objects, and a
-    time bound: here one warm-up and one timed evaluation of the 24,000-atom box."""
+    time bound: here the three warm-up evaluations asked for and one timed evaluation of
+    the 24,000-atom box."""
     import json
     import sys
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
@@ -210,7 +211,7 @@ def test_bench_reference_arm_json_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "evals/s" and d["higher_is_better"] is True
     assert d["metric"].startswith("force+energy evals/s")
-    assert d["steps"] == 1 and d["warmup"] == 1 and d["steps_requested"] == 1 and d["value"] > 0
+    assert d["steps"] == 1 and d["warmup"] == 3 and d["steps_requested"] == 1 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
@@ -239,3 +240,27 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for field, _ in py._fields_:
             assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
+
+
+def test_flop_counts_match_bench_constants(tmp_path):
+    """bench.py's FLOP/pair figures (the roofline numerator) are the counts that
+    tests/native/flop_count.cpp takes from the pair kernels' own per-pair mathematics."""
+    import shutil
+    import sys
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    exe = str(tmp_path / "flop_count")
+    subprocess.run([cxx, "-O0", "-std=c++17", "-I", os.path.join(ROOT, "mpidopenmmplugin_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "native", "flop_count.cpp"), "-o", exe], check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    mean = {}
+    for line in out.splitlines():
+        m = re.match(r"(k_\w+(?: mut)?)\s.*mean\s+(\d+) FLOP/pair", line)
+        if m:
+            mean[m.group(1)] = int(m.group(2))
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.FLOP_PER_PAIR == {"pair_kernel": mean["k_electrostatics mut"],
+                                   "dipole_field_pairs": mean["k_dipole_field"],
+                                   "fixed_field_pairs": mean["k_fixed_field"]}

@@ -357,3 +357,39 @@ def test_automatic_pme_parameters_and_force_side_queries():
     f.setMultipoleParameters(0, *p)
     f.updateParametersInContext(ctx)
     assert ctx.evaluate(pos, box)[0] != e
+
+
+_PORT_CACHE = {}
+
+
+def _port_water24k(eps):
+    """The oracle port's FP64 evaluation of the 24,000-atom box (order 5, Mutual) at
+    solver tolerance eps, once per process."""
+    from oracle import oracle as O
+    if eps not in _PORT_CACHE:
+        if not O.available("port"):
+            O.build("port")
+        f, pos, box = synthetic.workload("water24k", polarization=MPIDForce.Mutual)
+        f.setMutualInducedTargetEpsilon(eps)
+        _PORT_CACHE[eps] = (f, pos, box, O.evaluate(helpers.oracle_system(f, pos, box), "port"))
+    return _PORT_CACHE[eps]
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_water24k_order5_against_oracle(precision):
+    """The headline box (24,000 atoms, 72^3 grid, order-5 PME, Mutual) against the oracle
+    port's FP64 evaluation of the same inputs.  FP64 path (both solves to 1e-9 D):
+    energy 1e-8, forces 1e-7, induced dipoles 1e-6 relative.  Mixed path (1e-7 D, the
+    workload's tolerance, as is the port): the accuracy gates, energy 1e-6, forces 5e-6,
+    induced dipoles 5e-6."""
+    eps = 1e-9 if precision == "double" else 1e-7
+    f, pos, box, ref = _port_water24k(eps)
+    ctx, e, forces = run(f, pos, box, precision)
+    eerr = abs(e - ref.energy) / abs(ref.energy)
+    ferr = helpers.rel_rms(forces, ref.forces)
+    merr = helpers.rel_rms(ctx.getInducedDipoles(), ref.induced)
+    print("water24k %s vs oracle: energy %.3e force %.3e dipole %.3e" % (precision, eerr, ferr, merr))
+    if precision == "double":
+        assert eerr < 1e-8 and ferr < 1e-7 and merr < 1e-6
+    else:
+        assert eerr < 1e-6 and ferr < 5e-6 and merr < 5e-6
