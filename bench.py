@@ -177,7 +177,7 @@ def count_pairs_within(pos, box, cutoff):
 # counted from the kernels' own source by tests/native/flop_count.cpp and averaged over the
 # pair-distance distribution of a 0.9 nm cutoff with alpha = 3.4/nm.
 FLOP_PER_PAIR = {"pair_kernel": 2728,          # k_electrostatics<float, MUTUAL>
-                 "dipole_field_pairs": 154,    # k_dipole_field_packed (CG matrix-vector product)
+                 "dipole_field_pairs": 154,    # k_dipole_field_cg (CG matrix-vector product)
                  "fixed_field_pairs": 472}     # k_fixed_field<float>
 # DRAM bytes per launch (read + write) from one ncu capture of each kernel on the
 # 24,000-atom box with caches left warm (--cache-control none), summarised under
@@ -185,7 +185,7 @@ FLOP_PER_PAIR = {"pair_kernel": 2728,          # k_electrostatics<float, MUTUAL>
 DRAM_BYTES_PER_LAUNCH = {"pair_kernel": 29.42e6 + 0.39e6, "dipole_field_pairs": 32.86e6}
 DRAM_BYTES_SOURCE = "cold-cache ncu capture (profiles/k_dipole_field_packed_water24k_mutual.md)"
 KERNEL_NAMES = {"pair_kernel": "k_electrostatics<float, mutual> (energy/force/torque pair kernel)",
-                "dipole_field_pairs": "k_dipole_field_packed (FP32 T.mu pair kernel of the CG solver)",
+                "dipole_field_pairs": "k_dipole_field_cg (FP32 T.mu pair kernel of the CG solver)",
                 "fixed_field_pairs": "k_fixed_field<float> (permanent-field pair kernel)"}
 
 

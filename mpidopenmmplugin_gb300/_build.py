@@ -10,7 +10,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libmpid_gb300.so")
 SOURCES = ["mpid_context.cu"]
 DEPS = ["mpid_context.cu", "mpid_kernels.cuh", "mpid_math.cuh", "qi_tables.cuh", "pme_host.h", "df64.cuh",
-        "radial_tables.h"]
+        "radial_tables.h", "cg_radial.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -407,6 +407,7 @@ struct Context {
     // double-float inputs and Ewald tables of the mixed path's residual field
     DBuf<float2> offDF, muDF, tholeDF, dampDF;
     DBuf<float4> pack0, pack1;  // packed operands of the FP32 CG pair kernel
+    CgRadial cgR{};             // its radial-function polynomials (cg_radial.h)
     DBuf<float> tabG, tabGc, tabH, tabHc;
     RadialTableHost tabGh, tabHh;
     DBuf<unsigned> list;
@@ -592,6 +593,7 @@ struct Context {
             ef.reset(new Engine<float>());
             ef->init(n, npad, usePme, s.pme_order, s.grid, numSMs);
             pack0.alloc(npad); pack1.alloc(npad);
+            cgR = build_cg_radial(usePme ? s.ewald_alpha : 0.0, Prec<float>::kQuadX, list_cutoff());
             r32.alloc(3 * (size_t) npad); p32.alloc(3 * (size_t) npad); q32.alloc(3 * (size_t) npad);
             x32.alloc(3 * (size_t) npad); b32.alloc(3 * (size_t) npad); res32.alloc(3 * (size_t) npad);
             if (nPT) { ptMuF.alloc((size_t) nPT * 3 * npad); ptEF.alloc((size_t) nPT * 3 * npad); ptGF.alloc((size_t) nPT * 6 * npad); }
@@ -1115,7 +1117,7 @@ struct Context {
         }
         timer.begin(ST_DIPOLE_REAL, st);
         if (packed)
-            launch(k_dipole_field_packed, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), (const float4*) pack0.p,
+            launch(k_dipole_field_cg, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), cgR, (const float4*) pack0.p,
                    (const float4*) pack1.p, npad, (const int*) e.orig.p, e.fieldFx.p, (const int*) done.p);
         else
             launch(k_dipole_field<real, false, sizeof(real) == 8>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(),

@@ -6,13 +6,14 @@
 //   off[3][npad]       position minus its tile centre (real)
 //   mom[20][npad]      lab-frame q, dipole[3], Q6[6], O10[10] (real)
 //   alab[6][npad]      lab-frame polarisability, sroot[6][npad] its square root
-//   prm[npad]          (thole, damp, aniso flag, unused) in the arithmetic type; orig[npad]
+//   prm[npad]          (thole, damp, aniso flag, 1/damp or 0) in the arithmetic type; orig[npad]
 // Forces, torques and fields accumulate as 64-bit fixed point with 2^32 units.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "mpid_math.cuh"
 #include "df64.cuh"
+#include "cg_radial.h"
 
 namespace mpid {
 
@@ -326,7 +327,8 @@ __global__ void k_gather_atoms(int n, int npad, const int* __restrict__ order, M
         }
     const bool aniso = p.pol[0] != p.pol[1] || p.pol[0] != p.pol[2];
     const double damp = pow((p.pol[0] + p.pol[1] + p.pol[2]) / 3.0, 1.0 / 6.0);
-    at.prm[s] = Vec4<real>::make(real(mol.thole[i]), real(damp), aniso ? real(1) : real(0), real(0));
+    at.prm[s] = Vec4<real>::make(real(mol.thole[i]), real(damp), aniso ? real(1) : real(0),
+                                 real(damp > 0.0 ? 1.0 / damp : 0.0));
     if (prm64) {
         prm64[2 * i] = mol.thole[i];
         prm64[2 * i + 1] = damp;
@@ -737,12 +739,18 @@ k_dipole_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, uns
         for (int q = 0; q < 6; ++q) fx_add(grad + q * npad + t.si, acc[3 + q]);
 }
 
-// FP32 T.mu of the CG iterations with packed operands: per pair one 16-byte load of the
-// tile slot (shift, J in .w), and two of atom j: A0 = (offset, Thole width) and
-// A1 = (dipole, damping factor).  Same arithmetic as k_dipole_field<float, false>.
+// FP32 T.mu of the CG iterations: the induced-induced kernel K_u with the Thole width of
+// the pair (MPIDReferenceForce.cpp:4161-4281), with the radial functions of cg_radial.h
+// (one exponential and one polynomial for the Ewald part, 1/r from rsqrt and a Newton
+// step, Thole factors from the inverse damping factors).  Per pair one 16-byte load of
+// the tile slot (shift, J in .w) and two of atom j: A0 = (offset, Thole width) and
+// A1 = (S p, 1 / damping factor).  An atom without polarisability has 1/damping 0, which
+// fully damps its pairs; the operator B = I - S T S multiplies those pairs by its S = 0,
+// so that choice does not change the product.
+
 template <bool QUAD>
-__device__ __forceinline__ void dipole_field_packed_loop(const NbrList& nl, const float4* __restrict__ A0,
-                                                         const float4* __restrict__ A1, const PairTask& t, float* acc) {
+__device__ __forceinline__ void cg_field_loop(const NbrList& nl, const CgRadial& R, const float4* __restrict__ A0,
+                                              const float4* __restrict__ A1, const PairTask& t, float* acc) {
     const PairConsts<float>& pc = nl.cf;
     const float4 ai = A0[t.si], bi = A1[t.si];
     for (int k = t.k0; k < t.k1; ++k) {
@@ -756,12 +764,11 @@ __device__ __forceinline__ void dipole_field_packed_loop(const NbrList& nl, cons
         if (Jw < 0) min_image(d, pc.V, pc.iL);
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (nl.usePbc && r2 > pc.rc2) continue;
-        const float r = sqrtf(r2);
         const unsigned flag = (code >> 5) & 3u;
         const float a = flag == 1u ? ai.w + aj.w : pc.thole;  // flag 1: covalent scale 0
-        PairRadial<float, 0, 0, 2> pr;
-        pair_radial_branch<float, -1, -1, 2, QUAD>(r, pc.ew, 1.f, a, bi.w * bj.w, pr);
-        const float b[4] = {0.f, pr.bU[1], pr.bU[2], 0.f};
+        float b1, b2;
+        cg_pair_radial<QUAD>(R, r2, a, bi.w * bj.w, pc.ew.hi, pc.ew.lo, b1, b2);
+        const float b[4] = {0.f, b1, b2, 0.f};
         const float uj[3] = {bj.x, bj.y, bj.z};
         const float sI[3] = {-d[0], -d[1], -d[2]};
         float e[3], gr[6];
@@ -773,18 +780,35 @@ __device__ __forceinline__ void dipole_field_packed_loop(const NbrList& nl, cons
 }
 
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_dipole_field_packed(NbrList nl, const float4* __restrict__ A0, const float4* __restrict__ A1, int npad,
-                      const int* __restrict__ orig, unsigned long long* __restrict__ field, const int* __restrict__ skip) {
+k_dipole_field_cg(NbrList nl, CgRadial R, const float4* __restrict__ A0, const float4* __restrict__ A1, int npad,
+                  const int* __restrict__ orig, unsigned long long* __restrict__ field, const int* __restrict__ skip) {
     if (*skip) return;
+    __shared__ float part[kWarpsPerBlock][3][32];
     PairTask t;
-    if (!t.init(nl)) return;
-    if (orig[t.si] < 0) return;
+    const bool active = t.init(nl) && orig[t.si] >= 0;
     float acc[3] = {0.f, 0.f, 0.f};
-    if (t.quad)
-        dipole_field_packed_loop<true>(nl, A0, A1, t, acc);
-    else
-        dipole_field_packed_loop<false>(nl, A0, A1, t, acc);
-    for (int q = 0; q < 3; ++q) fx_add(field + q * npad + t.si, acc[q]);
+    if (active) {
+        if (t.quad)
+            cg_field_loop<true>(nl, R, A0, A1, t, acc);
+        else
+            cg_field_loop<false>(nl, R, A0, A1, t, acc);
+    }
+    // The sub-ranges of one work item are consecutive warps; within a block they add
+    // their partial fields in shared memory, so that an item makes one set of atomics
+    // per block (a fixed order: the sums stay deterministic).
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = min(nl.split, kWarpsPerBlock);
+    if (g > 1) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) part[w][q][lane] = acc[q];
+        __syncthreads();
+        if (w % g != 0) return;
+        for (int o = 1; o < g; ++o)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) acc[q] += part[w + o][q][lane];
+    }
+    if (active)
+        for (int q = 0; q < 3; ++q) fx_add(field + q * npad + t.si, acc[q]);
 }
 
 // A0 = (offset, Thole width) of the float engine's atoms.
@@ -2190,7 +2214,7 @@ __global__ void k_cg_direction_sroot(int npad, BoxDev box, const real* __restric
     real o[3];
     sym_mul(S, npad, s, v, o);
     for (int c = 0; c < 3; ++c) sp[c * npad + s] = o[c];
-    if (A1) A1[s] = Vec4<real>::make(o[0], o[1], o[2], prm[s].y);
+    if (A1) A1[s] = Vec4<real>::make(o[0], o[1], o[2], prm[s].w);  // (S p, 1 / damping)
     if (mfd) {
         mfd[s] = real(0);
         for (int j = 0; j < 3; ++j)

@@ -2,7 +2,7 @@
 // long double: b_n (n = 0..7) of erf(alpha r)/r below the branch threshold (Boys
 // function series) and of erfc(alpha r)/r above it, in float and in double.
 //
-//   g++ -O2 -std=c++17 -I mpidopenmmplugin_gb300/csrc mpidopenmmplugin_gb300/csrc/radial_check.cpp -o /tmp/radial_check
+//   g++ -O2 -std=c++17 -I mpidopenmmplugin_gb300/csrc tests/native/radial_check.cpp -o /tmp/radial_check
 //   /tmp/radial_check alpha cutoff
 //
 // Prints "name max_relative_error mean_signed_relative_error" per check; the mean of the

@@ -264,3 +264,27 @@ def test_flop_counts_match_bench_constants(tmp_path):
     assert bench.FLOP_PER_PAIR == {"pair_kernel": mean["k_electrostatics mut"],
                                    "dipole_field_pairs": mean["k_dipole_field"],
                                    "fixed_field_pairs": mean["k_fixed_field"]}
+
+
+@pytest.mark.parametrize("alpha,cutoff", [(3.4, 0.9), (3.5, 0.8), (4.0, 0.7)])
+def test_cg_radial_polynomials_against_long_double(tmp_path, alpha, cutoff):
+    """The CG pair kernel's radial functions (cg_radial.h: erfc(x) exp(x^2) and the Boys
+    functions as fitted polynomials, Thole factors from the inverse damping product)
+    against long double over the whole list range: b_1, b_2 within 6e-7 of the pair's
+    bare 1/r^3, 3/r^5, and no worse than the general FP32 radial functions of the other
+    pair kernels (tests/native/cg_radial_check.cpp)."""
+    import shutil
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    exe = str(tmp_path / "cg_radial_check")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "mpidopenmmplugin_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "native", "cg_radial_check.cpp"), "-o", exe], check=True)
+    out = subprocess.run([exe, str(alpha), str(cutoff)], check=True, capture_output=True, text=True).stdout
+    vals = {}
+    for line in out.splitlines():
+        p = line.split()
+        vals[p[0]] = (float(p[3]), float(p[8]))  # b1, b2 errors on the bare scale
+    poly, general = vals["polynomial"], vals["general"]
+    assert poly[0] < 6e-7 and poly[1] < 6e-7, out
+    assert poly[0] <= 1.1 * general[0] and poly[1] <= 1.1 * general[1], out
