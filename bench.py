@@ -180,10 +180,11 @@ FLOP_PER_PAIR = {"pair_kernel": 2728,          # k_electrostatics<float, MUTUAL>
                  "dipole_field_pairs": 154,    # k_dipole_field_cg (CG matrix-vector product)
                  "fixed_field_pairs": 472}     # k_fixed_field<float>
 # DRAM bytes per launch (read + write) from one ncu capture of each kernel on the
-# 24,000-atom box with caches left warm (--cache-control none), summarised under
-# profiles/; ncu is not run by this script.
-DRAM_BYTES_PER_LAUNCH = {"pair_kernel": 29.42e6 + 0.39e6, "dipole_field_pairs": 32.86e6}
-DRAM_BYTES_SOURCE = "cold-cache ncu capture (profiles/k_dipole_field_packed_water24k_mutual.md)"
+# 24,000-atom box with the caches as the evaluation leaves them (--cache-control none),
+# summarised under profiles/; ncu is not run by this script.
+DRAM_BYTES_PER_LAUNCH = {"pair_kernel": 59.1e3 + 88.6e3, "dipole_field_pairs": 59.4e3 + 139.3e3}
+DRAM_BYTES_SOURCE = ("ncu capture with warm caches (profiles/k_dipole_field_cg_water24k_mutual.md, "
+                     "profiles/k_electrostatics_water24k_mutual.md)")
 KERNEL_NAMES = {"pair_kernel": "k_electrostatics<float, mutual> (energy/force/torque pair kernel)",
                 "dipole_field_pairs": "k_dipole_field_cg (FP32 T.mu pair kernel of the CG solver)",
                 "fixed_field_pairs": "k_fixed_field<float> (permanent-field pair kernel)"}
