@@ -442,13 +442,16 @@ def run_evaluations(args, world, rank, local):
     hpos = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     hpos[:] = pos
     hforce = torch.zeros((n, 3), dtype=torch.float64, pin_memory=True).numpy()
-    for _ in range(2):
+    for _ in range(args.warmup):
         mixed.ctx.evaluate(hpos, box, forces=hforce)
     torch.cuda.synchronize()
+    e2e_calls = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
         hforce[:] = 0.0
+        t1 = time.perf_counter()
         mixed.ctx.evaluate(hpos, box, forces=hforce)
+        e2e_calls.append(1e3 * (time.perf_counter() - t1))
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
     e2e_ms = max_over_ranks(e2e_ms, world)
     if rank != 0:
@@ -506,16 +509,19 @@ def run_evaluations(args, world, rank, local):
     extra["serial_stages"] = {k: v for k, v in serial.items() if k != "stages"}
     extra["cufft_ms_per_step"] = serial["stages"].get("cufft")
 
-    # roofline of the dominant kernel: the pair kernel with the largest device time in the
-    # timed region; per launch = FLOP/pair x pairs within the cutoff
+    # roofline of the dominant kernel: the pair kernel with the largest share of the
+    # serial (additive) stage times -- in the replayed graphs a stage's time also counts the
+    # SMs it shares with the side streams; per launch = FLOP/pair x pairs within the cutoff
     npairs = count_pairs_within(pos, box, f.getCutoffDistance())
-    dom = max(FLOP_PER_PAIR, key=lambda k: stage_ms.get(k, 0.0))
+    dom = max(FLOP_PER_PAIR, key=lambda k: serial["stages"].get(k, 0.0))
     nl = max(1, stage_n.get(dom, 0))
     if dom == "dipole_field_pairs" and counts["cg"]:
         # the CG launches pairs once per iteration; the one launched while the host reads
         # the last iteration's convergence flag returns at once and does no pair work
         nl = min(nl, counts["cg"])
     pair_ms = stage_ms.get(dom, 0.0) / nl
+    ncg = max(1, min(stage_n.get("dipole_field_pairs", 0), counts["cg"]))
+    pair_ms_cg = stage_ms.get("dipole_field_pairs", 0.0) / ncg
     achieved = FLOP_PER_PAIR[dom] * npairs / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else None
     sn = serial["stages"]
     peaks = {}
@@ -527,7 +533,7 @@ def run_evaluations(args, world, rank, local):
     sms = props.multi_processor_count
     sm_mhz = clk.get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
     fp32_peak = sms * 128 * 2 * sm_mhz * 1e6 / 1e12
-    serial_launches = {"dipole_field_pairs": counts["cg"] / args.steps}
+    serial_launches = {"dipole_field_pairs": counts["cg"] / args.steps, "pair_kernel": 1.0, "fixed_field_pairs": 1.0}
     roofline = {"bound": "fp32", "kernel": KERNEL_NAMES[dom], "achieved": achieved, "peak": fp32_peak,
                 "unit": "TFLOP/s", "frac": (achieved / fp32_peak) if achieved else None,
                 "traffic": DRAM_BYTES_PER_LAUNCH.get(dom) if name == "water24k" else None,
@@ -544,6 +550,19 @@ def run_evaluations(args, world, rank, local):
         alone = sn[dom] / serial_launches[dom]
         roofline["ms_per_launch_serial"] = alone
         roofline["achieved_serial"] = FLOP_PER_PAIR[dom] * npairs / (alone * 1e-3) / 1e12
+    # every pair kernel: per launch in the serial schedule (alone on the GPU) and in the
+    # timed steps, with its algorithmic FLOP rate against the computed FP32 peak
+    pair_kernels = {}
+    for k in FLOP_PER_PAIR:
+        per = serial_launches.get(k)
+        if not per or k not in sn:
+            continue
+        alone = sn[k] / per
+        instep = stage_ms.get(k, 0.0) / max(1, stage_n.get(k, 0)) if k != "dipole_field_pairs" else pair_ms_cg
+        rate = FLOP_PER_PAIR[k] * npairs / (alone * 1e-3) / 1e12 if alone > 0 else None
+        pair_kernels[KERNEL_NAMES[k]] = {"ms_per_launch_serial": alone, "ms_per_launch_in_step": instep,
+                                         "tflops_serial": rate, "frac_serial": rate / fp32_peak if rate else None}
+    roofline["pair_kernels"] = pair_kernels
     nbytes = 3 * n * 8
     line = {
         "metric": METRIC if name == "water24k" else METRIC_288K, "value": value, "unit": "evals/s", "n_gpus": world,
@@ -554,7 +573,9 @@ def run_evaluations(args, world, rank, local):
                    "parallelism": "replicas only", "sms": sms,
                    "launch": "evaluation segments and CG iterations replayed from CUDA graphs on a created stream"},
         "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "evals/s", "h2d_bytes_per_step": 2 * nbytes,
-                "d2h_bytes_per_step": nbytes + 8},
+                "d2h_bytes_per_step": nbytes + 8, "warmup": args.warmup,
+                "ms_per_call": {"median": float(np.median(e2e_calls)), "max": float(np.max(e2e_calls)),
+                                "first": float(e2e_calls[0])}},
         "gpu_launches": counts["launches"],
         "roofline": roofline,
         "cpu_baseline": cpu,

@@ -393,11 +393,12 @@ struct Context {
     DBuf<int> covOff, covJ;
     DBuf<double> covS;
     // sort / tiles
-    DBuf<unsigned long long> keys, keysAlt;
+    DBuf<unsigned> keys, keysAlt;
     DBuf<int> order, orderAlt;          // atom index of each sorted slot
     DBuf<char> cubTemp;
     size_t cubBytes = 0;
     DBuf<double> pos, wpos, center, half;
+    DBuf<float4> centerF, halfF;        // the same in FP32 for the tile-pair tests
     // neighbour lists (tile lists, then per-atom lists; layouts in mpid_kernels.cuh)
     int tcap = 0, cap = 0, chunk = 32, nchunksL = 1, nchunksS = 0;
     DBuf<int> tileCount, tileJ, countL, countS, loL, loS, tmaxL, tmaxS, listMax;
@@ -446,8 +447,8 @@ struct Context {
     DBuf<double> partial, red, sc;
     DBuf<int> iter, done;
     DBuf<unsigned> counters;  // last-block counters of the fused CG reductions
-    DBuf<float> r32, p32, q32, x32, b32;
-    DBuf<double> r64, p64, q64, y64, b64, res64, Efix64;
+    DBuf<float> r32, p32, q32, x32, b32, s32;
+    DBuf<double> r64, p64, q64, y64, b64, res64, Efix64, s64;
     DBuf<float> res32;
     // extrapolated
     DBuf<float> ptMuF, ptEF, ptGF;
@@ -546,6 +547,7 @@ struct Context {
         cub::DeviceRadixSort::SortPairs(nullptr, cubBytes, keys.p, keysAlt.p, order.p, orderAlt.p, n);
         cubTemp.alloc(cubBytes);
         pos.alloc(3 * n); wpos.alloc(3 * n); center.alloc(3 * ntiles); half.alloc(3 * ntiles);
+        centerF.alloc(ntiles); halfF.alloc(ntiles);
         // list capacities from the density (regrown on overflow)
         tileCount.alloc(ntiles); countL.alloc(npad); countS.alloc(npad); loL.alloc(npad); loS.alloc(npad);
         tmaxL.alloc(ntiles); tmaxS.alloc(ntiles);
@@ -596,6 +598,7 @@ struct Context {
             cgR = build_cg_radial(usePme ? s.ewald_alpha : 0.0, Prec<float>::kQuadX, list_cutoff());
             r32.alloc(3 * (size_t) npad); p32.alloc(3 * (size_t) npad); q32.alloc(3 * (size_t) npad);
             x32.alloc(3 * (size_t) npad); b32.alloc(3 * (size_t) npad); res32.alloc(3 * (size_t) npad);
+            s32.alloc(3 * (size_t) npad);
             if (nPT) { ptMuF.alloc((size_t) nPT * 3 * npad); ptEF.alloc((size_t) nPT * 3 * npad); ptGF.alloc((size_t) nPT * 6 * npad); }
             if (s.polarization_type == MPID_MUTUAL) {
                 ed.reset(new Engine<double>());  // FP64 residual of the refinement loop
@@ -618,6 +621,7 @@ struct Context {
         if (s.polarization_type == MPID_MUTUAL) {
             r64.alloc(3 * (size_t) npad); p64.alloc(3 * (size_t) npad); q64.alloc(3 * (size_t) npad);
             y64.alloc(3 * (size_t) npad); b64.alloc(3 * (size_t) npad); res64.alloc(3 * (size_t) npad);
+            s64.alloc(3 * (size_t) npad);
             Efix64.alloc(3 * (size_t) npad);
         }
         if (usePme) {
@@ -924,15 +928,20 @@ struct Context {
             const double edge = std::cbrt(32.0 * vol / n);
             const int ncx = std::max(1, (int) std::lround(box.L[0] / edge));
             const int ncy = std::max(1, (int) std::lround(box.L[1] / edge));
-            launch(k_sort_keys, nblk(n, 256), 256, 0, st, n, pos.p, box, ncx, ncy, keys.p, orderAlt.p, wpos.p);
+            // key bits: the column index, then up to 16 bits of z (a quantum of L_z / 65536)
+            int colBits = 1;
+            while (colBits < 28 && (1LL << colBits) < (long long) ncx * ncy) ++colBits;
+            const int zBits = std::min(16, 32 - colBits);
+            launch(k_sort_keys, nblk(n, 256), 256, 0, st, n, pos.p, box, ncx, ncy, zBits, keys.p, orderAlt.p, wpos.p);
             ++t_library_calls;
             CUDA_CHECK(cub::DeviceRadixSort::SortPairs(cubTemp.p, cubBytes, keys.p, keysAlt.p, orderAlt.p, order.p, n, 0,
-                                                        64, st));
+                                                        colBits + zBits, st));
         } else {
             // No periodic box: keep the caller's order (all pairs interact).
             launch(k_identity_order, nblk(n, 256), 256, 0, st, n, (const double*) pos.p, order.p, wpos.p);
         }
-        launch(k_tile_bounds, nblk(ntiles, 128), 128, 0, st, n, ntiles, order.p, wpos.p, center.p, half.p);
+        launch(k_tile_bounds, nblk((long long) ntiles * 32, 128), 128, 0, st, n, ntiles, order.p, wpos.p, center.p,
+               half.p, centerF.p, halfF.p);
     }
 
     double list_cutoff() const { return usePme ? set.cutoff * (1.0 + 1e-6) + 1e-5 : 1e30; }
@@ -947,10 +956,10 @@ struct Context {
         // erfc / quadrature segment boundary: alpha r = kQuadX
         const float quadR2 = usePme ? (float) std::pow(Prec<float>::kQuadX / set.ewald_alpha, 2) : 0.f;
         CUDA_CHECK(cudaMemsetAsync(listMax.p, 0, 4 * sizeof(int), st));
-        launch(k_tile_list, nblk((long long) ntiles * 32, 128), 128, 0, st, ntiles, center.p, half.p, box, listCut,
+        launch(k_tile_list, ntiles, 32 * kTileListWarps, 0, st, ntiles, center.p, centerF.p, halfF.p, box, listCut,
                usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, shD.p, shDF.p, listMax.p);
         launch(k_atom_list<real>, ntiles, 32 * kListWarps, 0, st, ntiles, npad, (const real*) e.off.p,
-               (const int*) e.orig.p, box, cut2, quadR2, usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, covOff.p,
+               (const int*) e.orig.p, (const int*) e.rank.p, box, cut2, quadR2, usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, covOff.p,
                covJ.p, covS.p, cap, countL.p, countS.p, loL.p, loS.p, tmaxL.p, tmaxS.p, list.p, listMax.p + 1);
         CUDA_CHECK(cudaMemcpyAsync(hostMax, listMax.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
         if (record) CUDA_CHECK(cudaEventRecord(evLists, st));
@@ -1180,9 +1189,53 @@ struct Context {
 
     // One CG iteration: q = B p = p - S T S p, p.q, then the update and the scalars
     // (PCG: p from z = P r).  Launches only.
+    // The direction vector s of the single-reduction CG (one per precision).
+    template <typename real>
+    real* cg_s_vector() { return sizeof(real) == 4 ? (real*) (void*) s32.p : (real*) (void*) s64.p; }
+
+    // One single-reduction CG iteration (k_cgcg_* kernels): w = B r (real space beside the
+    // reciprocal chain on the side stream, then the self term), delta and alpha, then the
+    // update of p, s, x and r with gamma', beta' and the convergence test.  q holds w.
+    template <typename real, typename xreal>
+    void cgcg_iteration(Engine<real>& e, xreal* x, real* r, real* p, real* q, double target, int maxIter) {
+        cudaStream_t st = stream;
+        const int nb = nblk(npad, 256);
+        const bool packed = sizeof(real) == 4;  // FP32: packed-operand pair kernel
+        if (usePme) {
+            fork_pme();
+            cudaStream_t ps = pmeStream;
+            timer.begin(ST_PME, ps);
+            e.pme.template spread<4>(n, npad, box, e.mfd.p, done.p, ps);
+            convolve(e, done.p, ps);
+            e.pme.template gather<4>(n, npad, box, e.phiT.p, done.p, ps);
+            timer.end(ps);
+        }
+        timer.begin(ST_DIPOLE_REAL, st);
+        if (packed)
+            launch(k_dipole_field_cg, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), cgR, (const float4*) pack0.p,
+                   (const float4*) pack1.p, npad, (const int*) e.orig.p, e.fieldFx.p, (const int*) done.p);
+        else
+            launch(k_dipole_field<real, false, sizeof(real) == 8>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(),
+                   e.arrays(), (const real*) e.sp.p, e.fieldFx.p, (unsigned long long*) nullptr, (const int*) done.p);
+        timer.end(st);
+        if (usePme) join_pme();
+        launch(k_cgcg_finish<real>, nb, 256, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
+               usePme ? (const real*) e.phiT.p : (const real*) nullptr, (const real*) e.sroot.p, (const real*) r,
+               (const real*) e.sp.p, q, partial.p, counters.p, sc.p, (const int*) iter.p, (const int*) done.p);
+        launch(k_cgcg_update<real, xreal>, nb, 256, 0, st, n, npad, box, (const real*) e.sroot.p, sc.p, (const real*) q, p,
+               cg_s_vector<real>(), x, r, e.sp.p, usePme ? e.mfd.p : (real*) nullptr,
+               (const typename Vec4<real>::type*) e.prm.p, packed ? (typename Vec4<real>::type*) pack1.p : nullptr,
+               partial.p, counters.p, target, iter.p, maxIter, done.p);
+        CUDA_CHECK(cudaGetLastError());
+    }
+
     template <typename real, typename xreal>
     void cg_iteration(Engine<real>& e, xreal* x, real* r, real* p, real* q, double target, int maxIter, bool first) {
         const bool pcg = (set.flags & MPID_FLAG_NEAR_FIELD_PCG) != 0;
+        if (!pcg) {
+            cgcg_iteration(e, x, r, p, q, target, maxIter);
+            return;
+        }
         cg_matvec(e, pcg ? (const real*) e.zc.p : (const real*) r, p, q, first);
         launch(k_cg_update_scalars<real, xreal>, nblk(npad, 256), 256, 0, stream, n, npad, e.sroot.p, sc.p, p, q, x, r,
                partial.p, counters.p + 1, target, iter.p, maxIter, done.p, pcg ? 1 : 0);
@@ -1198,6 +1251,18 @@ struct Context {
     void cg_begin(Engine<real>& e, const real* b, xreal* x, real* r, real* p, real* q, double target, int maxIter) {
         cudaStream_t st = stream;
         const int nb = nblk(npad, 256);
+        if (!(set.flags & MPID_FLAG_NEAR_FIELD_PCG)) {
+            // single-reduction CG: r = b, x = p = s = 0, gamma, the test and the operator input
+            const bool packed = sizeof(real) == 4;
+            launch(k_cgcg_start<real, xreal>, nb, 256, 0, st, n, npad, box, (const real*) e.sroot.p, b, x, r, p,
+                   cg_s_vector<real>(), e.sp.p, usePme ? e.mfd.p : (real*) nullptr, (const typename Vec4<real>::type*) e.prm.p,
+                   packed ? (typename Vec4<real>::type*) pack1.p : nullptr, partial.p, counters.p, sc.p, target, iter.p,
+                   done.p);
+            CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));  // cleared again by each finish
+            CUDA_CHECK(cudaGetLastError());
+            if (graph_mode() && maxIter > 1) cg_iteration(e, x, r, p, q, target, maxIter, true);
+            return;
+        }
         launch(k_cg_start<real, xreal>, nb, 256, 0, st, npad, e.sroot.p, b, x, r, p, partial.p, nb);
         launch(k_reduce_partials, 1, 1024, 0, st, nb, 2, partial.p, red.p, nullptr);
         launch(k_cg_init_scalars, 1, 1, 0, st, sc.p, red.p, n, target, iter.p, done.p);
@@ -1561,11 +1626,20 @@ struct Context {
     template <typename real>
     void finish(Engine<real>& e, real* ptMu, real* ptE, real* ptG) {
         cudaStream_t st = stream;
+        CUDA_CHECK(cudaMemsetAsync(forceFx.p, 0, 3 * (size_t) npad * 8, st));
+        CUDA_CHECK(cudaMemsetAsync(torqueFx.p, 0, 3 * (size_t) npad * 8, st));
+        const NbrList tc = field_list();
+        const int eb = pair_tasks() * tc.split;
+        if ((size_t) eb > energyBlocks.n) throw Error(MPID_ERR_CUDA, "energy partials too small");
+        CUDA_CHECK(cudaMemsetAsync(energyBlocks.p, 0, eb * sizeof(double), st));
+        // The per-atom reciprocal/self terms and the FP64 energies of the covalently scaled
+        // pairs run on the side stream after the reciprocal potential of the final induced
+        // dipoles, beside the energy/force pair kernel on the main stream; both add into
+        // the same fixed-point force and torque accumulators (integer atomics: the sums do
+        // not depend on the order).
+        fork_pme();
+        cudaStream_t ps = pmeStream;
         if (usePme) {
-            // reciprocal potential of the final induced dipoles (35 terms), on the side
-            // stream while the energy/force pair kernel runs
-            fork_pme();
-            cudaStream_t ps = pmeStream;
             timer.begin(ST_PME, ps);
             launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, ps, npad, box, e.mu.p, e.mfd.p, nullptr);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, nullptr, ps);
@@ -1573,27 +1647,7 @@ struct Context {
             e.pme.template gather<35>(n, npad, box, e.phiD.p, nullptr, ps);
             timer.end(ps);
         }
-        CUDA_CHECK(cudaMemsetAsync(forceFx.p, 0, 3 * (size_t) npad * 8, st));
-        CUDA_CHECK(cudaMemsetAsync(torqueFx.p, 0, 3 * (size_t) npad * 8, st));
-        const NbrList tc = field_list();
-        const int eb = pair_tasks() * tc.split;
-        if ((size_t) eb > energyBlocks.n) throw Error(MPID_ERR_CUDA, "energy partials too small");
-        CUDA_CHECK(cudaMemsetAsync(energyBlocks.p, 0, eb * sizeof(double), st));
-        timer.begin(ST_PAIR, st);
-        const bool exact = (set.flags & MPID_FLAG_EXACT_ANISO_TORQUE) != 0;
-        const AtomArrays<real> aa = e.arrays();
-        if (set.polarization_type == MPID_MUTUAL && !exact)
-            launch(k_electrostatics<real, true, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
-                                                                                             torqueFx.p, energyBlocks.p);
-        else if (set.polarization_type == MPID_MUTUAL)
-            launch(k_electrostatics<real, true, false, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
-                                                                                              torqueFx.p, energyBlocks.p);
-        else
-            launch(k_electrostatics<real, false, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
-                                                                                              torqueFx.p, energyBlocks.p);
-        timer.end(st);
-        if (usePme) join_pme();
-        timer.begin(ST_FINISH, st);
+        timer.begin(ST_FINISH, ps);
         OptArgs opt{};
         if (set.polarization_type == MPID_EXTRAPOLATED) {
             opt.nPT = set.n_extrap;
@@ -1608,28 +1662,42 @@ struct Context {
         // per-atom work is long: blocks small enough that a small system spans the SMs
         const int rb = npad >= 256 * 2 * numSMs ? 256 : (npad >= 128 * numSMs ? 128 : (npad >= 64 * numSMs ? 64 : 32));
         const int nb = nblk(npad, rb);
-        launch(k_recip_self<real>, nb, rb, 0, st, n, npad, box, set.ewald_alpha, set.polarization_type,
-                                                usePme ? e.phiP.p : nullptr, e.phiD.p, e.mu.p, e.arrays(), mom64.p, opt,
-                                                forceFx.p, torqueFx.p, energyPartial.p);
-        launch(k_reduce_partials, 1, 1024, 0, st, nb, 1, energyPartial.p, energyOut.p, nullptr);
-        launch(k_reduce_partials, 1, 1024, 0, st, eb, 1, energyBlocks.p, energyOut.p + 1, nullptr);
+        launch(k_recip_self<real>, nb, rb, 0, ps, n, npad, box, set.ewald_alpha, set.polarization_type,
+               usePme ? e.phiP.p : nullptr, e.phiD.p, e.mu.p, e.arrays(), mom64.p, opt, forceFx.p, torqueFx.p,
+               energyPartial.p);
+        launch(k_reduce_partials, 1, 1024, 0, ps, nb, 1, energyPartial.p, energyOut.p, nullptr);
         if (nScaled) {
             const int sb = nblk(nScaled, 128);
             const int muIsFloat = sizeof(real) == 4 ? 1 : 0;
             if (set.polarization_type == MPID_MUTUAL)
-                launch(k_scaled_pair_energy<true>, sb, 128, 0, st, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad, mom64.p,
-                                                               prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0,
-                                                               set.cutoff, usePme ? set.ewald_alpha : 0.0,
-                                                               set.default_thole, scaledPartial.p);
+                launch(k_scaled_pair_energy<true>, sb, 128, 0, ps, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad,
+                       mom64.p, prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0, set.cutoff,
+                       usePme ? set.ewald_alpha : 0.0, set.default_thole, scaledPartial.p);
             else
-                launch(k_scaled_pair_energy<false>, sb, 128, 0, st, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad, mom64.p,
-                                                                prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0,
-                                                                set.cutoff, usePme ? set.ewald_alpha : 0.0,
-                                                                set.default_thole, scaledPartial.p);
-            launch(k_reduce_partials, 1, 1024, 0, st, sb, 1, scaledPartial.p, energyOut.p + 2, nullptr);
+                launch(k_scaled_pair_energy<false>, sb, 128, 0, ps, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad,
+                       mom64.p, prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0, set.cutoff,
+                       usePme ? set.ewald_alpha : 0.0, set.default_thole, scaledPartial.p);
+            launch(k_reduce_partials, 1, 1024, 0, ps, sb, 1, scaledPartial.p, energyOut.p + 2, nullptr);
         } else {
-            CUDA_CHECK(cudaMemsetAsync(energyOut.p + 2, 0, sizeof(double), st));
+            CUDA_CHECK(cudaMemsetAsync(energyOut.p + 2, 0, sizeof(double), ps));
         }
+        timer.end(ps);
+        timer.begin(ST_PAIR, st);
+        const bool exact = (set.flags & MPID_FLAG_EXACT_ANISO_TORQUE) != 0;
+        const AtomArrays<real> aa = e.arrays();
+        if (set.polarization_type == MPID_MUTUAL && !exact)
+            launch(k_electrostatics<real, true, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+                                                                                             torqueFx.p, energyBlocks.p);
+        else if (set.polarization_type == MPID_MUTUAL)
+            launch(k_electrostatics<real, true, false, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+                                                                                              torqueFx.p, energyBlocks.p);
+        else
+            launch(k_electrostatics<real, false, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+                                                                                              torqueFx.p, energyBlocks.p);
+        timer.end(st);
+        join_pme();
+        timer.begin(ST_FINISH, st);
+        launch(k_reduce_partials, 1, 1024, 0, st, eb, 1, energyBlocks.p, energyOut.p + 1, nullptr);
         launch(k_torque_map, nblk(n, 128), 128, 0, st, n, npad, pos.p, mol(), e.rank.p, torqueFx.p, forceFx.p);
         timer.end(st);
         CUDA_CHECK(cudaGetLastError());

@@ -74,10 +74,12 @@ __host__ __device__ __forceinline__ void min_image(real* d, const real* V, const
 // Spatial sort into near-cubic 32-atom tiles: the box is cut into x-y columns about
 // (32 / density)^(1/3) wide, columns are visited in a snake order, and atoms are sorted
 // along z inside each column (ascending in even, descending in odd columns so that a
-// tile running past the end of a column continues next to it).  Key: column index in
-// the high word, quantised z in the low word; the value is the atom index.
-__global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, int ncx, int ncy,
-                            unsigned long long* __restrict__ keys, int* __restrict__ vals, double* __restrict__ wpos) {
+// tile running past the end of a column continues next to it).  Key: column index above
+// zBits bits of quantised z (the radix sort then runs over the bits in use only); the
+// value is the atom index.  Atoms of one column closer in z than the quantum keep their
+// input order (the sort is stable).
+__global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, int ncx, int ncy, int zBits,
+                            unsigned* __restrict__ keys, int* __restrict__ vals, double* __restrict__ wpos) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double w[3], x[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
@@ -96,8 +98,8 @@ __global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, i
     if (cx & 1) cy = ncy - 1 - cy;  // snake through the columns
     const unsigned int col = (unsigned int) (cx * ncy + cy);
     double zf = (col & 1) ? 1.0 - w[2] : w[2];
-    unsigned int zq = (unsigned int) fmin(4294967295.0, zf * 4294967296.0);
-    keys[i] = ((unsigned long long) col << 32) | zq;
+    const unsigned int zq = (unsigned int) fmin(4294967295.0, zf * 4294967296.0);
+    keys[i] = (col << zBits) | (zq >> (32 - zBits));
     vals[i] = i;
 }
 
@@ -110,24 +112,37 @@ __global__ void k_identity_order(int n, const double* __restrict__ pos, int* __r
     for (int k = 0; k < 3; ++k) wpos[3 * i + k] = pos[3 * i + k];
 }
 
-// Tile centres and half extents from the wrapped positions of the sorted atoms.
+// Tile centres and half extents from the wrapped positions of the sorted atoms: one warp
+// per tile, one lane per atom, minima and maxima by shuffles.
 __global__ void k_tile_bounds(int n, int ntiles, const int* __restrict__ order,
                               const double* __restrict__ wpos, double* __restrict__ center,
-                              double* __restrict__ half) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntiles) return;
+                              double* __restrict__ half, float4* __restrict__ centerF, float4* __restrict__ halfF) {
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (t >= ntiles) return;  // whole warps
+    const int s = t * 32 + lane;
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int s = t * 32; s < min(n, t * 32 + 32); ++s) {
-        int i = order[s];
-        for (int k = 0; k < 3; ++k) {
-            double x = wpos[3 * i + k];
-            lo[k] = fmin(lo[k], x);
-            hi[k] = fmax(hi[k], x);
-        }
+    if (s < n) {
+        const int i = order[s];
+        for (int k = 0; k < 3; ++k) lo[k] = hi[k] = wpos[3 * i + k];
     }
-    for (int k = 0; k < 3; ++k) {
-        center[3 * t + k] = 0.5 * (lo[k] + hi[k]);
-        half[3 * t + k] = 0.5 * (hi[k] - lo[k]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fmin(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmax(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    if (lane < 3) {
+        const double l = lane == 0 ? lo[0] : (lane == 1 ? lo[1] : lo[2]);
+        const double h = lane == 0 ? hi[0] : (lane == 1 ? hi[1] : hi[2]);
+        center[3 * t + lane] = 0.5 * (l + h);
+        half[3 * t + lane] = 0.5 * (h - l);
+    }
+    if (lane == 0) {
+        centerF[t] = make_float4((float) (0.5 * (lo[0] + hi[0])), (float) (0.5 * (lo[1] + hi[1])),
+                                 (float) (0.5 * (lo[2] + hi[2])), 0.f);
+        halfF[t] = make_float4((float) (0.5 * (hi[0] - lo[0])), (float) (0.5 * (hi[1] - lo[1])),
+                               (float) (0.5 * (hi[2] - lo[2])), 0.f);
     }
 }
 
@@ -146,87 +161,113 @@ __global__ void k_tile_bounds(int n, int ntiles, const int* __restrict__ order,
 // ascending order and jlane ascending, so the lists and all sums over them are
 // reproducible.
 
-// One warp per tile I scans all tiles J.  A dimension whose extents plus the cutoff reach
-// half the box always counts as overlapping and marks the pair for per-pair imaging.
-__global__ void k_tile_list(int ntiles, const double* __restrict__ center, const double* __restrict__ half, BoxDev box,
-                            double cutoff, int usePbc, int tcap, int* __restrict__ tileCount, int* __restrict__ tileJ,
-                            float4* __restrict__ shF, double* __restrict__ shD, float2* __restrict__ shDF,
-                            int* __restrict__ maxTiles) {
-    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (I >= ntiles) return;
-    const float cI[3] = {(float) center[3 * I], (float) center[3 * I + 1], (float) center[3 * I + 2]};
-    const float hI[3] = {(float) half[3 * I], (float) half[3 * I + 1], (float) half[3 * I + 2]};
-    int base = 0;
-    for (int J0 = 0; J0 < ntiles; J0 += 32) {
-        const int J = J0 + lane;
-        bool hit = false, wrap = false;
-        double sh[3] = {0.0, 0.0, 0.0};
-        if (J < ntiles && usePbc && box.tri) {
-            // triclinic: the bounding boxes are tested at every lattice image next to the
-            // minimum image of the centres, and every hit is imaged pair by pair
-            const float cut = (float) cutoff * 1.0001f + 1e-4f;
-            float Vf[9], iLf[3];
-            for (int q = 0; q < 9; ++q) Vf[q] = (float) box.V[q];
-            for (int q = 0; q < 3; ++q) iLf[q] = (float) box.invL[q];
-            float dc[3], ext[3];
-            for (int k = 0; k < 3; ++k) {
-                dc[k] = (float) center[3 * J + k] - cI[k];
-                ext[k] = hI[k] + (float) half[3 * J + k];
-            }
-            min_image(dc, Vf, iLf);
-            float best = 3.0e38f;
-            for (int ia = -1; ia <= 1; ++ia)
-                for (int ib = -1; ib <= 1; ++ib)
-                    for (int ic = -1; ic <= 1; ++ic) {
-                        const float v[3] = {dc[0] + ia * Vf[0] + ib * Vf[3] + ic * Vf[6], dc[1] + ib * Vf[4] + ic * Vf[7],
-                                            dc[2] + ic * Vf[8]};
-                        float d2 = 0.f;
-                        for (int k = 0; k < 3; ++k) {
-                            const float g = fabsf(v[k]) - ext[k];
-                            if (g > 0.f) d2 += g * g;
-                        }
-                        best = fminf(best, d2);
-                    }
-            hit = best < cut * cut;
-            wrap = true;
-            if (hit) {
-                for (int k = 0; k < 3; ++k) sh[k] = center[3 * J + k] - center[3 * I + k];
-                min_image(sh, box.V, box.invL);
-            }
-        } else if (J < ntiles) {
-            // bounding-box test in float with a margin far above its rounding
-            const float cut = (float) cutoff * 1.0001f + 1e-4f;
-            float d2 = 0.f;
-            for (int k = 0; k < 3; ++k) {
-                const float Lk = (float) box.L[k];
-                float dc = cI[k] - (float) center[3 * J + k];
-                dc = -dc;
-                const float ext = hI[k] + (float) half[3 * J + k];
-                bool always = false;
-                if (usePbc) {
-                    always = ext + cut >= 0.5f * Lk;
-                    wrap = wrap || always;
-                    dc -= Lk * rintf(dc * (float) box.invL[k]);
-                }
-                const float g = fabsf(dc) - ext;
-                if (!always && g > 0.f) d2 += g * g;
-            }
-            hit = d2 < cut * cut;
-            if (hit)  // minimum-image shift of the centres in FP64
-                for (int k = 0; k < 3; ++k) {
-                    double dc = center[3 * J + k] - center[3 * I + k];
-                    if (usePbc) dc -= box.L[k] * rint(dc * box.invL[k]);
-                    sh[k] = dc;
-                }
+// Bounding-box test of tiles I and J.  A dimension whose extents plus the cutoff reach
+// half the box always counts as overlapping and marks the pair for per-pair imaging
+// (`wrap`); in a triclinic box the boxes are tested at every lattice image next to the
+// minimum image of the centres, and every hit is imaged pair by pair.
+__device__ __forceinline__ bool tile_pair_hit(int J, const float* cI, const float* hI,
+                                              const float4* __restrict__ centerF, const float4* __restrict__ halfF,
+                                              const BoxDev& box, double cutoff, int usePbc, bool& wrap) {
+    const float4 cJ = centerF[J], hJ = halfF[J];
+    const float cJv[3] = {cJ.x, cJ.y, cJ.z}, hJv[3] = {hJ.x, hJ.y, hJ.z};
+    const float cut = (float) cutoff * 1.0001f + 1e-4f;  // margin far above the float rounding
+    wrap = false;
+    if (usePbc && box.tri) {
+        float Vf[9], iLf[3];
+        for (int q = 0; q < 9; ++q) Vf[q] = (float) box.V[q];
+        for (int q = 0; q < 3; ++q) iLf[q] = (float) box.invL[q];
+        float dc[3], ext[3];
+        for (int k = 0; k < 3; ++k) {
+            dc[k] = cJv[k] - cI[k];
+            ext[k] = hI[k] + hJv[k];
         }
+        min_image(dc, Vf, iLf);
+        float best = 3.0e38f;
+        for (int ia = -1; ia <= 1; ++ia)
+            for (int ib = -1; ib <= 1; ++ib)
+                for (int ic = -1; ic <= 1; ++ic) {
+                    const float v[3] = {dc[0] + ia * Vf[0] + ib * Vf[3] + ic * Vf[6], dc[1] + ib * Vf[4] + ic * Vf[7],
+                                        dc[2] + ic * Vf[8]};
+                    float d2 = 0.f;
+                    for (int k = 0; k < 3; ++k) {
+                        const float g = fabsf(v[k]) - ext[k];
+                        if (g > 0.f) d2 += g * g;
+                    }
+                    best = fminf(best, d2);
+                }
+        wrap = true;
+        return best < cut * cut;
+    }
+    float d2 = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        const float Lk = (float) box.L[k];
+        float dc = cJv[k] - cI[k];
+        const float ext = hI[k] + hJv[k];
+        bool always = false;
+        if (usePbc) {
+            always = ext + cut >= 0.5f * Lk;
+            wrap = wrap || always;
+            dc -= Lk * rintf(dc * (float) box.invL[k]);
+        }
+        const float g = fabsf(dc) - ext;
+        if (!always && g > 0.f) d2 += g * g;
+    }
+    return d2 < cut * cut;
+}
+
+// One block of kTileListWarps warps per tile I; warp w scans the w-th contiguous range of
+// tiles J.  A first pass counts each warp's hits, a prefix sum over the warps gives their
+// offsets, and a second pass writes the hits in ascending J (an ordered ballot compaction
+// within each warp), so the list order is deterministic.
+constexpr int kTileListWarps = 8;
+
+__global__ void __launch_bounds__(32 * kTileListWarps)
+k_tile_list(int ntiles, const double* __restrict__ center, const float4* __restrict__ centerF,
+            const float4* __restrict__ halfF, BoxDev box, double cutoff, int usePbc, int tcap, int* __restrict__ tileCount, int* __restrict__ tileJ,
+            float4* __restrict__ shF, double* __restrict__ shD, float2* __restrict__ shDF,
+            int* __restrict__ maxTiles) {
+    __shared__ int wcount[kTileListWarps];
+    const int I = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (I >= ntiles) return;  // whole blocks
+    const float4 cI4 = centerF[I], hI4 = halfF[I];
+    const float cI[3] = {cI4.x, cI4.y, cI4.z}, hI[3] = {hI4.x, hI4.y, hI4.z};
+    const int span = (ntiles + kTileListWarps - 1) / kTileListWarps;
+    const int j0 = min(ntiles, w * span), j1 = min(ntiles, j0 + span);
+    int count = 0;
+    for (int J0 = j0; J0 < j1; J0 += 32) {
+        const int J = J0 + lane;
+        bool wrap = false;
+        const bool hit = J < j1 && tile_pair_hit(J, cI, hI, centerF, halfF, box, cutoff, usePbc, wrap);
+        count += __popc(__ballot_sync(0xffffffffu, hit));
+    }
+    if (lane == 0) wcount[w] = count;
+    __syncthreads();
+    int base = 0, total = 0;
+    for (int v = 0; v < kTileListWarps; ++v) {
+        if (v < w) base += wcount[v];
+        total += wcount[v];
+    }
+    for (int J0 = j0; J0 < j1; J0 += 32) {
+        const int J = J0 + lane;
+        bool wrap = false;
+        const bool hit = J < j1 && tile_pair_hit(J, cI, hI, centerF, halfF, box, cutoff, usePbc, wrap);
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (hit) {
             const int pos = base + __popc(m & ((1u << lane) - 1u));
             if (pos < tcap) {
+                // minimum-image shift of the centres in FP64
+                double sh[3];
+                for (int k = 0; k < 3; ++k) sh[k] = center[3 * J + k] - center[3 * I + k];
+                if (usePbc) {
+                    if (box.tri)
+                        min_image(sh, box.V, box.invL);
+                    else
+                        for (int k = 0; k < 3; ++k) sh[k] -= box.L[k] * rint(sh[k] * box.invL[k]);
+                }
                 const size_t s = (size_t) I * tcap + pos;
-                tileJ[s] = J | (wrap ? (int) 0x80000000 : 0);
-                shF[s] = make_float4((float) sh[0], (float) sh[1], (float) sh[2],
-                                     __int_as_float(J | (wrap ? (int) 0x80000000 : 0)));
+                const int code = J | (wrap ? (int) 0x80000000 : 0);
+                tileJ[s] = code;
+                shF[s] = make_float4((float) sh[0], (float) sh[1], (float) sh[2], __int_as_float(code));
                 for (int k = 0; k < 3; ++k) {
                     shD[3 * s + k] = sh[k];
                     const dfloat v = df_from_double(sh[k]);
@@ -236,9 +277,9 @@ __global__ void k_tile_list(int ntiles, const double* __restrict__ center, const
         }
         base += __popc(m);
     }
-    if (lane == 0) {
-        tileCount[I] = min(base, tcap);
-        atomicMax(maxTiles, base);
+    if (threadIdx.x == 0) {
+        tileCount[I] = min(total, tcap);
+        atomicMax(maxTiles, total);
     }
 }
 
@@ -369,18 +410,46 @@ __device__ __forceinline__ unsigned scale_flag(double sc) { return sc == 1.0 ? 0
 // are in ascending J order (and ascending j).
 constexpr int kListWarps = 8;
 
+// Covalent partners of an atom as bit masks over the 32 atoms of tile J: m1 the partners
+// of scale 0 (entry flag 1), m2 those of any other scale but 1 (flag 2).  pS holds the
+// sorted slots of the first kCache partners (-1 for none), pF their flags (2 bits each);
+// the partners beyond those are read from covJ.
+template <int kCache>
+__device__ __forceinline__ void partner_masks(int J, const int* pS, unsigned pF, int rest0, int rest1,
+                                              const int* __restrict__ covJ, const double* __restrict__ covS,
+                                              const int* __restrict__ rank, unsigned& m1, unsigned& m2) {
+    m1 = 0u;
+    m2 = 0u;
+#pragma unroll
+    for (int k = 0; k < kCache; ++k)
+        if ((pS[k] >> 5) == J) {
+            const unsigned b = 1u << (pS[k] & 31), f = (pF >> (2 * k)) & 3u;
+            if (f == 1u) m1 |= b;
+            else if (f == 2u) m2 |= b;
+        }
+    for (int k = rest0; k < rest1; ++k) {
+        const int sp = rank[covJ[k]];
+        if ((sp >> 5) == J) {
+            const unsigned f = scale_flag(covS[k]), b = 1u << (sp & 31);
+            if (f == 1u) m1 |= b;
+            else if (f == 2u) m2 |= b;
+        }
+    }
+}
+
 template <typename real>
-__global__ void __launch_bounds__(32 * kListWarps)
-k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __restrict__ orig, BoxDev box,
-            float cutoff2, float quadR2, int usePme, int tcap, const int* __restrict__ tileCount,
-            const int* __restrict__ tileJ, const float4* __restrict__ shF, const int* __restrict__ covOff,
-            const int* __restrict__ covJ, const double* __restrict__ covS, int cap, int* __restrict__ countL,
-            int* __restrict__ countS, int* __restrict__ loL, int* __restrict__ loS, int* __restrict__ tmaxL,
-            int* __restrict__ tmaxS, unsigned* __restrict__ list, int* __restrict__ maxCounts) {
+__global__ void __launch_bounds__(32 * kListWarps, 3)
+k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __restrict__ orig,
+            const int* __restrict__ rank, BoxDev box, float cutoff2, float quadR2, int usePme, int tcap,
+            const int* __restrict__ tileCount, const int* __restrict__ tileJ, const float4* __restrict__ shF,
+            const int* __restrict__ covOff, const int* __restrict__ covJ, const double* __restrict__ covS, int cap,
+            int* __restrict__ countL, int* __restrict__ countS, int* __restrict__ loL, int* __restrict__ loS,
+            int* __restrict__ tmaxL, int* __restrict__ tmaxS, unsigned* __restrict__ list, int* __restrict__ maxCounts) {
     constexpr int kCache = 8;
     constexpr int kMasks = 16;  // tile pairs per warp whose hits the first pass keeps for the second
     __shared__ int cnt[kListWarps][4][32];  // nL, nS, lowL, lowS per warp and lane
     __shared__ unsigned hits[kListWarps][kMasks][32], near[kListWarps][kMasks][32];
+    __shared__ float4 jat[kListWarps][32];  // the current J tile: offset and original index of each atom
     const int I = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (I >= ntiles) return;
     const int si = I * 32 + lane;
@@ -389,17 +458,18 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
     const float iL[3] = {(float) box.invL[0], (float) box.invL[1], (float) box.invL[2]};
     float Vb[9];
     for (int q = 0; q < 9; ++q) Vb[q] = (float) box.V[q];
-    // covalent partners of this atom: the first kCache in registers
+    // covalent partners of this atom by sorted slot: the first kCache in registers
     int cb = 0, ce = 0;
     if (origI >= 0) { cb = covOff[origI]; ce = covOff[origI + 1]; }
     const int ncached = min(ce - cb, kCache);
-    int pJ[kCache];
-    unsigned pF[kCache];
+    int pS[kCache];
+    unsigned pF = 0u;
 #pragma unroll
     for (int k = 0; k < kCache; ++k) {
-        pJ[k] = k < ncached ? covJ[cb + k] : -1;
-        pF[k] = k < ncached ? scale_flag(covS[cb + k]) : 0u;
+        pS[k] = k < ncached ? rank[covJ[cb + k]] : -1;
+        if (k < ncached) pF |= scale_flag(covS[cb + k]) << (2 * k);
     }
+    const int rest0 = cb + ncached, rest1 = ce;
     const int nt = tileCount[I];
     const int s0 = (w * nt) / kListWarps, s1 = ((w + 1) * nt) / kListWarps;
     unsigned* out = list + (size_t) I * cap * 32 + lane;
@@ -408,26 +478,19 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
     for (int pass = 0; pass < 2; ++pass) {
         int nL = 0, nS = 0, lowL = 0, lowS = 0;
         for (int s = s0; s < s1; ++s) {
+            const int Jw = tileJ[(size_t) I * tcap + s];
+            const int J = Jw & 0x7fffffff;
+            unsigned m1, m2;
+            partner_masks<kCache>(J, pS, pF, rest0, rest1, covJ, covS, rank, m1, m2);
             if (pass == 1 && s - s0 < kMasks) {
                 // second pass over a kept tile pair: only its hits, in the same order
                 if (!fits) continue;
-                const int J = tileJ[(size_t) I * tcap + s] & 0x7fffffff;
                 unsigned m = hits[w][s - s0][lane];
                 const unsigned q = near[w][s - s0][lane];
                 while (m) {
                     const int jl = __ffs(m) - 1;
                     m &= m - 1;
-                    const int oj = orig[J * 32 + jl];
-                    unsigned flag = 0;
-#pragma unroll
-                    for (int k = 0; k < kCache; ++k)
-                        if (pJ[k] == oj) flag = pF[k];
-                    if (ce - cb > kCache)
-                        for (int k = cb + kCache; k < ce; ++k)
-                            if (covJ[k] == oj) {
-                                flag = scale_flag(covS[k]);
-                                break;
-                            }
+                    const unsigned flag = ((m1 >> jl) & 1u) ? 1u : (((m2 >> jl) & 1u) ? 2u : 0u);
                     const bool quad = usePme && (((q >> jl) & 1u) || flag == 1u);
                     const unsigned code = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
                     out[(size_t) (quad ? cap - 1 - (baseS + nS) : baseL + nL) * 32] = code;
@@ -436,31 +499,21 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
                 continue;
             }
             unsigned hitMask = 0, nearMask = 0;
-            const int Jw = tileJ[(size_t) I * tcap + s];
-            const int J = Jw & 0x7fffffff;
             const bool wrap = Jw < 0;
             const float4 sh = shF[(size_t) I * tcap + s];
             const int sj = J * 32 + lane;
-            const float oj0 = (float) off[sj], oj1 = (float) off[npad + sj], oj2 = (float) off[2 * npad + sj];
-            const int origJl = orig[sj];
+            __syncwarp();
+            jat[w][lane] = make_float4((float) off[sj], (float) off[npad + sj], (float) off[2 * npad + sj],
+                                       __int_as_float(orig[sj]));
+            __syncwarp();
             for (int jl = 0; jl < 32; ++jl) {
-                float d[3] = {sh.x + (__shfl_sync(0xffffffffu, oj0, jl) - oi[0]),
-                              sh.y + (__shfl_sync(0xffffffffu, oj1, jl) - oi[1]),
-                              sh.z + (__shfl_sync(0xffffffffu, oj2, jl) - oi[2])};
-                const int oj = __shfl_sync(0xffffffffu, origJl, jl);
+                const float4 aj = jat[w][jl];
+                float d[3] = {sh.x + (aj.x - oi[0]), sh.y + (aj.y - oi[1]), sh.z + (aj.z - oi[2])};
+                const int oj = __float_as_int(aj.w);
                 if (wrap) min_image(d, Vb, iL);
                 const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
                 if (origI < 0 || oj < 0 || r2 >= cutoff2 || (J == I && jl == lane)) continue;
-                unsigned flag = 0;
-#pragma unroll
-                for (int k = 0; k < kCache; ++k)
-                    if (pJ[k] == oj) flag = pF[k];
-                if (ce - cb > kCache)
-                    for (int k = cb + kCache; k < ce; ++k)
-                        if (covJ[k] == oj) {
-                            flag = scale_flag(covS[k]);
-                            break;
-                        }
+                const unsigned flag = ((m1 >> jl) & 1u) ? 1u : (((m2 >> jl) & 1u) ? 2u : 0u);
                 const bool quad = usePme && (r2 < quadR2 || flag == 1u);
                 if (pass == 1 && fits) {
                     const unsigned code = ((unsigned) s << 7) | (flag << 5) | (unsigned) jl;
@@ -2309,6 +2362,183 @@ k_cg_update_scalars(int n, int npad, const real* __restrict__ S, double* __restr
                 sc[0] = rrNew;
             }
             sc[6] = 48.033324 * sqrt(srNew / n);
+            *iter += 1;
+            if (sc[6] < target || *iter >= maxIter || !(sc[6] == sc[6])) *done = 1;
+            *counter = 0u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Single-reduction CG (Chronopoulos and Gear) on B y = b, B = I - S T S: each iteration
+// makes one operator application w = B r and one global reduction per kernel,
+//   p = r + beta p, s = w + beta s, x += alpha p, r -= alpha s          (update)
+//   gamma' = r.r, beta' = gamma' / gamma                               (update)
+//   w' = B r', delta' = w'.r', alpha' = gamma' / (delta' - beta' gamma' / alpha)   (finish)
+// which is CG in exact arithmetic: the same iterates with two small kernels per
+// iteration instead of three.  sc: 0 gamma, 1 delta, 3 |S r|^2, 4 alpha, 5 beta,
+// 6 metric 48.033324 sqrt(|S r|^2 / n) (MPIDReferenceForce.cpp:1219).
+
+// The operator input of an iteration from r: sp = S r, its fractional dipoles for the
+// reciprocal-space spread and (FP32) the packed operand A1 = (S r, 1 / damping).
+template <typename real>
+__device__ __forceinline__ void cgcg_operator_input(int npad, int s, const BoxDev& box, const real* S, const real* v,
+                                                    real* sp, real* mfd, const typename Vec4<real>::type* prm,
+                                                    typename Vec4<real>::type* A1) {
+    real o[3];
+    sym_mul(S, npad, s, v, o);
+    for (int c = 0; c < 3; ++c) sp[c * npad + s] = o[c];
+    if (A1) A1[s] = Vec4<real>::make(o[0], o[1], o[2], prm[s].w);
+    if (mfd) {
+        mfd[s] = real(0);
+        for (int j = 0; j < 3; ++j)
+            mfd[(1 + j) * npad + s] = real(box.A[j][0]) * o[0] + real(box.A[j][1]) * o[1] + real(box.A[j][2]) * o[2];
+    }
+}
+
+// r = b, x = p = s = 0; gamma, the metric of r and the operator input of r.
+template <typename real, typename xreal>
+__global__ void __launch_bounds__(256)
+k_cgcg_start(int n, int npad, BoxDev box, const real* __restrict__ S, const real* __restrict__ b, xreal* __restrict__ x,
+             real* __restrict__ r, real* __restrict__ p, real* __restrict__ sv, real* __restrict__ sp,
+             real* __restrict__ mfd, const typename Vec4<real>::type* __restrict__ prm,
+             typename Vec4<real>::type* __restrict__ A1, double* __restrict__ partial, unsigned* __restrict__ counter,
+             double* __restrict__ sc, double target, int* __restrict__ iter, int* __restrict__ done) {
+    __shared__ double red[256];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, sr = 0.0;
+    if (s < npad) {
+        real v[3];
+        for (int c = 0; c < 3; ++c) {
+            v[c] = b[c * npad + s];
+            x[c * npad + s] = xreal(0);
+            r[c * npad + s] = v[c];
+            p[c * npad + s] = real(0);
+            sv[c * npad + s] = real(0);
+            rr += (double) v[c] * v[c];
+        }
+        real z[3];
+        sym_mul(S, npad, s, v, z);
+        sr = (double) z[0] * z[0] + (double) z[1] * z[1] + (double) z[2] * z[2];
+        cgcg_operator_input(npad, s, box, S, v, sp, mfd, prm, A1);
+    }
+    const double b0 = block_sum_256(rr, red);
+    const double b1 = block_sum_256(sr, red);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = b0;
+        partial[gridDim.x + blockIdx.x] = b1;
+    }
+    if (last_block(counter)) {
+        const double g = sum_partials_256(partial, gridDim.x, red);
+        const double m = sum_partials_256(partial + gridDim.x, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            sc[0] = g;
+            sc[3] = m;
+            sc[4] = 0.0;
+            sc[5] = 0.0;
+            sc[6] = 48.033324 * sqrt(m / n);
+            *iter = 0;
+            *done = (sc[6] < target) ? 1 : 0;
+            *counter = 0u;
+        }
+    }
+}
+
+// w = B r (real space from the fixed-point accumulator, which is cleared here, plus the
+// reciprocal and self terms), delta = w.r, then alpha (first iteration: gamma / delta).
+template <typename real>
+__global__ void __launch_bounds__(256)
+k_cgcg_finish(int n, int npad, BoxDev box, double selfCoef, unsigned long long* __restrict__ fx,
+              const real* __restrict__ phi, const real* __restrict__ S, const real* __restrict__ r,
+              const real* __restrict__ sp, real* __restrict__ w, double* __restrict__ partial,
+              unsigned* __restrict__ counter, double* __restrict__ sc, const int* __restrict__ iter,
+              const int* __restrict__ skip) {
+    __shared__ double red[256];
+    if (*skip) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (s < npad) {
+        real e[3];
+        for (int c = 0; c < 3; ++c) {
+            double v = 0.0;
+            if (s < n) {
+                v = fx_get(fx, c * npad + s) + selfCoef * (double) sp[c * npad + s];
+                if (phi) v -= box.A[0][c] * (double) phi[npad + s] + box.A[1][c] * (double) phi[2 * npad + s] +
+                              box.A[2][c] * (double) phi[3 * npad + s];
+            }
+            fx[c * npad + s] = 0ull;
+            e[c] = real(v);
+        }
+        real se[3];
+        sym_mul(S, npad, s, e, se);
+        for (int c = 0; c < 3; ++c) {
+            const real rv = r[c * npad + s];
+            const real wv = rv - se[c];
+            w[c * npad + s] = wv;
+            acc += (double) wv * (double) rv;
+        }
+    }
+    const double b = block_sum_256(acc, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = b;
+    if (last_block(counter)) {
+        const double delta = sum_partials_256(partial, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            const double g = sc[0], beta = sc[5];
+            sc[1] = delta;
+            sc[4] = *iter == 0 ? g / delta : g / (delta - beta * g / sc[4]);
+            *counter = 0u;
+        }
+    }
+}
+
+// p = r + beta p, s = w + beta s, x += alpha p, r -= alpha s; gamma' and beta', the
+// convergence test and the iteration limit (done = 1 stops the loop: the kernels of the
+// remaining iterations return at once), and the operator input of the new r.
+template <typename real, typename xreal>
+__global__ void __launch_bounds__(256)
+k_cgcg_update(int n, int npad, BoxDev box, const real* __restrict__ S, double* __restrict__ sc,
+              const real* __restrict__ w, real* __restrict__ p, real* __restrict__ sv, xreal* __restrict__ x,
+              real* __restrict__ r, real* __restrict__ sp, real* __restrict__ mfd,
+              const typename Vec4<real>::type* __restrict__ prm, typename Vec4<real>::type* __restrict__ A1,
+              double* __restrict__ partial, unsigned* __restrict__ counter, double target, int* __restrict__ iter,
+              int maxIter, int* __restrict__ done) {
+    __shared__ double red[256];
+    if (*done) return;
+    const double a = sc[4], beta = sc[5];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, sr = 0.0;
+    if (s < npad) {
+        real rv[3];
+        for (int c = 0; c < 3; ++c) {
+            const int k = c * npad + s;
+            const real pv = real((double) r[k] + beta * (double) p[k]);
+            const real svv = real((double) w[k] + beta * (double) sv[k]);
+            p[k] = pv;
+            sv[k] = svv;
+            x[k] += xreal(a * (double) pv);
+            rv[c] = real((double) r[k] - a * (double) svv);
+            r[k] = rv[c];
+            rr += (double) rv[c] * (double) rv[c];
+        }
+        real z[3];
+        sym_mul(S, npad, s, rv, z);
+        sr = (double) z[0] * z[0] + (double) z[1] * z[1] + (double) z[2] * z[2];
+        cgcg_operator_input(npad, s, box, S, rv, sp, mfd, prm, A1);
+    }
+    const double b0 = block_sum_256(rr, red);
+    const double b1 = block_sum_256(sr, red);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = b0;
+        partial[gridDim.x + blockIdx.x] = b1;
+    }
+    if (last_block(counter)) {
+        const double g = sum_partials_256(partial, gridDim.x, red);
+        const double m = sum_partials_256(partial + gridDim.x, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            sc[5] = g / sc[0];
+            sc[0] = g;
+            sc[3] = m;
+            sc[6] = 48.033324 * sqrt(m / n);
             *iter += 1;
             if (sc[6] < target || *iter >= maxIter || !(sc[6] == sc[6])) *done = 1;
             *counter = 0u;

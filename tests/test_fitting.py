@@ -402,3 +402,53 @@ def test_gradients_without_cutoff_match_oracle(pol):
                 helpers.rel_rms(gp[:, 3], ref.polgrad[:, 3]))
         print("nocutoff pol %d %s: multipole %.2e polarisability %.2e thole %.2e" % ((pol, precision) + errs))
         assert max(errs) < tol, (precision, errs)
+
+
+def _sharded_gpu_worker(rank, world, port, nboxes, out):
+    import os
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        systems, _ = fitting.water_batch(nboxes=nboxes, min_waters=128, max_waters=192)
+        sizes = [len(s[1]) for s in systems]
+        mine = fitting.shard_indices(sizes, rank, world)
+        with fitting.BoxBatch([systems[k] for k in mine], 2, precision="double", threads=2) as b:
+            e, _, g = b.evaluate(forces=False)
+        E, G = fitting.allreduce_results(e, mine, nboxes, g)
+        out.put((rank, mine, E.tolist(), G.tolist()))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_sharded_batch_on_gpu_matches_single_process():
+    """The sharded fitting step end to end: two ranks (gloo processes sharing the one GPU;
+    no kernel waits on another rank) each evaluate their shard_indices share of a 6-box
+    batch with a BoxBatch (FP64) and combine with allreduce_results; every rank then holds
+    the energies of all boxes and the per-type gradient of a single-process BoxBatch over
+    all boxes, to 1e-12."""
+    import multiprocessing as mp
+    import socket
+    nboxes = 6
+    ctx = mp.get_context("spawn")
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_sharded_gpu_worker, args=(r, 2, port, nboxes, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    systems, _ = fitting.water_batch(nboxes=nboxes, min_waters=128, max_waters=192)
+    with fitting.BoxBatch(systems, 2, precision="double", threads=2) as b:
+        e_ref, _, g_ref = b.evaluate(forces=False)
+    res = [q.get(timeout=600) for _ in procs]
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    shards = sorted(k for _, mine, _, _ in res for k in mine)
+    assert shards == list(range(nboxes)) and all(len(mine) > 0 for _, mine, _, _ in res)
+    for rank, mine, e, g in res:
+        assert np.allclose(e, e_ref, rtol=1e-12, atol=0), rank
+        assert np.abs(np.asarray(g) - g_ref).max() <= 1e-12 * np.abs(g_ref).max(), rank
