@@ -269,11 +269,16 @@ def run_fitting(args, world, rank, local):
     systems = [all_systems[k] for k in mine]
     out = {}
     grads = {}
-    arms = [("mixed", args.threads)]
+    # arms: (precision, host threads; 0 = one batched launch of all boxes' graphs)
+    main = ("mixed", 0)
+    arms = [main]
     if world == 1:
-        arms = ([("mixed", 1)] if args.threads != 1 else []) + arms + ([] if args.no_fp64 else [("double", args.threads)])
+        arms = arms + [("mixed", args.threads)] + ([] if args.no_fp64 else [("double", 0)])
     for precision, threads in arms:
-        with fitting.BoxBatch(systems, 2, precision=precision, threads=threads, device=local) as b:
+        with fitting.BoxBatch(systems, 2, precision=precision, threads=max(threads, 1), device=local,
+                              batched=threads == 0) as b:
+
+            tuned = b.autotune()  # recorded per GPU; a later run reuses the choice
 
             def step():
                 e, _, g = b.evaluate()
@@ -284,7 +289,7 @@ def run_fitting(args, world, rank, local):
             for _ in range(args.warmup):
                 step()
             torch.cuda.synchronize()
-            steps = args.steps if (precision, threads) == ("mixed", args.threads) else max(3, args.steps // 4)
+            steps = args.steps if (precision, threads) == main else max(3, args.steps // 4)
             with ClockSampler(local) as clocks:
                 barrier(world)
                 torch.cuda.synchronize()
@@ -297,26 +302,30 @@ def run_fitting(args, world, rank, local):
                 clocks.mark("stop")
             # kernel launches of one step: each box's last evaluation and gradient passes
             per_step = sum(c.stats()["kernel_launches"] for c in b.contexts)
-            out["%s_t%d" % (precision, threads)] = {"ms_per_step": dt * 1e3, "steps": steps,
-                                                    "launches_per_step": per_step}
-            if threads == args.threads:
+            label = "%s_%s" % (precision, "batched" if threads == 0 else "t%d" % threads)
+            out[label] = {"ms_per_step": dt * 1e3, "steps": steps, "launches_per_step": per_step,
+                          "launch_config": tuned[0], "autotune_ms": tuned[1]}
+            if threads == 0:
                 grads[precision] = g
                 if precision == "mixed":
                     clock_summary = clocks.summary()
-    ms = max_over_ranks(out["mixed_t%d" % args.threads]["ms_per_step"], world)
+    main_label = "mixed_batched"
+    ms = max_over_ranks(out[main_label]["ms_per_step"], world)
     if rank != 0:
         return
     gm = grads["mixed"]
     gd = grads.get("double")
-    main_arm = out["mixed_t%d" % args.threads]
+    main_arm = out[main_label]
     line = {"metric": FITTING_METRIC, "value": 1000.0 / ms, "unit": "steps/s", "n_gpus": world,
-            "steps": out["mixed_t%d" % args.threads]["steps"], "warmup": args.warmup, "ms_per_step": ms,
+            "steps": main_arm["steps"], "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded water boxes)",
             "config": {"workload": FITTING_WORKLOAD if args.boxes >= 64 else
                        "first %d boxes of %s" % (len(all_systems), FITTING_WORKLOAD),
-                       "atoms": natoms, "host_threads": args.threads,
-                       "solver_graphs": True,
+                       "atoms": natoms, "launch": "every box's whole evaluation (energy, forces, gradient "
+                                                   "passes) from its captured graph, launched as one parent graph or "
+                                                   "per box over a stream pool, as the autotuner chose",
+                       "comparison_host_threads": args.threads,
                        "device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                        "l2": "inputs copied from host each step"},
             "gpu_launches": main_arm["launches_per_step"] * main_arm["steps"],
@@ -602,7 +611,7 @@ def main():
     ap.add_argument("--workload", default="water24k", choices=["water24k", "water288k", "fitting64"],
                     help="water24k: the headline evaluation; water288k: the 288,000-atom box (mutual and OPT3); "
                          "fitting64: the batched per-type gradient workload")
-    ap.add_argument("--threads", type=int, default=8, help="host threads driving the boxes of fitting64")
+    ap.add_argument("--threads", type=int, default=16, help="host threads driving the boxes of fitting64 (comparison arm)")
     ap.add_argument("--boxes", type=int, default=64, help="fitting64: evaluate only the first N boxes (profiling)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

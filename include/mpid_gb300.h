@@ -204,6 +204,31 @@ int mpid_get_parameter_gradients(mpid_context* ctx, const double* positions, con
 int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, const double* box, double* forces,
                                  double* energy, double* multipole_grad, double* polarization_grad);
 
+/* Evaluate `count` independent contexts (PME, one device) at once: for each k, energy
+ * (energies[k]), forces ADDED to forces[k] (3n; forces or forces[k] may be NULL) and,
+ * where multipole_grad / polarization_grad and their k-th pointer are non-NULL, the
+ * gradients of mpid_evaluate_with_gradients.  Host arrays.  No reference counterpart:
+ * the batched entry point of this library (parameter fitting over many small boxes).
+ * Each context's evaluation is captured once as a graph with no host synchronisation --
+ * list shape and mutual-solver length taken from its previous evaluation.  streams 0:
+ * the graphs of all contexts run as one launch of a parent graph; streams k > 0: each
+ * context's graph is launched on one of k streams.  After the launch each context's list sizes,
+ * solver convergence and FP64 residual are checked; a context that fails a check (or is
+ * evaluated for the first time) gets the ordinary evaluation instead, so the results are
+ * those of mpid_evaluate_with_gradients.  Calls are serialised within the process. */
+int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* const* positions, const double* const* boxes,
+                        double* const* forces, double* energies, double* const* multipole_grad,
+                        double* const* polarization_grad, int streams);
+
+/* Launch configuration: the largest number of sub-ranges each pair-kernel work item
+ * (32 atoms x 32 list entries) is cut into, one warp each -- a power of two up to 32, or
+ * 0 for the automatic choice, which cuts until a launch holds two waves of warps of the
+ * whole GPU.  Contexts evaluated together (mpid_evaluate_batch, host threads) share the
+ * GPU, where fewer, longer warps can be faster; the fitting module's autotuner picks the
+ * bound by timing.  Results differ only in the rounding of the FP32 partial sums.  No
+ * reference counterpart. */
+int mpid_set_work_split(mpid_context* ctx, int max_split);
+
 /* PME parameters in use (CalcMPIDForceKernel::getPMEParameters, mpidKernels.h:103). */
 int mpid_get_pme_parameters(mpid_context* ctx, double* alpha, int* nx, int* ny, int* nz);
 

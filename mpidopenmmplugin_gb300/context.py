@@ -24,7 +24,8 @@ MPID_FLAG_SERIAL_STAGES = 8
 C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multipoles", "mpid_set_covalent",
          "mpid_evaluate", "mpid_evaluate_device", "mpid_evaluate_device_noalloc", "mpid_get_dipoles",
          "mpid_get_pme_parameters", "mpid_get_stats", "mpid_last_error", "mpid_get_system_multipole_moments",
-         "mpid_get_electrostatic_potential", "mpid_get_parameter_gradients", "mpid_evaluate_with_gradients"]
+         "mpid_get_electrostatic_potential", "mpid_get_parameter_gradients", "mpid_evaluate_with_gradients",
+         "mpid_evaluate_batch", "mpid_set_work_split"]
 
 
 class Settings(ctypes.Structure):
@@ -105,6 +106,9 @@ def load_library(build=True):
     lib.mpid_get_electrostatic_potential.argtypes = [vp, dp, dp, dp, ctypes.c_int, dp]
     lib.mpid_get_parameter_gradients.argtypes = [vp, dp, dp, dp]
     lib.mpid_evaluate_with_gradients.argtypes = [vp, dp, dp, dp, dp, dp, dp]
+    pp = ctypes.POINTER(ctypes.c_void_p)
+    lib.mpid_evaluate_batch.argtypes = [pp, ctypes.c_int, pp, pp, pp, dp, pp, pp, ctypes.c_int]
+    lib.mpid_set_work_split.argtypes = [vp, ctypes.c_int]
     lib.mpid_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.mpid_last_error.argtypes = []
     lib.mpid_last_error.restype = ctypes.c_char_p
@@ -184,6 +188,7 @@ class MPIDContext:
                    (MPID_FLAG_SERIAL_STAGES if serial_stages else 0))
         self.n = n
         self.precision = precision
+        self.device = int(device)
         self._h = ctypes.c_void_p()
         self._check(self.lib.mpid_create(ctypes.byref(s), int(device), ctypes.byref(self._h)))
         self.update_parameters(force)
@@ -291,6 +296,11 @@ class MPIDContext:
             null if gm is None else _dp(gm), null if gp is None else _dp(gp)))
         return e.value, f, gm, gp
 
+    def setWorkSplit(self, max_split):
+        """Upper bound (power of two up to 32, 0 = automatic) of the warps each pair-kernel
+        work item is cut into (mpid_set_work_split)."""
+        self._check(self.lib.mpid_set_work_split(self._h, int(max_split)))
+
     def getPMEParametersInContext(self):
         a = ctypes.c_double()
         nx, ny, nz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
@@ -321,3 +331,46 @@ class MPIDContext:
             self.close()
         except Exception:
             pass
+
+
+def evaluate_batch(contexts, positions, boxes, forces=True, multipole=True, polarization=True, streams=0):
+    """mpid_evaluate_batch over MPIDContexts of PME systems on one device: each context's
+    whole evaluation runs from a captured graph, all of them in one launch of a parent
+    graph (streams=0) or each on one of `streams` streams (the first call of a context,
+    and any context whose list shape or solver length changed, takes the ordinary
+    evaluation).  Returns (energies (k,), forces [(n, 3)] or None, multipole gradients
+    [(n, 20)] or None, polarisation gradients [(n, 4)] or None)."""
+    k = len(contexts)
+    if k == 0:
+        return np.zeros(0), None, None, None
+    lib = contexts[0].lib
+    keep = []
+
+    def arr(shape):
+        a = np.zeros(shape)
+        keep.append(a)
+        return a
+
+    def ptrs(arrays):
+        out = (ctypes.c_void_p * k)(*[None if a is None else a.ctypes.data for a in arrays])
+        return ctypes.cast(out, ctypes.POINTER(ctypes.c_void_p)), out
+
+    pos = [np.ascontiguousarray(p, dtype=np.float64).reshape(c.n, 3) for c, p in zip(contexts, positions)]
+    bx = [np.ascontiguousarray(b, dtype=np.float64).reshape(9) for b in boxes]
+    fo = [arr((c.n, 3)) for c in contexts] if forces else None
+    gm = [arr((c.n, 20)) for c in contexts] if multipole else None
+    gp = [arr((c.n, 4)) for c in contexts] if polarization else None
+    e = np.zeros(k)
+    cp, cbuf = ptrs([None] * k)
+    for i, c in enumerate(contexts):
+        cbuf[i] = c._h.value
+    pp, pbuf = ptrs(pos)
+    bp, bbuf = ptrs(bx)
+    null = ctypes.POINTER(ctypes.c_void_p)()
+    fp = ptrs(fo) if fo is not None else (null, None)
+    mp = ptrs(gm) if gm is not None else (null, None)
+    qp = ptrs(gp) if gp is not None else (null, None)
+    contexts[0]._check(lib.mpid_evaluate_batch(cp, k, pp, bp, fp[0], _dp(e), mp[0], qp[0], int(streams)))
+    for c, p, b in zip(contexts, pos, bx):
+        c.last_positions, c.last_box = p.copy(), b.copy()
+    return e, fo, gm, gp

@@ -302,7 +302,9 @@ struct StageTimer {
         replayed.clear();
         for (int s = 0; s < ST_COUNT; ++s) { ms[s] = 0; launches[s] = 0; }
     }
+    bool off = false;  // set while a whole evaluation is captured for a batch (no stage events)
     void begin(int s, cudaStream_t st) {
+        if (off) return;
         if (capPool) {
             if (capNext + 2 > capPool->size()) return;
             capOpen = {s, (*capPool)[capNext], (*capPool)[capNext + 1]};
@@ -316,6 +318,7 @@ struct StageTimer {
         open = count;
     }
     void end(cudaStream_t st) {
+        if (off) return;
         if (capPool) {
             if (capOpen.stage < 0) return;
             CUDA_CHECK(cudaEventRecordWithFlags(capOpen.b, st, cudaEventRecordExternal));
@@ -344,9 +347,12 @@ struct StageTimer {
 };
 
 // ---------------------------------------------------------------------------
+static std::atomic<unsigned long long> g_context_ids{0};
+
 struct Context {
     mpid_settings set;
     int device = 0;
+    unsigned long long id = ++g_context_ids;  // never reused: batch graphs key on it
     int numSMs = 1;  // multiprocessors of the device, read at creation (launch sizes)
     int n = 0, npad = 0, ntiles = 0;
     bool usePme = false, mixed = true;
@@ -490,6 +496,8 @@ struct Context {
 
     ~Context() {
         for (auto& g : graphs) g.destroy();
+        full.destroy();
+        if (hostEparts) cudaFreeHost(hostEparts);
         timer.destroy();
         if (hostDone) cudaFreeHost(hostDone);
         if (hostSc) cudaFreeHost(hostSc);
@@ -907,9 +915,11 @@ struct Context {
     // them below a few thousand atoms).  The lists and results are the same.  Measured
     // on the 24,000-atom box: the CG pair kernel goes from 87 to 75 us per launch
     // (split 4); on a 660-atom box the FP32 CG field from 41 to 10 us.
+    int splitCap = 0;  // upper bound of field_split() (0: none); mpid_set_work_split
     int field_split() const {
+        const int cap = splitCap > 0 ? std::min(splitCap, chunk) : chunk;
         int split = 1;
-        while (split < chunk && (long long) pair_tasks() * split < 2LL * numSMs * 64) split *= 2;
+        while (split < cap && (long long) pair_tasks() * split < 2LL * numSMs * 64) split *= 2;
         return split;
     }
     NbrList field_list() const {
@@ -1341,7 +1351,7 @@ struct Context {
     // launches bake in: the segment, the device-buffer generation (any reallocation
     // anywhere changes it), the list buffers (the no-alloc call points them at its
     // scratch), the list shape and launch sizes, the box and the constants.
-    enum { kSegChunk = 1, kSegSetup, kSegSolveStart, kSegFinish, kSegGradients };
+    enum { kSegChunk = 1, kSegSetup, kSegSolveStart, kSegFinish, kSegGradients, kSegFull };
 
     static void key_put(std::vector<long long>& k, const void* v, size_t bytes) {
         const size_t o = k.size();
@@ -1805,6 +1815,190 @@ struct Context {
         return energy;
     }
 
+    // ----- batched evaluation (mpid_evaluate_batch) -----
+    // One complete evaluation (set-up, permanent field, induced dipoles, forces and
+    // energy, optionally the gradient passes) captured as a graph with no host
+    // synchronisation, so that the graphs of many contexts run as one launch.  The values
+    // an ordinary evaluation decides on the host between its segments come from the
+    // previous evaluation of the context: the list capacities, work-item counts and launch
+    // sizes, and the number of CG iterations (the last solve's plus one).  The graph
+    // copies to pinned host memory what decides whether its results stand -- the list
+    // maxima, the solver's done flag, iteration count and metric, the FP64 residual of the
+    // mixed path -- and batch_ok() checks them after the launch.
+    struct FullGraph {
+        std::vector<long long> key;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;  // for launches of this context's graph on its own
+        long long nodes = 0, library = 0;
+        int K = 0;
+        unsigned long long generation = 0;  // changes with every capture
+        void destroy() {
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+            exec = nullptr;
+            graph = nullptr;
+            key.clear();
+        }
+    } full;
+    double* hostEparts = nullptr;  // pinned: the energy parts of a batched evaluation
+    bool batchReady = false;       // an ordinary evaluation has sized the lists and the solver
+
+    // The captured body (launches only).
+    void batch_body(bool mg, bool pg, int K) {
+        cudaStream_t st = stream;
+        if (mixed) {
+            Engine<float>& e = *ef;
+            sort_and_tiles();
+            prepare_engine(e, true);
+            launch(k_pack_atoms, nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
+                   pack0.p);
+            if (ed) {
+                CUDA_CHECK(cudaEventRecord(evRefStart, st));
+                CUDA_CHECK(cudaStreamWaitEvent(refStream, evRefStart, 0));
+                {
+                    RefStreams scope(*this);
+                    prepare_engine(*ed, false);
+                    launch(k_df_atoms, nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p, tholeDF.p,
+                           dampDF.p);
+                }
+                CUDA_CHECK(cudaEventRecord(evRefStart, refStream));
+                CUDA_CHECK(cudaStreamWaitEvent(st, evRefStart, 0));
+            }
+            launch_lists(e, false);  // the list maxima go to hostMax
+            fixed_field(e);
+            if (set.polarization_type == MPID_MUTUAL) {
+                mutual_mixed_start(e);
+                cg_begin<float, float>(e, b32.p, x32.p, r32.p, p32.p, q32.p, inner_target(), K);
+                for (int i = 0; i < K; ++i) cg_iteration<float, float>(e, x32.p, r32.p, p32.p, q32.p, inner_target(), K, i == 0);
+                CUDA_CHECK(cudaMemcpyAsync(hostDone + 256, iter.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+                launch_check(e, *ed);  // the FP64 residual to refHost, beside the force/energy phase
+                finish(e, ptMuF.p, ptEF.p, ptGF.p);
+                CUDA_CHECK(cudaStreamWaitEvent(st, evRefDone, 0));
+            } else {
+                solve_dipoles(e, ptMuF.p, ptEF.p, ptGF.p);
+                finish(e, ptMuF.p, ptEF.p, ptGF.p);
+            }
+            launch(k_forces_out, nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, forcesOut.p);
+        } else {
+            Engine<double>& e = *ed;
+            sort_and_tiles();
+            prepare_engine(e, true);
+            launch_lists(e, false);
+            fixed_field(e);
+            if (set.polarization_type == MPID_MUTUAL) {
+                cg_begin<double, double>(e, e.SE.p, y64.p, r64.p, p64.p, q64.p, set.mutual_eps, K);
+                for (int i = 0; i < K; ++i)
+                    cg_iteration<double, double>(e, y64.p, r64.p, p64.p, q64.p, set.mutual_eps, K, i == 0);
+                CUDA_CHECK(cudaMemcpyAsync(hostDone + 256, iter.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CUDA_CHECK(cudaMemcpyAsync(hostSc, sc.p, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+                launch(k_mu_from_y<double, double>, nblk(npad, 128), 128, 0, st, npad, e.sroot.p, y64.p, e.mu.p);
+                finish(e, ptMuD.p, ptED.p, ptGD.p);
+            } else {
+                solve_dipoles(e, ptMuD.p, ptED.p, ptGD.p);
+                finish(e, ptMuD.p, ptED.p, ptGD.p);
+            }
+            launch(k_forces_out, nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, forcesOut.p);
+        }
+        CUDA_CHECK(cudaMemcpyAsync(hostEparts, energyOut.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (mg || pg) {
+            gradPrepared = false;
+            if (mg) multipole_gradient_launches();
+            if (pg) polarization_gradient_launches();
+        }
+        CUDA_CHECK(cudaGetLastError());
+    }
+
+    // The context's batch graph for the current list shape, box and solver length,
+    // captured when it changed; returns true if it was captured now.
+    bool ensure_batch_graph(bool mg, bool pg) {
+        if (mg || pg) gradient_buffers(mg, pg);  // allocations before the key and the capture
+        if (!hostEparts) CUDA_CHECK(cudaMallocHost(&hostEparts, 3 * sizeof(double)));
+        const int K = set.polarization_type == MPID_MUTUAL ? std::max(1, std::min(set.max_iter, predictedIters + 1)) : 0;
+        std::vector<long long> key = graph_key(kSegFull);
+        const long long more[] = {K, mg ? 1 : 0, pg ? 1 : 0};
+        key_put(key, more, sizeof more);
+        if (full.graph && full.key == key) return false;
+        full.destroy();
+        cudaStream_t st = stream;
+        const bool wasActive = graphsActive;
+        graphsActive = false;  // the body launches directly into this capture
+        timer.off = true;
+        const long long l0 = t_launches, c0 = t_library_calls;
+        cudaGraph_t graph = nullptr;
+        CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            batch_body(mg, pg, K);
+        } catch (...) {
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            (void) cudaGetLastError();
+            timer.off = false;
+            graphsActive = wasActive;
+            t_launches = l0;
+            t_library_calls = c0;
+            throw;
+        }
+        const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        timer.off = false;
+        graphsActive = wasActive;
+        full.nodes = t_launches - l0;
+        full.library = t_library_calls - c0;
+        t_launches = l0;
+        t_library_calls = c0;
+        CUDA_CHECK(ce);
+        full.graph = graph;
+        full.key = key;
+        full.K = K;
+        full.generation = ++graphClock;
+        ++stats.graph_captures;
+        return true;
+    }
+
+    // After a batch launch: whether this context's results stand (its lists fitted the
+    // capacities and work items the graph was built with, its solver converged).  Also
+    // fills the statistics of the evaluation.
+    bool batch_ok() {
+        const int mTiles = hostMax[0], mTotal = hostMax[1], mL = hostMax[2], mS = hostMax[3];
+        lastTiles = mTiles;
+        lastMaxList = mTotal;
+        stats.max_neighbours = mTotal;
+        if (mTiles > tcap || mTotal > cap) return false;
+        if ((mL + chunk - 1) / chunk > nchunksL || (mS + chunk - 1) / chunk > nchunksS) return false;
+        stats.solver_iterations = 0;
+        stats.refinement_steps = 0;
+        stats.solver_residual = 0.0;
+        if (set.polarization_type == MPID_MUTUAL) {
+            const int used = hostDone[256];
+            stats.solver_iterations = used;
+            if (mixed) {
+                const double metric = 48.033324 * std::sqrt(*refHost / n);
+                stats.refinement_steps = 1;
+                stats.solver_residual = metric;
+                if (!(metric < set.mutual_eps)) return false;
+            } else {
+                stats.solver_residual = hostSc[6];
+                if (!(hostSc[6] < set.mutual_eps)) return false;
+            }
+            predictedIters = used;
+        } else if (set.polarization_type == MPID_EXTRAPOLATED) {
+            stats.solver_iterations = set.n_extrap - 1;
+        }
+        stats.energy_parts[0] = hostEparts[0];
+        stats.energy_parts[1] = hostEparts[1];
+        stats.energy_parts[2] = hostEparts[2];
+        stats.kernel_launches = (int) full.nodes;
+        stats.library_calls = (int) full.library;
+        stats.graph_replays = 1;
+        for (int k = 0; k < ST_COUNT; ++k) {
+            stats.ms_stage[k] = 0.0;
+            stats.stage_launches[k] = 0;
+        }
+        stats.ms_total = 0.0;
+        evaluated = true;
+        gradPrepared = true;  // the graph ran the gradient passes' preparation
+        return true;
+    }
+
     // Evaluation with the neighbour lists and per-task energies in `scratch` (the static
     // array above, kNoAllocBytes); allocates nothing and never grows a buffer.
     double evaluate_device_noalloc(const double* d_pos, const double* hbox, double* d_forces, double* d_energy,
@@ -2095,8 +2289,19 @@ struct Context {
     // Both gradient passes after an evaluation: with graphs, one captured segment (the
     // FP64 inputs of the pass, then each pass), then the copies to the host.
     void gradients(double* multipoleHost, double* polarizationHost) {
-        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
         const bool mg = multipoleHost != nullptr, pg = polarizationHost != nullptr;
+        if (!mg && !pg) {
+            if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
+            return;
+        }
+        gradients_device(mg, pg);
+        if (mg) CUDA_CHECK(cudaMemcpyAsync(multipoleHost, gradOut.p, (size_t) 20 * n * 8, cudaMemcpyDeviceToHost, stream));
+        if (pg) CUDA_CHECK(cudaMemcpyAsync(polarizationHost, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, stream));
+    }
+
+    // The gradient passes into gradOut / polOut (device), replayed from a graph.
+    void gradients_device(bool mg, bool pg) {
+        if (!evaluated) throw Error(MPID_ERR_STATE, "no evaluation has been run");
         if (!mg && !pg) return;
         gradient_buffers(mg, pg);
         const bool prepared = gradPrepared;
@@ -2111,8 +2316,6 @@ struct Context {
         stats.kernel_launches += (int) (t_launches - launches0);
         stats.library_calls += (int) (t_library_calls - library0);
         gradPrepared = true;  // a replay does not run gradient_engine's host side
-        if (mg) CUDA_CHECK(cudaMemcpyAsync(multipoleHost, gradOut.p, (size_t) 20 * n * 8, cudaMemcpyDeviceToHost, stream));
-        if (pg) CUDA_CHECK(cudaMemcpyAsync(polarizationHost, polOut.p, (size_t) 4 * n * 8, cudaMemcpyDeviceToHost, stream));
     }
 
     void get_dipoles(int which, double* host) {
@@ -2345,6 +2548,178 @@ int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, con
     MPID_API_END
 }
 
+// The launch of the whole-evaluation graphs of many contexts: either one parent graph
+// whose children are the contexts' graphs, rebuilt when a child is captured anew or the
+// set of contexts changes (keyed by context ids, which are never reused, and capture
+// generations), or each context's graph on one of a pool of streams.
+namespace {
+struct BatchGraph {
+    std::vector<unsigned long long> key;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaStream_t> streams;  // per-context launches
+    std::vector<cudaEvent_t> joins;
+    int device = -1;
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key.clear();
+    }
+};
+std::mutex g_batchMutex;
+BatchGraph g_batch;
+}  // namespace
+
+// The ordinary evaluation of one context of a batch at its host inputs, into its own
+// buffers (used for the first call of a context and for results a batch graph could not
+// stand behind).
+static double batch_fallback(Context& c, const double* positions, const double* box, const double* forces, bool mg,
+                             bool pg) {
+    const size_t n3 = 3 * (size_t) c.n;
+    CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions, n3 * 8, cudaMemcpyHostToDevice, c.stream));
+    if (forces)
+        CUDA_CHECK(cudaMemcpyAsync(c.forcesOut.p, forces, n3 * 8, cudaMemcpyHostToDevice, c.stream));
+    else
+        CUDA_CHECK(cudaMemsetAsync(c.forcesOut.p, 0, n3 * 8, c.stream));
+    const double e = c.evaluate_device(c.pos.p, box, c.forcesOut.p, nullptr);
+    if (mg || pg) c.gradients_device(mg, pg);
+    c.batchReady = true;
+    return e;
+}
+
+int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* const* positions, const double* const* boxes,
+                        double* const* forces, double* energies, double* const* multipole_grad,
+                        double* const* polarization_grad, int streams) {
+    MPID_API_BEGIN
+    if (streams < 0 || streams > 128) throw Error(MPID_ERR_INVALID, "streams must be in 0..128");
+    if (count < 0 || (count > 0 && (!ctxs || !positions || !boxes || !energies)))
+        throw Error(MPID_ERR_INVALID, "null argument");
+    if (count == 0) return MPID_OK;
+    const int device = ctxs[0] ? ctxs[0]->ctx.device : 0;
+    for (int k = 0; k < count; ++k) {
+        if (!ctxs[k] || !positions[k] || !boxes[k]) throw Error(MPID_ERR_INVALID, "null argument");
+        if (ctxs[k]->ctx.device != device) throw Error(MPID_ERR_INVALID, "mpid_evaluate_batch: contexts on different devices");
+        if (!ctxs[k]->ctx.usePme) throw Error(MPID_ERR_INVALID, "mpid_evaluate_batch supports PME contexts only");
+    }
+    mpid::DeviceScope scope(device);
+    std::lock_guard<std::mutex> lock(g_batchMutex);
+    std::vector<char> graphed(count, 0);
+    std::vector<double> eFallback(count, 0.0);
+    bool changed = false;
+    for (int k = 0; k < count; ++k) {
+        Context& c = ctxs[k]->ctx;
+        const bool mg = multipole_grad && multipole_grad[k], pg = polarization_grad && polarization_grad[k];
+        const double* fin = forces ? forces[k] : nullptr;
+        c.stream = c.hostStream;
+        c.bind_streams();
+        if (!c.batchReady) {
+            eFallback[k] = batch_fallback(c, positions[k], boxes[k], fin, mg, pg);
+            continue;
+        }
+        const size_t n3 = 3 * (size_t) c.n;
+        CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions[k], n3 * 8, cudaMemcpyHostToDevice, c.stream));
+        if (fin)
+            CUDA_CHECK(cudaMemcpyAsync(c.forcesOut.p, fin, n3 * 8, cudaMemcpyHostToDevice, c.stream));
+        else
+            CUDA_CHECK(cudaMemsetAsync(c.forcesOut.p, 0, n3 * 8, c.stream));
+        c.set_box(boxes[k]);
+        c.stats.graph_captures = 0;
+        changed = c.ensure_batch_graph(mg, pg) || changed;
+        CUDA_CHECK(cudaStreamSynchronize(c.stream));
+        graphed[k] = 1;
+    }
+    // the parent graph of the graphed contexts
+    std::vector<unsigned long long> key;
+    for (int k = 0; k < count; ++k)
+        if (graphed[k]) {
+            key.push_back(ctxs[k]->ctx.id);
+            key.push_back(ctxs[k]->ctx.full.generation);
+        }
+    if (g_batch.device != device) {
+        g_batch.reset();
+        if (g_batch.stream) cudaStreamDestroy(g_batch.stream);
+        for (cudaStream_t q : g_batch.streams) cudaStreamDestroy(q);
+        for (cudaEvent_t ev : g_batch.joins) cudaEventDestroy(ev);
+        g_batch.stream = nullptr;
+        g_batch.streams.clear();
+        g_batch.joins.clear();
+        g_batch.device = device;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&g_batch.stream, cudaStreamNonBlocking));
+    }
+    if (!key.empty() && streams > 0) {
+        // each context's graph on one of `streams` streams, joined into the batch stream
+        while ((int) g_batch.streams.size() < streams) {
+            cudaStream_t q;
+            cudaEvent_t ev;
+            CUDA_CHECK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+            CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            g_batch.streams.push_back(q);
+            g_batch.joins.push_back(ev);
+        }
+        int j = 0;
+        for (int k = 0; k < count; ++k)
+            if (graphed[k]) {
+                Context& c = ctxs[k]->ctx;
+                if (!c.full.exec) CUDA_CHECK(cudaGraphInstantiate(&c.full.exec, c.full.graph, 0));
+                CUDA_CHECK(cudaGraphLaunch(c.full.exec, g_batch.streams[j % streams]));
+                ++j;
+            }
+        for (int q = 0; q < std::min(j, streams); ++q) {
+            CUDA_CHECK(cudaEventRecord(g_batch.joins[q], g_batch.streams[q]));
+            CUDA_CHECK(cudaStreamWaitEvent(g_batch.stream, g_batch.joins[q], 0));
+        }
+        CUDA_CHECK(cudaStreamSynchronize(g_batch.stream));
+    } else if (!key.empty()) {
+        if (changed || g_batch.key != key || !g_batch.exec) {
+            g_batch.reset();
+            cudaGraph_t parent = nullptr;
+            CUDA_CHECK(cudaGraphCreate(&parent, 0));
+            for (int k = 0; k < count; ++k)
+                if (graphed[k]) {
+                    cudaGraphNode_t node;
+                    const cudaError_t rc = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, ctxs[k]->ctx.full.graph);
+                    if (rc != cudaSuccess) {
+                        cudaGraphDestroy(parent);
+                        CUDA_CHECK(rc);
+                    }
+                }
+            const cudaError_t rc = cudaGraphInstantiate(&g_batch.exec, parent, 0);
+            cudaGraphDestroy(parent);
+            CUDA_CHECK(rc);
+            g_batch.key = key;
+        }
+        CUDA_CHECK(cudaGraphLaunch(g_batch.exec, g_batch.stream));
+        CUDA_CHECK(cudaStreamSynchronize(g_batch.stream));
+    }
+    // results, and the ordinary evaluation of any context whose graph results do not stand
+    for (int k = 0; k < count; ++k) {
+        Context& c = ctxs[k]->ctx;
+        const bool mg = multipole_grad && multipole_grad[k], pg = polarization_grad && polarization_grad[k];
+        double e = eFallback[k];
+        if (graphed[k]) {
+            if (c.batch_ok()) {
+                e = c.stats.energy_parts[0] + c.stats.energy_parts[1] + c.stats.energy_parts[2];
+            } else {
+                c.full.destroy();  // captured anew with the new list shape or solver length
+                e = batch_fallback(c, positions[k], boxes[k], forces ? forces[k] : nullptr, mg, pg);
+            }
+        }
+        energies[k] = e;
+        const size_t n3 = 3 * (size_t) c.n;
+        if (forces && forces[k])
+            CUDA_CHECK(cudaMemcpyAsync(forces[k], c.forcesOut.p, n3 * 8, cudaMemcpyDeviceToHost, c.stream));
+        if (mg)
+            CUDA_CHECK(cudaMemcpyAsync(multipole_grad[k], c.gradOut.p, (size_t) 20 * c.n * 8, cudaMemcpyDeviceToHost,
+                                       c.stream));
+        if (pg)
+            CUDA_CHECK(cudaMemcpyAsync(polarization_grad[k], c.polOut.p, (size_t) 4 * c.n * 8, cudaMemcpyDeviceToHost,
+                                       c.stream));
+        CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    }
+    return MPID_OK;
+    MPID_API_END
+}
+
 int mpid_get_dipoles(mpid_context* ctx, int which, double* out) {
     MPID_API_BEGIN
     if (!ctx || !out) throw Error(MPID_ERR_INVALID, "null argument");
@@ -2363,6 +2738,16 @@ int mpid_get_pme_parameters(mpid_context* ctx, double* alpha, int* nx, int* ny, 
     if (nx) *nx = ctx->ctx.set.grid[0];
     if (ny) *ny = ctx->ctx.set.grid[1];
     if (nz) *nz = ctx->ctx.set.grid[2];
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_set_work_split(mpid_context* ctx, int max_split) {
+    MPID_API_BEGIN
+    if (!ctx) throw Error(MPID_ERR_INVALID, "null argument");
+    if (max_split < 0 || max_split > 32 || (max_split & (max_split - 1)) != 0)
+        throw Error(MPID_ERR_INVALID, "max_split must be 0 or a power of two up to 32");
+    ctx->ctx.splitCap = max_split;
     return MPID_OK;
     MPID_API_END
 }

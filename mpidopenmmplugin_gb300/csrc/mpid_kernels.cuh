@@ -886,7 +886,7 @@ struct DfAtoms {
     const float2* off;
     const float2* mu;
     const float2* thole;
-    const float2* damp;
+    const float2* damp;  // 1 / damping factor (0 for an atom without polarisability)
 };
 
 struct DfRadial {
@@ -931,7 +931,7 @@ __global__ void k_df_atoms(int npad, const double* __restrict__ off, const doubl
         offDF[k * npad + i] = make_float2(v.hi, v.lo);
     }
     const double4_16a p = prm[i];
-    const dfloat t = df_from_double(p.x), d = df_from_double(p.y);
+    const dfloat t = df_from_double(p.x), d = df_from_double(p.w);  // Thole width, 1 / damping (0: none)
     tholeDF[i] = make_float2(t.hi, t.lo);
     dampDF[i] = make_float2(d.hi, d.lo);
 }
@@ -972,10 +972,10 @@ __device__ __forceinline__ void df_field_loop(const NbrList& nl, const DfRadial&
         const dfloat r5inv = df_mul(bB1, rinv2);       // 1/r^5
         // Thole: oneMinus_n = e^-s P_n(s), P_1 = 1 + s + s^2/2, P_2 = P_1 + s^3/6
         dfloat om1 = df_from_float(0.f), om2 = df_from_float(0.f);
-        const dfloat dd = df_mul(dpi, df_load(A.damp, sj));
+        const dfloat dd = df_mul(dpi, df_load(A.damp, sj));  // 1 / (d_i d_j), 0 without damping
         if (dd.hi > 0.f) {
             const dfloat a = flag == 1u ? df_add(thi, df_load(A.thole, sj)) : df_make(R.tholeDefault.x, R.tholeDefault.y);
-            const dfloat sT = df_div(df_mul(a, r), dd);
+            const dfloat sT = df_mul(df_mul(a, r), dd);
             if (sT.hi < 50.f) {
                 const dfloat e = df_exp_neg(sT);
                 const dfloat s2h = df_mul(df_mul(sT, sT), 0.5f);

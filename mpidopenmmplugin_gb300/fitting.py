@@ -85,18 +85,21 @@ class BoxBatch:
     """Independent boxes sharing per-type parameters.
 
     systems: list of (force, positions (n, 3) nm, box (3, 3) nm, types (n,) ints).
-    precision: "mixed" or "double", as MPIDContext.  threads: host threads driving the
-    contexts concurrently.  solver_graphs: each context replays its mutual solver's
-    iterations from captured CUDA graphs (MPIDContext).
+    precision: "mixed" or "double", as MPIDContext.  batched: every box's whole evaluation
+    (energy, forces, gradient passes) runs from a captured graph and all boxes in one
+    launch (mpid_evaluate_batch); otherwise host threads drive the contexts
+    concurrently, each replaying its evaluation's segments from graphs (solver_graphs).
     """
 
-    def __init__(self, systems, ntypes, precision="mixed", threads=8, device=0, solver_graphs=True):
+    def __init__(self, systems, ntypes, precision="mixed", threads=8, device=0, solver_graphs=True, batched=True):
         self.ntypes = int(ntypes)
         self.systems = [(f, np.asarray(p, dtype=np.float64), np.asarray(b, dtype=np.float64), np.asarray(t))
                         for f, p, b, t in systems]
         self.contexts = [MPIDContext(f, precision=precision, device=device, box=b, solver_graphs=solver_graphs)
                          for f, p, b, t in self.systems]
         self.threads = max(1, int(threads))
+        self.batched = bool(batched)
+        self.batch_streams = 0  # batched launch: 0 one parent graph, k > 0 per-box graphs on k streams
         self._pool = _cf.ThreadPoolExecutor(max_workers=self.threads)
 
     def set_parameters(self, params):
@@ -117,12 +120,80 @@ class BoxBatch:
     def evaluate(self, forces=True):
         """Energies (nbox,) kJ/mol, per-box forces (list of (n, 3) or None) and the gradient
         of the summed energy with respect to the per-type parameters (ntypes, 24)."""
+        if self.batched:
+            from .context import evaluate_batch
+            energies, fo, gm, gp = evaluate_batch(self.contexts, [s[1] for s in self.systems],
+                                                  [s[2] for s in self.systems], forces=forces,
+                                                  streams=self.batch_streams)
+            grad = np.zeros((self.ntypes, NPARAM))
+            for (f, p, b, t), m, q in zip(self.systems, gm, gp):
+                grad[:, :20] += per_type(m, t, self.ntypes)
+                grad[:, 20:] += per_type(q, t, self.ntypes)
+            return energies, (fo if forces else [None] * len(self.systems)), grad
         results = list(self._pool.map(lambda k: self._one(k, forces), range(len(self.systems))))
         energies = np.array([r[0] for r in results])
         grad = np.zeros((self.ntypes, NPARAM))
         for r in results:
             grad += r[2]
         return energies, [r[1] for r in results], grad
+
+    def tuning_key(self):
+        """The workload class a tuning result applies to: GPU (name, multiprocessors),
+        launch mode, precision and batch shape (boxes, mean atoms per box to 100)."""
+        import torch
+        props = torch.cuda.get_device_properties(self.contexts[0].device if self.contexts else 0)
+        sizes = [len(sy[1]) for sy in self.systems]
+        return "%s|%d|%s|%s|%dx%d" % (props.name, props.multi_processor_count, "batched" if self.batched else "threads",
+                                      self.contexts[0].precision, len(sizes), int(round(np.mean(sizes) / 100.0)) * 100)
+
+    def set_work_split(self, max_split):
+        for c in self.contexts:
+            c.setWorkSplit(max_split)
+
+    def configure(self, config):
+        """Apply a launch configuration {"max_split": bound of the pair kernels' work split
+        (MPIDContext.setWorkSplit), "streams": batched launch mode (0 one parent graph,
+        k > 0 per-box graphs on k streams)}."""
+        self.set_work_split(int(config.get("max_split", 0)))
+        self.batch_streams = int(config.get("streams", 0))
+
+    def autotune(self, splits=(0, 1, 2, 4, 8), streams=(0, 16, 32), repeats=3, path=None, use_cache=True):
+        """Launch-configuration autotuner: times evaluate() of this batch under each
+        combination of the pair kernels' work-split bound and (batched mode) the launch
+        mode, keeps the fastest, and records it per GPU and workload class (tuning_key) in a
+        JSON file beside the built library, where later batches of the same class find it.
+        Returns (chosen configuration, {configuration label: ms per evaluate})."""
+        import json
+        import os
+        import time
+        path = path or os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "tuning.json")
+        key = self.tuning_key()
+        table = {}
+        if os.path.exists(path):
+            try:
+                table = json.load(open(path))
+            except ValueError:
+                table = {}
+        if use_cache and key in table:
+            best = table[key]["config"]
+            self.configure(best)
+            return best, table[key]["ms"]
+        configs = [{"max_split": int(m), "streams": int(q)} for m in splits for q in (streams if self.batched else (0,))]
+        times = {}
+        for cfg in configs:
+            self.configure(cfg)
+            self.evaluate()  # captures the graphs of this configuration
+            t0 = time.perf_counter()
+            for _ in range(repeats):
+                self.evaluate()
+            times["split%d_streams%d" % (cfg["max_split"], cfg["streams"])] = 1e3 * (time.perf_counter() - t0) / repeats
+        best = configs[min(range(len(configs)), key=lambda i: list(times.values())[i])]
+        self.configure(best)
+        table[key] = {"config": best, "ms": times}
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "w") as fh:
+            json.dump(table, fh, indent=1, sort_keys=True)
+        return best, times
 
     def close(self):
         self._pool.shutdown(wait=True)

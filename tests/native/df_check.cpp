@@ -1,7 +1,7 @@
 // Host check of the double-float arithmetic and the tabulated Ewald radial functions
 // used by the mixed path's residual field, against long double.
 //
-//   g++ -O2 -std=c++17 -I mpidopenmmplugin_gb300/csrc mpidopenmmplugin_gb300/csrc/df_check.cpp -o /tmp/df_check
+//   g++ -O2 -std=c++17 -I mpidopenmmplugin_gb300/csrc tests/native/df_check.cpp -o /tmp/df_check
 //   /tmp/df_check alpha cutoff
 //
 // Prints one line "name max_relative_error" per check.

@@ -452,3 +452,64 @@ def test_sharded_batch_on_gpu_matches_single_process():
     for rank, mine, e, g in res:
         assert np.allclose(e, e_ref, rtol=1e-12, atol=0), rank
         assert np.abs(np.asarray(g) - g_ref).max() <= 1e-12 * np.abs(g_ref).max(), rank
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["mixed", "double"])
+def test_batched_graph_matches_per_box_evaluations(precision):
+    """mpid_evaluate_batch (each box's whole evaluation from a captured graph, all boxes in
+    one launch) against the same boxes evaluated one context at a time: energies, forces
+    and per-type gradients to 1e-10 relative, for three calls in a row (the first takes
+    the ordinary evaluation and sizes the graphs, the later ones run from them) and for a
+    call after one box's atoms moved."""
+    systems, _ = fitting.water_batch(nboxes=6, min_waters=128, max_waters=192)
+    with fitting.BoxBatch(systems, 2, precision=precision, threads=1, batched=False) as ref, \
+            fitting.BoxBatch(systems, 2, precision=precision, batched=True) as bb:
+        e0, f0, g0 = ref.evaluate()
+
+        def check(e1, f1, g1, e0, f0, g0):
+            assert np.allclose(e1, e0, rtol=1e-10, atol=0)
+            for a, b in zip(f1, f0):
+                assert np.abs(a - b).max() <= 1e-10 * np.abs(b).max()
+            assert np.abs(g1 - g0).max() <= 1e-10 * np.abs(g0).max()
+
+        for step in range(3):
+            e1, f1, g1 = bb.evaluate()
+            check(e1, f1, g1, e0, f0, g0)
+            if step > 0:
+                assert all(c.stats()["graph_replays"] == 1 for c in bb.contexts)
+        # one box moves: its list and solver may change; results follow the new positions
+        f, pos, box, types = systems[2]
+        moved = pos + np.random.default_rng(4).normal(scale=0.003, size=pos.shape)
+        for b in (ref, bb):
+            b.systems[2] = (f, moved, box, types)
+        e0, f0, g0 = ref.evaluate()
+        e1, f1, g1 = bb.evaluate()
+        check(e1, f1, g1, e0, f0, g0)
+
+
+@pytest.mark.gpu
+def test_autotuner_records_and_reuses_its_choice(tmp_path):
+    """BoxBatch.autotune times the batch under each launch configuration (work-split bound
+    of the pair kernels, batched launch mode), keeps the fastest, records it per GPU and
+    workload class and reuses the record; the results under any configuration are those of
+    the default one up to the rounding of the FP32 partial sums, which the split groups
+    differently (energies 1e-7, per-type gradients 1e-6 relative: within the mixed path's
+    own accuracy against FP64)."""
+    import json
+    systems, _ = fitting.water_batch(nboxes=4, min_waters=128, max_waters=160)
+    path = str(tmp_path / "tuning.json")
+    with fitting.BoxBatch(systems, 2, precision="mixed", batched=True) as b:
+        e0, _, g0 = b.evaluate()
+        best, times = b.autotune(splits=(0, 2), streams=(0, 4), repeats=1, path=path)
+        assert best in [{"max_split": m, "streams": q} for m in (0, 2) for q in (0, 4)] and len(times) == 4
+        rec = json.load(open(path))
+        assert rec[b.tuning_key()]["config"] == best
+        again, times2 = b.autotune(splits=(0, 2), streams=(0, 4), repeats=1, path=path)  # from the record
+        assert again == best and times2 == times
+        for cfg in ({"max_split": 2, "streams": 4}, {"max_split": 0, "streams": 0}):
+            b.configure(cfg)
+            e1, _, g1 = b.evaluate()
+            print(cfg, np.abs(e1 / e0 - 1).max(), np.abs(g1 - g0).max() / np.abs(g0).max())
+            assert np.allclose(e1, e0, rtol=1e-7, atol=0)
+            assert np.abs(g1 - g0).max() <= 1e-6 * np.abs(g0).max()
