@@ -301,10 +301,13 @@ def run_fitting(args, world, rank, local):
                 dt = (time.perf_counter() - t0) / steps
                 clocks.mark("stop")
             # kernel launches of one step: each box's last evaluation and gradient passes
-            per_step = sum(c.stats()["kernel_launches"] for c in b.contexts)
+            per_step = b.launches()
             label = "%s_%s" % (precision, "batched" if threads == 0 else "t%d" % threads)
             out[label] = {"ms_per_step": dt * 1e3, "steps": steps, "launches_per_step": per_step,
                           "launch_config": tuned[0], "autotune_ms": tuned[1]}
+            if b.batched and b.batch_launch == 0:
+                # device time of the last step's fused graph (CUDA events around its launch)
+                out[label]["device_ms_per_step"] = b.contexts[0].stats()["ms_total"]
             if threads == 0:
                 grads[precision] = g
                 if precision == "mixed":
@@ -322,9 +325,10 @@ def run_fitting(args, world, rank, local):
             "data": "synthetic (seeded water boxes)",
             "config": {"workload": FITTING_WORKLOAD if args.boxes >= 64 else
                        "first %d boxes of %s" % (len(all_systems), FITTING_WORKLOAD),
-                       "atoms": natoms, "launch": "every box's whole evaluation (energy, forces, gradient "
-                                                   "passes) from its captured graph, launched as one parent graph or "
-                                                   "per box over a stream pool, as the autotuner chose",
+                       "atoms": natoms, "launch": "all boxes in one mpid_evaluate_batch call with no per-box host "
+                                                   "synchronisation: fused (one launch per operation over every box, "
+                                                   "batched cuFFT per grid size, one CUDA graph) or per-box graphs "
+                                                   "over a stream pool, as the autotuner chose",
                        "comparison_host_threads": args.threads,
                        "device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                        "l2": "inputs copied from host each step"},

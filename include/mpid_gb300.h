@@ -209,16 +209,24 @@ int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, con
  * where multipole_grad / polarization_grad and their k-th pointer are non-NULL, the
  * gradients of mpid_evaluate_with_gradients.  Host arrays.  No reference counterpart:
  * the batched entry point of this library (parameter fitting over many small boxes).
- * Each context's evaluation is captured once as a graph with no host synchronisation --
- * list shape and mutual-solver length taken from its previous evaluation.  streams 0:
- * the graphs of all contexts run as one launch of a parent graph; streams k > 0: each
- * context's graph is launched on one of k streams.  After the launch each context's list sizes,
- * solver convergence and FP64 residual are checked; a context that fails a check (or is
- * evaluated for the first time) gets the ordinary evaluation instead, so the results are
- * those of mpid_evaluate_with_gradients.  Calls are serialised within the process. */
+ * Each context's evaluation runs with no host synchronisation -- list shape and
+ * mutual-solver length taken from its previous evaluation -- in one of three launch modes:
+ *   launch_mode 0 (fused): one launch per operation for all boxes.  Every box's evaluation
+ *     is recorded as a sequence of operations, and operation i of all boxes becomes one
+ *     kernel launch over the blocks of every box (each block runs its own box's
+ *     parameters), or one batched cuFFT transform per grid size; the sequence is captured
+ *     as one CUDA graph and replayed while no box changes shape.  Boxes of at most 4096
+ *     atoms that all request the same gradients.
+ *   launch_mode -1: each box's evaluation is a graph of its own; the graphs of all boxes
+ *     run as one launch of a parent graph.
+ *   launch_mode k > 0: each box's graph is launched on one of k streams.
+ * After the launch each context's list sizes, solver convergence and FP64 residual are
+ * checked; a context that fails a check (or is evaluated for the first time) gets the
+ * ordinary evaluation instead, so the results are those of mpid_evaluate_with_gradients.
+ * Calls are serialised within the process; a context may appear once per call. */
 int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* const* positions, const double* const* boxes,
                         double* const* forces, double* energies, double* const* multipole_grad,
-                        double* const* polarization_grad, int streams);
+                        double* const* polarization_grad, int launch_mode);
 
 /* Launch configuration: the largest number of sub-ranges each pair-kernel work item
  * (32 atoms x 32 list entries) is cut into, one warp each -- a power of two up to 32, or

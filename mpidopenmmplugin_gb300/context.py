@@ -333,23 +333,29 @@ class MPIDContext:
             pass
 
 
-def evaluate_batch(contexts, positions, boxes, forces=True, multipole=True, polarization=True, streams=0):
-    """mpid_evaluate_batch over MPIDContexts of PME systems on one device: each context's
-    whole evaluation runs from a captured graph, all of them in one launch of a parent
-    graph (streams=0) or each on one of `streams` streams (the first call of a context,
-    and any context whose list shape or solver length changed, takes the ordinary
-    evaluation).  Returns (energies (k,), forces [(n, 3)] or None, multipole gradients
-    [(n, 20)] or None, polarisation gradients [(n, 4)] or None)."""
+def evaluate_batch(contexts, positions, boxes, forces=True, multipole=True, polarization=True, launch=0, flat=False):
+    """mpid_evaluate_batch over MPIDContexts of PME systems on one device.  launch 0
+    (fused): one kernel launch per operation for all boxes (each box's evaluation recorded
+    once, operation i of every box launched together, FFTs batched per grid size; boxes of
+    at most 4096 atoms); -1: each box's evaluation as a graph, all in one parent graph;
+    k > 0: each box's graph on one of k streams.  The first call of a context, and any
+    context whose list shape or solver length changed, takes the ordinary evaluation.
+    Returns (energies (k,), forces [(n, 3)] or None, multipole gradients [(n, 20)] or
+    None, polarisation gradients [(n, 4)] or None); the per-box arrays are consecutive
+    rows of one array per quantity, which flat=True returns instead ((sum n, 3), ...)."""
     k = len(contexts)
     if k == 0:
         return np.zeros(0), None, None, None
     lib = contexts[0].lib
     keep = []
 
-    def arr(shape):
-        a = np.zeros(shape)
-        keep.append(a)
-        return a
+    sizes = [c.n for c in contexts]
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+
+    def rows(width):
+        whole = np.zeros((int(offsets[-1]), width))
+        keep.append(whole)
+        return whole, [whole[offsets[i]:offsets[i + 1]] for i in range(k)]
 
     def ptrs(arrays):
         out = (ctypes.c_void_p * k)(*[None if a is None else a.ctypes.data for a in arrays])
@@ -357,9 +363,9 @@ def evaluate_batch(contexts, positions, boxes, forces=True, multipole=True, pola
 
     pos = [np.ascontiguousarray(p, dtype=np.float64).reshape(c.n, 3) for c, p in zip(contexts, positions)]
     bx = [np.ascontiguousarray(b, dtype=np.float64).reshape(9) for b in boxes]
-    fo = [arr((c.n, 3)) for c in contexts] if forces else None
-    gm = [arr((c.n, 20)) for c in contexts] if multipole else None
-    gp = [arr((c.n, 4)) for c in contexts] if polarization else None
+    fo_all, fo = rows(3) if forces else (None, None)
+    gm_all, gm = rows(20) if multipole else (None, None)
+    gp_all, gp = rows(4) if polarization else (None, None)
     e = np.zeros(k)
     cp, cbuf = ptrs([None] * k)
     for i, c in enumerate(contexts):
@@ -370,7 +376,9 @@ def evaluate_batch(contexts, positions, boxes, forces=True, multipole=True, pola
     fp = ptrs(fo) if fo is not None else (null, None)
     mp = ptrs(gm) if gm is not None else (null, None)
     qp = ptrs(gp) if gp is not None else (null, None)
-    contexts[0]._check(lib.mpid_evaluate_batch(cp, k, pp, bp, fp[0], _dp(e), mp[0], qp[0], int(streams)))
+    contexts[0]._check(lib.mpid_evaluate_batch(cp, k, pp, bp, fp[0], _dp(e), mp[0], qp[0], int(launch)))
     for c, p, b in zip(contexts, pos, bx):
         c.last_positions, c.last_box = p.copy(), b.copy()
+    if flat:
+        return e, fo_all, gm_all, gp_all
     return e, fo, gm, gp

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <cub/device/device_radix_sort.cuh>
+#include <cuda/std/tuple>
+#include <cuda/std/utility>
 
 #include <algorithm>
 #include <atomic>
@@ -17,6 +19,7 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -83,16 +86,219 @@ struct DeviceScope {
 };
 
 // Kernel launches made by this thread (every launch of the library goes through
-// launch(); evaluations report their own count).
+// launch<F>(); evaluations report their own count).
 static thread_local long long t_launches = 0;
 
-template <typename... KArgs, typename... Args>
-static inline void launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args&&... args) {
-    kernel<<<grid, block, smem, st>>>(std::forward<Args>(args)...);
+// ---------------------------------------------------------------------------
+// Launch wrappers of the kernel bodies (MPID_KERNEL void F(KGrid<MT, MB>, P...)).
+//  - k_one<F>: one launch of F, its parameters in the launch, the hardware block index.
+//  - k_boxes<F>: one launch of F for many boxes (independent systems) at once.  The
+//    launch's blocks are the concatenation of every box's blocks; a block finds its box
+//    by a binary search over the boxes' first blocks and runs F with that box's
+//    parameters and its rank within the box.  The parameter sets of all boxes travel in
+//    the launch's parameter space (__grid_constant__, read through the constant cache),
+//    up to BoxParams::kBoxes boxes per launch.
+// Three variants each: the body's launch bounds in full, the thread bound only, none.
+template <class F> struct KernelTraits;
+template <int MT, int MB, class... P>
+struct KernelTraits<void (*)(KGrid<MT, MB>, P...)> {
+    static constexpr int maxThreads = MT, minBlocks = MB;
+    using Args = cuda::std::tuple<P...>;
+    using Grid = KGrid<MT, MB>;
+};
+template <auto F> using KTraits = KernelTraits<decltype(F)>;
+
+template <class Args>
+struct BoxParams {
+    // as many boxes as keep the launch parameters within 31,000 bytes (the limit is 32,764)
+    static constexpr int kBoxes = (int) ((31000 - 16) / (sizeof(Args) + 4)) < 64 ? (int) ((31000 - 16) / (sizeof(Args) + 4)) : 64;
+    int count;
+    unsigned first[kBoxes + 1];  // first block of each box; first[count] = blocks of the launch
+    Args args[kBoxes];
+};
+
+template <auto F, class Args, size_t... I>
+__device__ __forceinline__ void run_box_body(const Args& a, typename KTraits<F>::Grid g, cuda::std::index_sequence<I...>) {
+    F(g, cuda::std::get<I>(a)...);
+}
+template <auto F>
+__device__ __forceinline__ void run_boxes(const BoxParams<typename KTraits<F>::Args>& bp) {
+    using Args = typename KTraits<F>::Args;
+    const unsigned b = blockIdx.x;
+    int lo = 0, hi = bp.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (bp.first[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    run_box_body<F>(bp.args[lo], typename KTraits<F>::Grid{b - bp.first[lo], bp.first[lo + 1] - bp.first[lo]},
+                    cuda::std::make_index_sequence<cuda::std::tuple_size<Args>::value>{});
+}
+
+template <auto F, class... P>
+__global__ void k_one(P... p) { F(typename KTraits<F>::Grid{blockIdx.x, gridDim.x}, p...); }
+template <auto F, class... P>
+__global__ void __launch_bounds__(KTraits<F>::maxThreads) k_one_t(P... p) {
+    F(typename KTraits<F>::Grid{blockIdx.x, gridDim.x}, p...);
+}
+template <auto F, class... P>
+__global__ void __launch_bounds__(KTraits<F>::maxThreads, KTraits<F>::minBlocks) k_one_tb(P... p) {
+    F(typename KTraits<F>::Grid{blockIdx.x, gridDim.x}, p...);
+}
+template <auto F>
+__global__ void k_boxes(const __grid_constant__ BoxParams<typename KTraits<F>::Args> bp) { run_boxes<F>(bp); }
+template <auto F>
+__global__ void __launch_bounds__(KTraits<F>::maxThreads) k_boxes_t(const __grid_constant__ BoxParams<typename KTraits<F>::Args> bp) {
+    run_boxes<F>(bp);
+}
+template <auto F>
+__global__ void __launch_bounds__(KTraits<F>::maxThreads, KTraits<F>::minBlocks)
+    k_boxes_tb(const __grid_constant__ BoxParams<typename KTraits<F>::Args> bp) {
+    run_boxes<F>(bp);
+}
+
+template <class T> static inline T implicit_arg(T v) { return v; }
+
+template <auto F, class Args> struct Launcher;
+template <auto F, class... P>
+struct Launcher<F, cuda::std::tuple<P...>> {
+    template <class... A>
+    static void one(dim3 grid, dim3 block, size_t smem, cudaStream_t st, A&&... a) {
+        if constexpr (KTraits<F>::maxThreads == 0)
+            k_one<F, P...><<<grid, block, smem, st>>>(implicit_arg<P>(std::forward<A>(a))...);
+        else if constexpr (KTraits<F>::minBlocks == 0)
+            k_one_t<F, P...><<<grid, block, smem, st>>>(implicit_arg<P>(std::forward<A>(a))...);
+        else
+            k_one_tb<F, P...><<<grid, block, smem, st>>>(implicit_arg<P>(std::forward<A>(a))...);
+    }
+    template <class... A>
+    static cuda::std::tuple<P...> pack(A&&... a) { return cuda::std::tuple<P...>(implicit_arg<P>(std::forward<A>(a))...); }
+};
+
+template <auto F>
+static void launch_boxes_now(const BoxParams<typename KTraits<F>::Args>& bp, dim3 block, size_t smem, cudaStream_t st) {
+    const dim3 grid(bp.first[bp.count]);
+    if constexpr (KTraits<F>::maxThreads == 0)
+        k_boxes<F><<<grid, block, smem, st>>>(bp);
+    else if constexpr (KTraits<F>::minBlocks == 0)
+        k_boxes_t<F><<<grid, block, smem, st>>>(bp);
+    else
+        k_boxes_tb<F><<<grid, block, smem, st>>>(bp);
+}
+
+// ---------------------------------------------------------------------------
+// Recording of an evaluation's device work (fused multi-box evaluation): while a thread
+// has a recorder, launch<F>() and the op_* helpers append operations to it instead of
+// issuing them.  Streams and events are dropped: the operations are kept in issue
+// order, which is a valid serial order of the evaluation (every dependency, by stream
+// order or by event, points from an earlier-issued operation to a later one).
+struct RecKernel {
+    dim3 grid, block;
+    size_t smem = 0;
+    virtual ~RecKernel() = default;
+    virtual const void* body() const = 0;  // one address per kernel body
+    // one launch (or one per BoxParams::kBoxes boxes) of this body for all of `group`
+    virtual void launch_group(const std::vector<const RecKernel*>& group, cudaStream_t st) const = 0;
+};
+template <auto F>
+struct RecKernelOf : RecKernel {
+    typename KTraits<F>::Args args;
+    static const void* tag() {
+        static const char t = 0;
+        return &t;
+    }
+    const void* body() const override { return tag(); }
+    void launch_group(const std::vector<const RecKernel*>& group, cudaStream_t st) const override {
+        using BP = BoxParams<typename KTraits<F>::Args>;
+        std::unique_ptr<BP> bp(new BP());
+        for (size_t s = 0; s < group.size(); s += BP::kBoxes) {
+            const size_t m = std::min<size_t>(BP::kBoxes, group.size() - s);
+            bp->count = (int) m;
+            unsigned total = 0;
+            size_t smemMax = 0;
+            for (size_t i = 0; i < m; ++i) {
+                const auto* r = static_cast<const RecKernelOf<F>*>(group[s + i]);
+                bp->first[i] = total;
+                bp->args[i] = r->args;
+                total += r->grid.x;
+                smemMax = std::max(smemMax, r->smem);
+            }
+            bp->first[m] = total;
+            launch_boxes_now<F>(*bp, block, smemMax, st);
+            ++t_launches;
+        }
+    }
+};
+
+struct RecOp {
+    enum Kind { KERNEL, FILL, COPY, FFT } kind;
+    std::unique_ptr<RecKernel> k;                // KERNEL
+    void* dst = nullptr;                         // FILL, COPY, FFT (output grid)
+    const void* src = nullptr;                   // COPY, FFT (input grid)
+    size_t bytes = 0;                            // FILL, COPY
+    int value = 0;                               // FILL (byte value)
+    int fftDims[3] = {0, 0, 0}, fftPrec = 0, fftForward = 0;  // FFT: grid, 4 or 8 byte reals, direction
+};
+
+struct OpRecorder {
+    std::vector<RecOp> ops;
+};
+static thread_local OpRecorder* t_recorder = nullptr;
+
+template <auto F, class... A>
+static inline void launch(dim3 grid, dim3 block, size_t smem, cudaStream_t st, A&&... a) {
+    using L = Launcher<F, typename KTraits<F>::Args>;
+    if (t_recorder) {
+        if (grid.y != 1 || grid.z != 1) throw std::logic_error("recorded launches must be one-dimensional");
+        std::unique_ptr<RecKernelOf<F>> r(new RecKernelOf<F>());
+        r->grid = grid;
+        r->block = block;
+        r->smem = smem;
+        r->args = L::pack(std::forward<A>(a)...);
+        RecOp op;
+        op.kind = RecOp::KERNEL;
+        op.k = std::move(r);
+        t_recorder->ops.push_back(std::move(op));
+        return;
+    }
+    L::one(grid, block, smem, st, std::forward<A>(a)...);
     ++t_launches;
 }
 // cuFFT executions and cub sorts (library code launching its own kernels).
 static thread_local long long t_library_calls = 0;
+
+// Device work other than kernels, recorded like launches while a recorder is active.
+static inline void op_memset(void* p, int value, size_t bytes, cudaStream_t st) {
+    if (t_recorder) {
+        RecOp op;
+        op.kind = RecOp::FILL;
+        op.dst = p;
+        op.value = value;
+        op.bytes = bytes;
+        t_recorder->ops.push_back(std::move(op));
+        return;
+    }
+    CUDA_CHECK(cudaMemsetAsync(p, value, bytes, st));
+}
+// A device-to-device copy, or a device-to-host copy into pinned (device-mapped) memory.
+static inline void op_copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
+    if (t_recorder) {
+        RecOp op;
+        op.kind = RecOp::COPY;
+        op.dst = dst;
+        op.src = src;
+        op.bytes = bytes;
+        t_recorder->ops.push_back(std::move(op));
+        return;
+    }
+    CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, kind, st));
+}
+static inline void op_record(cudaEvent_t ev, cudaStream_t st) {
+    if (!t_recorder) CUDA_CHECK(cudaEventRecord(ev, st));
+}
+static inline void op_wait(cudaStream_t st, cudaEvent_t ev) {
+    if (!t_recorder) CUDA_CHECK(cudaStreamWaitEvent(st, ev, 0));
+}
 
 // Device allocations made by any buffer so far: captured graphs key on it, so that no
 // graph outlives a pointer it holds.
@@ -174,35 +380,55 @@ struct PmeStage {
     }
     void bsplines(int n, int npad, const int* sorted, const double* wpos, const BoxDev& box, cudaStream_t st) {
         if (order == 5)
-            launch(k_bsplines<real, 5>, nblk(npad, 128), 128, 0, st, npad, n, sorted, wpos, box, theta.p, igrid.p);
+            launch<k_bsplines<real, 5>>(nblk(npad, 128), 128, 0, st, npad, n, sorted, wpos, box, theta.p, igrid.p);
         else
-            launch(k_bsplines<real, 6>, nblk(npad, 128), 128, 0, st, npad, n, sorted, wpos, box, theta.p, igrid.p);
+            launch<k_bsplines<real, 6>>(nblk(npad, 128), 128, 0, st, npad, n, sorted, wpos, box, theta.p, igrid.p);
     }
     template <int NCOMP>
     void spread(int n, int npad, const BoxDev& box, const real* mf, const int* skip, cudaStream_t st) {
         const long long threads = (long long) n * order * order;
         if (order == 5)
-            launch(k_spread<real, 5, NCOMP>, nblk(threads, 256), 256, 0, st, n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
+            launch<k_spread<real, 5, NCOMP>>(nblk(threads, 256), 256, 0, st, n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
         else
-            launch(k_spread<real, 6, NCOMP>, nblk(threads, 256), 256, 0, st, n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
-        launch(k_grid_finish<real>, std::min<long long>(nblk(G, 256), (long long) sms * 16), 256, 0, st, G, acc.p, rgrid.p,
+            launch<k_spread<real, 6, NCOMP>>(nblk(threads, 256), 256, 0, st, n, npad, box, mf, theta.p, igrid.p, acc.p, skip);
+        launch<k_grid_finish<real>>(std::min<long long>(nblk(G, 256), (long long) sms * 16), 256, 0, st, G, acc.p, rgrid.p,
                skip);
     }
+    // Real-to-half-complex transform of rgrid into cgrid (forward) or back (inverse).
+    void fft(bool forward) {
+        if (t_recorder) {
+            RecOp op;
+            op.kind = RecOp::FFT;
+            op.src = forward ? (const void*) rgrid.p : (const void*) cgrid.p;
+            op.dst = forward ? (void*) cgrid.p : (void*) rgrid.p;
+            op.fftDims[0] = nx;
+            op.fftDims[1] = ny;
+            op.fftDims[2] = nz;
+            op.fftPrec = (int) sizeof(real);
+            op.fftForward = forward ? 1 : 0;
+            t_recorder->ops.push_back(std::move(op));
+            return;
+        }
+        if (forward)
+            FftTypes<real>::exec_fwd(fwd, rgrid.p, cgrid.p);
+        else
+            FftTypes<real>::exec_inv(inv, cgrid.p, rgrid.p);
+    }
     void convolve(const double* influence, const int* skip, cudaStream_t st) {
-        FftTypes<real>::exec_fwd(fwd, rgrid.p, cgrid.p);
-        launch(k_convolve<real>, std::min<long long>(nblk(Gh, 256), (long long) sms * 16), 256, 0, st, Gh, influence,
+        fft(true);
+        launch<k_convolve<real>>(std::min<long long>(nblk(Gh, 256), (long long) sms * 16), 256, 0, st, Gh, influence,
                cgrid.p, skip);
-        FftTypes<real>::exec_inv(inv, cgrid.p, rgrid.p);
+        fft(false);
     }
     template <int NTERM>
     void gather(int n, int npad, const BoxDev& box, real* phi, const int* skip, cudaStream_t st) {
         if (order == 5) {
             using G = GatherShape<real, 5, NTERM>;
-            launch(k_gather<real, 5, NTERM>, nblk(npad, G::atoms), G::threads, 0, st, n, npad, box, theta.p, igrid.p,
+            launch<k_gather<real, 5, NTERM>>(nblk(npad, G::atoms), G::threads, 0, st, n, npad, box, theta.p, igrid.p,
                    rgrid.p, phi, skip);
         } else {
             using G = GatherShape<real, 6, NTERM>;
-            launch(k_gather<real, 6, NTERM>, nblk(npad, G::atoms), G::threads, 0, st, n, npad, box, theta.p, igrid.p,
+            launch<k_gather<real, 6, NTERM>>(nblk(npad, G::atoms), G::threads, 0, st, n, npad, box, theta.p, igrid.p,
                    rgrid.p, phi, skip);
         }
     }
@@ -381,12 +607,12 @@ struct Context {
     double* refHost = nullptr;  // pinned: squared residual sum of the pending check
     int refOuter = 0, refTotal = 0;
     void fork_pme() {
-        CUDA_CHECK(cudaEventRecord(evFork, stream));
-        CUDA_CHECK(cudaStreamWaitEvent(pmeStream, evFork, 0));
+        op_record(evFork, stream);
+        op_wait(pmeStream, evFork);
     }
     void join_pme() {
-        CUDA_CHECK(cudaEventRecord(evJoin, pmeStream));
-        CUDA_CHECK(cudaStreamWaitEvent(stream, evJoin, 0));
+        op_record(evJoin, pmeStream);
+        op_wait(stream, evJoin);
     }
     bool ownStream = false;
 
@@ -804,7 +1030,7 @@ struct Context {
             for (int i = 0; i < 3; ++i) box.A[j][i] = usePme ? set.grid[j] * R[i][j] : 0.0;
         if (usePme && std::memcmp(lastBox, b, sizeof(lastBox)) != 0) {
             const size_t Gh = (size_t) set.grid[0] * set.grid[1] * (set.grid[2] / 2 + 1);
-            launch(k_influence, std::min<long long>(nblk(Gh, 256), (long long) numSMs * 8), 256, 0, stream, box, set.ewald_alpha,
+            launch<k_influence>(std::min<long long>(nblk(Gh, 256), (long long) numSMs * 8), 256, 0, stream, box, set.ewald_alpha,
                    modx.p, mody.p, modz.p, L[0] * L[1] * L[2], influence.p);
             CUDA_CHECK(cudaGetLastError());
             std::memcpy(lastBox, b, sizeof(lastBox));
@@ -942,15 +1168,21 @@ struct Context {
             int colBits = 1;
             while (colBits < 28 && (1LL << colBits) < (long long) ncx * ncy) ++colBits;
             const int zBits = std::min(16, 32 - colBits);
-            launch(k_sort_keys, nblk(n, 256), 256, 0, st, n, pos.p, box, ncx, ncy, zBits, keys.p, orderAlt.p, wpos.p);
-            ++t_library_calls;
-            CUDA_CHECK(cub::DeviceRadixSort::SortPairs(cubTemp.p, cubBytes, keys.p, keysAlt.p, orderAlt.p, order.p, n, 0,
-                                                        colBits + zBits, st));
+            launch<k_sort_keys>(nblk(n, 256), 256, 0, st, n, pos.p, box, ncx, ncy, zBits, keys.p, orderAlt.p, wpos.p);
+            if (t_recorder) {
+                // a recorded (fused multi-box) evaluation sorts each box in one block
+                if (n > kBlockSortMax) throw Error(MPID_ERR_INVALID, "fused batch: a box has more than 4096 atoms");
+                launch<k_sort_block>(1, 1024, 0, st, n, (const unsigned*) keys.p, (const int*) orderAlt.p, order.p);
+            } else {
+                ++t_library_calls;
+                CUDA_CHECK(cub::DeviceRadixSort::SortPairs(cubTemp.p, cubBytes, keys.p, keysAlt.p, orderAlt.p, order.p, n,
+                                                            0, colBits + zBits, st));
+            }
         } else {
             // No periodic box: keep the caller's order (all pairs interact).
-            launch(k_identity_order, nblk(n, 256), 256, 0, st, n, (const double*) pos.p, order.p, wpos.p);
+            launch<k_identity_order>(nblk(n, 256), 256, 0, st, n, (const double*) pos.p, order.p, wpos.p);
         }
-        launch(k_tile_bounds, nblk((long long) ntiles * 32, 128), 128, 0, st, n, ntiles, order.p, wpos.p, center.p,
+        launch<k_tile_bounds>(nblk((long long) ntiles * 32, 128), 128, 0, st, n, ntiles, order.p, wpos.p, center.p,
                half.p, centerF.p, halfF.p);
     }
 
@@ -965,13 +1197,13 @@ struct Context {
         const float cut2 = usePme ? (float) (listCut * listCut) : 3.0e38f;
         // erfc / quadrature segment boundary: alpha r = kQuadX
         const float quadR2 = usePme ? (float) std::pow(Prec<float>::kQuadX / set.ewald_alpha, 2) : 0.f;
-        CUDA_CHECK(cudaMemsetAsync(listMax.p, 0, 4 * sizeof(int), st));
-        launch(k_tile_list, ntiles, 32 * kTileListWarps, 0, st, ntiles, center.p, centerF.p, halfF.p, box, listCut,
+        op_memset(listMax.p, 0, 4 * sizeof(int), st);
+        launch<k_tile_list>(ntiles, 32 * kTileListWarps, 0, st, ntiles, center.p, centerF.p, halfF.p, box, listCut,
                usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, shD.p, shDF.p, listMax.p);
-        launch(k_atom_list<real>, ntiles, 32 * kListWarps, 0, st, ntiles, npad, (const real*) e.off.p,
+        launch<k_atom_list<real>>(ntiles, 32 * kListWarps, 0, st, ntiles, npad, (const real*) e.off.p,
                (const int*) e.orig.p, (const int*) e.rank.p, box, cut2, quadR2, usePme ? 1 : 0, tcap, tileCount.p, tileJ.p, shF.p, covOff.p,
                covJ.p, covS.p, cap, countL.p, countS.p, loL.p, loS.p, tmaxL.p, tmaxS.p, list.p, listMax.p + 1);
-        CUDA_CHECK(cudaMemcpyAsync(hostMax, listMax.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        op_copy(hostMax, listMax.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, st);
         if (record) CUDA_CHECK(cudaEventRecord(evLists, st));
     }
 
@@ -1010,13 +1242,13 @@ struct Context {
     template <typename real>
     void prepare_engine(Engine<real>& e, bool main) {
         cudaStream_t st = stream;
-        launch(k_gather_atoms<real>, nblk(npad, 128), 128, 0, st, n, npad, order.p, mol(), pos.p, wpos.p, center.p, e.arrays(),
+        launch<k_gather_atoms<real>>(nblk(npad, 128), 128, 0, st, n, npad, order.p, mol(), pos.p, wpos.p, center.p, e.arrays(),
                                                                main ? mom64.p : nullptr, main ? prm64.p : nullptr);
         if (usePme) {
             e.pme.set_stream(pmeStream);
             e.pme.bsplines(n, npad, order.p, wpos.p, box, st);
             // the refinement engine spreads induced dipoles only
-            if (main) launch(k_frac_multipoles<real>, nblk(npad, 128), 128, 0, st, npad, box, e.mom.p, e.mf.p);
+            if (main) launch<k_frac_multipoles<real>>(nblk(npad, 128), 128, 0, st, npad, box, e.mom.p, e.mf.p);
         }
         CUDA_CHECK(cudaGetLastError());
     }
@@ -1033,14 +1265,14 @@ struct Context {
         PmeStage<real>& p = e.pme;
         timer.end(ps);
         timer.begin(ST_FFT, ps);
-        FftTypes<real>::exec_fwd(p.fwd, p.rgrid.p, p.cgrid.p);
+        p.fft(true);
         timer.end(ps);
         timer.begin(ST_PME, ps);
-        launch(k_convolve<real>, std::min<long long>(nblk(p.Gh, 256), (long long) p.sms * 16), 256, 0, ps, p.Gh,
+        launch<k_convolve<real>>(std::min<long long>(nblk(p.Gh, 256), (long long) p.sms * 16), 256, 0, ps, p.Gh,
                (const double*) influence.p, p.cgrid.p, skip);
         timer.end(ps);
         timer.begin(ST_FFT, ps);
-        FftTypes<real>::exec_inv(p.inv, p.cgrid.p, p.rgrid.p);
+        p.fft(false);
         timer.end(ps);
         timer.begin(ST_PME, ps);
     }
@@ -1053,7 +1285,7 @@ struct Context {
     template <typename real>
     void fixed_field(Engine<real>& e) {
         cudaStream_t st = stream;
-        CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
+        op_memset(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st);
         if (usePme) {
             fork_pme();
             cudaStream_t ps = pmeStream;
@@ -1064,10 +1296,10 @@ struct Context {
             timer.end(ps);
         }
         timer.begin(ST_FIXED_REAL, st);
-        launch(k_fixed_field<real>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), e.fieldFx.p);
+        launch<k_fixed_field<real>>(field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), e.fieldFx.p);
         timer.end(st);
         if (usePme) join_pme();
-        launch(k_record_fixed<real>, nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
+        launch<k_record_fixed<real>>(nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
                                                                usePme ? e.phiP.p : nullptr, e.arrays(), e.Efix.p, e.muD.p,
                                                                e.SE.p);
         CUDA_CHECK(cudaGetLastError());
@@ -1077,12 +1309,12 @@ struct Context {
     template <typename real>
     void dipole_field(Engine<real>& e, const real* mu, real* E, real* G, const int* skip, int nterm = 4) {
         cudaStream_t st = stream;
-        CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));
+        op_memset(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st);
         if (usePme) {
             fork_pme();
             cudaStream_t ps = pmeStream;
             timer.begin(ST_PME, ps);
-            launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, ps, npad, box, mu, e.mfd.p, skip);
+            launch<k_frac_dipoles<real>>(nblk(npad, 128), 128, 0, ps, npad, box, mu, e.mfd.p, skip);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, skip, ps);
             convolve(e, skip, ps);
             if (nterm == 4)
@@ -1097,20 +1329,20 @@ struct Context {
         timer.begin(mixed && sizeof(real) == 8 ? ST_REFINE_REAL : ST_DIPOLE_REAL, st);
         if (mixed && sizeof(real) == 8) {
             // residual refinement: real-space part in double-float on the FP32 pipes
-            launch(k_to_df, nblk(3LL * npad, 256), 256, 0, st, 3 * npad, (const double*) mu, muDF.p);
-            launch(k_dipole_field_df, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), df_radial(), df_atoms(),
+            launch<k_to_df>(nblk(3LL * npad, 256), 256, 0, st, 3 * npad, (const double*) mu, muDF.p);
+            launch<k_dipole_field_df>(field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), df_radial(), df_atoms(),
                    (const int*) e.orig.p, e.fieldFx.p);
         } else if (G) {
-            CUDA_CHECK(cudaMemsetAsync(e.gradFx.p, 0, 6 * (size_t) npad * 8, st));
-            launch(k_dipole_field<real, true, sizeof(real) == 8>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), mu, e.fieldFx.p,
+            op_memset(e.gradFx.p, 0, 6 * (size_t) npad * 8, st);
+            launch<k_dipole_field<real, true, sizeof(real) == 8>>(field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), mu, e.fieldFx.p,
                                                                                      e.gradFx.p, skip);
         } else {
-            launch(k_dipole_field<real, false, sizeof(real) == 8>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), mu,
+            launch<k_dipole_field<real, false, sizeof(real) == 8>>(field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), mu,
                                                                                       e.fieldFx.p, nullptr, skip);
         }
         timer.end(st);
         if (usePme) join_pme();
-        launch(k_dipole_field_total<real>, nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p, e.gradFx.p,
+        launch<k_dipole_field_total<real>>(nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p, e.gradFx.p,
                                                                      usePme ? e.phiT.p : nullptr, nterm, mu, E, G, skip);
         CUDA_CHECK(cudaGetLastError());
     }
@@ -1122,7 +1354,7 @@ struct Context {
         cudaStream_t st = stream;
         const int nb = nblk(npad, 256);
         const bool packed = sizeof(real) == 4;  // FP32: packed-operand pair kernel
-        launch(k_cg_direction_sroot<real>, nblk(npad, 128), 128, 0, st, npad, box, e.sroot.p, sc.p, first ? 1 : 0, r,
+        launch<k_cg_direction_sroot<real>>(nblk(npad, 128), 128, 0, st, npad, box, e.sroot.p, sc.p, first ? 1 : 0, r,
                p, e.sp.p, usePme ? e.mfd.p : (real*) nullptr, (const typename Vec4<real>::type*) e.prm.p,
                packed ? (typename Vec4<real>::type*) pack1.p : nullptr, done.p);
         if (usePme) {
@@ -1136,14 +1368,14 @@ struct Context {
         }
         timer.begin(ST_DIPOLE_REAL, st);
         if (packed)
-            launch(k_dipole_field_cg, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), cgR, (const float4*) pack0.p,
+            launch<k_dipole_field_cg>(field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), cgR, (const float4*) pack0.p,
                    (const float4*) pack1.p, npad, (const int*) e.orig.p, e.fieldFx.p, (const int*) done.p);
         else
-            launch(k_dipole_field<real, false, sizeof(real) == 8>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(),
+            launch<k_dipole_field<real, false, sizeof(real) == 8>>(field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(),
                    e.arrays(), (const real*) e.sp.p, e.fieldFx.p, (unsigned long long*) nullptr, (const int*) done.p);
         timer.end(st);
         if (usePme) join_pme();
-        launch(k_cg_matvec_finish<real>, nb, 256, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
+        launch<k_cg_matvec_finish<real>>(nb, 256, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
                usePme ? (const real*) e.phiT.p : (const real*) nullptr, (const real*) e.sroot.p, (const real*) p,
                (const real*) e.sp.p, q, partial.p, counters.p, sc.p, (const int*) done.p);
     }
@@ -1153,9 +1385,9 @@ struct Context {
     void precondition(Engine<real>& e, const real* r, real* p, bool first) {
         cudaStream_t st = stream;
         if (nchunksS > 0)
-            launch(k_precond_field<real>, std::max(1, nblk(ntiles * nchunksS, kWarpsPerBlock)), 32 * kWarpsPerBlock, 0, st,
+            launch<k_precond_field<real>>(std::max(1, nblk(ntiles * nchunksS, kWarpsPerBlock)), 32 * kWarpsPerBlock, 0, st,
                    nbr_list(), e.arrays(), r, e.precFx.p, (const int*) done.p);
-        launch(k_precond_finish<real>, nblk(npad, 256), 256, 0, st, n, npad, (const real*) e.sroot.p, e.precFx.p, r, e.zc.p,
+        launch<k_precond_finish<real>>(nblk(npad, 256), 256, 0, st, n, npad, (const real*) e.sroot.p, e.precFx.p, r, e.zc.p,
                p, first ? 1 : 0, partial.p, counters.p + 2, sc.p, (const int*) done.p);
     }
 
@@ -1222,17 +1454,17 @@ struct Context {
         }
         timer.begin(ST_DIPOLE_REAL, st);
         if (packed)
-            launch(k_dipole_field_cg, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), cgR, (const float4*) pack0.p,
+            launch<k_dipole_field_cg>(field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), cgR, (const float4*) pack0.p,
                    (const float4*) pack1.p, npad, (const int*) e.orig.p, e.fieldFx.p, (const int*) done.p);
         else
-            launch(k_dipole_field<real, false, sizeof(real) == 8>, field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(),
+            launch<k_dipole_field<real, false, sizeof(real) == 8>>(field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(),
                    e.arrays(), (const real*) e.sp.p, e.fieldFx.p, (unsigned long long*) nullptr, (const int*) done.p);
         timer.end(st);
         if (usePme) join_pme();
-        launch(k_cgcg_finish<real>, nb, 256, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
+        launch<k_cgcg_finish<real>>(nb, 256, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
                usePme ? (const real*) e.phiT.p : (const real*) nullptr, (const real*) e.sroot.p, (const real*) r,
                (const real*) e.sp.p, q, partial.p, counters.p, sc.p, (const int*) iter.p, (const int*) done.p);
-        launch(k_cgcg_update<real, xreal>, nb, 256, 0, st, n, npad, box, (const real*) e.sroot.p, sc.p, (const real*) q, p,
+        launch<k_cgcg_update<real, xreal>>(nb, 256, 0, st, n, npad, box, (const real*) e.sroot.p, sc.p, (const real*) q, p,
                cg_s_vector<real>(), x, r, e.sp.p, usePme ? e.mfd.p : (real*) nullptr,
                (const typename Vec4<real>::type*) e.prm.p, packed ? (typename Vec4<real>::type*) pack1.p : nullptr,
                partial.p, counters.p, target, iter.p, maxIter, done.p);
@@ -1247,7 +1479,7 @@ struct Context {
             return;
         }
         cg_matvec(e, pcg ? (const real*) e.zc.p : (const real*) r, p, q, first);
-        launch(k_cg_update_scalars<real, xreal>, nblk(npad, 256), 256, 0, stream, n, npad, e.sroot.p, sc.p, p, q, x, r,
+        launch<k_cg_update_scalars<real, xreal>>(nblk(npad, 256), 256, 0, stream, n, npad, e.sroot.p, sc.p, p, q, x, r,
                partial.p, counters.p + 1, target, iter.p, maxIter, done.p, pcg ? 1 : 0);
         if (pcg) precondition(e, r, p, false);
         CUDA_CHECK(cudaGetLastError());
@@ -1264,21 +1496,21 @@ struct Context {
         if (!(set.flags & MPID_FLAG_NEAR_FIELD_PCG)) {
             // single-reduction CG: r = b, x = p = s = 0, gamma, the test and the operator input
             const bool packed = sizeof(real) == 4;
-            launch(k_cgcg_start<real, xreal>, nb, 256, 0, st, n, npad, box, (const real*) e.sroot.p, b, x, r, p,
+            launch<k_cgcg_start<real, xreal>>(nb, 256, 0, st, n, npad, box, (const real*) e.sroot.p, b, x, r, p,
                    cg_s_vector<real>(), e.sp.p, usePme ? e.mfd.p : (real*) nullptr, (const typename Vec4<real>::type*) e.prm.p,
                    packed ? (typename Vec4<real>::type*) pack1.p : nullptr, partial.p, counters.p, sc.p, target, iter.p,
                    done.p);
-            CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));  // cleared again by each finish
+            op_memset(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st);  // cleared again by each finish
             CUDA_CHECK(cudaGetLastError());
             if (graph_mode() && maxIter > 1) cg_iteration(e, x, r, p, q, target, maxIter, true);
             return;
         }
-        launch(k_cg_start<real, xreal>, nb, 256, 0, st, npad, e.sroot.p, b, x, r, p, partial.p, nb);
-        launch(k_reduce_partials, 1, 1024, 0, st, nb, 2, partial.p, red.p, nullptr);
-        launch(k_cg_init_scalars, 1, 1, 0, st, sc.p, red.p, n, target, iter.p, done.p);
-        CUDA_CHECK(cudaMemsetAsync(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st));  // cleared again by each matvec
+        launch<k_cg_start<real, xreal>>(nb, 256, 0, st, npad, e.sroot.p, b, x, r, p, partial.p, nb);
+        launch<k_reduce_partials>(1, 1024, 0, st, nb, 2, partial.p, red.p, nullptr);
+        launch<k_cg_init_scalars>(1, 1, 0, st, sc.p, red.p, n, target, iter.p, done.p);
+        op_memset(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st);  // cleared again by each matvec
         if (set.flags & MPID_FLAG_NEAR_FIELD_PCG) {
-            CUDA_CHECK(cudaMemsetAsync(e.precFx.p, 0, 3 * (size_t) npad * 8, st));  // cleared by each application
+            op_memset(e.precFx.p, 0, 3 * (size_t) npad * 8, st);  // cleared by each application
             precondition(e, r, p, true);
         }
         CUDA_CHECK(cudaGetLastError());
@@ -1329,8 +1561,8 @@ struct Context {
                 }
             }
         }
-        CUDA_CHECK(cudaMemcpyAsync(hostDone + 256, iter.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaMemcpyAsync(hostSc, sc.p, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        op_copy(hostDone + 256, iter.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+        op_copy(hostSc, sc.p, 8 * sizeof(double), cudaMemcpyDeviceToHost, st);
         CUDA_CHECK(cudaStreamSynchronize(st));
         const int used = hostDone[256];
         if (finalMetric) *finalMetric = hostSc[6];
@@ -1461,7 +1693,7 @@ struct Context {
 
     template <typename real>
     void alpha_times(Engine<real>& e, const real* E, real* out) {
-        launch(k_alpha_times<real>, nblk(npad, 128), 128, 0, stream, npad, e.alab.p, E, out);
+        launch<k_alpha_times<real>>(nblk(npad, 128), 128, 0, stream, npad, e.alab.p, E, out);
     }
 
     // Induced dipoles into e.mu (sorted) for the configured polarisation type.
@@ -1473,7 +1705,7 @@ struct Context {
         stats.refinement_steps = 0;
         stats.solver_residual = 0.0;
         if (set.polarization_type == MPID_DIRECT) {
-            CUDA_CHECK(cudaMemcpyAsync(e.mu.p, e.muD.p, n3 * sizeof(real), cudaMemcpyDeviceToDevice, st));
+            op_copy(e.mu.p, e.muD.p, n3 * sizeof(real), cudaMemcpyDeviceToDevice, st);
             return;
         }
         if (set.polarization_type == MPID_EXTRAPOLATED) {
@@ -1485,14 +1717,14 @@ struct Context {
                 cbar[i] = 0.0;
                 for (int j = i; j < nPT; ++j) cbar[i] += set.extrap_coeffs[j];
             }
-            CUDA_CHECK(cudaMemcpyAsync(ptMu, e.muD.p, n3 * sizeof(real), cudaMemcpyDeviceToDevice, st));
+            op_copy(ptMu, e.muD.p, n3 * sizeof(real), cudaMemcpyDeviceToDevice, st);
             for (int m = 0; m + 1 < nPT; ++m) {
                 dipole_field(e, ptMu + m * n3, ptE + m * n3, ptG + m * 2 * n3, nullptr, 10);
                 alpha_times(e, ptE + m * n3, ptMu + (m + 1) * n3);
             }
-            CUDA_CHECK(cudaMemsetAsync(e.mu.p, 0, n3 * sizeof(real), st));
+            op_memset(e.mu.p, 0, n3 * sizeof(real), st);
             for (int m = 0; m < nPT; ++m)
-                launch(k_axpy<real>, nblk((long long) n3, 256), 256, 0, st, (int) n3, real(cbar[m]), ptMu + m * n3, e.mu.p);
+                launch<k_axpy<real>>(nblk((long long) n3, 256), 256, 0, st, (int) n3, real(cbar[m]), ptMu + m * n3, e.mu.p);
             stats.solver_iterations = nPT - 1;
             CUDA_CHECK(cudaGetLastError());
             return;
@@ -1505,7 +1737,7 @@ struct Context {
         int it = cg_solve<double, double>(e, e.SE.p, y64.p, r64.p, p64.p, q64.p, set.mutual_eps, set.max_iter, &metric);
         stats.solver_iterations = it;
         stats.solver_residual = metric;
-        launch(k_mu_from_y<double, double>, nblk(npad, 128), 128, 0, stream, npad, e.sroot.p, y64.p, e.mu.p);
+        launch<k_mu_from_y<double, double>>(nblk(npad, 128), 128, 0, stream, npad, e.sroot.p, y64.p, e.mu.p);
         if (!(metric < set.mutual_eps)) not_converged(it, metric);
     }
 
@@ -1526,10 +1758,10 @@ struct Context {
     void mutual_mixed_start(Engine<float>& e) {
         cudaStream_t st = stream;
         const size_t n3 = 3 * (size_t) npad;
-        CUDA_CHECK(cudaMemsetAsync(Efix64.p, 0, n3 * 8, st));
-        launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3, e.Efix.p, Efix64.p);
-        CUDA_CHECK(cudaMemsetAsync(y64.p, 0, n3 * 8, st));
-        CUDA_CHECK(cudaMemcpyAsync(b32.p, e.SE.p, n3 * 4, cudaMemcpyDeviceToDevice, st));
+        op_memset(Efix64.p, 0, n3 * 8, st);
+        launch<k_axpy_to_double<float>>(nblk((long long) n3, 256), 256, 0, st, (int) n3, e.Efix.p, Efix64.p);
+        op_memset(y64.p, 0, n3 * 8, st);
+        op_copy(b32.p, e.SE.p, n3 * 4, cudaMemcpyDeviceToDevice, st);
     }
 
     // inner FP32 solves stop at half the target: the FP64 residual then meets the target
@@ -1552,20 +1784,20 @@ struct Context {
         cudaStream_t st = stream;
         const int nb = nblk(npad, 256);
         const size_t n3 = 3 * (size_t) npad;
-        launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3, x32.p, y64.p);
-        launch(k_mu_from_y<double, float>, nblk(npad, 128), 128, 0, st, npad, d.sroot.p, y64.p, e.mu.p);
-        CUDA_CHECK(cudaEventRecord(evRefStart, st));
+        launch<k_axpy_to_double<float>>(nblk((long long) n3, 256), 256, 0, st, (int) n3, x32.p, y64.p);
+        launch<k_mu_from_y<double, float>>(nblk(npad, 128), 128, 0, st, npad, d.sroot.p, y64.p, e.mu.p);
+        op_record(evRefStart, st);
         // the check, on the refinement streams (members swapped for the launches)
         RefStreams scope(*this);
         cudaStream_t rs = stream;
-        CUDA_CHECK(cudaStreamWaitEvent(rs, evRefStart, 0));
+        op_wait(rs, evRefStart);
         if (usePme) d.pme.set_stream(pmeStream);
-        launch(k_mu_from_y<double, double>, nblk(npad, 128), 128, 0, rs, npad, d.sroot.p, y64.p, d.mu.p);
+        launch<k_mu_from_y<double, double>>(nblk(npad, 128), 128, 0, rs, npad, d.sroot.p, y64.p, d.mu.p);
         dipole_field(d, d.mu.p, d.Etmp.p, (double*) nullptr, nullptr, 4);
-        launch(k_refine_residual, nb, 256, 0, rs, npad, d.sroot.p, Efix64.p, d.Etmp.p, y64.p, res64.p, res32.p, partial.p);
-        launch(k_reduce_partials, 1, 1024, 0, rs, nb, 1, partial.p, red.p, nullptr);
-        CUDA_CHECK(cudaMemcpyAsync(refHost, red.p, 8, cudaMemcpyDeviceToHost, rs));
-        CUDA_CHECK(cudaEventRecord(evRefDone, rs));
+        launch<k_refine_residual>(nb, 256, 0, rs, npad, d.sroot.p, Efix64.p, d.Etmp.p, y64.p, res64.p, res32.p, partial.p);
+        launch<k_reduce_partials>(1, 1024, 0, rs, nb, 1, partial.p, red.p, nullptr);
+        op_copy(refHost, red.p, 8, cudaMemcpyDeviceToHost, rs);
+        op_record(evRefDone, rs);
     }
 
     // The refinement streams and their fork/join events take the place of the main ones
@@ -1636,12 +1868,12 @@ struct Context {
     template <typename real>
     void finish(Engine<real>& e, real* ptMu, real* ptE, real* ptG) {
         cudaStream_t st = stream;
-        CUDA_CHECK(cudaMemsetAsync(forceFx.p, 0, 3 * (size_t) npad * 8, st));
-        CUDA_CHECK(cudaMemsetAsync(torqueFx.p, 0, 3 * (size_t) npad * 8, st));
+        op_memset(forceFx.p, 0, 3 * (size_t) npad * 8, st);
+        op_memset(torqueFx.p, 0, 3 * (size_t) npad * 8, st);
         const NbrList tc = field_list();
         const int eb = pair_tasks() * tc.split;
         if ((size_t) eb > energyBlocks.n) throw Error(MPID_ERR_CUDA, "energy partials too small");
-        CUDA_CHECK(cudaMemsetAsync(energyBlocks.p, 0, eb * sizeof(double), st));
+        op_memset(energyBlocks.p, 0, eb * sizeof(double), st);
         // The per-atom reciprocal/self terms and the FP64 energies of the covalently scaled
         // pairs run on the side stream after the reciprocal potential of the final induced
         // dipoles, beside the energy/force pair kernel on the main stream; both add into
@@ -1651,7 +1883,7 @@ struct Context {
         cudaStream_t ps = pmeStream;
         if (usePme) {
             timer.begin(ST_PME, ps);
-            launch(k_frac_dipoles<real>, nblk(npad, 128), 128, 0, ps, npad, box, e.mu.p, e.mfd.p, nullptr);
+            launch<k_frac_dipoles<real>>(nblk(npad, 128), 128, 0, ps, npad, box, e.mu.p, e.mfd.p, nullptr);
             e.pme.template spread<4>(n, npad, box, e.mfd.p, nullptr, ps);
             convolve(e, nullptr, ps);
             e.pme.template gather<35>(n, npad, box, e.phiD.p, nullptr, ps);
@@ -1672,43 +1904,43 @@ struct Context {
         // per-atom work is long: blocks small enough that a small system spans the SMs
         const int rb = npad >= 256 * 2 * numSMs ? 256 : (npad >= 128 * numSMs ? 128 : (npad >= 64 * numSMs ? 64 : 32));
         const int nb = nblk(npad, rb);
-        launch(k_recip_self<real>, nb, rb, 0, ps, n, npad, box, set.ewald_alpha, set.polarization_type,
+        launch<k_recip_self<real>>(nb, rb, 0, ps, n, npad, box, set.ewald_alpha, set.polarization_type,
                usePme ? e.phiP.p : nullptr, e.phiD.p, e.mu.p, e.arrays(), mom64.p, opt, forceFx.p, torqueFx.p,
                energyPartial.p);
-        launch(k_reduce_partials, 1, 1024, 0, ps, nb, 1, energyPartial.p, energyOut.p, nullptr);
+        launch<k_reduce_partials>(1, 1024, 0, ps, nb, 1, energyPartial.p, energyOut.p, nullptr);
         if (nScaled) {
             const int sb = nblk(nScaled, 128);
             const int muIsFloat = sizeof(real) == 4 ? 1 : 0;
             if (set.polarization_type == MPID_MUTUAL)
-                launch(k_scaled_pair_energy<true>, sb, 128, 0, ps, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad,
+                launch<k_scaled_pair_energy<true>>(sb, 128, 0, ps, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad,
                        mom64.p, prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0, set.cutoff,
                        usePme ? set.ewald_alpha : 0.0, set.default_thole, scaledPartial.p);
             else
-                launch(k_scaled_pair_energy<false>, sb, 128, 0, ps, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad,
+                launch<k_scaled_pair_energy<false>>(sb, 128, 0, ps, nScaled, scaledPairs.p, scaledScale.p, e.rank.p, npad,
                        mom64.p, prm64.p, e.mu.p, muIsFloat, pos.p, box, usePme ? 1 : 0, set.cutoff,
                        usePme ? set.ewald_alpha : 0.0, set.default_thole, scaledPartial.p);
-            launch(k_reduce_partials, 1, 1024, 0, ps, sb, 1, scaledPartial.p, energyOut.p + 2, nullptr);
+            launch<k_reduce_partials>(1, 1024, 0, ps, sb, 1, scaledPartial.p, energyOut.p + 2, nullptr);
         } else {
-            CUDA_CHECK(cudaMemsetAsync(energyOut.p + 2, 0, sizeof(double), ps));
+            op_memset(energyOut.p + 2, 0, sizeof(double), ps);
         }
         timer.end(ps);
         timer.begin(ST_PAIR, st);
         const bool exact = (set.flags & MPID_FLAG_EXACT_ANISO_TORQUE) != 0;
         const AtomArrays<real> aa = e.arrays();
         if (set.polarization_type == MPID_MUTUAL && !exact)
-            launch(k_electrostatics<real, true, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+            launch<k_electrostatics<real, true, true, true>>(field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                              torqueFx.p, energyBlocks.p);
         else if (set.polarization_type == MPID_MUTUAL)
-            launch(k_electrostatics<real, true, false, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+            launch<k_electrostatics<real, true, false, true>>(field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
         else
-            launch(k_electrostatics<real, false, true, true>, field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
+            launch<k_electrostatics<real, false, true, true>>(field_blocks(), 32 * kWarpsPerBlock, 0, st, tc, aa, e.mu.p, forceFx.p,
                                                                                               torqueFx.p, energyBlocks.p);
         timer.end(st);
         join_pme();
         timer.begin(ST_FINISH, st);
-        launch(k_reduce_partials, 1, 1024, 0, st, eb, 1, energyBlocks.p, energyOut.p + 1, nullptr);
-        launch(k_torque_map, nblk(n, 128), 128, 0, st, n, npad, pos.p, mol(), e.rank.p, torqueFx.p, forceFx.p);
+        launch<k_reduce_partials>(1, 1024, 0, st, eb, 1, energyBlocks.p, energyOut.p + 1, nullptr);
+        launch<k_torque_map>(nblk(n, 128), 128, 0, st, n, npad, pos.p, mol(), e.rank.p, torqueFx.p, forceFx.p);
         timer.end(st);
         CUDA_CHECK(cudaGetLastError());
     }
@@ -1734,22 +1966,22 @@ struct Context {
             replay(graph_key(kSegSetup), [&] {
                 sort_and_tiles();
                 prepare_engine(e, true);
-                launch(k_pack_atoms, nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
+                launch<k_pack_atoms>(nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
                        pack0.p);
                 if (ed) {
                     // the FP64 engine of the residual check is prepared on the check's stream,
                     // beside the list build (it is first read by the check)
-                    CUDA_CHECK(cudaEventRecord(evRefStart, st));
-                    CUDA_CHECK(cudaStreamWaitEvent(refStream, evRefStart, 0));
+                    op_record(evRefStart, st);
+                    op_wait(refStream, evRefStart);
                     {
                         RefStreams scope(*this);
                         prepare_engine(*ed, false);
-                        launch(k_df_atoms, nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p,
+                        launch<k_df_atoms>(nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p,
                                tholeDF.p, dampDF.p);
                     }
                     if (graph_mode()) {  // a captured side stream joins back before the capture ends
-                        CUDA_CHECK(cudaEventRecord(evRefStart, refStream));
-                        CUDA_CHECK(cudaStreamWaitEvent(st, evRefStart, 0));
+                        op_record(evRefStart, refStream);
+                        op_wait(st, evRefStart);
                     }
                 }
                 launch_lists(e, false);
@@ -1771,7 +2003,7 @@ struct Context {
                 solve_dipoles(e, ptMuF.p, ptEF.p, ptGF.p);
                 finish(e, ptMuF.p, ptEF.p, ptGF.p);
             }
-            launch(k_forces_out, nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, d_forces);
+            launch<k_forces_out>(nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, d_forces);
         } else {
             Engine<double>& e = *ed;
             sort_and_tiles();
@@ -1787,7 +2019,7 @@ struct Context {
             else
                 solve_dipoles(e, ptMuD.p, ptED.p, ptGD.p);
             finish(e, ptMuD.p, ptED.p, ptGD.p);
-            launch(k_forces_out, nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, d_forces);
+            launch<k_forces_out>(nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, d_forces);
         }
         CUDA_CHECK(cudaGetLastError());
         double eparts[3] = {0, 0, 0};  // reciprocal + self, real space, scaled pairs
@@ -1850,19 +2082,19 @@ struct Context {
             Engine<float>& e = *ef;
             sort_and_tiles();
             prepare_engine(e, true);
-            launch(k_pack_atoms, nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
+            launch<k_pack_atoms>(nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
                    pack0.p);
             if (ed) {
-                CUDA_CHECK(cudaEventRecord(evRefStart, st));
-                CUDA_CHECK(cudaStreamWaitEvent(refStream, evRefStart, 0));
+                op_record(evRefStart, st);
+                op_wait(refStream, evRefStart);
                 {
                     RefStreams scope(*this);
                     prepare_engine(*ed, false);
-                    launch(k_df_atoms, nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p, tholeDF.p,
+                    launch<k_df_atoms>(nblk(npad, 128), 128, 0, stream, npad, ed->off.p, ed->prm.p, offDF.p, tholeDF.p,
                            dampDF.p);
                 }
-                CUDA_CHECK(cudaEventRecord(evRefStart, refStream));
-                CUDA_CHECK(cudaStreamWaitEvent(st, evRefStart, 0));
+                op_record(evRefStart, refStream);
+                op_wait(st, evRefStart);
             }
             launch_lists(e, false);  // the list maxima go to hostMax
             fixed_field(e);
@@ -1870,15 +2102,15 @@ struct Context {
                 mutual_mixed_start(e);
                 cg_begin<float, float>(e, b32.p, x32.p, r32.p, p32.p, q32.p, inner_target(), K);
                 for (int i = 0; i < K; ++i) cg_iteration<float, float>(e, x32.p, r32.p, p32.p, q32.p, inner_target(), K, i == 0);
-                CUDA_CHECK(cudaMemcpyAsync(hostDone + 256, iter.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+                op_copy(hostDone + 256, iter.p, sizeof(int), cudaMemcpyDeviceToHost, st);
                 launch_check(e, *ed);  // the FP64 residual to refHost, beside the force/energy phase
                 finish(e, ptMuF.p, ptEF.p, ptGF.p);
-                CUDA_CHECK(cudaStreamWaitEvent(st, evRefDone, 0));
+                op_wait(st, evRefDone);
             } else {
                 solve_dipoles(e, ptMuF.p, ptEF.p, ptGF.p);
                 finish(e, ptMuF.p, ptEF.p, ptGF.p);
             }
-            launch(k_forces_out, nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, forcesOut.p);
+            launch<k_forces_out>(nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, forcesOut.p);
         } else {
             Engine<double>& e = *ed;
             sort_and_tiles();
@@ -1889,17 +2121,17 @@ struct Context {
                 cg_begin<double, double>(e, e.SE.p, y64.p, r64.p, p64.p, q64.p, set.mutual_eps, K);
                 for (int i = 0; i < K; ++i)
                     cg_iteration<double, double>(e, y64.p, r64.p, p64.p, q64.p, set.mutual_eps, K, i == 0);
-                CUDA_CHECK(cudaMemcpyAsync(hostDone + 256, iter.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-                CUDA_CHECK(cudaMemcpyAsync(hostSc, sc.p, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
-                launch(k_mu_from_y<double, double>, nblk(npad, 128), 128, 0, st, npad, e.sroot.p, y64.p, e.mu.p);
+                op_copy(hostDone + 256, iter.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+                op_copy(hostSc, sc.p, 8 * sizeof(double), cudaMemcpyDeviceToHost, st);
+                launch<k_mu_from_y<double, double>>(nblk(npad, 128), 128, 0, st, npad, e.sroot.p, y64.p, e.mu.p);
                 finish(e, ptMuD.p, ptED.p, ptGD.p);
             } else {
                 solve_dipoles(e, ptMuD.p, ptED.p, ptGD.p);
                 finish(e, ptMuD.p, ptED.p, ptGD.p);
             }
-            launch(k_forces_out, nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, forcesOut.p);
+            launch<k_forces_out>(nblk(n, 128), 128, 0, st, n, npad, e.rank.p, forceFx.p, forcesOut.p);
         }
-        CUDA_CHECK(cudaMemcpyAsync(hostEparts, energyOut.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        op_copy(hostEparts, energyOut.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st);
         if (mg || pg) {
             gradPrepared = false;
             if (mg) multipole_gradient_launches();
@@ -1913,7 +2145,7 @@ struct Context {
     bool ensure_batch_graph(bool mg, bool pg) {
         if (mg || pg) gradient_buffers(mg, pg);  // allocations before the key and the capture
         if (!hostEparts) CUDA_CHECK(cudaMallocHost(&hostEparts, 3 * sizeof(double)));
-        const int K = set.polarization_type == MPID_MUTUAL ? std::max(1, std::min(set.max_iter, predictedIters + 1)) : 0;
+        const int K = batch_iterations();
         std::vector<long long> key = graph_key(kSegFull);
         const long long more[] = {K, mg ? 1 : 0, pg ? 1 : 0};
         key_put(key, more, sizeof more);
@@ -1954,10 +2186,52 @@ struct Context {
         return true;
     }
 
+    // The context's evaluation recorded for a fused multi-box launch (the operations of
+    // batch_body in issue order, nothing issued), re-recorded when its shape changed;
+    // returns true if it was recorded now.  K: the CG iterations of the recording (the
+    // largest of the batch's boxes, so that every box issues the same sequence).
+    OpRecorder rec;
+    std::vector<long long> recKey;
+    unsigned long long recGeneration = 0;
+    bool ensure_recording(bool mg, bool pg, int K) {
+        if (mg || pg) gradient_buffers(mg, pg);
+        if (!hostEparts) CUDA_CHECK(cudaMallocHost(&hostEparts, 3 * sizeof(double)));
+        std::vector<long long> key = graph_key(kSegFull);
+        const long long more[] = {K, mg ? 1 : 0, pg ? 1 : 0};
+        key_put(key, more, sizeof more);
+        if (!rec.ops.empty() && recKey == key) return false;
+        rec.ops.clear();
+        recKey.clear();
+        const bool wasActive = graphsActive;
+        graphsActive = false;
+        timer.off = true;
+        OpRecorder* prev = t_recorder;
+        t_recorder = &rec;
+        try {
+            batch_body(mg, pg, K);
+        } catch (...) {
+            t_recorder = prev;
+            timer.off = false;
+            graphsActive = wasActive;
+            rec.ops.clear();
+            throw;
+        }
+        t_recorder = prev;
+        timer.off = false;
+        graphsActive = wasActive;
+        recKey = key;
+        recGeneration = ++graphClock;
+        return true;
+    }
+    // CG iterations a batch evaluation of this context runs (the last solve's plus one).
+    int batch_iterations() const {
+        return set.polarization_type == MPID_MUTUAL ? std::max(1, std::min(set.max_iter, predictedIters + 1)) : 0;
+    }
+
     // After a batch launch: whether this context's results stand (its lists fitted the
     // capacities and work items the graph was built with, its solver converged).  Also
     // fills the statistics of the evaluation.
-    bool batch_ok() {
+    bool batch_ok(long long launches, long long library) {
         const int mTiles = hostMax[0], mTotal = hostMax[1], mL = hostMax[2], mS = hostMax[3];
         lastTiles = mTiles;
         lastMaxList = mTotal;
@@ -1986,8 +2260,8 @@ struct Context {
         stats.energy_parts[0] = hostEparts[0];
         stats.energy_parts[1] = hostEparts[1];
         stats.energy_parts[2] = hostEparts[2];
-        stats.kernel_launches = (int) full.nodes;
-        stats.library_calls = (int) full.library;
+        stats.kernel_launches = (int) launches;
+        stats.library_calls = (int) library;
         stats.graph_replays = 1;
         for (int k = 0; k < ST_COUNT; ++k) {
             stats.ms_stage[k] = 0.0;
@@ -2049,14 +2323,14 @@ struct Context {
         const int* rk = mixed ? ef->rank.p : ed->rank.p;
         for (int pass = 0; pass < 2; ++pass) {
             if (mixed)
-                launch(k_moment_partials<float>, nb, 256, 0, st, n, npad, pass, (const double*) pos.p,
+                launch<k_moment_partials<float>>(nb, 256, 0, st, n, npad, pass, (const double*) pos.p,
                        (const double*) masses.p, rk, (const double*) mom64.p, (const float*) ef->mu.p,
                        (const double*) momentRed.p, momentPartial.p);
             else
-                launch(k_moment_partials<double>, nb, 256, 0, st, n, npad, pass, (const double*) pos.p,
+                launch<k_moment_partials<double>>(nb, 256, 0, st, n, npad, pass, (const double*) pos.p,
                        (const double*) masses.p, rk, (const double*) mom64.p, (const double*) ed->mu.p,
                        (const double*) momentRed.p, momentPartial.p);
-            launch(k_reduce_partials, 1, 1024, 0, st, nb, pass == 0 ? 4 : 16, (const double*) momentPartial.p,
+            launch<k_reduce_partials>(1, 1024, 0, st, nb, pass == 0 ? 4 : 16, (const double*) momentPartial.p,
                    momentRed.p, (const int*) nullptr);
         }
         double v[16];
@@ -2091,11 +2365,11 @@ struct Context {
         gridOut.alloc(ngrid);
         CUDA_CHECK(cudaMemcpyAsync(gridPts.p, hostGrid, 3 * (size_t) ngrid * 8, cudaMemcpyHostToDevice, st));
         if (mixed)
-            launch(k_potential_grid<float>, nblk(ngrid, 128), 128, 0, st, n, npad, ngrid, (const double*) gridPts.p,
+            launch<k_potential_grid<float>>(nblk(ngrid, 128), 128, 0, st, n, npad, ngrid, (const double*) gridPts.p,
                    (const double*) wpos.p, (const int*) ef->rank.p, (const double*) mom64.p, (const float*) ef->mu.p, box,
                    usePme ? 1 : 0, gridOut.p);
         else
-            launch(k_potential_grid<double>, nblk(ngrid, 128), 128, 0, st, n, npad, ngrid, (const double*) gridPts.p,
+            launch<k_potential_grid<double>>(nblk(ngrid, 128), 128, 0, st, n, npad, ngrid, (const double*) gridPts.p,
                    (const double*) wpos.p, (const int*) ed->rank.p, (const double*) mom64.p, (const double*) ed->mu.p,
                    box, usePme ? 1 : 0, gridOut.p);
         CUDA_CHECK(cudaMemcpyAsync(out, gridOut.p, (size_t) ngrid * 8, cudaMemcpyDeviceToHost, st));
@@ -2125,8 +2399,8 @@ struct Context {
         prepare_engine(d, true);
         if (dp != ed.get()) {
             const size_t n3 = 3 * (size_t) npad;
-            CUDA_CHECK(cudaMemsetAsync(d.mu.p, 0, n3 * 8, st));
-            launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3, (const float*) ef->mu.p,
+            op_memset(d.mu.p, 0, n3 * 8, st);
+            launch<k_axpy_to_double<float>>(nblk((long long) n3, 256), 256, 0, st, (int) n3, (const float*) ef->mu.p,
                    d.mu.p);
         }
         if (usePme) {
@@ -2135,7 +2409,7 @@ struct Context {
             d.pme.template spread<20>(n, npad, box, d.mf.p, nullptr, ps);
             d.pme.convolve(influence.p, nullptr, ps);
             d.pme.template gather<35>(n, npad, box, d.phiP.p, nullptr, ps);
-            launch(k_frac_dipoles<double>, nblk(npad, 128), 128, 0, ps, npad, box, (const double*) d.mu.p, d.mfd.p,
+            launch<k_frac_dipoles<double>>(nblk(npad, 128), 128, 0, ps, npad, box, (const double*) d.mu.p, d.mfd.p,
                    (const int*) nullptr);
             d.pme.template spread<4>(n, npad, box, d.mfd.p, nullptr, ps);
             d.pme.convolve(influence.p, nullptr, ps);
@@ -2197,7 +2471,7 @@ struct Context {
     void polarization_gradient_launches() {
         Engine<double>& d = gradient_engine();
         cudaStream_t st = stream;
-        CUDA_CHECK(cudaMemsetAsync(polFx.p, 0, (size_t) 2 * npad * 8, st));
+        op_memset(polFx.p, 0, (size_t) 2 * npad * 8, st);
         const int mutual = set.polarization_type == MPID_MUTUAL ? 1 : 0;
         // Extrapolated: the perturbation orders, their fields and the permanent field
         // (FP64 copies of the mixed path's FP32 ones for the FP64 parts)
@@ -2215,15 +2489,15 @@ struct Context {
             }
             if (mixed) {
                 const size_t n3 = 3 * (size_t) npad;
-                CUDA_CHECK(cudaMemsetAsync(gradPtMu.p, 0, (size_t) nPT * n3 * 8, st));
-                CUDA_CHECK(cudaMemsetAsync(gradPtE.p, 0, (size_t) std::max(nPT - 1, 1) * n3 * 8, st));
-                CUDA_CHECK(cudaMemsetAsync(gradEfix.p, 0, n3 * 8, st));
-                launch(k_axpy_to_double<float>, nblk((long long) nPT * n3, 256), 256, 0, st, (int) (nPT * n3),
+                op_memset(gradPtMu.p, 0, (size_t) nPT * n3 * 8, st);
+                op_memset(gradPtE.p, 0, (size_t) std::max(nPT - 1, 1) * n3 * 8, st);
+                op_memset(gradEfix.p, 0, n3 * 8, st);
+                launch<k_axpy_to_double<float>>(nblk((long long) nPT * n3, 256), 256, 0, st, (int) (nPT * n3),
                        (const float*) ptMuF.p, gradPtMu.p);
                 if (nPT > 1)
-                    launch(k_axpy_to_double<float>, nblk((long long) (nPT - 1) * n3, 256), 256, 0, st,
+                    launch<k_axpy_to_double<float>>(nblk((long long) (nPT - 1) * n3, 256), 256, 0, st,
                            (int) ((nPT - 1) * n3), (const float*) ptEF.p, gradPtE.p);
-                launch(k_axpy_to_double<float>, nblk((long long) n3, 256), 256, 0, st, (int) n3,
+                launch<k_axpy_to_double<float>>(nblk((long long) n3, 256), 256, 0, st, (int) n3,
                        (const float*) ef->Efix.p, gradEfix.p);
                 optF.mu = ptMuF.p;
                 optD.mu = gradPtMu.p;
@@ -2236,15 +2510,15 @@ struct Context {
         const int sL = gradient_split((long long) ntiles * nchunksL), sS = gradient_split((long long) ntiles * nchunksS);
         const int sA = gradient_split(pair_tasks());
         if (mixed && usePme) {
-            launch(k_polarization_gradient<float>, gradient_blocks(sL), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+            launch<k_polarization_gradient<float>>(gradient_blocks(sL), 32 * kWarpsPerBlock, 0, st, nbr_list(),
                    ef->arrays(), (const float*) ef->mu.p, mutual, optF, polFx.p, kSegErfc, sL);
-            launch(k_polarization_gradient<double>, gradient_blocks(sS), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+            launch<k_polarization_gradient<double>>(gradient_blocks(sS), 32 * kWarpsPerBlock, 0, st, nbr_list(),
                    d.arrays(), (const double*) d.mu.p, mutual, optD, polFx.p, kSegQuad, sS);
         } else {
-            launch(k_polarization_gradient<double>, gradient_blocks(sA), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+            launch<k_polarization_gradient<double>>(gradient_blocks(sA), 32 * kWarpsPerBlock, 0, st, nbr_list(),
                    d.arrays(), (const double*) d.mu.p, mutual, optD, polFx.p, kSegAll, sA);
         }
-        launch(k_polarization_gradient_finish<double>, nblk(n, 32), 32, 0, st, n, npad, (const int*) order.p, mol(),
+        launch<k_polarization_gradient_finish<double>>(nblk(n, 32), 32, 0, st, n, npad, (const int*) order.p, mol(),
                (const double*) pos.p, (const unsigned long long*) polFx.p, (const double*) d.mu.p, optD, efixD, ptED,
                polOut.p);
         CUDA_CHECK(cudaGetLastError());
@@ -2267,19 +2541,19 @@ struct Context {
     void multipole_gradient_launches() {
         Engine<double>& d = gradient_engine();
         cudaStream_t st = stream;
-        CUDA_CHECK(cudaMemsetAsync(gradFx.p, 0, (size_t) 20 * npad * 8, st));
+        op_memset(gradFx.p, 0, (size_t) 20 * npad * 8, st);
         const int sL = gradient_split((long long) ntiles * nchunksL), sS = gradient_split((long long) ntiles * nchunksS);
         const int sA = gradient_split(pair_tasks());
         if (mixed && usePme) {
-            launch(k_multipole_gradient<float>, gradient_blocks(sL), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+            launch<k_multipole_gradient<float>>(gradient_blocks(sL), 32 * kWarpsPerBlock, 0, st, nbr_list(),
                    ef->arrays(), (const float*) ef->mu.p, gradFx.p, kSegErfc, sL);
-            launch(k_multipole_gradient<double>, gradient_blocks(sS), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+            launch<k_multipole_gradient<double>>(gradient_blocks(sS), 32 * kWarpsPerBlock, 0, st, nbr_list(),
                    d.arrays(), (const double*) d.mu.p, gradFx.p, kSegQuad, sS);
         } else {
-            launch(k_multipole_gradient<double>, gradient_blocks(sA), 32 * kWarpsPerBlock, 0, st, nbr_list(),
+            launch<k_multipole_gradient<double>>(gradient_blocks(sA), 32 * kWarpsPerBlock, 0, st, nbr_list(),
                    d.arrays(), (const double*) d.mu.p, gradFx.p, kSegAll, sA);
         }
-        launch(k_gradient_finish<double>, nblk(n, 32), 32, 0, st, n, npad, box, usePme ? set.ewald_alpha : 0.0,
+        launch<k_gradient_finish<double>>(nblk(n, 32), 32, 0, st, n, npad, box, usePme ? set.ewald_alpha : 0.0,
                usePme ? 1 : 0, (const int*) order.p, mol(), (const double*) pos.p, (const unsigned long long*) gradFx.p,
                (const double*) d.phiP.p, (const double*) d.phiD.p, (const double*) mom64.p, (const double*) d.mu.p,
                gradOut.p);
@@ -2323,18 +2597,326 @@ struct Context {
         if (which < 0 || which > 3) throw Error(MPID_ERR_INVALID, "which must be 0, 1, 2 or 3");
         if (which == 3) {  // permanent field: reuse the induced-dipole output path with mom = 0
             if (mixed)
-                launch(k_dipoles_out<float>, nblk(n, 128), 128, 0, stream, n, npad, 0, ef->rank.p, ef->mom.p, ef->Efix.p, forcesOut.p);
+                launch<k_dipoles_out<float>>(nblk(n, 128), 128, 0, stream, n, npad, 0, ef->rank.p, ef->mom.p, ef->Efix.p, forcesOut.p);
             else
-                launch(k_dipoles_out<double>, nblk(n, 128), 128, 0, stream, n, npad, 0, ed->rank.p, ed->mom.p, ed->Efix.p, forcesOut.p);
+                launch<k_dipoles_out<double>>(nblk(n, 128), 128, 0, stream, n, npad, 0, ed->rank.p, ed->mom.p, ed->Efix.p, forcesOut.p);
         } else if (mixed)
-            launch(k_dipoles_out<float>, nblk(n, 128), 128, 0, stream, n, npad, which, ef->rank.p, ef->mom.p, ef->mu.p, forcesOut.p);
+            launch<k_dipoles_out<float>>(nblk(n, 128), 128, 0, stream, n, npad, which, ef->rank.p, ef->mom.p, ef->mu.p, forcesOut.p);
         else
-            launch(k_dipoles_out<double>, nblk(n, 128), 128, 0, stream, n, npad, which, ed->rank.p, ed->mom.p, ed->mu.p, forcesOut.p);
+            launch<k_dipoles_out<double>>(nblk(n, 128), 128, 0, stream, n, npad, which, ed->rank.p, ed->mom.p, ed->mu.p, forcesOut.p);
         CUDA_CHECK(cudaGetLastError());
         CUDA_CHECK(cudaMemcpyAsync(host, forcesOut.p, 3 * (size_t) n * 8, cudaMemcpyDeviceToHost, stream));
         CUDA_CHECK(cudaStreamSynchronize(stream));
     }
 };
+
+// ---------------------------------------------------------------------------
+// Fused multi-box evaluation.  Every box of a batch records its evaluation (the same
+// sequence of operations for every box; box-specific parameters and launch sizes).
+// Operation i of all boxes then becomes one multi-box operation:
+//  - a kernel: one k_boxes launch of its body over the blocks of all boxes (one per
+//    distinct block shape, and per BoxParams::kBoxes boxes);
+//  - a fill or copy: one k_fill_bytes / k_copy_bytes launch over all boxes;
+//  - an FFT: the boxes' grids are gathered into one array per grid size, transformed
+//    by one batched cuFFT plan (cufftPlanMany) per size, and scattered back.
+// The sequence is captured once as one CUDA graph and replayed while no box's recording
+// changes.  One stream: the boxes' own parallel branches (reciprocal space beside real
+// space) run one after the other, the parallelism being across boxes.
+template <auto F, class... A>
+static std::unique_ptr<RecKernel> make_rec(dim3 grid, dim3 block, size_t smem, A&&... a) {
+    std::unique_ptr<RecKernelOf<F>> r(new RecKernelOf<F>());
+    r->grid = grid;
+    r->block = block;
+    r->smem = smem;
+    r->args = Launcher<F, typename KTraits<F>::Args>::pack(std::forward<A>(a)...);
+    return r;
+}
+
+struct FusedBatch {
+    std::vector<unsigned long long> key;  // per box: context id, recording generation
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t evStart = nullptr, evStop = nullptr;
+    int device = -1;
+    long long launches = 0, library = 0;  // per replay
+    std::map<std::vector<int>, cufftHandle> plans;  // (bytes per real, forward, nx, ny, nz, count)
+    DBuf<unsigned char> arenaIn, arenaOut;
+    // Pinned staging of the host arrays, one DMA copy each way at the graph's start and
+    // end, scattered to and gathered from the boxes' device buffers by one launch each:
+    // per box, positions and incoming forces (6n doubles at inOff), forces, multipole and
+    // polarisation gradients (3n + 20n + 4n at outOff, the gradients when requested).
+    double* hostIn = nullptr;
+    double* hostOut = nullptr;
+    size_t hostInCount = 0, hostOutCount = 0;
+    DBuf<double> devIn, devOut;  // device copies of the staging (one DMA copy each way)
+    // The recorded copies into the boxes' pinned host variables (list maxima, solver
+    // state, FP64 residual, energies) land in devOut too, at `offset` doubles, and reach
+    // their host destination after the launch (in recording order): kernels writing the
+    // host memory directly would cost a host-memory round trip per box and operation.
+    struct HostCopy {
+        void* dst;
+        size_t offset, bytes;
+    };
+    std::vector<HostCopy> hostCopies;
+    std::vector<size_t> inOff, outOff;
+    void reset_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key.clear();
+    }
+    void release() {
+        reset_graph();
+        for (auto& kv : plans) cufftDestroy(kv.second);
+        plans.clear();
+        arenaIn.free();
+        arenaOut.free();
+        devIn.free();
+        devOut.free();
+        if (hostIn) cudaFreeHost(hostIn);
+        if (hostOut) cudaFreeHost(hostOut);
+        hostIn = hostOut = nullptr;
+        hostInCount = hostOutCount = 0;
+        if (evStart) cudaEventDestroy(evStart);
+        if (evStop) cudaEventDestroy(evStop);
+        evStart = evStop = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+// One launch copying every (dst, src, bytes) of `copies` (k_copy_bytes, one entry per copy).
+static void copy_group(const std::vector<std::tuple<void*, const void*, size_t>>& copies, cudaStream_t st) {
+    if (copies.empty()) return;
+    std::vector<std::unique_ptr<RecKernel>> tmp;
+    std::vector<const RecKernel*> grp;
+    for (const auto& c : copies) {
+        const size_t bytes = std::get<2>(c);
+        tmp.push_back(make_rec<k_copy_bytes>(std::max(1, std::min(64, nblk((long long) (bytes / 16), 256))), 256, 0,
+                                             (unsigned char*) std::get<0>(c), (const unsigned char*) std::get<1>(c), bytes));
+        grp.push_back(tmp.back().get());
+    }
+    grp[0]->launch_group(grp, st);
+}
+
+static size_t fft_bytes(const RecOp& op, bool input) {
+    const size_t G = (size_t) op.fftDims[0] * op.fftDims[1] * op.fftDims[2];
+    const size_t Gh = (size_t) op.fftDims[0] * op.fftDims[1] * (op.fftDims[2] / 2 + 1);
+    const bool realSide = (op.fftForward != 0) == input;
+    return realSide ? G * op.fftPrec : Gh * 2 * op.fftPrec;
+}
+static size_t align256(size_t b) { return (b + 255) & ~(size_t) 255; }
+
+// The boxes of an FFT operation grouped by grid size, each with its offsets in the
+// gather (input) and result (output) arrays; returns the bytes of both.
+struct FftSlot {
+    int box;
+    size_t in, out;
+};
+static std::map<std::vector<int>, std::vector<FftSlot>> fft_groups(const std::vector<const RecOp*>& ops, size_t& inBytes,
+                                                                   size_t& outBytes) {
+    std::map<std::vector<int>, std::vector<FftSlot>> groups;
+    for (int b = 0; b < (int) ops.size(); ++b)
+        groups[{ops[b]->fftDims[0], ops[b]->fftDims[1], ops[b]->fftDims[2]}].push_back({b, 0, 0});
+    inBytes = outBytes = 0;
+    for (auto& kv : groups) {
+        inBytes = align256(inBytes);
+        outBytes = align256(outBytes);
+        for (FftSlot& sl : kv.second) {
+            sl.in = inBytes;
+            sl.out = outBytes;
+            inBytes += fft_bytes(*ops[sl.box], true);
+            outBytes += fft_bytes(*ops[sl.box], false);
+        }
+    }
+    return groups;
+}
+
+static void fused_fft(FusedBatch& fb, const std::vector<const RecOp*>& ops, cudaStream_t st) {
+    size_t inBytes, outBytes;
+    const auto groups = fft_groups(ops, inBytes, outBytes);
+    const RecOp& a = *ops[0];
+    std::vector<std::unique_ptr<RecKernel>> gather, scatter;
+    for (const auto& kv : groups)
+        for (const FftSlot& sl : kv.second) {
+            const RecOp& op = *ops[sl.box];
+            const size_t bi = fft_bytes(op, true), bo = fft_bytes(op, false);
+            gather.push_back(make_rec<k_copy_bytes>(std::max(1, std::min(64, nblk((long long) (bi / 16), 256))), 256, 0,
+                                                    fb.arenaIn.p + sl.in, (const unsigned char*) op.src, bi));
+            scatter.push_back(make_rec<k_copy_bytes>(std::max(1, std::min(64, nblk((long long) (bo / 16), 256))), 256, 0,
+                                                     (unsigned char*) op.dst, (const unsigned char*) fb.arenaOut.p + sl.out, bo));
+        }
+    std::vector<const RecKernel*> g(gather.size()), s(scatter.size());
+    for (size_t i = 0; i < gather.size(); ++i) {
+        g[i] = gather[i].get();
+        s[i] = scatter[i].get();
+    }
+    g[0]->launch_group(g, st);
+    for (const auto& kv : groups) {
+        const std::vector<int> pk = {a.fftPrec, a.fftForward, kv.first[0], kv.first[1], kv.first[2], (int) kv.second.size()};
+        cufftHandle h = fb.plans.at(pk);
+        CUFFT_CHECK(cufftSetStream(h, st));
+        void* in = fb.arenaIn.p + kv.second[0].in;
+        void* out = fb.arenaOut.p + kv.second[0].out;
+        if (a.fftPrec == 4 && a.fftForward)
+            CUFFT_CHECK(cufftExecR2C(h, (cufftReal*) in, (cufftComplex*) out));
+        else if (a.fftPrec == 4)
+            CUFFT_CHECK(cufftExecC2R(h, (cufftComplex*) in, (cufftReal*) out));
+        else if (a.fftForward)
+            CUFFT_CHECK(cufftExecD2Z(h, (cufftDoubleReal*) in, (cufftDoubleComplex*) out));
+        else
+            CUFFT_CHECK(cufftExecZ2D(h, (cufftDoubleComplex*) in, (cufftDoubleReal*) out));
+        ++t_library_calls;
+    }
+    s[0]->launch_group(s, st);
+}
+
+// Checks that the boxes' recordings match operation by operation, prepares the FFT
+// plans and arrays, and captures the fused sequence as fb's graph.
+static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool mg, bool pg) {
+    const size_t L = boxes[0]->rec.ops.size();
+    for (Context* c : boxes)
+        if (c->rec.ops.size() != L)
+            throw Error(MPID_ERR_INVALID, "fused batch: the boxes' evaluations differ in their operations");
+    size_t inMax = 0, outMax = 0;
+    std::vector<std::vector<int>> planKeys;
+    std::vector<const RecOp*> ops(boxes.size());
+    for (size_t i = 0; i < L; ++i) {
+        const RecOp& a = boxes[0]->rec.ops[i];
+        for (size_t b = 0; b < boxes.size(); ++b) {
+            const RecOp& o = boxes[b]->rec.ops[i];
+            ops[b] = &o;
+            const bool same = o.kind == a.kind && (a.kind != RecOp::KERNEL || o.k->body() == a.k->body()) &&
+                              (a.kind != RecOp::FFT || (o.fftPrec == a.fftPrec && o.fftForward == a.fftForward));
+            if (!same) throw Error(MPID_ERR_INVALID, "fused batch: the boxes' evaluations differ in their operations");
+        }
+        if (a.kind == RecOp::FFT) {
+            size_t ib, ob;
+            for (const auto& kv : fft_groups(ops, ib, ob))
+                planKeys.push_back({a.fftPrec, a.fftForward, kv.first[0], kv.first[1], kv.first[2], (int) kv.second.size()});
+            inMax = std::max(inMax, ib);
+            outMax = std::max(outMax, ob);
+        }
+    }
+    fb.reset_graph();
+    // pinned staging of the inputs and outputs
+    size_t nIn = 0, nOut = 0;
+    fb.inOff.assign(boxes.size(), 0);
+    fb.outOff.assign(boxes.size(), 0);
+    for (size_t b = 0; b < boxes.size(); ++b) {
+        const size_t n = (size_t) boxes[b]->n;
+        fb.inOff[b] = nIn;
+        fb.outOff[b] = nOut;
+        nIn += (6 * n + 1) & ~(size_t) 1;  // 16-byte aligned starts
+        nOut += (3 * n + (mg ? 20 * n : 0) + (pg ? 4 * n : 0) + 1) & ~(size_t) 1;
+    }
+    if (nIn > fb.hostInCount) {
+        if (fb.hostIn) cudaFreeHost(fb.hostIn);
+        fb.hostIn = nullptr;
+        fb.hostInCount = 0;
+        CUDA_CHECK(cudaMallocHost(&fb.hostIn, nIn * sizeof(double)));
+        fb.hostInCount = nIn;
+    }
+    // device slots of the copies into host memory
+    fb.hostCopies.clear();
+    for (size_t i = 0; i < L; ++i)
+        for (Context* c : boxes) {
+            const RecOp& o = c->rec.ops[i];
+            if (o.kind != RecOp::COPY) continue;
+            cudaPointerAttributes at{};
+            CUDA_CHECK(cudaPointerGetAttributes(&at, o.dst));
+            if (at.type != cudaMemoryTypeHost) continue;
+            fb.hostCopies.push_back({o.dst, nOut, o.bytes});
+            nOut += ((o.bytes + 15) / 16) * 2;
+        }
+    if (nOut > fb.hostOutCount) {
+        if (fb.hostOut) cudaFreeHost(fb.hostOut);
+        fb.hostOut = nullptr;
+        fb.hostOutCount = 0;
+        CUDA_CHECK(cudaMallocHost(&fb.hostOut, nOut * sizeof(double)));
+        fb.hostOutCount = nOut;
+    }
+    if (!fb.evStart) CUDA_CHECK(cudaEventCreate(&fb.evStart));
+    if (!fb.evStop) CUDA_CHECK(cudaEventCreate(&fb.evStop));
+    std::vector<std::tuple<void*, const void*, size_t>> copyIn, copyOut;
+    fb.devIn.alloc(nIn);
+    fb.devOut.alloc(nOut);
+    for (size_t b = 0; b < boxes.size(); ++b) {
+        Context& c = *boxes[b];
+        const size_t n = (size_t) c.n;
+        const double* in = fb.devIn.p + fb.inOff[b];
+        double* out = fb.devOut.p + fb.outOff[b];
+        copyIn.emplace_back(c.pos.p, in, 3 * n * 8);
+        copyIn.emplace_back(c.forcesOut.p, in + 3 * n, 3 * n * 8);
+        copyOut.emplace_back(out, c.forcesOut.p, 3 * n * 8);
+        if (mg) copyOut.emplace_back(out + 3 * n, c.gradOut.p, 20 * n * 8);
+        if (pg) copyOut.emplace_back(out + 3 * n + (mg ? 20 * n : 0), c.polOut.p, 4 * n * 8);
+    }
+    if (inMax) fb.arenaIn.alloc(inMax);
+    if (outMax) fb.arenaOut.alloc(outMax);
+    for (const auto& pk : planKeys) {
+        if (fb.plans.count(pk)) continue;
+        int dims[3] = {pk[2], pk[3], pk[4]};
+        const cufftType t = pk[0] == 4 ? (pk[1] ? CUFFT_R2C : CUFFT_C2R) : (pk[1] ? CUFFT_D2Z : CUFFT_Z2D);
+        cufftHandle h;
+        CUFFT_CHECK(cufftPlanMany(&h, 3, dims, nullptr, 1, 0, nullptr, 1, 0, t, pk[5]));
+        fb.plans[pk] = h;
+    }
+    cudaStream_t st = fb.stream;
+    const long long l0 = t_launches, c0 = t_library_calls;
+    cudaGraph_t graph = nullptr;
+    CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    size_t nextHost = 0;  // the next host-destination copy (same order as the slots)
+    try {
+        CUDA_CHECK(cudaMemcpyAsync(fb.devIn.p, fb.hostIn, nIn * sizeof(double), cudaMemcpyHostToDevice, st));
+        copy_group(copyIn, st);
+        for (size_t i = 0; i < L; ++i) {
+            for (size_t b = 0; b < boxes.size(); ++b) ops[b] = &boxes[b]->rec.ops[i];
+            const RecOp& a = *ops[0];
+            if (a.kind == RecOp::KERNEL) {
+                std::map<std::vector<unsigned>, std::vector<const RecKernel*>> byBlock;
+                for (const RecOp* o : ops) byBlock[{o->k->block.x, o->k->block.y, o->k->block.z}].push_back(o->k.get());
+                for (const auto& kv : byBlock) kv.second[0]->launch_group(kv.second, st);
+            } else if (a.kind == RecOp::FFT) {
+                fused_fft(fb, ops, st);
+            } else {
+                std::vector<std::unique_ptr<RecKernel>> tmp;
+                std::vector<const RecKernel*> grp;
+                for (const RecOp* o : ops) {
+                    const int blocks = std::max(1, std::min(64, nblk((long long) (o->bytes / 16), 256)));
+                    if (o->kind == RecOp::FILL) {
+                        tmp.push_back(make_rec<k_fill_bytes>(blocks, 256, 0, (unsigned char*) o->dst, o->value, o->bytes));
+                    } else {
+                        unsigned char* dst = (unsigned char*) o->dst;
+                        if (nextHost < fb.hostCopies.size() && fb.hostCopies[nextHost].dst == o->dst)
+                            dst = (unsigned char*) (fb.devOut.p + fb.hostCopies[nextHost++].offset);
+                        tmp.push_back(make_rec<k_copy_bytes>(blocks, 256, 0, dst, (const unsigned char*) o->src, o->bytes));
+                    }
+                    grp.push_back(tmp.back().get());
+                }
+                grp[0]->launch_group(grp, st);
+            }
+        }
+        copy_group(copyOut, st);
+        CUDA_CHECK(cudaMemcpyAsync(fb.hostOut, fb.devOut.p, nOut * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaGetLastError());
+        if (nextHost != fb.hostCopies.size()) throw Error(MPID_ERR_STATE, "fused batch: host copies out of order");
+    } catch (...) {
+        cudaStreamEndCapture(st, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        (void) cudaGetLastError();
+        t_launches = l0;
+        t_library_calls = c0;
+        throw;
+    }
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    fb.launches = t_launches - l0;
+    fb.library = t_library_calls - c0;
+    t_launches = l0;
+    t_library_calls = c0;
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(&fb.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    CUDA_CHECK(ce);
+}
 
 }  // namespace mpid
 
@@ -2568,6 +3150,7 @@ struct BatchGraph {
 };
 std::mutex g_batchMutex;
 BatchGraph g_batch;
+mpid::FusedBatch g_fused;
 }  // namespace
 
 // The ordinary evaluation of one context of a batch at its host inputs, into its own
@@ -2589,9 +3172,9 @@ static double batch_fallback(Context& c, const double* positions, const double* 
 
 int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* const* positions, const double* const* boxes,
                         double* const* forces, double* energies, double* const* multipole_grad,
-                        double* const* polarization_grad, int streams) {
+                        double* const* polarization_grad, int launch_mode) {
     MPID_API_BEGIN
-    if (streams < 0 || streams > 128) throw Error(MPID_ERR_INVALID, "streams must be in 0..128");
+    if (launch_mode < -1 || launch_mode > 128) throw Error(MPID_ERR_INVALID, "launch_mode must be in -1..128");
     if (count < 0 || (count > 0 && (!ctxs || !positions || !boxes || !energies)))
         throw Error(MPID_ERR_INVALID, "null argument");
     if (count == 0) return MPID_OK;
@@ -2600,9 +3183,36 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
         if (!ctxs[k] || !positions[k] || !boxes[k]) throw Error(MPID_ERR_INVALID, "null argument");
         if (ctxs[k]->ctx.device != device) throw Error(MPID_ERR_INVALID, "mpid_evaluate_batch: contexts on different devices");
         if (!ctxs[k]->ctx.usePme) throw Error(MPID_ERR_INVALID, "mpid_evaluate_batch supports PME contexts only");
+        for (int q = 0; q < k; ++q)
+            if (ctxs[q] == ctxs[k]) throw Error(MPID_ERR_INVALID, "mpid_evaluate_batch: a context appears twice");
+    }
+    const bool fused = launch_mode == 0;
+    if (fused) {
+        const bool mg0 = multipole_grad && multipole_grad[0], pg0 = polarization_grad && polarization_grad[0];
+        for (int k = 0; k < count; ++k) {
+            const bool mg = multipole_grad && multipole_grad[k], pg = polarization_grad && polarization_grad[k];
+            if (mg != mg0 || pg != pg0)
+                throw Error(MPID_ERR_INVALID, "fused batch: every box must request the same gradients");
+            if (ctxs[k]->ctx.n > mpid::kBlockSortMax)
+                throw Error(MPID_ERR_INVALID, "fused batch: boxes of at most 4096 atoms (use launch_mode > 0)");
+        }
     }
     mpid::DeviceScope scope(device);
     std::lock_guard<std::mutex> lock(g_batchMutex);
+    if (g_batch.device != device) {
+        g_batch.reset();
+        if (g_batch.stream) cudaStreamDestroy(g_batch.stream);
+        for (cudaStream_t q : g_batch.streams) cudaStreamDestroy(q);
+        for (cudaEvent_t ev : g_batch.joins) cudaEventDestroy(ev);
+        g_batch.stream = nullptr;
+        g_batch.streams.clear();
+        g_batch.joins.clear();
+        g_fused.release();
+        g_batch.device = device;
+        g_fused.device = device;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&g_batch.stream, cudaStreamNonBlocking));
+        CUDA_CHECK(cudaStreamCreateWithFlags(&g_fused.stream, cudaStreamNonBlocking));
+    }
     std::vector<char> graphed(count, 0);
     std::vector<double> eFallback(count, 0.0);
     bool changed = false;
@@ -2616,91 +3226,148 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
             eFallback[k] = batch_fallback(c, positions[k], boxes[k], fin, mg, pg);
             continue;
         }
-        const size_t n3 = 3 * (size_t) c.n;
-        CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions[k], n3 * 8, cudaMemcpyHostToDevice, c.stream));
-        if (fin)
-            CUDA_CHECK(cudaMemcpyAsync(c.forcesOut.p, fin, n3 * 8, cudaMemcpyHostToDevice, c.stream));
-        else
-            CUDA_CHECK(cudaMemsetAsync(c.forcesOut.p, 0, n3 * 8, c.stream));
+        // per-box graphs: inputs on the box's stream (the fused graph copies them from its
+        // pinned staging)
+        if (!fused) {
+            const size_t n3 = 3 * (size_t) c.n;
+            CUDA_CHECK(cudaMemcpyAsync(c.pos.p, positions[k], n3 * 8, cudaMemcpyHostToDevice, c.stream));
+            if (fin)
+                CUDA_CHECK(cudaMemcpyAsync(c.forcesOut.p, fin, n3 * 8, cudaMemcpyHostToDevice, c.stream));
+            else
+                CUDA_CHECK(cudaMemsetAsync(c.forcesOut.p, 0, n3 * 8, c.stream));
+        }
         c.set_box(boxes[k]);
         c.stats.graph_captures = 0;
-        changed = c.ensure_batch_graph(mg, pg) || changed;
-        CUDA_CHECK(cudaStreamSynchronize(c.stream));
+        if (!fused) {
+            changed = c.ensure_batch_graph(mg, pg) || changed;
+            CUDA_CHECK(cudaStreamSynchronize(c.stream));
+        }
         graphed[k] = 1;
     }
-    // the parent graph of the graphed contexts
-    std::vector<unsigned long long> key;
-    for (int k = 0; k < count; ++k)
-        if (graphed[k]) {
-            key.push_back(ctxs[k]->ctx.id);
-            key.push_back(ctxs[k]->ctx.full.generation);
-        }
-    if (g_batch.device != device) {
-        g_batch.reset();
-        if (g_batch.stream) cudaStreamDestroy(g_batch.stream);
-        for (cudaStream_t q : g_batch.streams) cudaStreamDestroy(q);
-        for (cudaEvent_t ev : g_batch.joins) cudaEventDestroy(ev);
-        g_batch.stream = nullptr;
-        g_batch.streams.clear();
-        g_batch.joins.clear();
-        g_batch.device = device;
-        CUDA_CHECK(cudaStreamCreateWithFlags(&g_batch.stream, cudaStreamNonBlocking));
-    }
-    if (!key.empty() && streams > 0) {
-        // each context's graph on one of `streams` streams, joined into the batch stream
-        while ((int) g_batch.streams.size() < streams) {
-            cudaStream_t q;
-            cudaEvent_t ev;
-            CUDA_CHECK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
-            CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-            g_batch.streams.push_back(q);
-            g_batch.joins.push_back(ev);
-        }
-        int j = 0;
+    long long launches = 0, library = 0;
+    float fusedMs = 0.f;
+    std::vector<int> slot(count, -1);  // a fused box's index in the staging
+    if (fused) {
+        // every box records the same number of CG iterations: the most any box needs
+        std::vector<Context*> run;
+        int K = 0;
         for (int k = 0; k < count; ++k)
             if (graphed[k]) {
-                Context& c = ctxs[k]->ctx;
-                if (!c.full.exec) CUDA_CHECK(cudaGraphInstantiate(&c.full.exec, c.full.graph, 0));
-                CUDA_CHECK(cudaGraphLaunch(c.full.exec, g_batch.streams[j % streams]));
-                ++j;
+                slot[k] = (int) run.size();
+                run.push_back(&ctxs[k]->ctx);
+                K = std::max(K, ctxs[k]->ctx.batch_iterations());
             }
-        for (int q = 0; q < std::min(j, streams); ++q) {
-            CUDA_CHECK(cudaEventRecord(g_batch.joins[q], g_batch.streams[q]));
-            CUDA_CHECK(cudaStreamWaitEvent(g_batch.stream, g_batch.joins[q], 0));
+        std::vector<unsigned long long> key;
+        const bool mg = multipole_grad && multipole_grad[0], pg = polarization_grad && polarization_grad[0];
+        for (Context* c : run) {
+            changed = c->ensure_recording(mg, pg, K) || changed;
+            key.push_back(c->id);
+            key.push_back(c->recGeneration);
         }
-        CUDA_CHECK(cudaStreamSynchronize(g_batch.stream));
-    } else if (!key.empty()) {
-        if (changed || g_batch.key != key || !g_batch.exec) {
-            g_batch.reset();
-            cudaGraph_t parent = nullptr;
-            CUDA_CHECK(cudaGraphCreate(&parent, 0));
+        if (!run.empty()) {
+            if (changed || g_fused.key != key || !g_fused.exec) {
+                mpid::fused_build(g_fused, run, mg, pg);
+                g_fused.key = key;
+                for (Context* c : run) ++c->stats.graph_captures;
+            }
+            for (int k = 0; k < count; ++k) {
+                if (slot[k] < 0) continue;
+                const size_t n3 = 3 * (size_t) ctxs[k]->ctx.n;
+                double* in = g_fused.hostIn + g_fused.inOff[slot[k]];
+                std::memcpy(in, positions[k], n3 * 8);
+                if (forces && forces[k])
+                    std::memcpy(in + n3, forces[k], n3 * 8);
+                else
+                    std::memset(in + n3, 0, n3 * 8);
+            }
+            CUDA_CHECK(cudaEventRecord(g_fused.evStart, g_fused.stream));
+            CUDA_CHECK(cudaGraphLaunch(g_fused.exec, g_fused.stream));
+            CUDA_CHECK(cudaEventRecord(g_fused.evStop, g_fused.stream));
+            CUDA_CHECK(cudaStreamSynchronize(g_fused.stream));
+            CUDA_CHECK(cudaEventElapsedTime(&fusedMs, g_fused.evStart, g_fused.evStop));
+            for (const auto& hc : g_fused.hostCopies) std::memcpy(hc.dst, g_fused.hostOut + hc.offset, hc.bytes);
+            launches = g_fused.launches;
+            library = g_fused.library;
+        }
+    } else {
+        // the parent graph of the graphed contexts
+        std::vector<unsigned long long> key;
+        for (int k = 0; k < count; ++k)
+            if (graphed[k]) {
+                key.push_back(ctxs[k]->ctx.id);
+                key.push_back(ctxs[k]->ctx.full.generation);
+            }
+        const int streams = launch_mode;
+        if (!key.empty() && streams > 0) {
+            // each context's graph on one of `streams` streams, joined into the batch stream
+            while ((int) g_batch.streams.size() < streams) {
+                cudaStream_t q;
+                cudaEvent_t ev;
+                CUDA_CHECK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+                CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                g_batch.streams.push_back(q);
+                g_batch.joins.push_back(ev);
+            }
+            int j = 0;
             for (int k = 0; k < count; ++k)
                 if (graphed[k]) {
-                    cudaGraphNode_t node;
-                    const cudaError_t rc = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, ctxs[k]->ctx.full.graph);
-                    if (rc != cudaSuccess) {
-                        cudaGraphDestroy(parent);
-                        CUDA_CHECK(rc);
-                    }
+                    Context& c = ctxs[k]->ctx;
+                    if (!c.full.exec) CUDA_CHECK(cudaGraphInstantiate(&c.full.exec, c.full.graph, 0));
+                    CUDA_CHECK(cudaGraphLaunch(c.full.exec, g_batch.streams[j % streams]));
+                    ++j;
                 }
-            const cudaError_t rc = cudaGraphInstantiate(&g_batch.exec, parent, 0);
-            cudaGraphDestroy(parent);
-            CUDA_CHECK(rc);
-            g_batch.key = key;
+            for (int q = 0; q < std::min(j, streams); ++q) {
+                CUDA_CHECK(cudaEventRecord(g_batch.joins[q], g_batch.streams[q]));
+                CUDA_CHECK(cudaStreamWaitEvent(g_batch.stream, g_batch.joins[q], 0));
+            }
+            CUDA_CHECK(cudaStreamSynchronize(g_batch.stream));
+        } else if (!key.empty()) {
+            if (changed || g_batch.key != key || !g_batch.exec) {
+                g_batch.reset();
+                cudaGraph_t parent = nullptr;
+                CUDA_CHECK(cudaGraphCreate(&parent, 0));
+                for (int k = 0; k < count; ++k)
+                    if (graphed[k]) {
+                        cudaGraphNode_t node;
+                        const cudaError_t rc = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, ctxs[k]->ctx.full.graph);
+                        if (rc != cudaSuccess) {
+                            cudaGraphDestroy(parent);
+                            CUDA_CHECK(rc);
+                        }
+                    }
+                const cudaError_t rc = cudaGraphInstantiate(&g_batch.exec, parent, 0);
+                cudaGraphDestroy(parent);
+                CUDA_CHECK(rc);
+                g_batch.key = key;
+            }
+            CUDA_CHECK(cudaGraphLaunch(g_batch.exec, g_batch.stream));
+            CUDA_CHECK(cudaStreamSynchronize(g_batch.stream));
         }
-        CUDA_CHECK(cudaGraphLaunch(g_batch.exec, g_batch.stream));
-        CUDA_CHECK(cudaStreamSynchronize(g_batch.stream));
     }
-    // results, and the ordinary evaluation of any context whose graph results do not stand
+    // results, and the ordinary evaluation of any context whose batched results do not stand
     for (int k = 0; k < count; ++k) {
         Context& c = ctxs[k]->ctx;
         const bool mg = multipole_grad && multipole_grad[k], pg = polarization_grad && polarization_grad[k];
         double e = eFallback[k];
         if (graphed[k]) {
-            if (c.batch_ok()) {
+            const bool ok = fused ? c.batch_ok(launches, library) : c.batch_ok(c.full.nodes, c.full.library);
+            if (ok) {
                 e = c.stats.energy_parts[0] + c.stats.energy_parts[1] + c.stats.energy_parts[2];
+                if (fused) {
+                    // the whole fused launch's device time, and the outputs from the staging
+                    c.stats.ms_total = fusedMs;
+                    const size_t n = (size_t) c.n;
+                    const double* out = g_fused.hostOut + g_fused.outOff[slot[k]];
+                    if (forces && forces[k]) std::memcpy(forces[k], out, 3 * n * 8);
+                    if (mg) std::memcpy(multipole_grad[k], out + 3 * n, 20 * n * 8);
+                    if (pg) std::memcpy(polarization_grad[k], out + 3 * n + (mg ? 20 * n : 0), 4 * n * 8);
+                    energies[k] = e;
+                    continue;
+                }
             } else {
-                c.full.destroy();  // captured anew with the new list shape or solver length
+                // recorded or captured anew with the new list shape or solver length
+                c.full.destroy();
+                c.rec.ops.clear();
                 e = batch_fallback(c, positions[k], boxes[k], forces ? forces[k] : nullptr, mg, pg);
             }
         }
@@ -2714,8 +3381,8 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
         if (pg)
             CUDA_CHECK(cudaMemcpyAsync(polarization_grad[k], c.polOut.p, (size_t) 4 * c.n * 8, cudaMemcpyDeviceToHost,
                                        c.stream));
-        CUDA_CHECK(cudaStreamSynchronize(c.stream));
     }
+    for (int k = 0; k < count; ++k) CUDA_CHECK(cudaStreamSynchronize(ctxs[k]->ctx.stream));
     return MPID_OK;
     MPID_API_END
 }

@@ -17,6 +17,19 @@
 
 namespace mpid {
 
+// Every kernel is written as a device body that takes its block index and block count
+// from a KGrid instead of blockIdx.x / gridDim.x, so that the same body runs either as
+// a launch of its own (the block index is the hardware one) or as the share of one box
+// in a launch over many boxes (the block index is the block's rank within its box; see
+// the launch wrappers in mpid_context.cu).  MT and MB are the body's launch bounds
+// (maximum threads per block, minimum resident blocks per SM; 0 when it has none).
+template <int MT = 0, int MB = 0>
+struct KGrid {
+    unsigned bx;  // block index within the launch (or within the box)
+    unsigned nb;  // blocks of the launch (or of the box)
+};
+#define MPID_KERNEL __device__ __forceinline__
+
 constexpr double kFixedScale = 4294967296.0;       // 2^32
 constexpr double kFixedInv = 1.0 / 4294967296.0;
 constexpr double kElectric = 138.935455846;        // MPIDReferenceForce.cpp:38
@@ -78,9 +91,9 @@ __host__ __device__ __forceinline__ void min_image(real* d, const real* V, const
 // zBits bits of quantised z (the radix sort then runs over the bits in use only); the
 // value is the atom index.  Atoms of one column closer in z than the quantum keep their
 // input order (the sort is stable).
-__global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, int ncx, int ncy, int zBits,
+MPID_KERNEL void k_sort_keys(KGrid<> kg, int n, const double* __restrict__ pos, BoxDev box, int ncx, int ncy, int zBits,
                             unsigned* __restrict__ keys, int* __restrict__ vals, double* __restrict__ wpos) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = kg.bx * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double w[3], x[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
     // into [0, ax) x [0, by) x [0, cz): c, then b, then a (a lattice translation)
@@ -103,10 +116,41 @@ __global__ void k_sort_keys(int n, const double* __restrict__ pos, BoxDev box, i
     vals[i] = i;
 }
 
+// The same order as the radix sort of (key, atom index) pairs, for one box of at most
+// kBlockSortMax atoms in one block of 1024 threads: a bitonic sort of the 64-bit words
+// key << 32 | index in shared memory (keys are distinct once the index is appended, so
+// any correct sort gives the stable order).  Used where many boxes are set up in one
+// launch, one block per box.
+constexpr int kBlockSortMax = 4096;
+MPID_KERNEL void k_sort_block(KGrid<1024> kg, int n, const unsigned* __restrict__ keys, const int* __restrict__ vals,
+                              int* __restrict__ order) {
+    __shared__ unsigned long long s[kBlockSortMax];
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x)
+        s[i] = i < n ? ((unsigned long long) keys[i] << 32) | (unsigned) vals[i] : ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const unsigned long long a = s[i], b = s[l];
+                    if ((a > b) == ((i & k) == 0)) {
+                        s[i] = b;
+                        s[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) order[i] = (int) (unsigned) s[i];
+}
+
 // No-cutoff systems keep the caller's order.
-__global__ void k_identity_order(int n, const double* __restrict__ pos, int* __restrict__ order,
+MPID_KERNEL void k_identity_order(KGrid<> kg, int n, const double* __restrict__ pos, int* __restrict__ order,
                                  double* __restrict__ wpos) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = kg.bx * blockDim.x + threadIdx.x;
     if (i >= n) return;
     order[i] = i;
     for (int k = 0; k < 3; ++k) wpos[3 * i + k] = pos[3 * i + k];
@@ -114,10 +158,10 @@ __global__ void k_identity_order(int n, const double* __restrict__ pos, int* __r
 
 // Tile centres and half extents from the wrapped positions of the sorted atoms: one warp
 // per tile, one lane per atom, minima and maxima by shuffles.
-__global__ void k_tile_bounds(int n, int ntiles, const int* __restrict__ order,
+MPID_KERNEL void k_tile_bounds(KGrid<> kg, int n, int ntiles, const int* __restrict__ order,
                               const double* __restrict__ wpos, double* __restrict__ center,
                               double* __restrict__ half, float4* __restrict__ centerF, float4* __restrict__ halfF) {
-    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int t = (kg.bx * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (t >= ntiles) return;  // whole warps
     const int s = t * 32 + lane;
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -221,13 +265,12 @@ __device__ __forceinline__ bool tile_pair_hit(int J, const float* cI, const floa
 // within each warp), so the list order is deterministic.
 constexpr int kTileListWarps = 8;
 
-__global__ void __launch_bounds__(32 * kTileListWarps)
-k_tile_list(int ntiles, const double* __restrict__ center, const float4* __restrict__ centerF,
+MPID_KERNEL void k_tile_list(KGrid<(32 * kTileListWarps)> kg, int ntiles, const double* __restrict__ center, const float4* __restrict__ centerF,
             const float4* __restrict__ halfF, BoxDev box, double cutoff, int usePbc, int tcap, int* __restrict__ tileCount, int* __restrict__ tileJ,
             float4* __restrict__ shF, double* __restrict__ shD, float2* __restrict__ shDF,
             int* __restrict__ maxTiles) {
     __shared__ int wcount[kTileListWarps];
-    const int I = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int I = kg.bx, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (I >= ntiles) return;  // whole blocks
     const float4 cI4 = centerF[I], hI4 = halfF[I];
     const float cI[3] = {cI4.x, cI4.y, cI4.z}, hI[3] = {hI4.x, hI4.y, hI4.z};
@@ -311,11 +354,11 @@ struct MolArrays {  // original order, FP64, as given through the API
 };
 
 template <typename real>
-__global__ void k_gather_atoms(int n, int npad, const int* __restrict__ order, MolArrays mol,
+MPID_KERNEL void k_gather_atoms(KGrid<> kg, int n, int npad, const int* __restrict__ order, MolArrays mol,
                                const double* __restrict__ pos, const double* __restrict__ wpos,
                                const double* __restrict__ center, AtomArrays<real> at, double* __restrict__ mom64,
                                double* __restrict__ prm64) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     if (s >= n) {
         for (int k = 0; k < 3; ++k) at.off[k * npad + s] = real(0);
@@ -438,8 +481,7 @@ __device__ __forceinline__ void partner_masks(int J, const int* pS, unsigned pF,
 }
 
 template <typename real>
-__global__ void __launch_bounds__(32 * kListWarps, 3)
-k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __restrict__ orig,
+MPID_KERNEL void k_atom_list(KGrid<(32 * kListWarps), 3> kg, int ntiles, int npad, const real* __restrict__ off, const int* __restrict__ orig,
             const int* __restrict__ rank, BoxDev box, float cutoff2, float quadR2, int usePme, int tcap,
             const int* __restrict__ tileCount, const int* __restrict__ tileJ, const float4* __restrict__ shF,
             const int* __restrict__ covOff, const int* __restrict__ covJ, const double* __restrict__ covS, int cap,
@@ -450,7 +492,7 @@ k_atom_list(int ntiles, int npad, const real* __restrict__ off, const int* __res
     __shared__ int cnt[kListWarps][4][32];  // nL, nS, lowL, lowS per warp and lane
     __shared__ unsigned hits[kListWarps][kMasks][32], near[kListWarps][kMasks][32];
     __shared__ float4 jat[kListWarps][32];  // the current J tile: offset and original index of each atom
-    const int I = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int I = kg.bx, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (I >= ntiles) return;
     const int si = I * 32 + lane;
     const float oi[3] = {(float) off[si], (float) off[npad + si], (float) off[2 * npad + si]};
@@ -620,12 +662,12 @@ struct PairTask {
     }
     // Work items: all erfc-segment items (tile-major), then all quadrature-segment items,
     // so that resident warps mostly run the same branch of the code.
-    __device__ __forceinline__ bool init(const NbrList& nl) { return init_split(nl, nl.split); }
+    __device__ __forceinline__ bool init(const NbrList& nl, unsigned bx) { return init_split(nl, nl.split, bx); }
     // The same items, each cut into `split` consecutive sub-ranges of chunk / split
     // entries (split divides the chunk), one warp per sub-range: more warps for kernels
     // whose per-pair work is long (the FP64 gradient passes of small systems).
-    __device__ __forceinline__ bool init_split(const NbrList& nl, int split) {
-        const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    __device__ __forceinline__ bool init_split(const NbrList& nl, int split, unsigned bx) {
+        const int w = (bx * blockDim.x + threadIdx.x) >> 5;
         const int item = w / split, part = w - item * split;
         const int nLong = nl.ntiles * nl.nchunksL;
         lane = threadIdx.x & 31;
@@ -713,10 +755,9 @@ __device__ __forceinline__ void fixed_field_loop(const NbrList& nl, const AtomAr
 }
 
 template <typename real>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_fixed_field(NbrList nl, AtomArrays<real> at, unsigned long long* __restrict__ field) {
+MPID_KERNEL void k_fixed_field(KGrid<(32 * kWarpsPerBlock)> kg, NbrList nl, AtomArrays<real> at, unsigned long long* __restrict__ field) {
     PairTask t;
-    if (!t.init(nl)) return;
+    if (!t.init(nl, kg.bx)) return;
     const int origI = at.orig[t.si];
     if (origI < 0) return;
     real Ei[3] = {real(0), real(0), real(0)};
@@ -771,12 +812,11 @@ __device__ __forceinline__ void dipole_field_loop(const NbrList& nl, const AtomA
 }
 
 template <typename real, bool GRAD, bool HALF>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_dipole_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ field,
+MPID_KERNEL void k_dipole_field(KGrid<(32 * kWarpsPerBlock)> kg, NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ field,
                unsigned long long* __restrict__ grad, const int* __restrict__ skip) {
     if (skip && *skip) return;
     PairTask t;
-    if (!t.init(nl)) return;
+    if (!t.init(nl, kg.bx)) return;
     if (at.orig[t.si] < 0) return;
     constexpr int NACC = GRAD ? 9 : 3;
     real acc[NACC];
@@ -832,13 +872,12 @@ __device__ __forceinline__ void cg_field_loop(const NbrList& nl, const CgRadial&
     }
 }
 
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_dipole_field_cg(NbrList nl, CgRadial R, const float4* __restrict__ A0, const float4* __restrict__ A1, int npad,
+MPID_KERNEL void k_dipole_field_cg(KGrid<(32 * kWarpsPerBlock)> kg, NbrList nl, CgRadial R, const float4* __restrict__ A0, const float4* __restrict__ A1, int npad,
                   const int* __restrict__ orig, unsigned long long* __restrict__ field, const int* __restrict__ skip) {
     if (*skip) return;
     __shared__ float part[kWarpsPerBlock][3][32];
     PairTask t;
-    const bool active = t.init(nl) && orig[t.si] >= 0;
+    const bool active = t.init(nl, kg.bx) && orig[t.si] >= 0;
     float acc[3] = {0.f, 0.f, 0.f};
     if (active) {
         if (t.quad)
@@ -865,9 +904,9 @@ k_dipole_field_cg(NbrList nl, CgRadial R, const float4* __restrict__ A0, const f
 }
 
 // A0 = (offset, Thole width) of the float engine's atoms.
-__global__ void k_pack_atoms(int npad, const float* __restrict__ off, const float4* __restrict__ prm,
+MPID_KERNEL void k_pack_atoms(KGrid<> kg, int npad, const float* __restrict__ off, const float4* __restrict__ prm,
                              float4* __restrict__ A0) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     A0[s] = make_float4(off[s], off[npad + s], off[2 * npad + s], prm[s].x);
 }
@@ -914,17 +953,17 @@ __device__ __forceinline__ void fx_add_df(unsigned long long* p, dfloat v) {
 }
 
 // float2 copies of FP64 arrays
-__global__ void k_to_df(int count, const double* __restrict__ src, float2* __restrict__ dst) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+MPID_KERNEL void k_to_df(KGrid<> kg, int count, const double* __restrict__ src, float2* __restrict__ dst) {
+    const int i = kg.bx * blockDim.x + threadIdx.x;
     if (i >= count) return;
     const dfloat v = df_from_double(src[i]);
     dst[i] = make_float2(v.hi, v.lo);
 }
 
 // df offsets, Thole widths and damping factors of the FP64 engine's atoms
-__global__ void k_df_atoms(int npad, const double* __restrict__ off, const double4_16a* __restrict__ prm,
+MPID_KERNEL void k_df_atoms(KGrid<> kg, int npad, const double* __restrict__ off, const double4_16a* __restrict__ prm,
                            float2* __restrict__ offDF, float2* __restrict__ tholeDF, float2* __restrict__ dampDF) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = kg.bx * blockDim.x + threadIdx.x;
     if (i >= npad) return;
     for (int k = 0; k < 3; ++k) {
         const dfloat v = df_from_double(off[k * npad + i]);
@@ -1010,10 +1049,9 @@ __device__ __forceinline__ void df_field_loop(const NbrList& nl, const DfRadial&
     }
 }
 
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_dipole_field_df(NbrList nl, DfRadial R, DfAtoms A, const int* __restrict__ orig, unsigned long long* __restrict__ field) {
+MPID_KERNEL void k_dipole_field_df(KGrid<(32 * kWarpsPerBlock)> kg, NbrList nl, DfRadial R, DfAtoms A, const int* __restrict__ orig, unsigned long long* __restrict__ field) {
     PairTask t;
-    if (!t.init(nl)) return;
+    if (!t.init(nl, kg.bx)) return;
     if (orig[t.si] < 0) return;
     dfloat acc[3] = {df_from_float(0.f), df_from_float(0.f), df_from_float(0.f)};
     if (t.quad)
@@ -1091,11 +1129,10 @@ __device__ __forceinline__ void electrostatics_loop(const NbrList& nl, const Ato
 
 // out: force[3][npad], torque[3][npad] fixed point; energy[warp task] (already x kElectric).
 template <typename real, bool MUTUAL, bool REF_ANISO_TORQUE, bool HALF>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, sizeof(real) == 4 ? 4 : 1)
-k_electrostatics(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ force,
+MPID_KERNEL void k_electrostatics(KGrid<(32 * kWarpsPerBlock), (sizeof(real) == 4 ? 4 : 1)> kg, NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ force,
                  unsigned long long* __restrict__ torque, double* __restrict__ energy) {
     PairTask t;
-    const bool active = t.init(nl);
+    const bool active = t.init(nl, kg.bx);
     const int npad = at.npad, si = t.si;
     const int origI = active ? at.orig[si] : -1;
     KahanSum<real> eSum;
@@ -1116,7 +1153,7 @@ k_electrostatics(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, u
     // FP64 energy of the work item: warp sum, written per item (fixed-order reduction later)
     double e = eSum.value();
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int w = (kg.bx * blockDim.x + threadIdx.x) >> 5;
     if (t.lane == 0 && w < t.tasks(nl)) energy[w] = e * kElectric;
 }
 
@@ -1124,13 +1161,13 @@ k_electrostatics(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, u
 // most of the reciprocal interaction of bonded atoms and are far larger than the total,
 // so they are summed at full precision; forces and torques stay in the tile kernel.
 template <bool MUTUAL>
-__global__ void k_scaled_pair_energy(int npairs, const int2* __restrict__ pr, const double* __restrict__ prs,
+MPID_KERNEL void k_scaled_pair_energy(KGrid<> kg, int npairs, const int2* __restrict__ pr, const double* __restrict__ prs,
                                      const int* __restrict__ rank, int npad, const double* __restrict__ mom64,
                                      const double* __restrict__ prm64, const void* __restrict__ muv, int muIsFloat,
                                      const double* __restrict__ pos, BoxDev box, int usePbc, double cutoff,
                                      double ewald, double defaultThole, double* __restrict__ partial) {
     __shared__ double red[128];
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = kg.bx * blockDim.x + threadIdx.x;
     const EwaldAlpha<double> ew(ewald);
     double e = 0.0;
     if (p < npairs) {
@@ -1164,7 +1201,7 @@ __global__ void k_scaled_pair_energy(int npairs, const int2* __restrict__ pr, co
         if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) partial[kg.bx] = red[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -1174,11 +1211,11 @@ __global__ void k_scaled_pair_energy(int npairs, const int2* __restrict__ pr, co
 // electric constant.  FP64; one thread per grid point, all threads reading the same atom
 // at the same time.
 template <typename real>
-__global__ void k_potential_grid(int n, int npad, int ngrid, const double* __restrict__ grid,
+MPID_KERNEL void k_potential_grid(KGrid<> kg, int n, int npad, int ngrid, const double* __restrict__ grid,
                                  const double* __restrict__ wpos, const int* __restrict__ rank,
                                  const double* __restrict__ mom64, const real* __restrict__ mu, BoxDev box, int usePbc,
                                  double* __restrict__ out) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = kg.bx * blockDim.x + threadIdx.x;
     if (g >= ngrid) return;
     const double gx = grid[3 * g], gy = grid[3 * g + 1], gz = grid[3 * g + 2];
     double acc = 0.0;
@@ -1207,13 +1244,12 @@ __global__ void k_potential_grid(int n, int npad, int ngrid, const double* __res
 // com = red[1..3] / red[0]) sums charge, dipole (3), traced second moment (6: xx xy xz yy
 // yz zz) and the atoms' lab quadrupoles (6).
 template <typename real>
-__global__ void __launch_bounds__(256)
-k_moment_partials(int n, int npad, int pass, const double* __restrict__ pos, const double* __restrict__ masses,
+MPID_KERNEL void k_moment_partials(KGrid<256> kg, int n, int npad, int pass, const double* __restrict__ pos, const double* __restrict__ masses,
                   const int* __restrict__ rank, const double* __restrict__ mom64, const real* __restrict__ mu,
                   const double* __restrict__ red, double* __restrict__ partial) {
     constexpr int NV = 16;
     __shared__ double sh[NV][256];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = kg.bx * blockDim.x + threadIdx.x;
     double v[NV];
     for (int k = 0; k < NV; ++k) v[k] = 0.0;
     if (i < n) {
@@ -1247,7 +1283,7 @@ k_moment_partials(int n, int npad, int pass, const double* __restrict__ pos, con
             for (int k = 0; k < NV; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x < NV) partial[threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x][0];
+    if (threadIdx.x < NV) partial[threadIdx.x * kg.nb + kg.bx] = sh[threadIdx.x][0];
 }
 
 // ---------------------------------------------------------------------------
@@ -1381,11 +1417,10 @@ __device__ __forceinline__ void gradient_loop(const NbrList& nl, const AtomArray
 constexpr int kSegErfc = 1, kSegQuad = 2, kSegAll = 3;
 
 template <typename real>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_multipole_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ gfx,
+MPID_KERNEL void k_multipole_gradient(KGrid<(32 * kWarpsPerBlock)> kg, NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, unsigned long long* __restrict__ gfx,
                      int segments, int split) {
     PairTask t;
-    if (!t.init_split(nl, split)) return;
+    if (!t.init_split(nl, split, kg.bx)) return;
     if (!(segments & (t.quad ? kSegQuad : kSegErfc))) return;
     const int origI = at.orig[t.si];
     if (origI < 0) return;
@@ -1419,11 +1454,11 @@ __device__ __forceinline__ bool api_frame(const MolArrays& mol, const double* __
 // YYZ XZZ YZZ ZZZ) through the frame rotation and the chirality flip.  out[20 n] by
 // original index, FP64.
 template <typename real>
-__global__ void k_gradient_finish(int n, int npad, BoxDev box, double alpha, int usePme, const int* __restrict__ order,
+MPID_KERNEL void k_gradient_finish(KGrid<> kg, int n, int npad, BoxDev box, double alpha, int usePme, const int* __restrict__ order,
                                   MolArrays mol, const double* __restrict__ pos, const unsigned long long* __restrict__ gfx,
                                   const real* __restrict__ phiP, const real* __restrict__ phiD,
                                   const double* __restrict__ mom64, const real* __restrict__ mu, double* __restrict__ out) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int i = order[s];
     double g[20];
@@ -1642,11 +1677,10 @@ __device__ __forceinline__ void polarization_loop(const NbrList& nl, const AtomA
 }
 
 template <typename real>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_polarization_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, int mutual,
+MPID_KERNEL void k_polarization_gradient(KGrid<(32 * kWarpsPerBlock)> kg, NbrList nl, AtomArrays<real> at, const real* __restrict__ mu, int mutual,
                         OptOrders<real> opt, unsigned long long* __restrict__ gfx, int segments, int split) {
     PairTask t;
-    if (!t.init_split(nl, split)) return;
+    if (!t.init_split(nl, split, kg.bx)) return;
     if (!(segments & (t.quad ? kSegQuad : kSegErfc))) return;
     const int origI = at.orig[t.si];
     if (origI < 0) return;
@@ -1665,12 +1699,12 @@ k_polarization_gradient(NbrList nl, AtomArrays<real> at, const real* __restrict_
 // (molecular frame, per axis) with F_0 = the permanent field (Efix) and F_j = the field
 // of order j - 1 (ptE).
 template <typename real>
-__global__ void k_polarization_gradient_finish(int n, int npad, const int* __restrict__ order, MolArrays mol,
+MPID_KERNEL void k_polarization_gradient_finish(KGrid<> kg, int n, int npad, const int* __restrict__ order, MolArrays mol,
                                                const double* __restrict__ pos, const unsigned long long* __restrict__ gfx,
                                                const real* __restrict__ mu, OptOrders<real> opt,
                                                const real* __restrict__ Efix, const real* __restrict__ ptE,
                                                double* __restrict__ out) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int i = order[s];
     const double W = fx_get(gfx, s), Z = fx_get(gfx, npad + s);
@@ -1705,9 +1739,9 @@ __global__ void k_polarization_gradient_finish(int n, int npad, const int* __res
 // PME.  B-spline coefficients and weighted fractional multipoles per sorted atom.
 // theta layout: [3 dims][5 derivs][ORDER][npad]; igrid [3][npad].
 template <typename real, int ORDER>
-__global__ void k_bsplines(int npad, int n, const int* __restrict__ order, const double* __restrict__ wpos,
+MPID_KERNEL void k_bsplines(KGrid<> kg, int npad, int n, const int* __restrict__ order, const double* __restrict__ wpos,
                            BoxDev box, real* __restrict__ theta, int* __restrict__ igrid) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     if (s >= n) {
         for (int d = 0; d < 3; ++d) {
@@ -1738,8 +1772,8 @@ __global__ void k_bsplines(int npad, int n, const int* __restrict__ order, const
 }
 
 template <typename real>
-__global__ void k_frac_multipoles(int npad, BoxDev box, const real* __restrict__ mom, real* __restrict__ mf) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+MPID_KERNEL void k_frac_multipoles(KGrid<> kg, int npad, BoxDev box, const real* __restrict__ mom, real* __restrict__ mf) {
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     LabMoments<real> m;
     load_moments(mom, npad, s, m);
@@ -1764,11 +1798,11 @@ template <> struct GridAcc<double> {
 // Spread NCOMP weighted fractional components (20 = full multipole, 4 = charge +
 // dipole) on the grid: one thread per (atom, x, y) stencil column.
 template <typename real, int ORDER, int NCOMP>
-__global__ void k_spread(int n, int npad, BoxDev box, const real* __restrict__ mf, const real* __restrict__ theta,
+MPID_KERNEL void k_spread(KGrid<> kg, int n, int npad, BoxDev box, const real* __restrict__ mf, const real* __restrict__ theta,
                          const int* __restrict__ igrid, typename GridAcc<real>::type* __restrict__ grid,
                          const int* __restrict__ skip) {
     if (skip && *skip) return;
-    const long long tid = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    const long long tid = (long long) kg.bx * blockDim.x + threadIdx.x;
     if (tid >= (long long) n * ORDER * ORDER) return;
     const int s = (int) (tid / (ORDER * ORDER));
     const int ix = (int) (tid % (ORDER * ORDER)) / ORDER, iy = (int) (tid % ORDER);
@@ -1801,10 +1835,10 @@ __global__ void k_spread(int n, int npad, BoxDev box, const real* __restrict__ m
 
 // Fixed-point (or FP64) accumulation grid -> FFT input, clearing the accumulator.
 template <typename real>
-__global__ void k_grid_finish(size_t total, typename GridAcc<real>::type* __restrict__ acc, real* __restrict__ out,
+MPID_KERNEL void k_grid_finish(KGrid<> kg, size_t total, typename GridAcc<real>::type* __restrict__ acc, real* __restrict__ out,
                               const int* __restrict__ skip) {
     if (skip && *skip) return;
-    for (size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t) gridDim.x * blockDim.x) {
+    for (size_t i = (size_t) kg.bx * blockDim.x + threadIdx.x; i < total; i += (size_t) kg.nb * blockDim.x) {
         if constexpr (sizeof(real) == 4) {
             out[i] = (real) ((double) (long long) acc[i] * kFixedInv);
         } else {
@@ -1816,11 +1850,11 @@ __global__ void k_grid_finish(size_t total, typename GridAcc<real>::type* __rest
 
 // Reciprocal influence function on the half-complex grid (kx, ky, kz <= nz/2),
 // MPIDReferenceForce.cpp:3329-3366: exp(-pi^2 m^2/alpha^2)/(pi V m^2 B(m)), 0 at m = 0.
-__global__ void k_influence(BoxDev box, double alpha, const double* __restrict__ modx, const double* __restrict__ mody,
+MPID_KERNEL void k_influence(KGrid<> kg, BoxDev box, double alpha, const double* __restrict__ modx, const double* __restrict__ mody,
                             const double* __restrict__ modz, double volume, double* __restrict__ out) {
     const int nx = box.grid[0], ny = box.grid[1], nz = box.grid[2], nzh = nz / 2 + 1;
     const size_t total = (size_t) nx * ny * nzh;
-    for (size_t idx = (size_t) blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t) gridDim.x * blockDim.x) {
+    for (size_t idx = (size_t) kg.bx * blockDim.x + threadIdx.x; idx < total; idx += (size_t) kg.nb * blockDim.x) {
         const int kz = (int) (idx % nzh);
         const int ky = (int) ((idx / nzh) % ny);
         const int kx = (int) (idx / ((size_t) nzh * ny));
@@ -1843,10 +1877,10 @@ template <> struct Cplx<float> { typedef float2 type; };
 template <> struct Cplx<double> { typedef double2 type; };
 
 template <typename real>
-__global__ void k_convolve(size_t total, const double* __restrict__ influence, typename Cplx<real>::type* __restrict__ g,
+MPID_KERNEL void k_convolve(KGrid<> kg, size_t total, const double* __restrict__ influence, typename Cplx<real>::type* __restrict__ g,
                            const int* __restrict__ skip) {
     if (skip && *skip) return;
-    for (size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t) gridDim.x * blockDim.x) {
+    for (size_t i = (size_t) kg.bx * blockDim.x + threadIdx.x; i < total; i += (size_t) kg.nb * blockDim.x) {
         const real f = (real) influence[i];
         typename Cplx<real>::type v = g[i];
         v.x *= f;
@@ -1871,15 +1905,14 @@ struct GatherShape {
 };
 
 template <typename real, int ORDER, int NTERM>
-__global__ void __launch_bounds__(GatherShape<real, ORDER, NTERM>::threads)
-k_gather(int n, int npad, BoxDev box, const real* __restrict__ theta, const int* __restrict__ igrid,
+MPID_KERNEL void k_gather(KGrid<(GatherShape<real, ORDER, NTERM>::threads)> kg, int n, int npad, BoxDev box, const real* __restrict__ theta, const int* __restrict__ igrid,
          const real* __restrict__ grid, real* __restrict__ phi, const int* __restrict__ skip) {
     if (skip && *skip) return;
     constexpr int APB = GatherShape<real, ORDER, NTERM>::atoms;
     constexpr int MAXD = NTERM == 4 ? 1 : (NTERM == 10 ? 2 : 4);
     __shared__ real part[ORDER][NTERM][APB];
     const int a = threadIdx.x % APB, iz = threadIdx.x / APB;
-    const int s0 = blockIdx.x * APB, s = s0 + a;
+    const int s0 = kg.bx * APB, s = s0 + a;
     real acc[NTERM];
 #pragma unroll
     for (int k = 0; k < NTERM; ++k) acc[k] = real(0);
@@ -1958,10 +1991,10 @@ __device__ __forceinline__ void sym_mul(const real* S, int npad, int s, const re
 // Total permanent field E = real space (fixed point) - A^T grad phi_recip + self term
 // (MPIDReferenceForce.cpp:2922-2949), then mu_direct = alpha E and S E.
 template <typename real>
-__global__ void k_record_fixed(int n, int npad, BoxDev box, double selfCoef, const unsigned long long* __restrict__ fx,
+MPID_KERNEL void k_record_fixed(KGrid<> kg, int n, int npad, BoxDev box, double selfCoef, const unsigned long long* __restrict__ fx,
                                const real* __restrict__ phi, AtomArrays<real> at, real* __restrict__ Efix,
                                real* __restrict__ muD, real* __restrict__ SE) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     real E[3] = {real(0), real(0), real(0)};
     if (s < n) {
@@ -1985,10 +2018,10 @@ __global__ void k_record_fixed(int n, int npad, BoxDev box, double selfCoef, con
 
 // sp = S p, and its fractional dipole for the spread (charge slot zero).
 template <typename real>
-__global__ void k_apply_sroot(int npad, BoxDev box, const real* __restrict__ S, const real* __restrict__ p,
+MPID_KERNEL void k_apply_sroot(KGrid<> kg, int npad, BoxDev box, const real* __restrict__ S, const real* __restrict__ p,
                               real* __restrict__ sp, real* __restrict__ mfd, const int* __restrict__ skip) {
     if (skip && *skip) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     real v[3] = {p[s], p[npad + s], p[2 * npad + s]}, o[3];
     sym_mul(S, npad, s, v, o);
@@ -2002,10 +2035,10 @@ __global__ void k_apply_sroot(int npad, BoxDev box, const real* __restrict__ S, 
 
 // Fractional dipoles of a dipole field (for spreading mu directly).
 template <typename real>
-__global__ void k_frac_dipoles(int npad, BoxDev box, const real* __restrict__ mu, real* __restrict__ mfd,
+MPID_KERNEL void k_frac_dipoles(KGrid<> kg, int npad, BoxDev box, const real* __restrict__ mu, real* __restrict__ mfd,
                                const int* __restrict__ skip) {
     if (skip && *skip) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     const real o[3] = {mu[s], mu[npad + s], mu[2 * npad + s]};
     mfd[s] = real(0);
@@ -2017,12 +2050,12 @@ __global__ void k_frac_dipoles(int npad, BoxDev box, const real* __restrict__ mu
 // (MPIDReferenceForce.cpp:4073-4141).  Writes E (and optionally the gradient with the
 // reciprocal part added, MPIDReferenceForce.cpp:4094-4130).
 template <typename real>
-__global__ void k_dipole_field_total(int n, int npad, BoxDev box, double selfCoef, const unsigned long long* __restrict__ fx,
+MPID_KERNEL void k_dipole_field_total(KGrid<> kg, int n, int npad, BoxDev box, double selfCoef, const unsigned long long* __restrict__ fx,
                                      const unsigned long long* __restrict__ gfx, const real* __restrict__ phi, int nterm,
                                      const real* __restrict__ mu, real* __restrict__ E, real* __restrict__ G,
                                      const int* __restrict__ skip) {
     if (skip && *skip) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     for (int c = 0; c < 3; ++c) {
         double e = 0.0;
@@ -2053,12 +2086,12 @@ __global__ void k_dipole_field_total(int n, int npad, BoxDev box, double selfCoe
 
 // q = p - S E (the CG operator B = I - S T S applied to p) and per-block partial p.q.
 template <typename real>
-__global__ void k_cg_finish_matvec(int npad, const real* __restrict__ S, const real* __restrict__ p,
+MPID_KERNEL void k_cg_finish_matvec(KGrid<> kg, int npad, const real* __restrict__ S, const real* __restrict__ p,
                                    const real* __restrict__ E, real* __restrict__ q, double* __restrict__ partial,
                                    const int* __restrict__ skip) {
     __shared__ double red[256];
     if (skip && *skip) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     double acc = 0.0;
     if (s < npad) {
         real e[3] = {E[s], E[npad + s], E[2 * npad + s]}, se[3];
@@ -2076,11 +2109,11 @@ __global__ void k_cg_finish_matvec(int npad, const real* __restrict__ S, const r
         if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) partial[kg.bx] = red[0];
 }
 
 // Deterministic final reduction of per-block partials (one block).
-__global__ void k_reduce_partials(int nblocks, int nvals, const double* __restrict__ partial, double* __restrict__ out,
+MPID_KERNEL void k_reduce_partials(KGrid<> kg, int nblocks, int nvals, const double* __restrict__ partial, double* __restrict__ out,
                                   const int* __restrict__ skip) {
     __shared__ double red[1024];
     if (skip && *skip) return;
@@ -2101,13 +2134,13 @@ __global__ void k_reduce_partials(int nblocks, int nvals, const double* __restri
 // CG scalars: slot 0 rr, 1 pq, 2 rr_new, 3 |S r|^2, 4 alpha, 5 beta, 6 metric.
 // x += a p, r -= a q; partials of r.r and |S r|^2.
 template <typename real, typename xreal>
-__global__ void k_cg_update(int npad, const real* __restrict__ S, double* __restrict__ sc, const real* __restrict__ p,
+MPID_KERNEL void k_cg_update(KGrid<> kg, int npad, const real* __restrict__ S, double* __restrict__ sc, const real* __restrict__ p,
                             const real* __restrict__ q, xreal* __restrict__ x, real* __restrict__ r,
                             double* __restrict__ partial, int nblocks, const int* __restrict__ skip) {
     __shared__ double red[2][256];
     if (skip && *skip) return;
     const double a = sc[0] / sc[1];
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     double rr = 0.0, sr = 0.0;
     if (s < npad) {
         real rv[3];
@@ -2132,14 +2165,14 @@ __global__ void k_cg_update(int npad, const real* __restrict__ S, double* __rest
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        partial[blockIdx.x] = red[0][0];
-        partial[nblocks + blockIdx.x] = red[1][0];
+        partial[kg.bx] = red[0][0];
+        partial[nblocks + kg.bx] = red[1][0];
     }
 }
 
 // After the reductions: beta, convergence test 48.033324 sqrt(|S r|^2 / n) < target
 // (MPIDReferenceForce.cpp:1219), iteration limit.  done[0] = 1 stops the loop.
-__global__ void k_cg_scalars(double* __restrict__ sc, const double* __restrict__ red, int n, double target,
+MPID_KERNEL void k_cg_scalars(KGrid<> kg, double* __restrict__ sc, const double* __restrict__ red, int n, double target,
                              int* __restrict__ iter, int maxIter, int* __restrict__ done) {
     if (*done) return;
     sc[2] = red[0];
@@ -2152,10 +2185,10 @@ __global__ void k_cg_scalars(double* __restrict__ sc, const double* __restrict__
 }
 
 template <typename real>
-__global__ void k_cg_direction(int npad, const double* __restrict__ sc, const real* __restrict__ r, real* __restrict__ p,
+MPID_KERNEL void k_cg_direction(KGrid<> kg, int npad, const double* __restrict__ sc, const real* __restrict__ r, real* __restrict__ p,
                                const int* __restrict__ skip) {
     if (skip && *skip) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     const double b = sc[5];
     for (int c = 0; c < 3; ++c) p[c * npad + s] = real((double) r[c * npad + s] + b * (double) p[c * npad + s]);
@@ -2163,10 +2196,10 @@ __global__ void k_cg_direction(int npad, const double* __restrict__ sc, const re
 
 // Initial CG state from the right-hand side: r = p = b, x = 0, partials of r.r and |S r|^2.
 template <typename real, typename xreal>
-__global__ void k_cg_start(int npad, const real* __restrict__ S, const real* __restrict__ b, xreal* __restrict__ x,
+MPID_KERNEL void k_cg_start(KGrid<> kg, int npad, const real* __restrict__ S, const real* __restrict__ b, xreal* __restrict__ x,
                            real* __restrict__ r, real* __restrict__ p, double* __restrict__ partial, int nblocks) {
     __shared__ double red[2][256];
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     double rr = 0.0, sr = 0.0;
     if (s < npad) {
         real v[3];
@@ -2192,12 +2225,12 @@ __global__ void k_cg_start(int npad, const real* __restrict__ S, const real* __r
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        partial[blockIdx.x] = red[0][0];
-        partial[nblocks + blockIdx.x] = red[1][0];
+        partial[kg.bx] = red[0][0];
+        partial[nblocks + kg.bx] = red[1][0];
     }
 }
 
-__global__ void k_cg_init_scalars(double* __restrict__ sc, const double* __restrict__ red, int n, double target,
+MPID_KERNEL void k_cg_init_scalars(KGrid<> kg, double* __restrict__ sc, const double* __restrict__ red, int n, double target,
                                   int* __restrict__ iter, int* __restrict__ done) {
     sc[0] = red[0];
     sc[3] = red[1];
@@ -2226,13 +2259,13 @@ __device__ __forceinline__ double block_sum_256(double v, double* red) {
     return t;
 }
 
-// True in exactly one block: the last of gridDim.x blocks to pass this point (after
-// each block has published its partials).
-__device__ __forceinline__ bool last_block(unsigned* counter) {
+// True in exactly one block: the last of the `nblocks` blocks sharing `counter` to pass
+// this point (after each block has published its partials).
+__device__ __forceinline__ bool last_block(unsigned* counter, unsigned nblocks) {
     __shared__ bool last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == nblocks - 1;
     __syncthreads();
     return last;
 }
@@ -2247,12 +2280,12 @@ __device__ __forceinline__ double sum_partials_256(const double* partial, int nb
 // Start of an iteration: p = r + beta p (not on the first), sp = S p and the fractional
 // dipoles of sp for the reciprocal-space spread.
 template <typename real>
-__global__ void k_cg_direction_sroot(int npad, BoxDev box, const real* __restrict__ S, const double* __restrict__ sc,
+MPID_KERNEL void k_cg_direction_sroot(KGrid<> kg, int npad, BoxDev box, const real* __restrict__ S, const double* __restrict__ sc,
                                      int first, const real* __restrict__ r, real* __restrict__ p, real* __restrict__ sp,
                                      real* __restrict__ mfd, const typename Vec4<real>::type* __restrict__ prm,
                                      typename Vec4<real>::type* __restrict__ A1, const int* __restrict__ skip) {
     if (*skip) return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     real v[3];
     if (first) {
@@ -2278,14 +2311,13 @@ __global__ void k_cg_direction_sroot(int npad, BoxDev box, const real* __restric
 // E = T sp (real space from the fixed-point accumulator, which is cleared here, plus
 // reciprocal and self terms), q = p - S E, and sc[1] = p.q.
 template <typename real>
-__global__ void __launch_bounds__(256)
-k_cg_matvec_finish(int n, int npad, BoxDev box, double selfCoef, unsigned long long* __restrict__ fx,
+MPID_KERNEL void k_cg_matvec_finish(KGrid<256> kg, int n, int npad, BoxDev box, double selfCoef, unsigned long long* __restrict__ fx,
                    const real* __restrict__ phi, const real* __restrict__ S, const real* __restrict__ p,
                    const real* __restrict__ sp, real* __restrict__ q, double* __restrict__ partial,
                    unsigned* __restrict__ counter, double* __restrict__ sc, const int* __restrict__ skip) {
     __shared__ double red[256];
     if (*skip) return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     double acc = 0.0;
     if (s < npad) {
         real e[3];
@@ -2309,9 +2341,9 @@ k_cg_matvec_finish(int n, int npad, BoxDev box, double selfCoef, unsigned long l
         }
     }
     const double b = block_sum_256(acc, red);
-    if (threadIdx.x == 0) partial[blockIdx.x] = b;
-    if (last_block(counter)) {
-        const double pq = sum_partials_256(partial, gridDim.x, red);
+    if (threadIdx.x == 0) partial[kg.bx] = b;
+    if (last_block(counter, kg.nb)) {
+        const double pq = sum_partials_256(partial, kg.nb, red);
         if (threadIdx.x == 0) {
             sc[1] = pq;
             *counter = 0u;
@@ -2323,15 +2355,14 @@ k_cg_matvec_finish(int n, int npad, BoxDev box, double selfCoef, unsigned long l
 // 48.033324 sqrt(|S r|^2 / n) < target (MPIDReferenceForce.cpp:1219) and the iteration
 // limit; done = 1 stops the loop.  sc: 0 rr, 1 pq, 2 rr_new, 3 |S r|^2, 5 beta, 6 metric.
 template <typename real, typename xreal>
-__global__ void __launch_bounds__(256)
-k_cg_update_scalars(int n, int npad, const real* __restrict__ S, double* __restrict__ sc, const real* __restrict__ p,
+MPID_KERNEL void k_cg_update_scalars(KGrid<256> kg, int n, int npad, const real* __restrict__ S, double* __restrict__ sc, const real* __restrict__ p,
                     const real* __restrict__ q, xreal* __restrict__ x, real* __restrict__ r, double* __restrict__ partial,
                     unsigned* __restrict__ counter, double target, int* __restrict__ iter, int maxIter,
                     int* __restrict__ done, int pcg) {
     __shared__ double red[256];
     if (*done) return;
     const double a = sc[0] / sc[1];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     double rr = 0.0, sr = 0.0;
     if (s < npad) {
         real rv[3];
@@ -2348,12 +2379,12 @@ k_cg_update_scalars(int n, int npad, const real* __restrict__ S, double* __restr
     const double b0 = block_sum_256(rr, red);
     const double b1 = block_sum_256(sr, red);
     if (threadIdx.x == 0) {
-        partial[blockIdx.x] = b0;
-        partial[gridDim.x + blockIdx.x] = b1;
+        partial[kg.bx] = b0;
+        partial[kg.nb + kg.bx] = b1;
     }
-    if (last_block(counter)) {
-        const double rrNew = sum_partials_256(partial, gridDim.x, red);
-        const double srNew = sum_partials_256(partial + gridDim.x, gridDim.x, red);
+    if (last_block(counter, kg.nb)) {
+        const double rrNew = sum_partials_256(partial, kg.nb, red);
+        const double srNew = sum_partials_256(partial + kg.nb, kg.nb, red);
         if (threadIdx.x == 0) {
             sc[2] = rrNew;
             sc[3] = srNew;
@@ -2398,14 +2429,13 @@ __device__ __forceinline__ void cgcg_operator_input(int npad, int s, const BoxDe
 
 // r = b, x = p = s = 0; gamma, the metric of r and the operator input of r.
 template <typename real, typename xreal>
-__global__ void __launch_bounds__(256)
-k_cgcg_start(int n, int npad, BoxDev box, const real* __restrict__ S, const real* __restrict__ b, xreal* __restrict__ x,
+MPID_KERNEL void k_cgcg_start(KGrid<256> kg, int n, int npad, BoxDev box, const real* __restrict__ S, const real* __restrict__ b, xreal* __restrict__ x,
              real* __restrict__ r, real* __restrict__ p, real* __restrict__ sv, real* __restrict__ sp,
              real* __restrict__ mfd, const typename Vec4<real>::type* __restrict__ prm,
              typename Vec4<real>::type* __restrict__ A1, double* __restrict__ partial, unsigned* __restrict__ counter,
              double* __restrict__ sc, double target, int* __restrict__ iter, int* __restrict__ done) {
     __shared__ double red[256];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     double rr = 0.0, sr = 0.0;
     if (s < npad) {
         real v[3];
@@ -2425,12 +2455,12 @@ k_cgcg_start(int n, int npad, BoxDev box, const real* __restrict__ S, const real
     const double b0 = block_sum_256(rr, red);
     const double b1 = block_sum_256(sr, red);
     if (threadIdx.x == 0) {
-        partial[blockIdx.x] = b0;
-        partial[gridDim.x + blockIdx.x] = b1;
+        partial[kg.bx] = b0;
+        partial[kg.nb + kg.bx] = b1;
     }
-    if (last_block(counter)) {
-        const double g = sum_partials_256(partial, gridDim.x, red);
-        const double m = sum_partials_256(partial + gridDim.x, gridDim.x, red);
+    if (last_block(counter, kg.nb)) {
+        const double g = sum_partials_256(partial, kg.nb, red);
+        const double m = sum_partials_256(partial + kg.nb, kg.nb, red);
         if (threadIdx.x == 0) {
             sc[0] = g;
             sc[3] = m;
@@ -2447,15 +2477,14 @@ k_cgcg_start(int n, int npad, BoxDev box, const real* __restrict__ S, const real
 // w = B r (real space from the fixed-point accumulator, which is cleared here, plus the
 // reciprocal and self terms), delta = w.r, then alpha (first iteration: gamma / delta).
 template <typename real>
-__global__ void __launch_bounds__(256)
-k_cgcg_finish(int n, int npad, BoxDev box, double selfCoef, unsigned long long* __restrict__ fx,
+MPID_KERNEL void k_cgcg_finish(KGrid<256> kg, int n, int npad, BoxDev box, double selfCoef, unsigned long long* __restrict__ fx,
               const real* __restrict__ phi, const real* __restrict__ S, const real* __restrict__ r,
               const real* __restrict__ sp, real* __restrict__ w, double* __restrict__ partial,
               unsigned* __restrict__ counter, double* __restrict__ sc, const int* __restrict__ iter,
               const int* __restrict__ skip) {
     __shared__ double red[256];
     if (*skip) return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     double acc = 0.0;
     if (s < npad) {
         real e[3];
@@ -2479,9 +2508,9 @@ k_cgcg_finish(int n, int npad, BoxDev box, double selfCoef, unsigned long long* 
         }
     }
     const double b = block_sum_256(acc, red);
-    if (threadIdx.x == 0) partial[blockIdx.x] = b;
-    if (last_block(counter)) {
-        const double delta = sum_partials_256(partial, gridDim.x, red);
+    if (threadIdx.x == 0) partial[kg.bx] = b;
+    if (last_block(counter, kg.nb)) {
+        const double delta = sum_partials_256(partial, kg.nb, red);
         if (threadIdx.x == 0) {
             const double g = sc[0], beta = sc[5];
             sc[1] = delta;
@@ -2495,8 +2524,7 @@ k_cgcg_finish(int n, int npad, BoxDev box, double selfCoef, unsigned long long* 
 // convergence test and the iteration limit (done = 1 stops the loop: the kernels of the
 // remaining iterations return at once), and the operator input of the new r.
 template <typename real, typename xreal>
-__global__ void __launch_bounds__(256)
-k_cgcg_update(int n, int npad, BoxDev box, const real* __restrict__ S, double* __restrict__ sc,
+MPID_KERNEL void k_cgcg_update(KGrid<256> kg, int n, int npad, BoxDev box, const real* __restrict__ S, double* __restrict__ sc,
               const real* __restrict__ w, real* __restrict__ p, real* __restrict__ sv, xreal* __restrict__ x,
               real* __restrict__ r, real* __restrict__ sp, real* __restrict__ mfd,
               const typename Vec4<real>::type* __restrict__ prm, typename Vec4<real>::type* __restrict__ A1,
@@ -2505,7 +2533,7 @@ k_cgcg_update(int n, int npad, BoxDev box, const real* __restrict__ S, double* _
     __shared__ double red[256];
     if (*done) return;
     const double a = sc[4], beta = sc[5];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     double rr = 0.0, sr = 0.0;
     if (s < npad) {
         real rv[3];
@@ -2528,12 +2556,12 @@ k_cgcg_update(int n, int npad, BoxDev box, const real* __restrict__ S, double* _
     const double b0 = block_sum_256(rr, red);
     const double b1 = block_sum_256(sr, red);
     if (threadIdx.x == 0) {
-        partial[blockIdx.x] = b0;
-        partial[gridDim.x + blockIdx.x] = b1;
+        partial[kg.bx] = b0;
+        partial[kg.nb + kg.bx] = b1;
     }
-    if (last_block(counter)) {
-        const double g = sum_partials_256(partial, gridDim.x, red);
-        const double m = sum_partials_256(partial + gridDim.x, gridDim.x, red);
+    if (last_block(counter, kg.nb)) {
+        const double g = sum_partials_256(partial, kg.nb, red);
+        const double m = sum_partials_256(partial + kg.nb, kg.nb, red);
         if (threadIdx.x == 0) {
             sc[5] = g / sc[0];
             sc[0] = g;
@@ -2555,11 +2583,10 @@ k_cgcg_update(int n, int npad, BoxDev box, const real* __restrict__ S, double* _
 
 // w_i = T_n v over atom i's near pairs, v_j = S_j r_j (fixed-point accumulation).
 template <typename real>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_precond_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ r, unsigned long long* __restrict__ w,
+MPID_KERNEL void k_precond_field(KGrid<(32 * kWarpsPerBlock)> kg, NbrList nl, AtomArrays<real> at, const real* __restrict__ r, unsigned long long* __restrict__ w,
                 const int* __restrict__ skip) {
     if (*skip) return;
-    const int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int wi = (kg.bx * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (nl.nchunksS == 0) return;
     const int I = wi / nl.nchunksS;
     const int k0 = (wi - I * nl.nchunksS) * nl.chunk;
@@ -2601,14 +2628,13 @@ k_precond_field(NbrList nl, AtomArrays<real> at, const real* __restrict__ r, uns
 // z = r + S w (w read and cleared), r.z; on the first application also p = z and
 // sc[0] = r.z, afterwards sc[5] = beta = (r.z)_new / (r.z)_old and sc[0] = (r.z)_new.
 template <typename real>
-__global__ void __launch_bounds__(256)
-k_precond_finish(int n, int npad, const real* __restrict__ S, unsigned long long* __restrict__ wfx,
+MPID_KERNEL void k_precond_finish(KGrid<256> kg, int n, int npad, const real* __restrict__ S, unsigned long long* __restrict__ wfx,
                  const real* __restrict__ r, real* __restrict__ z, real* __restrict__ p, int first,
                  double* __restrict__ partial, unsigned* __restrict__ counter, double* __restrict__ sc,
                  const int* __restrict__ skip) {
     __shared__ double red[256];
     if (*skip) return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     double acc = 0.0;
     if (s < npad) {
         real wv[3];
@@ -2627,9 +2653,9 @@ k_precond_finish(int n, int npad, const real* __restrict__ S, unsigned long long
         }
     }
     const double b = block_sum_256(acc, red);
-    if (threadIdx.x == 0) partial[blockIdx.x] = b;
-    if (last_block(counter)) {
-        const double rz = sum_partials_256(partial, gridDim.x, red);
+    if (threadIdx.x == 0) partial[kg.bx] = b;
+    if (last_block(counter, kg.nb)) {
+        const double rz = sum_partials_256(partial, kg.nb, red);
         if (threadIdx.x == 0) {
             if (!first) sc[5] = rz / sc[0];
             sc[0] = rz;
@@ -2640,8 +2666,8 @@ k_precond_finish(int n, int npad, const real* __restrict__ S, unsigned long long
 
 // mu = S y (sorted), in the precision of the pair kernels.
 template <typename xreal, typename real>
-__global__ void k_mu_from_y(int npad, const xreal* __restrict__ S, const xreal* __restrict__ y, real* __restrict__ mu) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+MPID_KERNEL void k_mu_from_y(KGrid<> kg, int npad, const xreal* __restrict__ S, const xreal* __restrict__ y, real* __restrict__ mu) {
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     xreal v[3] = {y[s], y[npad + s], y[2 * npad + s]}, o[3];
     sym_mul(S, npad, s, v, o);
@@ -2650,11 +2676,11 @@ __global__ void k_mu_from_y(int npad, const xreal* __restrict__ S, const xreal* 
 
 // FP64 residual of the refinement loop: res = S (E + T S y) - y with T S y already in E2
 // (E2 = field of mu = S y, including reciprocal and self terms).  Partial |S res|^2.
-__global__ void k_refine_residual(int npad, const double* __restrict__ S, const double* __restrict__ Efix,
+MPID_KERNEL void k_refine_residual(KGrid<> kg, int npad, const double* __restrict__ S, const double* __restrict__ Efix,
                                   const double* __restrict__ E2, const double* __restrict__ y, double* __restrict__ res,
                                   float* __restrict__ res32, double* __restrict__ partial) {
     __shared__ double red[256];
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = kg.bx * blockDim.x + threadIdx.x;
     double acc = 0.0;
     if (s < npad) {
         double e[3] = {Efix[s] + E2[s], Efix[npad + s] + E2[npad + s], Efix[2 * npad + s] + E2[2 * npad + s]}, se[3];
@@ -2675,19 +2701,19 @@ __global__ void k_refine_residual(int npad, const double* __restrict__ S, const 
         if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) partial[kg.bx] = red[0];
 }
 
 template <typename real>
-__global__ void k_axpy_to_double(int npad3, const real* __restrict__ d, double* __restrict__ y) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+MPID_KERNEL void k_axpy_to_double(KGrid<> kg, int npad3, const real* __restrict__ d, double* __restrict__ y) {
+    int i = kg.bx * blockDim.x + threadIdx.x;
     if (i < npad3) y[i] += (double) d[i];
 }
 
 // mu_(m+1) = alpha E_m for the extrapolated solver; mu_out accumulates cbar-weighted sum.
 template <typename real>
-__global__ void k_alpha_times(int npad, const real* __restrict__ alab, const real* __restrict__ E, real* __restrict__ out) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+MPID_KERNEL void k_alpha_times(KGrid<> kg, int npad, const real* __restrict__ alab, const real* __restrict__ E, real* __restrict__ out) {
+    int s = kg.bx * blockDim.x + threadIdx.x;
     if (s >= npad) return;
     real v[3] = {E[s], E[npad + s], E[2 * npad + s]}, o[3];
     sym_mul(alab, npad, s, v, o);
@@ -2695,8 +2721,8 @@ __global__ void k_alpha_times(int npad, const real* __restrict__ alab, const rea
 }
 
 template <typename real>
-__global__ void k_axpy(int n3, real a, const real* __restrict__ x, real* __restrict__ y) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+MPID_KERNEL void k_axpy(KGrid<> kg, int n3, real a, const real* __restrict__ x, real* __restrict__ y) {
+    int i = kg.bx * blockDim.x + threadIdx.x;
     if (i < n3) y[i] += a * x[i];
 }
 
@@ -2711,12 +2737,12 @@ struct OptArgs {
 };
 
 template <typename real>
-__global__ void k_recip_self(int n, int npad, BoxDev box, double alpha, int polType, const real* __restrict__ phiP,
+MPID_KERNEL void k_recip_self(KGrid<> kg, int n, int npad, BoxDev box, double alpha, int polType, const real* __restrict__ phiP,
                              const real* __restrict__ phiD, const real* __restrict__ mu, AtomArrays<real> at,
                              const double* __restrict__ mom64, OptArgs opt, unsigned long long* __restrict__ force,
                              unsigned long long* __restrict__ torque, double* __restrict__ energyPartial) {
     __shared__ double red[256];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = kg.bx * blockDim.x + threadIdx.x;
     double eAcc = 0.0;
     if (s < n) {
         const bool aniso = at.prm[s].z != real(0);
@@ -2834,13 +2860,13 @@ __global__ void k_recip_self(int n, int npad, BoxDev box, double alpha, int polT
         if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) energyPartial[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) energyPartial[kg.bx] = red[0];
 }
 
 // Torque on each atom -> forces on it and its frame atoms (original order loop).
-__global__ void k_torque_map(int n, int npad, const double* __restrict__ pos, MolArrays mol, const int* __restrict__ rank,
+MPID_KERNEL void k_torque_map(KGrid<> kg, int n, int npad, const double* __restrict__ pos, MolArrays mol, const int* __restrict__ rank,
                              const unsigned long long* __restrict__ torque, unsigned long long* __restrict__ force) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = kg.bx * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int ax = mol.axis[i];
     if (ax == NoAxisType) return;
@@ -2862,9 +2888,9 @@ __global__ void k_torque_map(int n, int npad, const double* __restrict__ pos, Mo
 }
 
 // out[i] += F (accumulate, as OpenMM kernels add into the context force buffer).
-__global__ void k_forces_out(int n, int npad, const int* __restrict__ rank, const unsigned long long* __restrict__ force,
+MPID_KERNEL void k_forces_out(KGrid<> kg, int n, int npad, const int* __restrict__ rank, const unsigned long long* __restrict__ force,
                              double* __restrict__ out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = kg.bx * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int s = rank[i];
     for (int c = 0; c < 3; ++c) out[3 * i + c] += fx_get(force, c * npad + s);
@@ -2872,9 +2898,9 @@ __global__ void k_forces_out(int n, int npad, const int* __restrict__ rank, cons
 
 // Dipoles in original order: which 0 induced, 1 lab permanent, 2 total.
 template <typename real>
-__global__ void k_dipoles_out(int n, int npad, int which, const int* __restrict__ rank, const real* __restrict__ mom,
+MPID_KERNEL void k_dipoles_out(KGrid<> kg, int n, int npad, int which, const int* __restrict__ rank, const real* __restrict__ mom,
                               const real* __restrict__ mu, double* __restrict__ out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = kg.bx * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int s = rank[i];
     for (int c = 0; c < 3; ++c) {
@@ -2882,6 +2908,40 @@ __global__ void k_dipoles_out(int n, int npad, int which, const int* __restrict_
         if (which != 1) v += (double) mu[c * npad + s];
         if (which != 0) v += (double) mom[(1 + c) * npad + s];
         out[3 * i + c] = v;
+    }
+}
+
+
+// Byte fill and copy of one buffer, grid-stride (the memsets and device copies of an
+// evaluation when many boxes run as one launch per operation).  16- or 4-byte words when
+// the pointers and the size allow, else bytes.  The copy's destination may be pinned host
+// memory (mapped into the device's address space).
+MPID_KERNEL void k_fill_bytes(KGrid<> kg, unsigned char* __restrict__ p, int value, size_t bytes) {
+    const size_t stride = (size_t) kg.nb * blockDim.x;
+    const size_t t0 = (size_t) kg.bx * blockDim.x + threadIdx.x;
+    if ((((uintptr_t) p | bytes) & 15) == 0) {
+        const unsigned b = (unsigned) value & 0xffu, w = b * 0x01010101u;
+        const uint4 v = make_uint4(w, w, w, w);
+        uint4* q = (uint4*) p;
+        for (size_t i = t0; i < bytes / 16; i += stride) q[i] = v;
+    } else {
+        for (size_t i = t0; i < bytes; i += stride) p[i] = (unsigned char) value;
+    }
+}
+MPID_KERNEL void k_copy_bytes(KGrid<> kg, unsigned char* __restrict__ dst, const unsigned char* __restrict__ src,
+                              size_t bytes) {
+    const size_t stride = (size_t) kg.nb * blockDim.x;
+    const size_t t0 = (size_t) kg.bx * blockDim.x + threadIdx.x;
+    if ((((uintptr_t) dst | (uintptr_t) src | bytes) & 15) == 0) {
+        const uint4* a = (const uint4*) src;
+        uint4* q = (uint4*) dst;
+        for (size_t i = t0; i < bytes / 16; i += stride) q[i] = a[i];
+    } else if ((((uintptr_t) dst | (uintptr_t) src | bytes) & 3) == 0) {
+        const unsigned* a = (const unsigned*) src;
+        unsigned* q = (unsigned*) dst;
+        for (size_t i = t0; i < bytes / 4; i += stride) q[i] = a[i];
+    } else {
+        for (size_t i = t0; i < bytes; i += stride) dst[i] = src[i];
     }
 }
 

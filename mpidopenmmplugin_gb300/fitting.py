@@ -20,7 +20,7 @@ import concurrent.futures as _cf
 
 import numpy as np
 
-from .context import MPIDContext
+from .context import MPIDContext, MPIDError
 from .force import MPIDForce
 
 NPARAM = 24
@@ -30,10 +30,12 @@ COLUMNS = (["charge", "dipoleX", "dipoleY", "dipoleZ", "quadXX", "quadXY", "quad
 
 
 def per_type(grad, types, ntypes):
-    """(n, k) per-atom gradients -> (ntypes, k) sums over the atoms of each type."""
-    out = np.zeros((ntypes, grad.shape[1]))
-    np.add.at(out, np.asarray(types, dtype=np.int64), grad)
-    return out
+    """(n, k) per-atom gradients -> (ntypes, k) sums over the atoms of each type (one
+    matrix product with the atoms' one-hot type matrix)."""
+    t = np.asarray(types, dtype=np.int64)
+    onehot = np.zeros((ntypes, len(t)))
+    onehot[t, np.arange(len(t))] = 1.0
+    return onehot @ np.asarray(grad, dtype=np.float64)
 
 
 def project_traceless(g):
@@ -85,10 +87,12 @@ class BoxBatch:
     """Independent boxes sharing per-type parameters.
 
     systems: list of (force, positions (n, 3) nm, box (3, 3) nm, types (n,) ints).
-    precision: "mixed" or "double", as MPIDContext.  batched: every box's whole evaluation
-    (energy, forces, gradient passes) runs from a captured graph and all boxes in one
-    launch (mpid_evaluate_batch); otherwise host threads drive the contexts
-    concurrently, each replaying its evaluation's segments from graphs (solver_graphs).
+    precision: "mixed" or "double", as MPIDContext.  batched: all boxes evaluate in one
+    call of mpid_evaluate_batch (energy, forces, gradient passes) with no host
+    synchronisation per box; by default every operation of the evaluation is one kernel
+    launch for all boxes (launch mode 0, see evaluate_batch).  Otherwise host threads
+    drive the contexts concurrently, each replaying its evaluation's segments from graphs
+    (solver_graphs).
     """
 
     def __init__(self, systems, ntypes, precision="mixed", threads=8, device=0, solver_graphs=True, batched=True):
@@ -99,7 +103,7 @@ class BoxBatch:
                          for f, p, b, t in self.systems]
         self.threads = max(1, int(threads))
         self.batched = bool(batched)
-        self.batch_streams = 0  # batched launch: 0 one parent graph, k > 0 per-box graphs on k streams
+        self.batch_launch = 0  # batched launch mode: 0 fused, -1 one parent graph, k > 0 per-box graphs on k streams
         self._pool = _cf.ThreadPoolExecutor(max_workers=self.threads)
 
     def set_parameters(self, params):
@@ -124,18 +128,33 @@ class BoxBatch:
             from .context import evaluate_batch
             energies, fo, gm, gp = evaluate_batch(self.contexts, [s[1] for s in self.systems],
                                                   [s[2] for s in self.systems], forces=forces,
-                                                  streams=self.batch_streams)
+                                                  launch=self.batch_launch, flat=True)
+            # per-type sums over the atoms of all boxes at once
+            types = np.concatenate([np.asarray(s[3]) for s in self.systems])
             grad = np.zeros((self.ntypes, NPARAM))
-            for (f, p, b, t), m, q in zip(self.systems, gm, gp):
-                grad[:, :20] += per_type(m, t, self.ntypes)
-                grad[:, 20:] += per_type(q, t, self.ntypes)
-            return energies, (fo if forces else [None] * len(self.systems)), grad
+            grad[:, :20] = per_type(gm, types, self.ntypes)
+            grad[:, 20:] = per_type(gp, types, self.ntypes)
+            if forces:
+                ends = np.cumsum([len(s[1]) for s in self.systems])
+                fo = np.split(fo, ends[:-1])
+            else:
+                fo = [None] * len(self.systems)
+            return energies, fo, grad
         results = list(self._pool.map(lambda k: self._one(k, forces), range(len(self.systems))))
         energies = np.array([r[0] for r in results])
         grad = np.zeros((self.ntypes, NPARAM))
         for r in results:
             grad += r[2]
         return energies, [r[1] for r in results], grad
+
+    def launches(self):
+        """Kernel launches of the last evaluate(): those of the fused launch (which every
+        box shares) in launch mode 0, else the sum over the boxes' own evaluations."""
+        if not self.contexts:
+            return 0
+        if self.batched and self.batch_launch == 0:
+            return self.contexts[0].stats()["kernel_launches"]
+        return sum(c.stats()["kernel_launches"] for c in self.contexts)
 
     def tuning_key(self):
         """The workload class a tuning result applies to: GPU (name, multiprocessors),
@@ -152,17 +171,19 @@ class BoxBatch:
 
     def configure(self, config):
         """Apply a launch configuration {"max_split": bound of the pair kernels' work split
-        (MPIDContext.setWorkSplit), "streams": batched launch mode (0 one parent graph,
-        k > 0 per-box graphs on k streams)}."""
+        (MPIDContext.setWorkSplit), "launch": batched launch mode (0 fused, -1 one parent
+        graph, k > 0 per-box graphs on k streams)}."""
         self.set_work_split(int(config.get("max_split", 0)))
-        self.batch_streams = int(config.get("streams", 0))
+        self.batch_launch = int(config.get("launch", 0))
 
-    def autotune(self, splits=(0, 1, 2, 4, 8), streams=(0, 16, 32), repeats=3, path=None, use_cache=True):
+    def autotune(self, splits=(0, 1, 2, 4, 8), launches=(0, 32), repeats=3, path=None, use_cache=True):
         """Launch-configuration autotuner: times evaluate() of this batch under each
         combination of the pair kernels' work-split bound and (batched mode) the launch
         mode, keeps the fastest, and records it per GPU and workload class (tuning_key) in a
         JSON file beside the built library, where later batches of the same class find it.
-        Returns (chosen configuration, {configuration label: ms per evaluate})."""
+        A configuration the batch cannot run (the fused mode with a box above its size
+        limit) is skipped.  Returns (chosen configuration, {configuration label: ms per
+        evaluate})."""
         import json
         import os
         import time
@@ -178,16 +199,22 @@ class BoxBatch:
             best = table[key]["config"]
             self.configure(best)
             return best, table[key]["ms"]
-        configs = [{"max_split": int(m), "streams": int(q)} for m in splits for q in (streams if self.batched else (0,))]
-        times = {}
+        configs = [{"max_split": int(m), "launch": int(q)} for m in splits for q in (launches if self.batched else (0,))]
+        times, ran = {}, []
         for cfg in configs:
             self.configure(cfg)
-            self.evaluate()  # captures the graphs of this configuration
+            try:
+                self.evaluate()  # records / captures the graphs of this configuration
+            except MPIDError:
+                continue
             t0 = time.perf_counter()
             for _ in range(repeats):
                 self.evaluate()
-            times["split%d_streams%d" % (cfg["max_split"], cfg["streams"])] = 1e3 * (time.perf_counter() - t0) / repeats
-        best = configs[min(range(len(configs)), key=lambda i: list(times.values())[i])]
+            times["split%d_launch%d" % (cfg["max_split"], cfg["launch"])] = 1e3 * (time.perf_counter() - t0) / repeats
+            ran.append(cfg)
+        if not ran:
+            raise MPIDError("autotune: no configuration ran")
+        best = ran[min(range(len(ran)), key=lambda i: list(times.values())[i])]
         self.configure(best)
         table[key] = {"config": best, "ms": times}
         os.makedirs(os.path.dirname(path), exist_ok=True)

@@ -195,6 +195,9 @@ def test_batch_per_type_gradients(polarization):
     for f, _, _, _ in systems:
         f.setMutualInducedTargetEpsilon(1e-9)
     with dbl, fitting.BoxBatch(systems, 2, precision="mixed", threads=4) as mix:
+        # the second call of a batch runs its fused launches (the first sizes them)
+        dbl.evaluate(forces=False)
+        mix.evaluate(forces=False)
         _, _, gd = dbl.evaluate(forces=False)
         _, _, gmx = mix.evaluate(forces=False)
         h = 1e-2
@@ -455,23 +458,30 @@ def test_sharded_batch_on_gpu_matches_single_process():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("launch", [0, -1, 8])
 @pytest.mark.parametrize("precision", ["mixed", "double"])
-def test_batched_graph_matches_per_box_evaluations(precision):
-    """mpid_evaluate_batch (each box's whole evaluation from a captured graph, all boxes in
-    one launch) against the same boxes evaluated one context at a time: energies, forces
-    and per-type gradients to 1e-10 relative, for three calls in a row (the first takes
-    the ordinary evaluation and sizes the graphs, the later ones run from them) and for a
-    call after one box's atoms moved."""
+def test_batched_graph_matches_per_box_evaluations(precision, launch):
+    """mpid_evaluate_batch against the same boxes evaluated one context at a time, for
+    three calls in a row (the first takes the ordinary evaluation and sizes the graphs,
+    the later ones run batched) and for a call after one box's atoms moved.  Per-box
+    graphs (launch -1: one parent graph, 8: eight streams) run the per-box kernels as
+    they are: energies, forces and per-type gradients to 1e-10 relative.  The fused
+    launches (0) run the same kernel bodies with the same per-box parameters, but each
+    grid size's FFTs as one batched cuFFT plan, whose FP32 rounding differs from the
+    single-box plan's: FP64 to 1e-10, mixed to 1e-7 (energies), 1e-5 (forces) and 1e-6
+    (per-type gradients), relative."""
     systems, _ = fitting.water_batch(nboxes=6, min_waters=128, max_waters=192)
+    tol = (1e-10, 1e-10, 1e-10) if precision == "double" or launch != 0 else (1e-7, 1e-5, 1e-6)
     with fitting.BoxBatch(systems, 2, precision=precision, threads=1, batched=False) as ref, \
             fitting.BoxBatch(systems, 2, precision=precision, batched=True) as bb:
+        bb.configure({"launch": launch})
         e0, f0, g0 = ref.evaluate()
 
         def check(e1, f1, g1, e0, f0, g0):
-            assert np.allclose(e1, e0, rtol=1e-10, atol=0)
+            assert np.allclose(e1, e0, rtol=tol[0], atol=0), np.abs(e1 / e0 - 1).max()
             for a, b in zip(f1, f0):
-                assert np.abs(a - b).max() <= 1e-10 * np.abs(b).max()
-            assert np.abs(g1 - g0).max() <= 1e-10 * np.abs(g0).max()
+                assert np.abs(a - b).max() <= tol[1] * np.abs(b).max(), np.abs(a - b).max() / np.abs(b).max()
+            assert np.abs(g1 - g0).max() <= tol[2] * np.abs(g0).max(), np.abs(g1 - g0).max() / np.abs(g0).max()
 
         for step in range(3):
             e1, f1, g1 = bb.evaluate()
@@ -501,13 +511,13 @@ def test_autotuner_records_and_reuses_its_choice(tmp_path):
     path = str(tmp_path / "tuning.json")
     with fitting.BoxBatch(systems, 2, precision="mixed", batched=True) as b:
         e0, _, g0 = b.evaluate()
-        best, times = b.autotune(splits=(0, 2), streams=(0, 4), repeats=1, path=path)
-        assert best in [{"max_split": m, "streams": q} for m in (0, 2) for q in (0, 4)] and len(times) == 4
+        best, times = b.autotune(splits=(0, 2), launches=(0, 4), repeats=1, path=path)
+        assert best in [{"max_split": m, "launch": q} for m in (0, 2) for q in (0, 4)] and len(times) == 4
         rec = json.load(open(path))
         assert rec[b.tuning_key()]["config"] == best
-        again, times2 = b.autotune(splits=(0, 2), streams=(0, 4), repeats=1, path=path)  # from the record
+        again, times2 = b.autotune(splits=(0, 2), launches=(0, 4), repeats=1, path=path)  # from the record
         assert again == best and times2 == times
-        for cfg in ({"max_split": 2, "streams": 4}, {"max_split": 0, "streams": 0}):
+        for cfg in ({"max_split": 2, "launch": 4}, {"max_split": 0, "launch": 0}):
             b.configure(cfg)
             e1, _, g1 = b.evaluate()
             print(cfg, np.abs(e1 / e0 - 1).max(), np.abs(g1 - g0).max() / np.abs(g0).max())
