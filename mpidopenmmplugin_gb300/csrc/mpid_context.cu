@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <set>
 #include <memory>
 #include <mutex>
 #include <sstream>
@@ -189,9 +190,8 @@ static void launch_boxes_now(const BoxParams<typename KTraits<F>::Args>& bp, dim
 // ---------------------------------------------------------------------------
 // Recording of an evaluation's device work (fused multi-box evaluation): while a thread
 // has a recorder, launch<F>() and the op_* helpers append operations to it instead of
-// issuing them.  Streams and events are dropped: the operations are kept in issue
-// order, which is a valid serial order of the evaluation (every dependency, by stream
-// order or by event, points from an earlier-issued operation to a later one).
+// issuing them, each with the stream it was issued on; event records and waits are
+// operations too, so that the recording keeps the evaluation's stream structure.
 struct RecKernel {
     dim3 grid, block;
     size_t smem = 0;
@@ -231,7 +231,9 @@ struct RecKernelOf : RecKernel {
 };
 
 struct RecOp {
-    enum Kind { KERNEL, FILL, COPY, FFT } kind;
+    enum Kind { KERNEL, FILL, COPY, FFT, EV_RECORD, EV_WAIT } kind;
+    cudaStream_t stream = nullptr;               // the stream it was issued on
+    cudaEvent_t event = nullptr;                 // EV_RECORD, EV_WAIT
     std::unique_ptr<RecKernel> k;                // KERNEL
     void* dst = nullptr;                         // FILL, COPY, FFT (output grid)
     const void* src = nullptr;                   // COPY, FFT (input grid)
@@ -257,6 +259,7 @@ static inline void launch(dim3 grid, dim3 block, size_t smem, cudaStream_t st, A
         r->args = L::pack(std::forward<A>(a)...);
         RecOp op;
         op.kind = RecOp::KERNEL;
+        op.stream = st;
         op.k = std::move(r);
         t_recorder->ops.push_back(std::move(op));
         return;
@@ -272,6 +275,7 @@ static inline void op_memset(void* p, int value, size_t bytes, cudaStream_t st) 
     if (t_recorder) {
         RecOp op;
         op.kind = RecOp::FILL;
+        op.stream = st;
         op.dst = p;
         op.value = value;
         op.bytes = bytes;
@@ -285,6 +289,7 @@ static inline void op_copy(void* dst, const void* src, size_t bytes, cudaMemcpyK
     if (t_recorder) {
         RecOp op;
         op.kind = RecOp::COPY;
+        op.stream = st;
         op.dst = dst;
         op.src = src;
         op.bytes = bytes;
@@ -294,10 +299,26 @@ static inline void op_copy(void* dst, const void* src, size_t bytes, cudaMemcpyK
     CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, kind, st));
 }
 static inline void op_record(cudaEvent_t ev, cudaStream_t st) {
-    if (!t_recorder) CUDA_CHECK(cudaEventRecord(ev, st));
+    if (t_recorder) {
+        RecOp op;
+        op.kind = RecOp::EV_RECORD;
+        op.stream = st;
+        op.event = ev;
+        t_recorder->ops.push_back(std::move(op));
+        return;
+    }
+    CUDA_CHECK(cudaEventRecord(ev, st));
 }
 static inline void op_wait(cudaStream_t st, cudaEvent_t ev) {
-    if (!t_recorder) CUDA_CHECK(cudaStreamWaitEvent(st, ev, 0));
+    if (t_recorder) {
+        RecOp op;
+        op.kind = RecOp::EV_WAIT;
+        op.stream = st;
+        op.event = ev;
+        t_recorder->ops.push_back(std::move(op));
+        return;
+    }
+    CUDA_CHECK(cudaStreamWaitEvent(st, ev, 0));
 }
 
 // Device allocations made by any buffer so far: captured graphs key on it, so that no
@@ -374,9 +395,11 @@ struct PmeStage {
             cufftDestroy(inv);
         }
     }
+    cudaStream_t planStream = nullptr;  // the stream the plans run on
     void set_stream(cudaStream_t s) {
         CUFFT_CHECK(cufftSetStream(fwd, s));
         CUFFT_CHECK(cufftSetStream(inv, s));
+        planStream = s;
     }
     void bsplines(int n, int npad, const int* sorted, const double* wpos, const BoxDev& box, cudaStream_t st) {
         if (order == 5)
@@ -399,6 +422,7 @@ struct PmeStage {
         if (t_recorder) {
             RecOp op;
             op.kind = RecOp::FFT;
+            op.stream = planStream;
             op.src = forward ? (const void*) rgrid.p : (const void*) cgrid.p;
             op.dst = forward ? (void*) cgrid.p : (void*) rgrid.p;
             op.fftDims[0] = nx;
@@ -2620,8 +2644,8 @@ struct Context {
 //  - an FFT: the boxes' grids are gathered into one array per grid size, transformed
 //    by one batched cuFFT plan (cufftPlanMany) per size, and scattered back.
 // The sequence is captured once as one CUDA graph and replayed while no box's recording
-// changes.  One stream: the boxes' own parallel branches (reciprocal space beside real
-// space) run one after the other, the parallelism being across boxes.
+// changes, with the boxes' stream structure (lanes, below): a box's reciprocal-space
+// chain runs beside its real-space kernels as in a single-box evaluation.
 template <auto F, class... A>
 static std::unique_ptr<RecKernel> make_rec(dim3 grid, dim3 block, size_t smem, A&&... a) {
     std::unique_ptr<RecKernelOf<F>> r(new RecKernelOf<F>());
@@ -2640,7 +2664,16 @@ struct FusedBatch {
     int device = -1;
     long long launches = 0, library = 0;  // per replay
     std::map<std::vector<int>, cufftHandle> plans;  // (bytes per real, forward, nx, ny, nz, count)
-    DBuf<unsigned char> arenaIn, arenaOut;
+    // gather (input) and result (output) arrays of the batched FFTs, per lane (lanes may
+    // transform at the same time); the plans are per lane too
+    std::map<int, DBuf<unsigned char>> arenaIn, arenaOut;
+    // Streams and events on which the FFT groups of one operation (one per grid size)
+    // run side by side: each is only a few small cuFFT kernels.
+    std::vector<cudaStream_t> fftStreams;
+    std::vector<cudaEvent_t> fftEvents;  // [0] the fork, then one join per stream
+    // The lanes beyond the first (the boxes' side streams) and the events between them.
+    std::vector<cudaStream_t> laneStreams;
+    std::vector<cudaEvent_t> laneEvents;
     // Pinned staging of the host arrays, one DMA copy each way at the graph's start and
     // end, scattered to and gathered from the boxes' device buffers by one launch each:
     // per box, positions and incoming forces (6n doubles at inOff), forces, multipole and
@@ -2668,14 +2701,22 @@ struct FusedBatch {
         reset_graph();
         for (auto& kv : plans) cufftDestroy(kv.second);
         plans.clear();
-        arenaIn.free();
-        arenaOut.free();
+        arenaIn.clear();
+        arenaOut.clear();
         devIn.free();
         devOut.free();
         if (hostIn) cudaFreeHost(hostIn);
         if (hostOut) cudaFreeHost(hostOut);
         hostIn = hostOut = nullptr;
         hostInCount = hostOutCount = 0;
+        for (cudaStream_t q : fftStreams) cudaStreamDestroy(q);
+        for (cudaEvent_t ev : fftEvents) cudaEventDestroy(ev);
+        fftStreams.clear();
+        fftEvents.clear();
+        for (cudaStream_t q : laneStreams) cudaStreamDestroy(q);
+        for (cudaEvent_t ev : laneEvents) cudaEventDestroy(ev);
+        laneStreams.clear();
+        laneEvents.clear();
         if (evStart) cudaEventDestroy(evStart);
         if (evStop) cudaEventDestroy(evStop);
         evStart = evStop = nullptr;
@@ -2731,7 +2772,9 @@ static std::map<std::vector<int>, std::vector<FftSlot>> fft_groups(const std::ve
     return groups;
 }
 
-static void fused_fft(FusedBatch& fb, const std::vector<const RecOp*>& ops, cudaStream_t st) {
+static void fused_fft(FusedBatch& fb, const std::vector<const RecOp*>& ops, cudaStream_t st, int lane) {
+    DBuf<unsigned char>& arenaIn = fb.arenaIn[lane];
+    DBuf<unsigned char>& arenaOut = fb.arenaOut[lane];
     size_t inBytes, outBytes;
     const auto groups = fft_groups(ops, inBytes, outBytes);
     const RecOp& a = *ops[0];
@@ -2741,9 +2784,9 @@ static void fused_fft(FusedBatch& fb, const std::vector<const RecOp*>& ops, cuda
             const RecOp& op = *ops[sl.box];
             const size_t bi = fft_bytes(op, true), bo = fft_bytes(op, false);
             gather.push_back(make_rec<k_copy_bytes>(std::max(1, std::min(64, nblk((long long) (bi / 16), 256))), 256, 0,
-                                                    fb.arenaIn.p + sl.in, (const unsigned char*) op.src, bi));
+                                                    arenaIn.p + sl.in, (const unsigned char*) op.src, bi));
             scatter.push_back(make_rec<k_copy_bytes>(std::max(1, std::min(64, nblk((long long) (bo / 16), 256))), 256, 0,
-                                                     (unsigned char*) op.dst, (const unsigned char*) fb.arenaOut.p + sl.out, bo));
+                                                     (unsigned char*) op.dst, (const unsigned char*) arenaOut.p + sl.out, bo));
         }
     std::vector<const RecKernel*> g(gather.size()), s(scatter.size());
     for (size_t i = 0; i < gather.size(); ++i) {
@@ -2751,12 +2794,24 @@ static void fused_fft(FusedBatch& fb, const std::vector<const RecOp*>& ops, cuda
         s[i] = scatter[i].get();
     }
     g[0]->launch_group(g, st);
+    // the size groups side by side, each on its own stream, joined back into st
+    const int ng = (int) groups.size();
+    if (ng > 1) {
+        if ((int) fb.fftStreams.size() < ng || (int) fb.fftEvents.size() < ng + 1)
+            throw Error(MPID_ERR_STATE, "fused batch: FFT streams not prepared");
+        CUDA_CHECK(cudaEventRecord(fb.fftEvents[0], st));
+        for (int q = 0; q < ng; ++q) CUDA_CHECK(cudaStreamWaitEvent(fb.fftStreams[q], fb.fftEvents[0], 0));
+    }
+    int q = 0;
     for (const auto& kv : groups) {
-        const std::vector<int> pk = {a.fftPrec, a.fftForward, kv.first[0], kv.first[1], kv.first[2], (int) kv.second.size()};
+        const std::vector<int> pk = {a.fftPrec, a.fftForward, kv.first[0], kv.first[1], kv.first[2], (int) kv.second.size(),
+                                     lane};
         cufftHandle h = fb.plans.at(pk);
-        CUFFT_CHECK(cufftSetStream(h, st));
-        void* in = fb.arenaIn.p + kv.second[0].in;
-        void* out = fb.arenaOut.p + kv.second[0].out;
+        cudaStream_t gs = ng > 1 ? fb.fftStreams[q] : st;
+        ++q;
+        CUFFT_CHECK(cufftSetStream(h, gs));
+        void* in = arenaIn.p + kv.second[0].in;
+        void* out = arenaOut.p + kv.second[0].out;
         if (a.fftPrec == 4 && a.fftForward)
             CUFFT_CHECK(cufftExecR2C(h, (cufftReal*) in, (cufftComplex*) out));
         else if (a.fftPrec == 4)
@@ -2767,6 +2822,11 @@ static void fused_fft(FusedBatch& fb, const std::vector<const RecOp*>& ops, cuda
             CUFFT_CHECK(cufftExecZ2D(h, (cufftDoubleComplex*) in, (cufftDoubleReal*) out));
         ++t_library_calls;
     }
+    if (ng > 1)
+        for (int k = 0; k < ng; ++k) {
+            CUDA_CHECK(cudaEventRecord(fb.fftEvents[1 + k], fb.fftStreams[k]));
+            CUDA_CHECK(cudaStreamWaitEvent(st, fb.fftEvents[1 + k], 0));
+        }
     s[0]->launch_group(s, st);
 }
 
@@ -2777,8 +2837,11 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
     for (Context* c : boxes)
         if (c->rec.ops.size() != L)
             throw Error(MPID_ERR_INVALID, "fused batch: the boxes' evaluations differ in their operations");
-    size_t inMax = 0, outMax = 0;
-    std::vector<std::vector<int>> planKeys;
+    struct FftInfo {
+        size_t i, in, out;
+        std::vector<std::vector<int>> keys;
+    };
+    std::vector<FftInfo> fftInfo;
     std::vector<const RecOp*> ops(boxes.size());
     for (size_t i = 0; i < L; ++i) {
         const RecOp& a = boxes[0]->rec.ops[i];
@@ -2790,12 +2853,70 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
             if (!same) throw Error(MPID_ERR_INVALID, "fused batch: the boxes' evaluations differ in their operations");
         }
         if (a.kind == RecOp::FFT) {
-            size_t ib, ob;
-            for (const auto& kv : fft_groups(ops, ib, ob))
-                planKeys.push_back({a.fftPrec, a.fftForward, kv.first[0], kv.first[1], kv.first[2], (int) kv.second.size()});
-            inMax = std::max(inMax, ib);
-            outMax = std::max(outMax, ob);
+            FftInfo fi{i, 0, 0, {}};
+            for (const auto& kv : fft_groups(ops, fi.in, fi.out))
+                fi.keys.push_back({a.fftPrec, a.fftForward, kv.first[0], kv.first[1], kv.first[2], (int) kv.second.size()});
+            fftInfo.push_back(std::move(fi));
         }
+    }
+    // Lanes: each box's streams and events numbered by first use.  Boxes that follow the
+    // same code path number them alike, and the fused graph then runs lane l's
+    // operations on stream l with the recorded event dependencies between lanes (the
+    // reciprocal-space chain beside the real-space kernels, the FP64 residual check
+    // beside the force phase).  Otherwise one lane, and the events are dropped.
+    std::vector<int> laneOf(L, 0), slotOf(L, -1);
+    size_t nLanes = 1, nSlots = 0;
+    bool lanesOk = true;
+    for (size_t b = 0; b < boxes.size() && lanesOk; ++b) {
+        std::map<cudaStream_t, int> lane;
+        std::map<cudaEvent_t, int> slot;
+        lane[boxes[b]->rec.ops[0].stream] = 0;
+        for (size_t i = 0; i < L; ++i) {
+            const RecOp& o = boxes[b]->rec.ops[i];
+            auto it = lane.find(o.stream);
+            int l;
+            if (it == lane.end()) {
+                l = (int) lane.size();
+                lane[o.stream] = l;
+            } else {
+                l = it->second;
+            }
+            int e = -1;
+            if (o.kind == RecOp::EV_RECORD || o.kind == RecOp::EV_WAIT) {
+                auto jt = slot.find(o.event);
+                if (jt == slot.end()) {
+                    e = (int) slot.size();
+                    slot[o.event] = e;
+                } else {
+                    e = jt->second;
+                }
+            }
+            if (b == 0) {
+                laneOf[i] = l;
+                slotOf[i] = e;
+            } else if (laneOf[i] != l || slotOf[i] != e) {
+                lanesOk = false;
+                break;
+            }
+        }
+        if (b == 0) {
+            nLanes = lane.size();
+            nSlots = slot.size();
+        }
+    }
+    if (!lanesOk) {
+        std::fill(laneOf.begin(), laneOf.end(), 0);
+        nLanes = 1;
+    }
+    while (fb.laneStreams.size() + 1 < nLanes) {
+        cudaStream_t q;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+        fb.laneStreams.push_back(q);
+    }
+    while (fb.laneEvents.size() < nSlots + nLanes + 1) {
+        cudaEvent_t ev;
+        CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        fb.laneEvents.push_back(ev);
     }
     fb.reset_graph();
     // pinned staging of the inputs and outputs
@@ -2851,8 +2972,39 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
         if (mg) copyOut.emplace_back(out + 3 * n, c.gradOut.p, 20 * n * 8);
         if (pg) copyOut.emplace_back(out + 3 * n + (mg ? 20 * n : 0), c.polOut.p, 4 * n * 8);
     }
-    if (inMax) fb.arenaIn.alloc(inMax);
-    if (outMax) fb.arenaOut.alloc(outMax);
+    std::map<int, size_t> inMax, outMax;
+    std::vector<std::vector<int>> planKeys;
+    for (FftInfo& fi : fftInfo) {
+        const int lane = laneOf[fi.i];
+        inMax[lane] = std::max(inMax[lane], fi.in);
+        outMax[lane] = std::max(outMax[lane], fi.out);
+        for (auto& k : fi.keys) {
+            k.push_back(lane);
+            planKeys.push_back(k);
+        }
+    }
+    for (const auto& kv : inMax) fb.arenaIn[kv.first].alloc(kv.second);
+    for (const auto& kv : outMax) fb.arenaOut[kv.first].alloc(kv.second);
+    size_t maxGroups = 1;
+    for (size_t i = 0; i < L; ++i) {
+        if (boxes[0]->rec.ops[i].kind != RecOp::FFT) continue;
+        std::set<std::vector<int>> dims;
+        for (Context* c : boxes) {
+            const RecOp& o = c->rec.ops[i];
+            dims.insert({o.fftDims[0], o.fftDims[1], o.fftDims[2]});
+        }
+        maxGroups = std::max(maxGroups, dims.size());
+    }
+    while (fb.fftStreams.size() < maxGroups) {
+        cudaStream_t q;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+        fb.fftStreams.push_back(q);
+    }
+    while (fb.fftEvents.size() < maxGroups + 1) {
+        cudaEvent_t ev;
+        CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        fb.fftEvents.push_back(ev);
+    }
     for (const auto& pk : planKeys) {
         if (fb.plans.count(pk)) continue;
         int dims[3] = {pk[2], pk[3], pk[4]};
@@ -2869,15 +3021,36 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
     try {
         CUDA_CHECK(cudaMemcpyAsync(fb.devIn.p, fb.hostIn, nIn * sizeof(double), cudaMemcpyHostToDevice, st));
         copy_group(copyIn, st);
+        // lane l on stream lanes[l]; a lane joins the capture at its first operation (an
+        // event wait, or else a fork from lane 0 at that point)
+        std::vector<cudaStream_t> lanes(nLanes, st);
+        for (size_t l = 1; l < nLanes; ++l) lanes[l] = fb.laneStreams[l - 1];
+        std::vector<char> joined(nLanes, 0);
+        joined[0] = 1;
+        cudaEvent_t* slotEv = fb.laneEvents.data();
+        cudaEvent_t* laneEv = fb.laneEvents.data() + nSlots;  // forks and final joins
         for (size_t i = 0; i < L; ++i) {
             for (size_t b = 0; b < boxes.size(); ++b) ops[b] = &boxes[b]->rec.ops[i];
             const RecOp& a = *ops[0];
-            if (a.kind == RecOp::KERNEL) {
+            const int l = laneOf[i];
+            cudaStream_t ls = lanes[l];
+            if (!joined[l] && !(lanesOk && a.kind == RecOp::EV_WAIT)) {
+                CUDA_CHECK(cudaEventRecord(laneEv[nLanes], st));
+                CUDA_CHECK(cudaStreamWaitEvent(ls, laneEv[nLanes], 0));
+            }
+            joined[l] = 1;
+            if (a.kind == RecOp::EV_RECORD || a.kind == RecOp::EV_WAIT) {
+                if (!lanesOk) continue;
+                if (a.kind == RecOp::EV_RECORD)
+                    CUDA_CHECK(cudaEventRecord(slotEv[slotOf[i]], ls));
+                else
+                    CUDA_CHECK(cudaStreamWaitEvent(ls, slotEv[slotOf[i]], 0));
+            } else if (a.kind == RecOp::KERNEL) {
                 std::map<std::vector<unsigned>, std::vector<const RecKernel*>> byBlock;
                 for (const RecOp* o : ops) byBlock[{o->k->block.x, o->k->block.y, o->k->block.z}].push_back(o->k.get());
-                for (const auto& kv : byBlock) kv.second[0]->launch_group(kv.second, st);
+                for (const auto& kv : byBlock) kv.second[0]->launch_group(kv.second, ls);
             } else if (a.kind == RecOp::FFT) {
-                fused_fft(fb, ops, st);
+                fused_fft(fb, ops, ls, l);
             } else {
                 std::vector<std::unique_ptr<RecKernel>> tmp;
                 std::vector<const RecKernel*> grp;
@@ -2893,9 +3066,14 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
                     }
                     grp.push_back(tmp.back().get());
                 }
-                grp[0]->launch_group(grp, st);
+                grp[0]->launch_group(grp, ls);
             }
         }
+        for (size_t l = 1; l < nLanes; ++l)
+            if (joined[l]) {
+                CUDA_CHECK(cudaEventRecord(laneEv[l], lanes[l]));
+                CUDA_CHECK(cudaStreamWaitEvent(st, laneEv[l], 0));
+            }
         copy_group(copyOut, st);
         CUDA_CHECK(cudaMemcpyAsync(fb.hostOut, fb.devOut.p, nOut * sizeof(double), cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaGetLastError());
