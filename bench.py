@@ -272,13 +272,18 @@ def run_fitting(args, world, rank, local):
     # arms: (precision, host threads; 0 = one batched launch of all boxes' graphs)
     main = ("mixed", 0)
     arms = [main]
-    if world == 1:
+    if world == 1 and not args.main_only:
         arms = arms + [("mixed", args.threads)] + ([] if args.no_fp64 else [("double", 0)])
     for precision, threads in arms:
         with fitting.BoxBatch(systems, 2, precision=precision, threads=max(threads, 1), device=local,
                               batched=threads == 0) as b:
 
-            tuned = b.autotune()  # recorded per GPU; a later run reuses the choice
+            if args.launch_config:
+                m, q = (int(v) for v in args.launch_config.split(","))
+                b.configure({"max_split": m, "launch": q})
+                tuned = ({"max_split": m, "launch": q}, {})
+            else:
+                tuned = b.autotune()  # recorded per GPU; a later run reuses the choice
 
             def step():
                 e, _, g = b.evaluate()
@@ -617,6 +622,10 @@ def main():
                          "fitting64: the batched per-type gradient workload")
     ap.add_argument("--threads", type=int, default=16, help="host threads driving the boxes of fitting64 (comparison arm)")
     ap.add_argument("--boxes", type=int, default=64, help="fitting64: evaluate only the first N boxes (profiling)")
+    ap.add_argument("--launch-config", default=None, metavar="SPLIT,LAUNCH",
+                    help="fitting64: skip the autotuner; work-split bound and batched launch mode (0 fused, -1 one "
+                         "parent graph, k > 0 per-box graphs on k streams), e.g. 8,0 (profiling)")
+    ap.add_argument("--main-only", action="store_true", help="fitting64: time the batched mixed arm only (profiling)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.workload == "fitting64":
