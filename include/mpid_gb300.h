@@ -223,10 +223,21 @@ int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, con
  * After the launch each context's list sizes, solver convergence and FP64 residual are
  * checked; a context that fails a check (or is evaluated for the first time) gets the
  * ordinary evaluation instead, so the results are those of mpid_evaluate_with_gradients.
+ * type_grad: NULL, or [ntypes][24] per-type gradient sums over all boxes (see
+ * mpid_set_atom_types); per-atom gradients are then returned only where requested.
  * Calls are serialised within the process; a context may appear once per call. */
 int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* const* positions, const double* const* boxes,
                         double* const* forces, double* energies, double* const* multipole_grad,
-                        double* const* polarization_grad, int launch_mode);
+                        double* const* polarization_grad, double* type_grad, int launch_mode);
+
+/* Parameter types of the atoms (original order, 0 .. ntypes-1, ntypes <= 16; ntypes 0
+ * clears them) for the per-type gradient sums of mpid_evaluate_batch: with type_grad
+ * non-NULL the batch computes both gradient passes of every box and writes
+ * type_grad[t][24] = the sum over the atoms of type t of all boxes of the 20 multipole and
+ * 4 polarisation gradient components (the layout of multipole_grad and polarization_grad
+ * side by side), summed on the device per box and then over the boxes in order.  No
+ * reference counterpart (parameter fitting). */
+int mpid_set_atom_types(mpid_context* ctx, const int* types, int ntypes);
 
 /* Launch configuration: the largest number of sub-ranges each pair-kernel work item
  * (32 atoms x 32 list entries) is cut into, one warp each -- a power of two up to 32, or

@@ -25,7 +25,7 @@ C_API = ["mpid_default_settings", "mpid_create", "mpid_destroy", "mpid_set_multi
          "mpid_evaluate", "mpid_evaluate_device", "mpid_evaluate_device_noalloc", "mpid_get_dipoles",
          "mpid_get_pme_parameters", "mpid_get_stats", "mpid_last_error", "mpid_get_system_multipole_moments",
          "mpid_get_electrostatic_potential", "mpid_get_parameter_gradients", "mpid_evaluate_with_gradients",
-         "mpid_evaluate_batch", "mpid_set_work_split"]
+         "mpid_evaluate_batch", "mpid_set_work_split", "mpid_set_atom_types"]
 
 
 class Settings(ctypes.Structure):
@@ -107,8 +107,9 @@ def load_library(build=True):
     lib.mpid_get_parameter_gradients.argtypes = [vp, dp, dp, dp]
     lib.mpid_evaluate_with_gradients.argtypes = [vp, dp, dp, dp, dp, dp, dp]
     pp = ctypes.POINTER(ctypes.c_void_p)
-    lib.mpid_evaluate_batch.argtypes = [pp, ctypes.c_int, pp, pp, pp, dp, pp, pp, ctypes.c_int]
+    lib.mpid_evaluate_batch.argtypes = [pp, ctypes.c_int, pp, pp, pp, dp, pp, pp, dp, ctypes.c_int]
     lib.mpid_set_work_split.argtypes = [vp, ctypes.c_int]
+    lib.mpid_set_atom_types.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.c_int]
     lib.mpid_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.mpid_last_error.argtypes = []
     lib.mpid_last_error.restype = ctypes.c_char_p
@@ -296,6 +297,13 @@ class MPIDContext:
             null if gm is None else _dp(gm), null if gp is None else _dp(gp)))
         return e.value, f, gm, gp
 
+    def setAtomTypes(self, types, ntypes):
+        """Parameter types of the atoms (0 .. ntypes-1, ntypes <= 16) for the per-type
+        gradient sums of evaluate_batch(type_grad=True) (mpid_set_atom_types)."""
+        t = np.ascontiguousarray(types, dtype=np.int32).reshape(self.n)
+        self._check(self.lib.mpid_set_atom_types(self._h, t.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), int(ntypes)))
+        self.ntypes = int(ntypes)
+
     def setWorkSplit(self, max_split):
         """Upper bound (power of two up to 32, 0 = automatic) of the warps each pair-kernel
         work item is cut into (mpid_set_work_split)."""
@@ -333,7 +341,8 @@ class MPIDContext:
             pass
 
 
-def evaluate_batch(contexts, positions, boxes, forces=True, multipole=True, polarization=True, launch=0, flat=False):
+def evaluate_batch(contexts, positions, boxes, forces=True, multipole=True, polarization=True, launch=0, flat=False,
+                   type_grad=False):
     """mpid_evaluate_batch over MPIDContexts of PME systems on one device.  launch 0
     (fused): one kernel launch per operation for all boxes (each box's evaluation recorded
     once, operation i of every box launched together, FFTs batched per grid size; boxes of
@@ -342,7 +351,10 @@ def evaluate_batch(contexts, positions, boxes, forces=True, multipole=True, pola
     context whose list shape or solver length changed, takes the ordinary evaluation.
     Returns (energies (k,), forces [(n, 3)] or None, multipole gradients [(n, 20)] or
     None, polarisation gradients [(n, 4)] or None); the per-box arrays are consecutive
-    rows of one array per quantity, which flat=True returns instead ((sum n, 3), ...)."""
+    rows of one array per quantity, which flat=True returns instead ((sum n, 3), ...).
+    type_grad=True (every context with setAtomTypes) appends the (ntypes, 24) per-type
+    sums of the 20 multipole and 4 polarisation gradient components over all boxes,
+    summed on the device per box."""
     k = len(contexts)
     if k == 0:
         return np.zeros(0), None, None, None
@@ -376,9 +388,10 @@ def evaluate_batch(contexts, positions, boxes, forces=True, multipole=True, pola
     fp = ptrs(fo) if fo is not None else (null, None)
     mp = ptrs(gm) if gm is not None else (null, None)
     qp = ptrs(gp) if gp is not None else (null, None)
-    contexts[0]._check(lib.mpid_evaluate_batch(cp, k, pp, bp, fp[0], _dp(e), mp[0], qp[0], int(launch)))
+    tg = np.zeros((getattr(contexts[0], "ntypes", 0), 24)) if type_grad else None
+    tgp = _dp(tg) if type_grad else ctypes.POINTER(ctypes.c_double)()
+    contexts[0]._check(lib.mpid_evaluate_batch(cp, k, pp, bp, fp[0], _dp(e), mp[0], qp[0], tgp, int(launch)))
     for c, p, b in zip(contexts, pos, bx):
         c.last_positions, c.last_box = p.copy(), b.copy()
-    if flat:
-        return e, fo_all, gm_all, gp_all
-    return e, fo, gm, gp
+    out = (e, fo_all, gm_all, gp_all) if flat else (e, fo, gm, gp)
+    return out + (tg,) if type_grad else out

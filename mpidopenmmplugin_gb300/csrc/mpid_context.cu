@@ -696,6 +696,9 @@ struct Context {
     DBuf<double> masses, momentPartial, momentRed, gridPts, gridOut;  // system moments, potential
     DBuf<unsigned long long> gradFx;  // [20][npad] real-space parameter gradient
     DBuf<double> gradOut;             // [n][20]
+    DBuf<int> atomTypes;              // per-atom parameter type (original order), mpid_set_atom_types
+    std::vector<int> atomTypesHost;
+    int ntypes = 0;
     DBuf<unsigned long long> polFx;   // [2][npad] screening sums W, Z of the polarisation gradient
     DBuf<double> gradPtMu, gradPtE, gradEfix;  // FP64 copies of the mixed path's OPT orders and fields
     DBuf<double> polOut;              // [n][4]
@@ -2832,7 +2835,8 @@ static void fused_fft(FusedBatch& fb, const std::vector<const RecOp*>& ops, cuda
 
 // Checks that the boxes' recordings match operation by operation, prepares the FFT
 // plans and arrays, and captures the fused sequence as fb's graph.
-static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool mg, bool pg) {
+static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool mg, bool pg, bool outMg, bool outPg,
+                        bool typeSums) {
     const size_t L = boxes[0]->rec.ops.size();
     for (Context* c : boxes)
         if (c->rec.ops.size() != L)
@@ -2928,7 +2932,8 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
         fb.inOff[b] = nIn;
         fb.outOff[b] = nOut;
         nIn += (6 * n + 1) & ~(size_t) 1;  // 16-byte aligned starts
-        nOut += (3 * n + (mg ? 20 * n : 0) + (pg ? 4 * n : 0) + 1) & ~(size_t) 1;
+        nOut += (3 * n + (outMg ? 20 * n : 0) + (outPg ? 4 * n : 0) + (typeSums ? 24 * (size_t) boxes[b]->ntypes : 0) + 1) &
+                ~(size_t) 1;
     }
     if (nIn > fb.hostInCount) {
         if (fb.hostIn) cudaFreeHost(fb.hostIn);
@@ -2959,6 +2964,7 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
     if (!fb.evStart) CUDA_CHECK(cudaEventCreate(&fb.evStart));
     if (!fb.evStop) CUDA_CHECK(cudaEventCreate(&fb.evStop));
     std::vector<std::tuple<void*, const void*, size_t>> copyIn, copyOut;
+    std::vector<std::unique_ptr<RecKernel>> sums;  // per-type sums of each box's gradients
     fb.devIn.alloc(nIn);
     fb.devOut.alloc(nOut);
     for (size_t b = 0; b < boxes.size(); ++b) {
@@ -2969,9 +2975,15 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
         copyIn.emplace_back(c.pos.p, in, 3 * n * 8);
         copyIn.emplace_back(c.forcesOut.p, in + 3 * n, 3 * n * 8);
         copyOut.emplace_back(out, c.forcesOut.p, 3 * n * 8);
-        if (mg) copyOut.emplace_back(out + 3 * n, c.gradOut.p, 20 * n * 8);
-        if (pg) copyOut.emplace_back(out + 3 * n + (mg ? 20 * n : 0), c.polOut.p, 4 * n * 8);
+        if (outMg) copyOut.emplace_back(out + 3 * n, c.gradOut.p, 20 * n * 8);
+        if (outPg) copyOut.emplace_back(out + 3 * n + (outMg ? 20 * n : 0), c.polOut.p, 4 * n * 8);
+        if (typeSums)
+            sums.push_back(make_rec<k_type_sums>(1, 24 * 32, 0, c.n, (const int*) c.atomTypes.p, c.ntypes,
+                                                 (const double*) c.gradOut.p, (const double*) c.polOut.p,
+                                                 out + 3 * n + (outMg ? 20 * n : 0) + (outPg ? 4 * n : 0)));
     }
+    (void) mg;
+    (void) pg;
     std::map<int, size_t> inMax, outMax;
     std::vector<std::vector<int>> planKeys;
     for (FftInfo& fi : fftInfo) {
@@ -3074,6 +3086,11 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
                 CUDA_CHECK(cudaEventRecord(laneEv[l], lanes[l]));
                 CUDA_CHECK(cudaStreamWaitEvent(st, laneEv[l], 0));
             }
+        if (!sums.empty()) {
+            std::vector<const RecKernel*> grp;
+            for (const auto& r : sums) grp.push_back(r.get());
+            grp[0]->launch_group(grp, st);
+        }
         copy_group(copyOut, st);
         CUDA_CHECK(cudaMemcpyAsync(fb.hostOut, fb.devOut.p, nOut * sizeof(double), cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaGetLastError());
@@ -3180,6 +3197,26 @@ int mpid_set_covalent(mpid_context* ctx, const int* offsets, const int* index) {
     if (!ctx || !offsets) throw Error(MPID_ERR_INVALID, "null argument");
     mpid::DeviceScope scope(ctx->ctx.device);
     ctx->ctx.set_covalent(offsets, index);
+    return MPID_OK;
+    MPID_API_END
+}
+
+int mpid_set_atom_types(mpid_context* ctx, const int* types, int ntypes) {
+    MPID_API_BEGIN
+    if (!ctx || (!types && ntypes > 0)) throw Error(MPID_ERR_INVALID, "null argument");
+    if (ntypes < 0 || ntypes > mpid::kMaxTypeSums) throw Error(MPID_ERR_INVALID, "ntypes must be in 0..16");
+    Context& c = ctx->ctx;
+    for (int i = 0; i < c.n && ntypes > 0; ++i)
+        if (types[i] < 0 || types[i] >= ntypes) throw Error(MPID_ERR_INVALID, "atom type out of range");
+    mpid::DeviceScope scope(c.device);
+    if (ntypes > 0) {
+        c.atomTypes.alloc(std::max(c.n, 1));
+        CUDA_CHECK(cudaMemcpy(c.atomTypes.p, types, (size_t) c.n * sizeof(int), cudaMemcpyHostToDevice));
+        c.atomTypesHost.assign(types, types + c.n);
+    } else {
+        c.atomTypesHost.clear();
+    }
+    c.ntypes = ntypes;
     return MPID_OK;
     MPID_API_END
 }
@@ -3350,7 +3387,7 @@ static double batch_fallback(Context& c, const double* positions, const double* 
 
 int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* const* positions, const double* const* boxes,
                         double* const* forces, double* energies, double* const* multipole_grad,
-                        double* const* polarization_grad, int launch_mode) {
+                        double* const* polarization_grad, double* type_grad, int launch_mode) {
     MPID_API_BEGIN
     if (launch_mode < -1 || launch_mode > 128) throw Error(MPID_ERR_INVALID, "launch_mode must be in -1..128");
     if (count < 0 || (count > 0 && (!ctxs || !positions || !boxes || !energies)))
@@ -3364,12 +3401,23 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
         for (int q = 0; q < k; ++q)
             if (ctxs[q] == ctxs[k]) throw Error(MPID_ERR_INVALID, "mpid_evaluate_batch: a context appears twice");
     }
+    // per-atom gradient outputs requested, and the gradients computed (also for type sums)
+    auto outMg = [&](int k) { return multipole_grad && multipole_grad[k]; };
+    auto outPg = [&](int k) { return polarization_grad && polarization_grad[k]; };
+    auto wantMg = [&](int k) { return type_grad || outMg(k); };
+    auto wantPg = [&](int k) { return type_grad || outPg(k); };
+    const int nt = ctxs[0]->ctx.ntypes;
+    if (type_grad) {
+        for (int k = 0; k < count; ++k)
+            if (ctxs[k]->ctx.ntypes <= 0 || ctxs[k]->ctx.ntypes != nt)
+                throw Error(MPID_ERR_INVALID, "type_grad: every context needs the same atom types (mpid_set_atom_types)");
+        std::fill(type_grad, type_grad + (size_t) 24 * nt, 0.0);
+    }
+    std::vector<std::vector<double>> boxSums(type_grad ? count : 0);  // per box [nt][24]
     const bool fused = launch_mode == 0;
     if (fused) {
-        const bool mg0 = multipole_grad && multipole_grad[0], pg0 = polarization_grad && polarization_grad[0];
         for (int k = 0; k < count; ++k) {
-            const bool mg = multipole_grad && multipole_grad[k], pg = polarization_grad && polarization_grad[k];
-            if (mg != mg0 || pg != pg0)
+            if (outMg(k) != outMg(0) || outPg(k) != outPg(0))
                 throw Error(MPID_ERR_INVALID, "fused batch: every box must request the same gradients");
             if (ctxs[k]->ctx.n > mpid::kBlockSortMax)
                 throw Error(MPID_ERR_INVALID, "fused batch: boxes of at most 4096 atoms (use launch_mode > 0)");
@@ -3396,7 +3444,7 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
     bool changed = false;
     for (int k = 0; k < count; ++k) {
         Context& c = ctxs[k]->ctx;
-        const bool mg = multipole_grad && multipole_grad[k], pg = polarization_grad && polarization_grad[k];
+        const bool mg = wantMg(k), pg = wantPg(k);
         const double* fin = forces ? forces[k] : nullptr;
         c.stream = c.hostStream;
         c.bind_streams();
@@ -3436,7 +3484,8 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
                 K = std::max(K, ctxs[k]->ctx.batch_iterations());
             }
         std::vector<unsigned long long> key;
-        const bool mg = multipole_grad && multipole_grad[0], pg = polarization_grad && polarization_grad[0];
+        const bool mg = wantMg(0), pg = wantPg(0);
+        key.push_back((outMg(0) ? 1 : 0) | (outPg(0) ? 2 : 0) | (type_grad ? 4 : 0) | ((unsigned long long) nt << 8));
         for (Context* c : run) {
             changed = c->ensure_recording(mg, pg, K) || changed;
             key.push_back(c->id);
@@ -3444,7 +3493,7 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
         }
         if (!run.empty()) {
             if (changed || g_fused.key != key || !g_fused.exec) {
-                mpid::fused_build(g_fused, run, mg, pg);
+                mpid::fused_build(g_fused, run, mg, pg, outMg(0), outPg(0), type_grad != nullptr);
                 g_fused.key = key;
                 for (Context* c : run) ++c->stats.graph_captures;
             }
@@ -3525,7 +3574,7 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
     // results, and the ordinary evaluation of any context whose batched results do not stand
     for (int k = 0; k < count; ++k) {
         Context& c = ctxs[k]->ctx;
-        const bool mg = multipole_grad && multipole_grad[k], pg = polarization_grad && polarization_grad[k];
+        const bool mg = wantMg(k), pg = wantPg(k);
         double e = eFallback[k];
         if (graphed[k]) {
             const bool ok = fused ? c.batch_ok(launches, library) : c.batch_ok(c.full.nodes, c.full.library);
@@ -3537,8 +3586,16 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
                     const size_t n = (size_t) c.n;
                     const double* out = g_fused.hostOut + g_fused.outOff[slot[k]];
                     if (forces && forces[k]) std::memcpy(forces[k], out, 3 * n * 8);
-                    if (mg) std::memcpy(multipole_grad[k], out + 3 * n, 20 * n * 8);
-                    if (pg) std::memcpy(polarization_grad[k], out + 3 * n + (mg ? 20 * n : 0), 4 * n * 8);
+                    size_t o = 3 * n;
+                    if (outMg(k)) {
+                        std::memcpy(multipole_grad[k], out + o, 20 * n * 8);
+                        o += 20 * n;
+                    }
+                    if (outPg(k)) {
+                        std::memcpy(polarization_grad[k], out + o, 4 * n * 8);
+                        o += 4 * n;
+                    }
+                    if (type_grad) boxSums[k].assign(out + o, out + o + (size_t) 24 * nt);
                     energies[k] = e;
                     continue;
                 }
@@ -3550,17 +3607,31 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
             }
         }
         energies[k] = e;
-        const size_t n3 = 3 * (size_t) c.n;
+        const size_t n = (size_t) c.n;
         if (forces && forces[k])
-            CUDA_CHECK(cudaMemcpyAsync(forces[k], c.forcesOut.p, n3 * 8, cudaMemcpyDeviceToHost, c.stream));
-        if (mg)
-            CUDA_CHECK(cudaMemcpyAsync(multipole_grad[k], c.gradOut.p, (size_t) 20 * c.n * 8, cudaMemcpyDeviceToHost,
-                                       c.stream));
-        if (pg)
-            CUDA_CHECK(cudaMemcpyAsync(polarization_grad[k], c.polOut.p, (size_t) 4 * c.n * 8, cudaMemcpyDeviceToHost,
-                                       c.stream));
+            CUDA_CHECK(cudaMemcpyAsync(forces[k], c.forcesOut.p, 3 * n * 8, cudaMemcpyDeviceToHost, c.stream));
+        if (outMg(k))
+            CUDA_CHECK(cudaMemcpyAsync(multipole_grad[k], c.gradOut.p, 20 * n * 8, cudaMemcpyDeviceToHost, c.stream));
+        if (outPg(k))
+            CUDA_CHECK(cudaMemcpyAsync(polarization_grad[k], c.polOut.p, 4 * n * 8, cudaMemcpyDeviceToHost, c.stream));
+        if (type_grad) {
+            // per-type sums on the host from this box's per-atom gradients
+            std::vector<double> g(20 * n), q(4 * n);
+            CUDA_CHECK(cudaMemcpyAsync(g.data(), c.gradOut.p, 20 * n * 8, cudaMemcpyDeviceToHost, c.stream));
+            CUDA_CHECK(cudaMemcpyAsync(q.data(), c.polOut.p, 4 * n * 8, cudaMemcpyDeviceToHost, c.stream));
+            CUDA_CHECK(cudaStreamSynchronize(c.stream));
+            boxSums[k].assign((size_t) 24 * nt, 0.0);
+            for (size_t a = 0; a < n; ++a) {
+                double* row = boxSums[k].data() + 24 * (size_t) c.atomTypesHost[a];
+                for (int m = 0; m < 20; ++m) row[m] += g[20 * a + m];
+                for (int m = 0; m < 4; ++m) row[20 + m] += q[4 * a + m];
+            }
+        }
+        CUDA_CHECK(cudaStreamSynchronize(c.stream));
     }
-    for (int k = 0; k < count; ++k) CUDA_CHECK(cudaStreamSynchronize(ctxs[k]->ctx.stream));
+    if (type_grad)
+        for (int k = 0; k < count; ++k)
+            for (size_t m = 0; m < (size_t) 24 * nt; ++m) type_grad[m] += boxSums[k][m];
     return MPID_OK;
     MPID_API_END
 }

@@ -2945,4 +2945,33 @@ MPID_KERNEL void k_copy_bytes(KGrid<> kg, unsigned char* __restrict__ dst, const
     }
 }
 
+
+// Per-type sums of one box's parameter gradients (the 20 multipole and 4 polarisation
+// components of every atom, original order) for the fitting batch: warp c sums component
+// c, each lane over a stride of the atoms and per type, then a shuffle tree per type; out
+// holds [ntypes][24].  Fixed summation order.  One block of 24 warps per box.
+constexpr int kMaxTypeSums = 16;
+MPID_KERNEL void k_type_sums(KGrid<(24 * 32)> kg, int n, const int* __restrict__ types, int ntypes,
+                             const double* __restrict__ mgrad, const double* __restrict__ pgrad,
+                             double* __restrict__ out) {
+    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (c >= 24) return;
+    double acc[kMaxTypeSums];
+#pragma unroll
+    for (int t = 0; t < kMaxTypeSums; ++t) acc[t] = 0.0;
+    for (int i = lane; i < n; i += 32) {
+        const int t = types[i];
+        const double v = c < 20 ? mgrad[20 * (size_t) i + c] : pgrad[4 * (size_t) i + (c - 20)];
+#pragma unroll
+        for (int q = 0; q < kMaxTypeSums; ++q)
+            if (q == t) acc[q] += v;
+    }
+#pragma unroll
+    for (int q = 0; q < kMaxTypeSums; ++q) {
+        double v = acc[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && q < ntypes) out[24 * q + c] = v;
+    }
+}
+
 }  // namespace mpid

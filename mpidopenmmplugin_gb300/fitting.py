@@ -104,6 +104,10 @@ class BoxBatch:
         self.threads = max(1, int(threads))
         self.batched = bool(batched)
         self.batch_launch = 0  # batched launch mode: 0 fused, -1 one parent graph, k > 0 per-box graphs on k streams
+        if self.batched:
+            # per-type gradient sums on the device
+            for (f, p, b, t), ctx in zip(self.systems, self.contexts):
+                ctx.setAtomTypes(t, self.ntypes)
         self._pool = _cf.ThreadPoolExecutor(max_workers=self.threads)
 
     def set_parameters(self, params):
@@ -126,14 +130,10 @@ class BoxBatch:
         of the summed energy with respect to the per-type parameters (ntypes, 24)."""
         if self.batched:
             from .context import evaluate_batch
-            energies, fo, gm, gp = evaluate_batch(self.contexts, [s[1] for s in self.systems],
-                                                  [s[2] for s in self.systems], forces=forces,
-                                                  launch=self.batch_launch, flat=True)
-            # per-type sums over the atoms of all boxes at once
-            types = np.concatenate([np.asarray(s[3]) for s in self.systems])
-            grad = np.zeros((self.ntypes, NPARAM))
-            grad[:, :20] = per_type(gm, types, self.ntypes)
-            grad[:, 20:] = per_type(gp, types, self.ntypes)
+            energies, fo, _, _, grad = evaluate_batch(self.contexts, [s[1] for s in self.systems],
+                                                      [s[2] for s in self.systems], forces=forces, multipole=False,
+                                                      polarization=False, launch=self.batch_launch, flat=True,
+                                                      type_grad=True)
             if forces:
                 ends = np.cumsum([len(s[1]) for s in self.systems])
                 fo = np.split(fo, ends[:-1])

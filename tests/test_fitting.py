@@ -523,3 +523,26 @@ def test_autotuner_records_and_reuses_its_choice(tmp_path):
             print(cfg, np.abs(e1 / e0 - 1).max(), np.abs(g1 - g0).max() / np.abs(g0).max())
             assert np.allclose(e1, e0, rtol=1e-7, atol=0)
             assert np.abs(g1 - g0).max() <= 1e-6 * np.abs(g0).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("launch", [0, 8])
+def test_batch_type_sums_match_per_atom_gradients(launch):
+    """mpid_evaluate_batch's per-type gradient sums (type_grad, summed on the device per
+    box in the fused launch, on the host otherwise) against the per-type sums of the same
+    call's per-atom gradients, to 1e-12 relative; the first call (ordinary evaluations)
+    and a batched one."""
+    from mpidopenmmplugin_gb300.context import evaluate_batch
+    systems, _ = fitting.water_batch(nboxes=5, min_waters=128, max_waters=192)
+    ctxs = [MPIDContext(f, precision="mixed", box=b) for f, p, b, t in systems]
+    for (f, p, b, t), c in zip(systems, ctxs):
+        c.setAtomTypes(t, 2)
+    types = np.concatenate([t for _, _, _, t in systems])
+    for call in range(2):
+        e, fo, gm, gp, tg = evaluate_batch(ctxs, [s[1] for s in systems], [s[2] for s in systems], launch=launch,
+                                           flat=True, type_grad=True)
+        ref = np.hstack([fitting.per_type(gm, types, 2), fitting.per_type(gp, types, 2)])
+        assert tg.shape == (2, 24)
+        assert np.abs(tg - ref).max() <= 1e-12 * np.abs(ref).max(), (call, np.abs(tg - ref).max())
+    for c in ctxs:
+        c.close()
