@@ -546,3 +546,23 @@ def test_batch_type_sums_match_per_atom_gradients(launch):
         assert np.abs(tg - ref).max() <= 1e-12 * np.abs(ref).max(), (call, np.abs(tg - ref).max())
     for c in ctxs:
         c.close()
+
+
+@pytest.mark.gpu
+def test_fused_batch_beyond_one_launch_of_boxes():
+    """70 boxes: more than the 64 (or fewer, for large parameter sets) boxes whose
+    parameters one fused launch carries, so every fused operation is split into several
+    launches.  Energies, forces and per-type gradients against the per-box graphs (launch
+    mode 8), within the tolerances of the fused mixed path."""
+    systems, _ = fitting.water_batch(nboxes=70, min_waters=128, max_waters=136)
+    with fitting.BoxBatch(systems, 2, precision="mixed", batched=True) as fused, \
+            fitting.BoxBatch(systems, 2, precision="mixed", batched=True) as ref:
+        ref.configure({"launch": 8})
+        for _ in range(2):
+            e0, f0, g0 = ref.evaluate()
+            e1, f1, g1 = fused.evaluate()
+        assert fused.launches() < 600  # against about 126 per box (8,820) unfused
+        assert np.allclose(e1, e0, rtol=1e-7, atol=0), np.abs(e1 / e0 - 1).max()
+        for a, b in zip(f1, f0):
+            assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()
+        assert np.abs(g1 - g0).max() <= 1e-6 * np.abs(g0).max()
