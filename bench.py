@@ -48,8 +48,21 @@ WORKLOADS = {
                   "B-spline order 5, mutual polarisation to 1e-6 D (and OPT3 extrapolation), seeded synthetic "
                   "multipoles"),
 }
+WORKLOADS.update({
+    "water648": ("water648: 216 waters (648 atoms), 18.64 A box, cutoff 0.8 nm, alpha 3.5/nm, 24^3 grid, B-spline "
+                 "order 5, mutual polarisation to 1e-7 D, seeded synthetic multipoles"),
+    "solution61k": ("solution61k: 20,000 waters + 200 ethane-like solutes (61,600 atoms; solutes with anisotropic "
+                    "polarisabilities), 85.3 A box, cutoff 0.9 nm, alpha 3.4/nm, 96^3 grid, B-spline order 5, "
+                    "mutual polarisation to 1e-7 D (and Direct, OPT3), seeded synthetic multipoles"),
+})
 WORKLOAD = WORKLOADS["water24k"]
 METRIC_288K = "force+energy evals/s, 288k-atom water PME: mixed mutual (1e-6 D) vs OPT3 vs FP64"
+METRICS = {
+    "water24k": METRIC,
+    "water288k": METRIC_288K,
+    "water648": "force+energy evals/s, 648-atom water PME mutual pol: mixed vs FP64",
+    "solution61k": "force+energy evals/s, 61.6k-atom solution PME: mixed mutual vs Direct vs OPT3 vs FP64",
+}
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -430,7 +443,11 @@ def run_evaluations(args, world, rank, local):
 
     torch.cuda.set_device(local)
     name = args.workload
-    pols = [("mutual", MPIDForce.Mutual)] + ([("opt3", MPIDForce.Extrapolated)] if name == "water288k" else [])
+    pols = [("mutual", MPIDForce.Mutual)]
+    if name == "water288k":
+        pols.append(("opt3", MPIDForce.Extrapolated))
+    if name == "solution61k":
+        pols += [("direct", MPIDForce.Direct), ("opt3", MPIDForce.Extrapolated)]
     f, pos, box = synthetic.workload(name, polarization=MPIDForce.Mutual)
     n = f.getNumMultipoles()
     props = torch.cuda.get_device_properties(local)
@@ -504,7 +521,7 @@ def run_evaluations(args, world, rank, local):
                 extra["fp64_vs_oracle"] = errors_against(*fp64, ref.energy, ref.forces, ref.induced, helpers.rel_rms)
         except Exception as exc:
             cpu = {"value": None, "unit": "evals/s", "cores": 0, "kind": "port", "sample": "failed: %s" % exc}
-    # further polarisation types of the workload (water288k: OPT3)
+    # further polarisation types of the workload (water288k: OPT3; solution61k: Direct, OPT3)
     for label, pol in pols[1:]:
         f2 = synthetic.workload(name, polarization=pol)[0]
         arm = DeviceArm(torch, f2, pos, n, local, "mixed")
@@ -583,7 +600,7 @@ def run_evaluations(args, world, rank, local):
     roofline["pair_kernels"] = pair_kernels
     nbytes = 3 * n * 8
     line = {
-        "metric": METRIC if name == "water24k" else METRIC_288K, "value": value, "unit": "evals/s", "n_gpus": world,
+        "metric": METRICS[name], "value": value, "unit": "evals/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
         "config": {"workload": WORKLOADS[name], "precision": "mixed (FP32 kernels, FP64 energies and refinement)",
@@ -617,8 +634,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--workload", default="water24k", choices=["water24k", "water288k", "fitting64"],
+    ap.add_argument("--workload", default="water24k",
+                    choices=["water24k", "water288k", "water648", "solution61k", "fitting64"],
                     help="water24k: the headline evaluation; water288k: the 288,000-atom box (mutual and OPT3); "
+                         "water648: the 648-atom box; solution61k: the 61,600-atom solution (mutual, Direct, OPT3); "
                          "fitting64: the batched per-type gradient workload")
     ap.add_argument("--threads", type=int, default=16, help="host threads driving the boxes of fitting64 (comparison arm)")
     ap.add_argument("--boxes", type=int, default=64, help="fitting64: evaluate only the first N boxes (profiling)")
