@@ -1308,24 +1308,35 @@ struct Context {
         return usePme ? 4.0 / 3.0 * set.ewald_alpha * set.ewald_alpha * set.ewald_alpha / kSqrtPiRef : 0.0;
     }
 
-    // Permanent field -> Efix, muD, SE (and phiP for the reciprocal forces).
+    // Reciprocal part of the permanent field of engine e (phiP): spread of the 20
+    // multipole components, FFTs and the 35-term gather.  It needs no neighbour lists, so
+    // the set-up forks it onto the PME stream right after the atom frames and B-splines,
+    // beside the sort's successors and the list build, and joins it (fixed_recip_join) at
+    // the end of the set-up.
+    template <typename real>
+    void fixed_recip_fork(Engine<real>& e) {
+        if (!usePme) return;
+        fork_pme();
+        cudaStream_t ps = pmeStream;
+        timer.begin(ST_PME, ps);
+        e.pme.template spread<20>(n, npad, box, e.mf.p, nullptr, ps);
+        convolve(e, nullptr, ps);
+        e.pme.template gather<35>(n, npad, box, e.phiP.p, nullptr, ps);
+        timer.end(ps);
+    }
+    void fixed_recip_join() {
+        if (usePme) join_pme();
+    }
+
+    // Permanent field -> Efix, muD, SE: the real-space pairs plus the reciprocal part that
+    // the set-up computed (fixed_recip_fork).
     template <typename real>
     void fixed_field(Engine<real>& e) {
         cudaStream_t st = stream;
         op_memset(e.fieldFx.p, 0, 3 * (size_t) npad * 8, st);
-        if (usePme) {
-            fork_pme();
-            cudaStream_t ps = pmeStream;
-            timer.begin(ST_PME, ps);
-            e.pme.template spread<20>(n, npad, box, e.mf.p, nullptr, ps);
-            convolve(e, nullptr, ps);
-            e.pme.template gather<35>(n, npad, box, e.phiP.p, nullptr, ps);
-            timer.end(ps);
-        }
         timer.begin(ST_FIXED_REAL, st);
         launch<k_fixed_field<real>>(field_blocks(), 32 * kWarpsPerBlock, 0, st, field_list(), e.arrays(), e.fieldFx.p);
         timer.end(st);
-        if (usePme) join_pme();
         launch<k_record_fixed<real>>(nblk(npad, 128), 128, 0, st, n, npad, box, self_coef(), e.fieldFx.p,
                                                                usePme ? e.phiP.p : nullptr, e.arrays(), e.Efix.p, e.muD.p,
                                                                e.SE.p);
@@ -1993,6 +2004,7 @@ struct Context {
             replay(graph_key(kSegSetup), [&] {
                 sort_and_tiles();
                 prepare_engine(e, true);
+                fixed_recip_fork(e);  // beside the list build
                 launch<k_pack_atoms>(nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
                        pack0.p);
                 if (ed) {
@@ -2012,6 +2024,7 @@ struct Context {
                     }
                 }
                 launch_lists(e, false);
+                fixed_recip_join();
             });
             CUDA_CHECK(cudaEventRecord(evLists, st));
             finish_lists(e);
@@ -2035,7 +2048,9 @@ struct Context {
             Engine<double>& e = *ed;
             sort_and_tiles();
             prepare_engine(e, true);
+            fixed_recip_fork(e);  // beside the list build
             launch_lists(e);
+            fixed_recip_join();
             finish_lists(e);
             listsInScratch = growForbidden;
             stats.max_neighbours = lastMaxList;
@@ -2109,6 +2124,7 @@ struct Context {
             Engine<float>& e = *ef;
             sort_and_tiles();
             prepare_engine(e, true);
+            fixed_recip_fork(e);  // beside the list build
             launch<k_pack_atoms>(nblk(npad, 128), 128, 0, st, npad, (const float*) e.off.p, (const float4*) e.prm.p,
                    pack0.p);
             if (ed) {
@@ -2124,6 +2140,7 @@ struct Context {
                 op_wait(st, evRefStart);
             }
             launch_lists(e, false);  // the list maxima go to hostMax
+            fixed_recip_join();
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL) {
                 mutual_mixed_start(e);
@@ -2142,7 +2159,9 @@ struct Context {
             Engine<double>& e = *ed;
             sort_and_tiles();
             prepare_engine(e, true);
+            fixed_recip_fork(e);  // beside the list build
             launch_lists(e, false);
+            fixed_recip_join();
             fixed_field(e);
             if (set.polarization_type == MPID_MUTUAL) {
                 cg_begin<double, double>(e, e.SE.p, y64.p, r64.p, p64.p, q64.p, set.mutual_eps, K);
