@@ -2854,8 +2854,9 @@ static void fused_fft(FusedBatch& fb, const std::vector<const RecOp*>& ops, cuda
 
 // Checks that the boxes' recordings match operation by operation, prepares the FFT
 // plans and arrays, and captures the fused sequence as fb's graph.
-static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool mg, bool pg, bool outMg, bool outPg,
-                        bool typeSums) {
+// outMg / outPg: copy every box's per-atom multipole / polarisation gradients to the
+// staging; typeSums: reduce them per atom type on the device instead (k_type_sums).
+static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool outMg, bool outPg, bool typeSums) {
     const size_t L = boxes[0]->rec.ops.size();
     for (Context* c : boxes)
         if (c->rec.ops.size() != L)
@@ -3001,8 +3002,6 @@ static void fused_build(FusedBatch& fb, const std::vector<Context*>& boxes, bool
                                                  (const double*) c.gradOut.p, (const double*) c.polOut.p,
                                                  out + 3 * n + (outMg ? 20 * n : 0) + (outPg ? 4 * n : 0)));
     }
-    (void) mg;
-    (void) pg;
     std::map<int, size_t> inMax, outMax;
     std::vector<std::vector<int>> planKeys;
     for (FftInfo& fi : fftInfo) {
@@ -3512,7 +3511,7 @@ int mpid_evaluate_batch(mpid_context* const* ctxs, int count, const double* cons
         }
         if (!run.empty()) {
             if (changed || g_fused.key != key || !g_fused.exec) {
-                mpid::fused_build(g_fused, run, mg, pg, outMg(0), outPg(0), type_grad != nullptr);
+                mpid::fused_build(g_fused, run, outMg(0), outPg(0), type_grad != nullptr);
                 g_fused.key = key;
                 for (Context* c : run) ++c->stats.graph_captures;
             }
