@@ -216,7 +216,9 @@ int mpid_evaluate_with_gradients(mpid_context* ctx, const double* positions, con
  *     kernel launch over the blocks of every box (each block runs its own box's
  *     parameters), or one batched cuFFT transform per grid size; the sequence is captured
  *     as one CUDA graph and replayed while no box changes shape.  Boxes of at most 4096
- *     atoms that all request the same gradients.
+ *     atoms that all request the same gradients and evaluate the same way (precision,
+ *     polarisation type, covalently scaled pairs present or not); otherwise the call
+ *     fails with MPID_ERR_INVALID and launch_mode k > 0 takes the batch.
  *   launch_mode -1: each box's evaluation is a graph of its own; the graphs of all boxes
  *     run as one launch of a parent graph.
  *   launch_mode k > 0: each box's graph is launched on one of k streams.
