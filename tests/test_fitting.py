@@ -566,3 +566,45 @@ def test_fused_batch_beyond_one_launch_of_boxes():
         for a, b in zip(f1, f0):
             assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()
         assert np.abs(g1 - g0).max() <= 1e-6 * np.abs(g0).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["solution", "triclinic"])
+def test_fused_batch_on_solutes_and_triclinic_boxes(kind):
+    """The fused launch mode on boxes unlike the water batch: small solutions (ethanes with
+    anisotropic polarisabilities, 1-4 scaled pairs, so every box has covalently scaled
+    pair energies) and a triclinic box (the reference's triclinic fixture, its atoms
+    jittered per box).  Energies, forces and per-atom gradients against per-box graphs
+    (launch mode 8), within the tolerances of the fused mixed path, three calls in a row."""
+    from mpidopenmmplugin_gb300.context import evaluate_batch
+    systems = []
+    if kind == "solution":
+        for k in range(3):
+            f, pos, box = synthetic.solution_box(150 + 10 * k, 3, 17.5 + 0.4 * k, seed=31 + k)
+            f.setNonbondedMethod(MPIDForce.PME)
+            f.setCutoffDistance(0.7)
+            f.setPMEParameters(4.0, 18, 18, 18)
+            f.setPmeBSplineOrder(5)
+            f.setMutualInducedTargetEpsilon(1e-7)
+            systems.append((f, pos, box))
+    else:
+        fx = helpers.load_npz_fixture("triclinic_mutual.npz")
+        s = helpers.system_from_fixture(fx)
+        for k in range(3):
+            f = helpers.force_from_oracle_system(s)
+            pos = np.asarray(s.pos) + np.random.default_rng(40 + k).normal(scale=0.002, size=np.shape(s.pos))
+            systems.append((f, pos, np.asarray(s.box)))
+    ctxs = {launch: [MPIDContext(f, precision="mixed", box=b) for f, p, b in systems] for launch in (0, 8)}
+    pos = [p for _, p, _ in systems]
+    boxes = [b for _, _, b in systems]
+    for call in range(3):
+        e1, f1, m1, p1 = evaluate_batch(ctxs[0], pos, boxes, launch=0)
+        e0, f0, m0, p0 = evaluate_batch(ctxs[8], pos, boxes, launch=8)
+        assert np.allclose(e1, e0, rtol=1e-7, atol=0), (call, np.abs(e1 / e0 - 1).max())
+        for a, b in zip(f1, f0):
+            assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max(), call
+        for a, b in list(zip(m1, m0)) + list(zip(p1, p0)):
+            assert helpers.rel_rms(a, b) <= 1e-5, call
+    for cs in ctxs.values():
+        for c in cs:
+            c.close()
